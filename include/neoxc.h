@@ -1,0 +1,285 @@
+/*
+ * neoxc.h -- C-ABI of the GB300 engine for the NEO-RXCHF geminal-integral
+ * hot path (libneoxc_gb300.so).
+ *
+ * Every entry point replaces one reference Fortran routine and keeps its
+ * argument list, array layouts (column-major, packed indices of
+ * CS_Integrals/Spot_Check/pack_GAM.f) and output semantics (builders
+ * overwrite, Fock contractions accumulate into the caller's matrices,
+ * energies are overwritten).  Integers are int64_t (the reference is built
+ * with -integer-size 64), reals are double.  Array arguments are HOST
+ * memory unless the name starts with neoxc_dev_ (device pointers, work
+ * enqueued on `stream`, a cudaStream_t or NULL for the legacy stream).
+ *
+ * Return value: NEOXC_OK (0) or an error code; neoxc_last_error() gives a
+ * message.  No entry point aborts the process and none falls back to the
+ * CPU: without a usable GB300 device every compute call returns
+ * NEOXC_ERR_CUDA.
+ *
+ * Fortran callers can bind the neoxc_* symbols with ISO_C_BINDING
+ * interfaces (integer(c_int64_t), value, real(c_double)), or link the
+ * by-reference shims (gam2_ic1_, eg3ic1_, ...) which have exactly the
+ * reference's external-subroutine signatures.
+ */
+#ifndef NEOXC_H
+#define NEOXC_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NEOXC_OK 0
+#define NEOXC_ERR_ARG 1          /* inconsistent sizes / bad pointer     */
+#define NEOXC_ERR_CUDA 2         /* CUDA runtime error or no device      */
+#define NEOXC_ERR_NOMEM 3        /* device allocation failed             */
+#define NEOXC_ERR_UNSUPPORTED 4  /* shape outside the supported range    */
+#define NEOXC_ERR_IO 5           /* integral file could not be read      */
+
+const char* neoxc_last_error(void);
+int neoxc_version(void);
+/* 1 when a CUDA device of compute capability 10.3 is current, else 0. */
+int neoxc_device_ok(void);
+
+/* ---- packed index maps: CS_Integrals/Spot_Check/pack_GAM.f ------------ */
+/* pack_GAM.f:29-69 pack_4D */
+int64_t neoxc_pack_4d(int64_t n1, int64_t n2, int64_t n3, int64_t i1,
+                      int64_t i2, int64_t i3, int64_t i4);
+/* pack_GAM.f:72-105 index_GAM_2PK */
+int64_t neoxc_index_gam_2pk(int64_t nebf, int64_t npbf, int64_t ip,
+                            int64_t jp, int64_t ie1, int64_t je1,
+                            int64_t ie2, int64_t je2);
+/* pack_GAM.f:108-147 index_GAM_3PK */
+int64_t neoxc_index_gam_3pk(int64_t nebf, int64_t npbf, int64_t ip,
+                            int64_t jp, int64_t ie1, int64_t je1,
+                            int64_t ie2, int64_t je2, int64_t ie3,
+                            int64_t je3);
+/* pack_GAM.f:150-193 index_GAM_4PK and :196-239 index_GAM_4PK2 */
+int64_t neoxc_index_gam_4pk2(int64_t nebf, int64_t npbf, int64_t ip,
+                             int64_t jp, int64_t ie1, int64_t je1,
+                             int64_t ie2, int64_t je2, int64_t ie3,
+                             int64_t je3, int64_t ie4, int64_t je4);
+/* Device evaluation of a whole map in the reference's loop order
+ * (kind 0: GAM_ee pack_4D, 2/3/4: index_GAM_2PK/3PK/4PK2); out[count]. */
+int neoxc_index_map(int64_t kind, int64_t nebf, int64_t npbf, int64_t count,
+                    int64_t* out);
+
+/* ---- basis set-up done by the driver (xcneo_HYBRID.f) ----------------- */
+/* xcneo_HYBRID.f:1269-1307 make_KPE */
+int neoxc_make_kpe(int64_t nebf, int64_t npebf, const int64_t* AMPEB2C,
+                   int64_t* KPESTR, int64_t* KPEEND);
+
+/* ---- integral builders (overwrite their outputs) ---------------------- */
+/* gam_ee.f:2-169 calc_GAM_ee: GAM_ee(ngee) packed by pack_4D(je2,ie2,je1,ie1).
+ * The reference also writes GAM_ee.ufm; this call only fills the array. */
+int neoxc_calc_gam_ee(int64_t nebf, int64_t npebf, int64_t ngee,
+                      const int64_t* AMPEB2C, const double* AGEBFCC,
+                      const double* ELCEX, const int64_t* ELCAM,
+                      const double* ELCBFC, double* GAM_ee);
+
+/* gam2_IC1_OMP.f:2-212 GAM2_IC1 -> GM2ICR, GM2sICR (pair-symmetrised) */
+int neoxc_gam2_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                   int64_t ng2, int64_t ng2prm, int64_t nat, int64_t ngtg1,
+                   double pmass, const double* cat, const double* zan,
+                   const double* bcoef1, const double* gamma1,
+                   const int64_t* KPESTR, const int64_t* KPEEND,
+                   const int64_t* AMPEB2C, const double* AGEBFCC,
+                   const double* AGNBFCC, const double* ELCEX,
+                   const double* NUCEX, const int64_t* ELCAM,
+                   const int64_t* NUCAM, const double* ELCBFC,
+                   const double* NUCBFC, double* GM2ICR, double* GM2sICR);
+
+/* gam3_IC1_OMP.f:2-297 GAM3_IC1 -> GM3ICR (six-permutation symmetrised) */
+int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                   int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
+                   double pmass, const double* cat, const double* zan,
+                   const double* bcoef1, const double* gamma1,
+                   const int64_t* KPESTR, const int64_t* KPEEND,
+                   const int64_t* AMPEB2C, const double* AGEBFCC,
+                   const double* AGNBFCC, const double* ELCEX,
+                   const double* NUCEX, const int64_t* ELCAM,
+                   const int64_t* NUCAM, const double* ELCBFC,
+                   const double* NUCBFC, double* GM3ICR);
+
+/* rxchfne/rxchfne_gam2_IC1_OMP.f:2-243 RXCHFne_GAM2_IC1 -> GM2ICR (raw),
+ * GM2exICR (pair-averaged exchange term) */
+int neoxc_rxchfne_gam2_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf,
+                           int64_t npbf, int64_t ng2, int64_t ng2prm,
+                           int64_t nat, int64_t ngtg1, double pmass,
+                           const double* cat, const double* zan,
+                           const double* bcoef1, const double* gamma1,
+                           const int64_t* KPESTR, const int64_t* KPEEND,
+                           const int64_t* AMPEB2C, const double* AGEBFCC,
+                           const double* AGNBFCC, const double* ELCEX,
+                           const double* NUCEX, const int64_t* ELCAM,
+                           const int64_t* NUCAM, const double* ELCBFC,
+                           const double* NUCBFC, double* GM2ICR,
+                           double* GM2exICR);
+
+/* gam4_ICR_OMP.f:2-138 GAM4_ICR -> GAM_4(ng4) = gam_4/16.  The reference
+ * reads GAM_ee from GAM_ee.ufm; here it is an explicit argument. */
+int neoxc_gam4_icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ngee,
+                   int64_t ng2, int64_t ng4, const double* GAM_2s,
+                   const double* GAM_ee, double* GAM_4);
+
+/* ---- Fock / energy contractions (accumulate Fock, overwrite E) -------- */
+/* gam4_DSCF_OMP.f:2-139 GAM4_DSCF: fused gam_4 assembly + contraction, the
+ * gam_4 tensor is never stored.  GAM_ee / GAM_2s explicit (the reference
+ * reads GAM_ee.ufm / GAM_2s.ufm). */
+int neoxc_gam4_dscf(int64_t NG4CHK, int64_t ne, int64_t np, int64_t ngee,
+                    int64_t ng2, int64_t ng4, const double* GAM_ee,
+                    const double* GAM_2s, const double* DE, const double* DP,
+                    double* focke, double* fockp, double* E_gam4);
+
+/* gam4_ICR_OMP.f:273-376 EG4ICR */
+int neoxc_eg4icr(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                 const double* DE, const double* DP, const double* GM4ICR,
+                 double* focke, double* fockp, double* E_gam4);
+
+/* gam3_IC1_OMP.f:433-535 EG3IC1 */
+int neoxc_eg3ic1(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                 const double* DE, const double* DP, const double* GM3ICR,
+                 double* focke, double* fockp, double* E_gam3);
+
+/* gam2_IC1_OMP.f:339-443 EG2IC1: FE, FP accumulate; SE, SP, E, S
+ * overwritten. */
+int neoxc_eg2ic1(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                 const double* DE, const double* DP, const double* GM2ICR,
+                 const double* GM2SICR, double* FE, double* SE, double* FP,
+                 double* SP, double* E_gam2, double* S_gam2);
+
+/* rxchfne/rxchfne_omg2.f:2-116 RXCHFne_FAE_OMG2 */
+int neoxc_rxchfne_fae_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf,
+                           int64_t ng2, const double* DAE, const double* DBE,
+                           const double* DP, const double* GM2ICR,
+                           double* FAE, double* E_AE_OMG2);
+/* rxchfne/rxchfne_omg2.f:212-314 RXCHFne_FP_OMG2 */
+int neoxc_rxchfne_fp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf,
+                          int64_t ng2, int64_t NAE, int64_t NBE,
+                          const double* DAE, const double* DBE,
+                          const double* DP, const double* GM2ICR, double* FP,
+                          double* E_P_OMG2);
+/* rxchfne/rxchfne_omg2.f:409-511 RXCHFne_FBE_OMG2 */
+int neoxc_rxchfne_fbe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf,
+                           int64_t ng2, int64_t NAE, int64_t NBE,
+                           const double* DAE, const double* DBE,
+                           const double* DP, const double* GM2ICR,
+                           double* FBE, double* E_BE_OMG2);
+/* One pass over GM2ICR producing all three (no reference counterpart:
+ * the three routines above re-read the tensor once each). */
+int neoxc_rxchfne_omg2_fused(int64_t nebf, int64_t npbf, const double* DAE,
+                             const double* DBE, const double* DP,
+                             const double* GM2ICR, double* FAE, double* FP,
+                             double* FBE, double* E_OMG2);
+
+/* xchf1_independent/xchf1_fock.f:728-783 XCfock_correction */
+int neoxc_xcfock_correction(int64_t nebf, int64_t npbf, double E_total,
+                            double S_total, double H_expect,
+                            const double* se1, const double* sp1,
+                            const double* se2, const double* sp2,
+                            double* focke, double* fockp);
+
+/* ---- device-resident variants (no host copies; for SCF loops) --------- */
+int neoxc_dev_gam4_dscf(void* stream, int64_t ne, int64_t np,
+                        const double* d_GAM_ee, const double* d_GAM_2s,
+                        const double* d_DE, const double* d_DP,
+                        double* d_focke, double* d_fockp, double* d_E_gam4);
+int neoxc_dev_eg3ic1(void* stream, int64_t ne, int64_t np,
+                     const double* d_DE, const double* d_DP,
+                     const double* d_GM3ICR, double* d_focke,
+                     double* d_fockp, double* d_E_gam3);
+int neoxc_dev_eg2ic1(void* stream, int64_t ne, int64_t np,
+                     const double* d_DE, const double* d_DP,
+                     const double* d_GM2ICR, const double* d_GM2SICR,
+                     double* d_FE, double* d_SE, double* d_FP, double* d_SP,
+                     double* d_E_gam2, double* d_S_gam2);
+int neoxc_dev_rxchfne_omg2(void* stream, int64_t ne, int64_t np,
+                           const double* d_DAE, const double* d_DBE,
+                           const double* d_DP, const double* d_GM2ICR,
+                           double* d_FAE, double* d_FP, double* d_FBE,
+                           double* d_E);
+
+/* ---- Fortran external-subroutine shims (all arguments by reference) --- */
+/* Same argument lists as the reference subroutines; on error they print a
+ * message to stderr and record it for neoxc_last_error().  gam4_icr_ and
+ * gam4_dscf_ read GAM_ee.ufm (and GAM_2s.ufm) from the working directory
+ * like the reference; NEOXC_UFM_RECL sets the record length in bytes
+ * (default 8: RECL counted in bytes; 32 for ifort without byterecl). */
+void gam4_dscf_(const int64_t* NG4CHK, const int64_t* ne, const int64_t* np,
+                const int64_t* ngee, const int64_t* ng2, const int64_t* ng4,
+                const double* DE, const double* DP, double* focke,
+                double* fockp, double* E_gam4);
+void gam4_icr_(const int64_t* Nchunks, const int64_t* ne, const int64_t* np,
+               const int64_t* ngee, const int64_t* ng2, const int64_t* ng4,
+               const double* GAM_2s, double* GAM_4);
+void eg4icr_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+             const int64_t* ng4, const double* DE, const double* DP,
+             const double* GM4ICR, double* focke, double* fockp,
+             double* E_gam4);
+void eg3ic1_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+             const int64_t* ng3, const double* DE, const double* DP,
+             const double* GM3ICR, double* focke, double* fockp,
+             double* E_gam3);
+void eg2ic1_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+             const int64_t* ng2, const double* DE, const double* DP,
+             const double* GM2ICR, const double* GM2SICR, double* FE,
+             double* SE, double* FP, double* SP, double* E_gam2,
+             double* S_gam2);
+void gam2_ic1_(const int64_t* Nchunks, const int64_t* nebf,
+               const int64_t* npebf, const int64_t* npbf, const int64_t* ng2,
+               const int64_t* ng2prm, const int64_t* nat,
+               const int64_t* ngtg1, const double* pmass, const double* cat,
+               const double* zan, const double* bcoef1, const double* gamma1,
+               const int64_t* KPESTR, const int64_t* KPEEND,
+               const int64_t* AMPEB2C, const double* AGEBFCC,
+               const double* AGNBFCC, const double* ELCEX,
+               const double* NUCEX, const int64_t* ELCAM,
+               const int64_t* NUCAM, const double* ELCBFC,
+               const double* NUCBFC, double* GM2ICR, double* GM2sICR);
+void gam3_ic1_(const int64_t* Nchunks, const int64_t* nebf,
+               const int64_t* npebf, const int64_t* npbf, const int64_t* ng3,
+               const int64_t* ng3prm, const int64_t* nat,
+               const int64_t* ngtg1, const double* pmass, const double* cat,
+               const double* zan, const double* bcoef1, const double* gamma1,
+               const int64_t* KPESTR, const int64_t* KPEEND,
+               const int64_t* AMPEB2C, const double* AGEBFCC,
+               const double* AGNBFCC, const double* ELCEX,
+               const double* NUCEX, const int64_t* ELCAM,
+               const int64_t* NUCAM, const double* ELCBFC,
+               const double* NUCBFC, double* GM3ICR);
+void rxchfne_gam2_ic1_(const int64_t* Nchunks, const int64_t* nebf,
+                       const int64_t* npebf, const int64_t* npbf,
+                       const int64_t* ng2, const int64_t* ng2prm,
+                       const int64_t* nat, const int64_t* ngtg1,
+                       const double* pmass, const double* cat,
+                       const double* zan, const double* bcoef1,
+                       const double* gamma1, const int64_t* KPESTR,
+                       const int64_t* KPEEND, const int64_t* AMPEB2C,
+                       const double* AGEBFCC, const double* AGNBFCC,
+                       const double* ELCEX, const double* NUCEX,
+                       const int64_t* ELCAM, const int64_t* NUCAM,
+                       const double* ELCBFC, const double* NUCBFC,
+                       double* GM2ICR, double* GM2exICR);
+void rxchfne_fae_omg2_(const int64_t* Nchunks, const int64_t* nebf,
+                       const int64_t* npbf, const int64_t* ng2,
+                       const double* DAE, const double* DBE, const double* DP,
+                       const double* GM2ICR, double* FAE, double* E_AE_OMG2);
+void rxchfne_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf,
+                      const int64_t* npbf, const int64_t* ng2,
+                      const int64_t* NAE, const int64_t* NBE,
+                      const double* DAE, const double* DBE, const double* DP,
+                      const double* GM2ICR, double* FP, double* E_P_OMG2);
+void rxchfne_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf,
+                       const int64_t* npbf, const int64_t* ng2,
+                       const int64_t* NAE, const int64_t* NBE,
+                       const double* DAE, const double* DBE, const double* DP,
+                       const double* GM2ICR, double* FBE, double* E_BE_OMG2);
+void calc_gam_ee_(const int64_t* nebf, const int64_t* npebf,
+                  const int64_t* ngee, const int64_t* AMPEB2C,
+                  const double* AGEBFCC, const double* ELCEX,
+                  const int64_t* ELCAM, const double* ELCBFC);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEOXC_H */

@@ -1,0 +1,745 @@
+// abi.cu -- host side of the C-ABI declared in include/neoxc.h.
+//
+// Each neoxc_* entry point validates the reference's size arguments,
+// stages host arrays into device memory on the library stream, runs the
+// sm_103a kernels and copies results back (accumulating into the caller's
+// Fock matrices where the reference does add2fock).  There is no CPU
+// compute path: if CUDA is unusable the call returns NEOXC_ERR_CUDA.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/neoxc.h"
+#include "neoxc_internal.h"
+
+using namespace neoxc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CU(call)                                                           \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess)                                                 \
+      return set_err(e_ == cudaErrorMemoryAllocation ? NEOXC_ERR_NOMEM     \
+                                                     : NEOXC_ERR_CUDA,     \
+                     "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
+                     __FILE__, __LINE__);                                  \
+  } while (0)
+
+struct Ctx {
+  cudaStream_t stream = nullptr;
+  int device = -1;
+};
+
+std::mutex g_mu;
+Ctx g_ctx[64];
+
+// library stream of the current device (created on first use)
+int get_stream(cudaStream_t* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return set_err(NEOXC_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return set_err(NEOXC_ERR_CUDA, "device id %d", dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx& c = g_ctx[dev];
+  if (!c.stream) {
+    cudaDeviceProp p;
+    e = cudaGetDeviceProperties(&p, dev);
+    if (e != cudaSuccess)
+      return set_err(NEOXC_ERR_CUDA, "cudaGetDeviceProperties: %s",
+                     cudaGetErrorString(e));
+    if (!(p.major == 10 && p.minor == 3))
+      return set_err(NEOXC_ERR_CUDA,
+                     "device %d is sm_%d%d; this library is built for sm_103a",
+                     dev, p.major, p.minor);
+    e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+      return set_err(NEOXC_ERR_CUDA, "cudaStreamCreate: %s",
+                     cudaGetErrorString(e));
+    c.device = dev;
+  }
+  *out = c.stream;
+  return NEOXC_OK;
+}
+
+// Device buffer released on the stream it was allocated on.
+struct DBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+int dalloc(DBuf& b, size_t bytes, cudaStream_t s) {
+  b.s = s;
+  if (bytes == 0) bytes = 8;
+  cudaError_t e = cudaMallocAsync(&b.p, bytes, s);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return set_err(NEOXC_ERR_NOMEM, "device allocation of %zu bytes: %s",
+                   bytes, cudaGetErrorString(e));
+  }
+  return NEOXC_OK;
+}
+
+int upload(DBuf& b, const void* h, size_t bytes, cudaStream_t s) {
+  int rc = dalloc(b, bytes, s);
+  if (rc) return rc;
+  if (bytes) CU(cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, s));
+  return NEOXC_OK;
+}
+
+int finish(cudaStream_t s) {
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(s));
+  return NEOXC_OK;
+}
+
+#define RC(x)               \
+  do {                      \
+    int rc_ = (x);          \
+    if (rc_) return rc_;    \
+  } while (0)
+
+int need(bool ok, const char* what) {
+  return ok ? NEOXC_OK : set_err(NEOXC_ERR_ARG, "argument check failed: %s", what);
+}
+
+// ---- basis staging for the MD builders ------------------------------------
+struct SysUpload {
+  DevSystem d{};
+  DBuf eprim, pprim, kps, kpe, zan, cat, bgem, ggem;
+};
+
+int stage_system(SysUpload& u, cudaStream_t s, int64_t nebf, int64_t npebf,
+                 int64_t npbf, int64_t nat, int64_t ngtg, double pmass,
+                 const double* cat, const double* zan, const double* bcoef1,
+                 const double* gamma1, const int64_t* KPESTR,
+                 const int64_t* KPEEND, const double* AGEBFCC,
+                 const double* AGNBFCC, const double* ELCEX,
+                 const double* NUCEX, const int64_t* ELCAM,
+                 const int64_t* NUCAM, const double* ELCBFC,
+                 const double* NUCBFC) {
+  RC(need(nebf >= 1 && npebf >= nebf && npbf >= 1, "basis sizes"));
+  RC(need(nat >= 0 && nat <= kMaxNat, "nat within the supported range"));
+  RC(need(ngtg >= 1 && ngtg <= kMaxNG, "ngtg within the supported range"));
+  std::vector<DevPrim> ep(npebf), pp(npbf);
+  for (int64_t i = 0; i < npebf; i++) {
+    DevPrim& q = ep[i];
+    q.a = ELCEX[i];
+    q.coef = AGEBFCC[i];
+    for (int d = 0; d < 3; d++) {
+      q.c[d] = ELCBFC[i + npebf * d];
+      q.l[d] = (int)ELCAM[i + npebf * d];
+      if (q.l[d] < 0 || q.l[d] > kMaxL)
+        return set_err(NEOXC_ERR_UNSUPPORTED,
+                       "electronic primitive %lld has l=%d in one Cartesian "
+                       "direction (supported: 0..%d)",
+                       (long long)i + 1, q.l[d], kMaxL);
+    }
+    if (q.l[0] + q.l[1] + q.l[2] > 2)
+      return set_err(NEOXC_ERR_UNSUPPORTED,
+                     "electronic primitive %lld has total l > 2 (the MD "
+                     "kernels support Cartesian s, p, d)", (long long)i + 1);
+    q.pad = 0;
+  }
+  for (int64_t i = 0; i < npbf; i++) {
+    DevPrim& q = pp[i];
+    q.a = NUCEX[i];
+    q.coef = AGNBFCC[i];
+    for (int d = 0; d < 3; d++) {
+      q.c[d] = NUCBFC[i + npbf * d];
+      q.l[d] = (int)NUCAM[i + npbf * d];
+      if (q.l[d] < 0 || q.l[d] > kMaxL)
+        return set_err(NEOXC_ERR_UNSUPPORTED,
+                       "nuclear primitive %lld has l=%d in one Cartesian "
+                       "direction (supported: 0..%d)",
+                       (long long)i + 1, q.l[d], kMaxL);
+    }
+    if (q.l[0] + q.l[1] + q.l[2] > 2)
+      return set_err(NEOXC_ERR_UNSUPPORTED,
+                     "nuclear primitive %lld has total l > 2 (the MD kernels "
+                     "support Cartesian s, p, d)", (long long)i + 1);
+    q.pad = 0;
+  }
+  std::vector<int> ks(nebf), ke(nebf);
+  for (int64_t i = 0; i < nebf; i++) {
+    ks[i] = (int)KPESTR[i] - 1;
+    ke[i] = (int)KPEEND[i] - 1;
+    if (ks[i] < 0 || ke[i] < ks[i] || ke[i] >= npebf)
+      return set_err(NEOXC_ERR_ARG, "KPESTR/KPEEND(%lld) out of range",
+                     (long long)i + 1);
+  }
+  RC(upload(u.eprim, ep.data(), sizeof(DevPrim) * npebf, s));
+  RC(upload(u.pprim, pp.data(), sizeof(DevPrim) * npbf, s));
+  RC(upload(u.kps, ks.data(), sizeof(int) * nebf, s));
+  RC(upload(u.kpe, ke.data(), sizeof(int) * nebf, s));
+  RC(upload(u.zan, zan, sizeof(double) * (nat ? nat : 1) * (nat ? 1 : 0), s));
+  RC(upload(u.cat, cat, sizeof(double) * 3 * nat, s));
+  RC(upload(u.bgem, bcoef1, sizeof(double) * ngtg, s));
+  RC(upload(u.ggem, gamma1, sizeof(double) * ngtg, s));
+  u.d.nebf = (int)nebf;
+  u.d.npebf = (int)npebf;
+  u.d.npbf = (int)npbf;
+  u.d.nat = (int)nat;
+  u.d.ngtg = (int)ngtg;
+  u.d.pmass = pmass;
+  u.d.eprim = u.eprim.as<DevPrim>();
+  u.d.pprim = u.pprim.as<DevPrim>();
+  u.d.kpestr = u.kps.as<int>();
+  u.d.kpeend = u.kpe.as<int>();
+  u.d.zan = u.zan.as<double>();
+  u.d.cat = u.cat.as<double>();
+  u.d.bgem = u.bgem.as<double>();
+  u.d.ggem = u.ggem.as<double>();
+  return NEOXC_OK;
+}
+
+// Fock accumulate: device result added to the caller's host matrix.
+int accumulate_back(double* host, const double* dev, int64_t n,
+                    cudaStream_t s) {
+  std::vector<double> tmp(n);
+  CU(cudaMemcpyAsync(tmp.data(), dev, sizeof(double) * n,
+                     cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  for (int64_t k = 0; k < n; k++) host[k] += tmp[k];
+  return NEOXC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* neoxc_last_error(void) { return g_err.c_str(); }
+int neoxc_version(void) { return 100; }
+
+int neoxc_device_ok(void) {
+  cudaStream_t s;
+  return get_stream(&s) == NEOXC_OK ? 1 : 0;
+}
+
+// ---- index maps --------------------------------------------------------------
+int64_t neoxc_pack_4d(int64_t n1, int64_t n2, int64_t n3, int64_t i1,
+                      int64_t i2, int64_t i3, int64_t i4) {
+  return 1 + (i1 - 1) + n1 * ((i2 - 1) + n2 * ((i3 - 1) + n3 * (i4 - 1)));
+}
+int64_t neoxc_index_gam_2pk(int64_t ne, int64_t np, int64_t ip, int64_t jp,
+                            int64_t ie1, int64_t je1, int64_t ie2,
+                            int64_t je2) {
+  return 1 + (je2 - 1) +
+         ne * ((ie2 - 1) +
+               ne * ((je1 - 1) + ne * ((ie1 - 1) + ne * ((jp - 1) + np * (ip - 1)))));
+}
+int64_t neoxc_index_gam_3pk(int64_t ne, int64_t np, int64_t ip, int64_t jp,
+                            int64_t ie1, int64_t je1, int64_t ie2,
+                            int64_t je2, int64_t ie3, int64_t je3) {
+  return 1 + (je3 - 1) +
+         ne * ((ie3 - 1) + ne * ((je2 - 1) + ne * ((ie2 - 1) +
+         ne * ((je1 - 1) + ne * ((ie1 - 1) + ne * ((jp - 1) + np * (ip - 1)))))));
+}
+int64_t neoxc_index_gam_4pk2(int64_t ne, int64_t np, int64_t ip, int64_t jp,
+                             int64_t ie1, int64_t je1, int64_t ie2,
+                             int64_t je2, int64_t ie3, int64_t je3,
+                             int64_t ie4, int64_t je4) {
+  return 1 + (je4 - 1) +
+         ne * ((ie4 - 1) + ne * ((je3 - 1) + ne * ((ie3 - 1) +
+         ne * ((je2 - 1) + ne * ((ie2 - 1) + ne * ((je1 - 1) +
+         ne * ((ie1 - 1) + ne * ((jp - 1) + np * (ip - 1)))))))));
+}
+
+int neoxc_index_map(int64_t kind, int64_t ne, int64_t np, int64_t count,
+                    int64_t* out) {
+  RC(need(out != nullptr && count >= 0, "output"));
+  int64_t total = kind == 0 ? ne * ne * ne * ne
+                : kind == 2 ? ne * ne * ne * ne * np * np
+                : kind == 3 ? ne * ne * ne * ne * ne * ne * np * np
+                : kind == 4 ? ne * ne * ne * ne * ne * ne * ne * ne * np * np
+                            : -1;
+  RC(need(total >= 0, "kind in {0,2,3,4}"));
+  RC(need(count <= total, "count <= size of the map"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf d;
+  RC(dalloc(d, sizeof(int64_t) * count, s));
+  CU(launch_index_fill((int)kind, (int)ne, (int)np, count, d.as<int64_t>(), s));
+  CU(cudaMemcpyAsync(out, d.p, sizeof(int64_t) * count, cudaMemcpyDeviceToHost,
+                     s));
+  return finish(s);
+}
+
+int neoxc_make_kpe(int64_t nebf, int64_t npebf, const int64_t* AMPEB2C,
+                   int64_t* KPESTR, int64_t* KPEEND) {
+  RC(need(nebf >= 1 && npebf >= nebf && AMPEB2C && KPESTR && KPEEND, "sizes"));
+  int64_t ichk = 1, ist = 1;
+  for (int64_t iep = 1; iep <= npebf; iep++) {
+    int64_t iec = AMPEB2C[iep - 1];
+    if (iec < 1 || iec > nebf)
+      return set_err(NEOXC_ERR_ARG, "AMPEB2C(%lld)=%lld out of range",
+                     (long long)iep, (long long)iec);
+    if (iec != ichk) {
+      ichk = ichk + 1;
+      if (iec - 2 < 0) return set_err(NEOXC_ERR_ARG, "AMPEB2C not ordered");
+      KPESTR[iec - 2] = ist;
+      KPEEND[iec - 2] = iep - 1;
+      ist = iep;
+    }
+    if (iep == npebf) {
+      KPESTR[iec - 1] = ist;
+      KPEEND[iec - 1] = iep;
+    }
+  }
+  return NEOXC_OK;
+}
+
+// ---- builders -----------------------------------------------------------------
+int neoxc_calc_gam_ee(int64_t nebf, int64_t npebf, int64_t ngee,
+                      const int64_t* AMPEB2C, const double* AGEBFCC,
+                      const double* ELCEX, const int64_t* ELCAM,
+                      const double* ELCBFC, double* GAM_ee) {
+  RC(need(ngee == nebf * nebf * nebf * nebf, "ngee == nebf**4"));
+  RC(need(GAM_ee && AMPEB2C && AGEBFCC && ELCEX && ELCAM && ELCBFC, "pointers"));
+  std::vector<int64_t> kps(nebf), kpe(nebf);
+  RC(neoxc_make_kpe(nebf, npebf, AMPEB2C, kps.data(), kpe.data()));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  // GAM_ee needs no nuclear basis or geminal; stage a 1-function stub
+  const double one = 1.0, zero3[3] = {0, 0, 0}, g1 = 1.0, b1 = 0.0;
+  const int64_t l0[3] = {0, 0, 0};
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, 1, 0, 1, 1.0, zero3, &one, &b1, &g1,
+                  kps.data(), kpe.data(), AGEBFCC, &one, ELCEX, &one, ELCAM,
+                  l0, ELCBFC, zero3));
+  DBuf d;
+  RC(dalloc(d, sizeof(double) * ngee, s));
+  CU(launch_gam_ee(u.d, d.as<double>(), s));
+  CU(cudaMemcpyAsync(GAM_ee, d.p, sizeof(double) * ngee,
+                     cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+static int gam2_common(int rx, int64_t nebf, int64_t npebf, int64_t npbf,
+                       int64_t ng2, int64_t nat, int64_t ngtg1, double pmass,
+                       const double* cat, const double* zan,
+                       const double* bcoef1, const double* gamma1,
+                       const int64_t* KPESTR, const int64_t* KPEEND,
+                       const double* AGEBFCC, const double* AGNBFCC,
+                       const double* ELCEX, const double* NUCEX,
+                       const int64_t* ELCAM, const int64_t* NUCAM,
+                       const double* ELCBFC, const double* NUCBFC,
+                       double* out1, double* out2) {
+  RC(need(ng2 == nebf * nebf * nebf * nebf * npbf * npbf,
+          "ng2 == nebf**4 * npbf**2"));
+  RC(need(out1 && out2, "output pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan,
+                  bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX,
+                  NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC));
+  DBuf d1, d2;
+  RC(dalloc(d1, sizeof(double) * ng2, s));
+  RC(dalloc(d2, sizeof(double) * ng2, s));
+  CU(launch_gam2_raw(u.d, rx, d1.as<double>(), d2.as<double>(), s));
+  CU(launch_gam2_symmetrize((int)nebf, (int)npbf, rx, d1.as<double>(),
+                            d2.as<double>(), s));
+  CU(cudaMemcpyAsync(out1, d1.p, sizeof(double) * ng2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(out2, d2.p, sizeof(double) * ng2, cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+int neoxc_gam2_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                   int64_t ng2, int64_t ng2prm, int64_t nat, int64_t ngtg1,
+                   double pmass, const double* cat, const double* zan,
+                   const double* bcoef1, const double* gamma1,
+                   const int64_t* KPESTR, const int64_t* KPEEND,
+                   const int64_t* AMPEB2C, const double* AGEBFCC,
+                   const double* AGNBFCC, const double* ELCEX,
+                   const double* NUCEX, const int64_t* ELCAM,
+                   const int64_t* NUCAM, const double* ELCBFC,
+                   const double* NUCBFC, double* GM2ICR, double* GM2sICR) {
+  (void)AMPEB2C;
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ng2prm == npebf * npebf * npebf * npebf * npbf * npbf, "ng2prm"));
+  return gam2_common(0, nebf, npebf, npbf, ng2, nat, ngtg1, pmass, cat, zan,
+                     bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX,
+                     NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, GM2ICR, GM2sICR);
+}
+
+int neoxc_rxchfne_gam2_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf,
+                           int64_t npbf, int64_t ng2, int64_t ng2prm,
+                           int64_t nat, int64_t ngtg1, double pmass,
+                           const double* cat, const double* zan,
+                           const double* bcoef1, const double* gamma1,
+                           const int64_t* KPESTR, const int64_t* KPEEND,
+                           const int64_t* AMPEB2C, const double* AGEBFCC,
+                           const double* AGNBFCC, const double* ELCEX,
+                           const double* NUCEX, const int64_t* ELCAM,
+                           const int64_t* NUCAM, const double* ELCBFC,
+                           const double* NUCBFC, double* GM2ICR,
+                           double* GM2exICR) {
+  (void)AMPEB2C;
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ng2prm == npebf * npebf * npebf * npebf * npbf * npbf, "ng2prm"));
+  return gam2_common(1, nebf, npebf, npbf, ng2, nat, ngtg1, pmass, cat, zan,
+                     bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX,
+                     NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, GM2ICR, GM2exICR);
+}
+
+int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                   int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
+                   double pmass, const double* cat, const double* zan,
+                   const double* bcoef1, const double* gamma1,
+                   const int64_t* KPESTR, const int64_t* KPEEND,
+                   const int64_t* AMPEB2C, const double* AGEBFCC,
+                   const double* AGNBFCC, const double* ELCEX,
+                   const double* NUCEX, const int64_t* ELCAM,
+                   const int64_t* NUCAM, const double* ELCBFC,
+                   const double* NUCBFC, double* GM3ICR) {
+  (void)AMPEB2C;
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  int64_t n6 = nebf * nebf * nebf * nebf * nebf * nebf;
+  RC(need(ng3 == n6 * npbf * npbf, "ng3 == nebf**6 * npbf**2"));
+  int64_t p6 = npebf * npebf * npebf * npebf * npebf * npebf;
+  RC(need(ng3prm == p6 * npbf * npbf, "ng3prm"));
+  RC(need(GM3ICR != nullptr, "output pointer"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan,
+                  bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX,
+                  NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC));
+  DBuf d;
+  RC(dalloc(d, sizeof(double) * ng3, s));
+  CU(launch_gam3_raw(u.d, d.as<double>(), s));
+  CU(launch_gam3_symmetrize((int)nebf, (int)npbf, d.as<double>(), s));
+  CU(cudaMemcpyAsync(GM3ICR, d.p, sizeof(double) * ng3, cudaMemcpyDeviceToHost,
+                     s));
+  return finish(s);
+}
+
+int neoxc_gam4_icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ngee,
+                   int64_t ng2, int64_t ng4, const double* GAM_2s,
+                   const double* GAM_ee, double* GAM_4) {
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ngee == ne * ne * ne * ne, "ngee == ne**4"));
+  RC(need(ng2 == ngee * np * np, "ng2 == ne**4 np**2"));
+  RC(need(ng4 == ngee * ngee * np * np, "ng4 == ne**8 np**2"));
+  RC(need(GAM_2s && GAM_ee && GAM_4, "pointers"));
+  if (ne > kGam4MaxNE)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "gam_4 element kernels: ne <= %d",
+                   kGam4MaxNE);
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dg2, dee, d4;
+  RC(upload(dg2, GAM_2s, sizeof(double) * ng2, s));
+  RC(upload(dee, GAM_ee, sizeof(double) * ngee, s));
+  RC(dalloc(d4, sizeof(double) * ng4, s));
+  CU(launch_gam4_icr((int)ne, (int)np, dee.as<double>(), dg2.as<double>(),
+                     d4.as<double>(), s));
+  CU(cudaMemcpyAsync(GAM_4, d4.p, sizeof(double) * ng4, cudaMemcpyDeviceToHost,
+                     s));
+  return finish(s);
+}
+
+// ---- contractions -------------------------------------------------------------
+int neoxc_dev_gam4_dscf(void* stream, int64_t ne, int64_t np,
+                        const double* d_gee, const double* d_g2s,
+                        const double* d_DE, const double* d_DP,
+                        double* d_focke, double* d_fockp, double* d_E) {
+  RC(need(ne >= 1 && np >= 1, "sizes"));
+  if (ne > kGam4MaxNE)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "gam_4 element kernels: ne <= %d",
+                   kGam4MaxNE);
+  cudaStream_t s = (cudaStream_t)stream;
+  DBuf scr;
+  RC(dalloc(scr, sizeof(double) * gam4_partial_doubles((int)ne, (int)np), s));
+  CU(launch_gam4_dscf((int)ne, (int)np, d_gee, d_g2s, d_DE, d_DP,
+                      scr.as<double>(), d_focke, d_fockp, d_E, s));
+  return NEOXC_OK;
+}
+
+int neoxc_gam4_dscf(int64_t NG4CHK, int64_t ne, int64_t np, int64_t ngee,
+                    int64_t ng2, int64_t ng4, const double* GAM_ee,
+                    const double* GAM_2s, const double* DE, const double* DP,
+                    double* focke, double* fockp, double* E_gam4) {
+  RC(need(NG4CHK >= 1, "NG4CHK >= 1"));
+  RC(need(ngee == ne * ne * ne * ne, "ngee == ne**4"));
+  RC(need(ng2 == ngee * np * np, "ng2 == ne**4 np**2"));
+  RC(need(ng4 == ngee * ngee * np * np, "ng4 == ne**8 np**2"));
+  RC(need(GAM_ee && GAM_2s && DE && DP && focke && fockp && E_gam4, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dee, dg2, dde, ddp, dfe, dfp, dE;
+  RC(upload(dee, GAM_ee, sizeof(double) * ngee, s));
+  RC(upload(dg2, GAM_2s, sizeof(double) * ng2, s));
+  RC(upload(dde, DE, sizeof(double) * ne * ne, s));
+  RC(upload(ddp, DP, sizeof(double) * np * np, s));
+  RC(dalloc(dfe, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfp, sizeof(double) * np * np, s));
+  RC(dalloc(dE, sizeof(double), s));
+  CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * np * np, s));
+  RC(neoxc_dev_gam4_dscf(s, ne, np, dee.as<double>(), dg2.as<double>(),
+                         dde.as<double>(), ddp.as<double>(), dfe.as<double>(),
+                         dfp.as<double>(), dE.as<double>()));
+  RC(accumulate_back(focke, dfe.as<double>(), ne * ne, s));
+  RC(accumulate_back(fockp, dfp.as<double>(), np * np, s));
+  CU(cudaMemcpyAsync(E_gam4, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+int neoxc_eg4icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ng4,
+                 const double* DE, const double* DP, const double* GM4ICR,
+                 double* focke, double* fockp, double* E_gam4) {
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ng4 == ne * ne * ne * ne * ne * ne * ne * ne * np * np,
+          "ng4 == ne**8 np**2"));
+  RC(need(DE && DP && GM4ICR && focke && fockp && E_gam4, "pointers"));
+  if (ne > kGam4MaxNE)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "EG4ICR: ne <= %d", kGam4MaxNE);
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dg, dde, ddp, dfe, dfp, dE, scr;
+  RC(upload(dg, GM4ICR, sizeof(double) * ng4, s));
+  RC(upload(dde, DE, sizeof(double) * ne * ne, s));
+  RC(upload(ddp, DP, sizeof(double) * np * np, s));
+  RC(dalloc(dfe, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfp, sizeof(double) * np * np, s));
+  RC(dalloc(dE, sizeof(double), s));
+  RC(dalloc(scr, sizeof(double) * eg4_partial_doubles((int)ne, (int)np), s));
+  CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * np * np, s));
+  CU(launch_eg4icr((int)ne, (int)np, dde.as<double>(), ddp.as<double>(),
+                   dg.as<double>(), scr.as<double>(), dfe.as<double>(),
+                   dfp.as<double>(), dE.as<double>(), s));
+  RC(accumulate_back(focke, dfe.as<double>(), ne * ne, s));
+  RC(accumulate_back(fockp, dfp.as<double>(), np * np, s));
+  CU(cudaMemcpyAsync(E_gam4, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+int neoxc_dev_eg3ic1(void* stream, int64_t ne, int64_t np, const double* d_DE,
+                     const double* d_DP, const double* d_g3, double* d_focke,
+                     double* d_fockp, double* d_E) {
+  RC(need(ne >= 1 && np >= 1, "sizes"));
+  if (ne > 20) return set_err(NEOXC_ERR_UNSUPPORTED, "EG3IC1: ne <= 20");
+  cudaStream_t s = (cudaStream_t)stream;
+  DBuf scr;
+  RC(dalloc(scr, sizeof(double) * eg3_partial_doubles((int)ne, (int)np), s));
+  CU(launch_eg3ic1((int)ne, (int)np, d_DE, d_DP, d_g3, scr.as<double>(),
+                   d_focke, d_fockp, d_E, s));
+  return NEOXC_OK;
+}
+
+int neoxc_eg3ic1(int64_t Nchunks, int64_t ne, int64_t np, int64_t ng3,
+                 const double* DE, const double* DP, const double* GM3ICR,
+                 double* focke, double* fockp, double* E_gam3) {
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ng3 == ne * ne * ne * ne * ne * ne * np * np, "ng3 == ne**6 np**2"));
+  RC(need(DE && DP && GM3ICR && focke && fockp && E_gam3, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dg, dde, ddp, dfe, dfp, dE;
+  RC(upload(dg, GM3ICR, sizeof(double) * ng3, s));
+  RC(upload(dde, DE, sizeof(double) * ne * ne, s));
+  RC(upload(ddp, DP, sizeof(double) * np * np, s));
+  RC(dalloc(dfe, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfp, sizeof(double) * np * np, s));
+  RC(dalloc(dE, sizeof(double), s));
+  CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * np * np, s));
+  RC(neoxc_dev_eg3ic1(s, ne, np, dde.as<double>(), ddp.as<double>(),
+                      dg.as<double>(), dfe.as<double>(), dfp.as<double>(),
+                      dE.as<double>()));
+  RC(accumulate_back(focke, dfe.as<double>(), ne * ne, s));
+  RC(accumulate_back(fockp, dfp.as<double>(), np * np, s));
+  CU(cudaMemcpyAsync(E_gam3, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+int neoxc_dev_eg2ic1(void* stream, int64_t ne, int64_t np, const double* d_DE,
+                     const double* d_DP, const double* d_g2,
+                     const double* d_g2s, double* d_FE, double* d_SE,
+                     double* d_FP, double* d_SP, double* d_E, double* d_S) {
+  RC(need(ne >= 1 && np >= 1, "sizes"));
+  cudaStream_t s = (cudaStream_t)stream;
+  DBuf scr;
+  RC(dalloc(scr, sizeof(double) * eg2_partial_doubles((int)ne, (int)np), s));
+  CU(launch_eg2ic1((int)ne, (int)np, d_DE, d_DP, d_g2, d_g2s, scr.as<double>(),
+                   d_FE, d_SE, d_FP, d_SP, d_E, d_S, s));
+  return NEOXC_OK;
+}
+
+int neoxc_eg2ic1(int64_t Nchunks, int64_t ne, int64_t np, int64_t ng2,
+                 const double* DE, const double* DP, const double* GM2ICR,
+                 const double* GM2SICR, double* FE, double* SE, double* FP,
+                 double* SP, double* E_gam2, double* S_gam2) {
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ng2 == ne * ne * ne * ne * np * np, "ng2 == ne**4 np**2"));
+  RC(need(DE && DP && GM2ICR && GM2SICR && FE && SE && FP && SP && E_gam2 &&
+              S_gam2, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dg, dgs, dde, ddp, dfe, dse, dfp, dsp, dE;
+  RC(upload(dg, GM2ICR, sizeof(double) * ng2, s));
+  RC(upload(dgs, GM2SICR, sizeof(double) * ng2, s));
+  RC(upload(dde, DE, sizeof(double) * ne * ne, s));
+  RC(upload(ddp, DP, sizeof(double) * np * np, s));
+  RC(dalloc(dfe, sizeof(double) * ne * ne, s));
+  RC(dalloc(dse, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfp, sizeof(double) * np * np, s));
+  RC(dalloc(dsp, sizeof(double) * np * np, s));
+  RC(dalloc(dE, 2 * sizeof(double), s));
+  CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * np * np, s));
+  RC(neoxc_dev_eg2ic1(s, ne, np, dde.as<double>(), ddp.as<double>(),
+                      dg.as<double>(), dgs.as<double>(), dfe.as<double>(),
+                      dse.as<double>(), dfp.as<double>(), dsp.as<double>(),
+                      dE.as<double>(), dE.as<double>() + 1));
+  RC(accumulate_back(FE, dfe.as<double>(), ne * ne, s));
+  RC(accumulate_back(FP, dfp.as<double>(), np * np, s));
+  CU(cudaMemcpyAsync(SE, dse.p, sizeof(double) * ne * ne, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(SP, dsp.p, sizeof(double) * np * np, cudaMemcpyDeviceToHost, s));
+  double e2[2];
+  CU(cudaMemcpyAsync(e2, dE.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RC(finish(s));
+  *E_gam2 = e2[0];
+  *S_gam2 = e2[1];
+  return NEOXC_OK;
+}
+
+int neoxc_dev_rxchfne_omg2(void* stream, int64_t ne, int64_t np,
+                           const double* d_DAE, const double* d_DBE,
+                           const double* d_DP, const double* d_g2,
+                           double* d_FAE, double* d_FP, double* d_FBE,
+                           double* d_E) {
+  RC(need(ne >= 1 && np >= 1 && ne * ne <= 16384, "sizes"));
+  cudaStream_t s = (cudaStream_t)stream;
+  DBuf scr;
+  RC(dalloc(scr, sizeof(double) * omg2_partial_doubles((int)ne, (int)np), s));
+  CU(launch_rxchfne_omg2((int)ne, (int)np, d_DAE, d_DBE, d_DP, d_g2,
+                         scr.as<double>(), d_FAE, d_FP, d_FBE, d_E, s));
+  return NEOXC_OK;
+}
+
+static int omg2_host(int64_t ne, int64_t np, const double* DAE,
+                     const double* DBE, const double* DP, const double* G,
+                     double* FAE, double* FP, double* FBE, double* E) {
+  RC(need(DAE && DBE && DP && G && E, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  const int64_t ng2 = ne * ne * ne * ne * np * np;
+  DBuf dg, da, db, dp, dfa, dfp, dfb, dE;
+  RC(upload(dg, G, sizeof(double) * ng2, s));
+  RC(upload(da, DAE, sizeof(double) * ne * ne, s));
+  RC(upload(db, DBE, sizeof(double) * ne * ne, s));
+  RC(upload(dp, DP, sizeof(double) * np * np, s));
+  RC(dalloc(dfa, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfb, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfp, sizeof(double) * np * np, s));
+  RC(dalloc(dE, sizeof(double), s));
+  CU(cudaMemsetAsync(dfa.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfb.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * np * np, s));
+  RC(neoxc_dev_rxchfne_omg2(s, ne, np, da.as<double>(), db.as<double>(),
+                            dp.as<double>(), dg.as<double>(),
+                            FAE ? dfa.as<double>() : nullptr,
+                            FP ? dfp.as<double>() : nullptr,
+                            FBE ? dfb.as<double>() : nullptr, dE.as<double>()));
+  if (FAE) RC(accumulate_back(FAE, dfa.as<double>(), ne * ne, s));
+  if (FBE) RC(accumulate_back(FBE, dfb.as<double>(), ne * ne, s));
+  if (FP) RC(accumulate_back(FP, dfp.as<double>(), np * np, s));
+  CU(cudaMemcpyAsync(E, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+int neoxc_rxchfne_fae_omg2(int64_t Nchunks, int64_t ne, int64_t np,
+                           int64_t ng2, const double* DAE, const double* DBE,
+                           const double* DP, const double* G, double* FAE,
+                           double* E) {
+  RC(need(Nchunks >= 1 && ng2 == ne * ne * ne * ne * np * np && FAE, "sizes"));
+  return omg2_host(ne, np, DAE, DBE, DP, G, FAE, nullptr, nullptr, E);
+}
+int neoxc_rxchfne_fp_omg2(int64_t Nchunks, int64_t ne, int64_t np,
+                          int64_t ng2, int64_t NAE, int64_t NBE,
+                          const double* DAE, const double* DBE,
+                          const double* DP, const double* G, double* FP,
+                          double* E) {
+  (void)NAE;
+  (void)NBE;
+  RC(need(Nchunks >= 1 && ng2 == ne * ne * ne * ne * np * np && FP, "sizes"));
+  return omg2_host(ne, np, DAE, DBE, DP, G, nullptr, FP, nullptr, E);
+}
+int neoxc_rxchfne_fbe_omg2(int64_t Nchunks, int64_t ne, int64_t np,
+                           int64_t ng2, int64_t NAE, int64_t NBE,
+                           const double* DAE, const double* DBE,
+                           const double* DP, const double* G, double* FBE,
+                           double* E) {
+  (void)NAE;
+  (void)NBE;
+  RC(need(Nchunks >= 1 && ng2 == ne * ne * ne * ne * np * np && FBE, "sizes"));
+  return omg2_host(ne, np, DAE, DBE, DP, G, nullptr, nullptr, FBE, E);
+}
+int neoxc_rxchfne_omg2_fused(int64_t ne, int64_t np, const double* DAE,
+                             const double* DBE, const double* DP,
+                             const double* G, double* FAE, double* FP,
+                             double* FBE, double* E) {
+  RC(need(ne >= 1 && np >= 1 && FAE && FP && FBE, "sizes"));
+  return omg2_host(ne, np, DAE, DBE, DP, G, FAE, FP, FBE, E);
+}
+
+int neoxc_xcfock_correction(int64_t ne, int64_t np, double E_total,
+                            double S_total, double H_expect,
+                            const double* se1, const double* sp1,
+                            const double* se2, const double* sp2,
+                            double* focke, double* fockp) {
+  (void)E_total;
+  RC(need(ne >= 1 && np >= 1 && se1 && sp1 && se2 && sp2 && focke && fockp,
+          "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf a, b, c, d, fe, fp;
+  RC(upload(a, se1, sizeof(double) * ne * ne, s));
+  RC(upload(b, sp1, sizeof(double) * np * np, s));
+  RC(upload(c, se2, sizeof(double) * ne * ne, s));
+  RC(upload(d, sp2, sizeof(double) * np * np, s));
+  RC(upload(fe, focke, sizeof(double) * ne * ne, s));
+  RC(upload(fp, fockp, sizeof(double) * np * np, s));
+  CU(launch_xcfock_correction((int)ne, (int)np, S_total, H_expect,
+                              a.as<double>(), b.as<double>(), c.as<double>(),
+                              d.as<double>(), fe.as<double>(), fp.as<double>(),
+                              s));
+  CU(cudaMemcpyAsync(focke, fe.p, sizeof(double) * ne * ne,
+                     cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(fockp, fp.p, sizeof(double) * np * np,
+                     cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+}  // extern "C"

@@ -1,0 +1,455 @@
+// k_md.cu -- contracted geminal-integral builders on sm_103a (FP64).
+//
+// Reference:
+//   gam_ee.f:2-169 (calc_GAM_ee)                 -> gam_ee_kernel
+//   gam_2_OMP.f:546-1077 (xcalc_GAM2_MD),
+//   gam2_CONV_OMP.f:388-579 (contract_omega2_conv),
+//   gam2_IC1_OMP.f:214-337 (thread_gam2_IC1)     -> gam2_raw_kernel
+//   rxchfne/rxchfne_gam_2_OMP.f:2-530,
+//   rxchfne/rxchfne_gam2_IC1_OMP.f:245-340       -> gam2_raw_kernel<RX>
+//   gam2_IC1_OMP.f:136-185, rxchfne_gam2_IC1_OMP.f:184-201
+//                                                -> gam2_sym_kernel
+//   gam_3_OMP.f:617-984 (xcalc_GAM3_MD),
+//   gam3_CONV_OMP.f:479-705, gam3_IC1_OMP.f:299-431 -> gam3_raw_kernel
+//   gam3_IC1_OMP.f:143-262                       -> gam3_sym_kernel
+//
+// Work decomposition: one warp per contracted tuple (its packed index is
+// the warp id, since the reference's loop order equals the packing order);
+// the lanes split the tuple's primitive combinations and the contraction
+// is a warp-shuffle reduction.  Each lane evaluates the reference's
+// per-primitive integrand with the factorised MD kernels of md_math.cuh,
+// re-using one Boys'-lemma/derivative setup for every integral that shares
+// a particle order and geminal assignment.
+#include "md_math.cuh"
+#include "neoxc_internal.h"
+
+namespace neoxc {
+namespace {
+
+using md::G3;
+using md::G4;
+using md::Prim;
+
+__device__ __forceinline__ Prim to_prim(const DevPrim& d) {
+  Prim p;
+  p.a = d.a;
+  for (int k = 0; k < 3; k++) {
+    p.c[k] = d.c[k];
+    p.l[k] = d.l[k];
+  }
+  return p;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void gam6(double* g, int slot_a, double va,
+                                     int slot_b, double vb) {
+  for (int k = 0; k < 6; k++) g[k] = 0.0;
+  if (slot_a >= 0) g[slot_a] = va;
+  if (slot_b >= 0) g[slot_b] = vb;
+}
+enum { A12 = 0, A13, A23, B12, B13, B23 };
+
+__device__ __forceinline__ void perm3(const Prim* X, int a, int b, int c,
+                                      Prim* Y) {
+  Y[0] = X[a];
+  Y[1] = X[b];
+  Y[2] = X[c];
+}
+
+// gam_2_OMP.f:546-1077 xcalc_GAM2_MD.  Particles (e1, e2, p).
+__device__ void xcalc_gam2(const Prim* A, const Prim* B, const DevSystem& S,
+                           G3& st, double& ansE, double& ansS) {
+  const int ng = S.ngtg, nat = S.nat;
+  const double* b = S.bgem;
+  const double* gm = S.ggem;
+  Prim A132[3], B132[3], A312[3], B312[3];
+  perm3(A, 0, 2, 1, A132);
+  perm3(B, 0, 2, 1, B132);
+  perm3(A, 2, 0, 1, A312);
+  perm3(B, 2, 0, 1, B312);
+  double g[6];
+  double gTE = 0, gVEC = 0, gVEE = 0, gVEP = 0;
+  for (int ik = 0; ik < ng; ik++) {
+    gam6(g, A23, gm[ik], -1, 0.0);
+    md::g3_setup(st, A, B, g, 2);
+    double xgTE = md::g3_ke(st, 0.0, 1.0);
+    double xgVEC = 0.0;
+    for (int ia = 0; ia < nat; ia++)
+      xgVEC = xgVEC - S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
+    double xgVEE = md::underflow(md::g3_vee(st));
+    md::g3_setup(st, A132, B132, g, 0);
+    double xgVEP = -md::underflow(md::g3_vee(st));
+    gTE = gTE + b[ik] * xgTE;
+    gVEC = gVEC + b[ik] * xgVEC;
+    gVEP = gVEP + b[ik] * xgVEP;
+    gVEE = gVEE + b[ik] * xgVEE;
+  }
+  double gTPg = 0, gTEg1 = 0, gTEg2 = 0, gTEg3 = 0, gVPCg = 0, gVECg1 = 0,
+         gVECg2 = 0, gVEPg1 = 0, gVEPg2 = 0, gVEEg1 = 0, gVEEg2 = 0, gsg = 0;
+  for (int ik = 0; ik < ng; ik++)
+    for (int il = 0; il < ng; il++) {
+      const double gk = gm[ik], gl = gm[il], bb = b[ik] * b[il];
+      // order (p, e1, e2): gA12 = g(p,e1), gB13 = g(p,e2)
+      gam6(g, A12, gk, B13, gl);
+      md::g3_setup(st, A312, B312, g, 2);
+      double xgTPg = md::g3_ke(st, gl, S.pmass);
+      double xgVPCg = 0.0;
+      for (int ia = 0; ia < nat; ia++)
+        xgVPCg = xgVPCg + S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
+      // order (e1, e2, p): A13, B23
+      gam6(g, A13, gk, B23, gl);
+      md::g3_setup(st, A, B, g, 2);
+      double xgTEg1 = md::g3_ke(st, 0.0, 1.0);
+      double xgVECg1 = 0.0;
+      for (int ia = 0; ia < nat; ia++)
+        xgVECg1 = xgVECg1 - S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
+      double xgVEEg2 = md::underflow(md::g3_vee(st));
+      double xgsg = md::g3_overlap(st);
+      // A23, B13
+      gam6(g, A23, gk, B13, gl);
+      md::g3_setup(st, A, B, g, 2);
+      double xgTEg2 = md::g3_ke(st, gl, 1.0);
+      // A23, B23
+      gam6(g, A23, gk, B23, gl);
+      md::g3_setup(st, A, B, g, 2);
+      double xgTEg3 = md::g3_ke(st, 0.0, 1.0);
+      double xgVECg2 = 0.0;
+      for (int ia = 0; ia < nat; ia++)
+        xgVECg2 = xgVECg2 - S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
+      // A13, B13
+      gam6(g, A13, gk, B13, gl);
+      md::g3_setup(st, A, B, g, 0);
+      double xgVEEg1 = md::underflow(md::g3_vee(st));
+      // order (e1, p, e2): A12 B23 and A23 B23
+      gam6(g, A12, gk, B23, gl);
+      md::g3_setup(st, A132, B132, g, 0);
+      double xgVEPg1 = -md::underflow(md::g3_vee(st));
+      gam6(g, A23, gk, B23, gl);
+      md::g3_setup(st, A132, B132, g, 0);
+      double xgVEPg2 = -md::underflow(md::g3_vee(st));
+      gTPg = gTPg + bb * xgTPg;
+      gTEg1 = gTEg1 + bb * xgTEg1;
+      gTEg2 = gTEg2 + bb * xgTEg2;
+      gTEg3 = gTEg3 + bb * xgTEg3;
+      gVPCg = gVPCg + bb * xgVPCg;
+      gVECg1 = gVECg1 + bb * xgVECg1;
+      gVECg2 = gVECg2 + bb * xgVECg2;
+      gVEPg1 = gVEPg1 + bb * xgVEPg1;
+      gVEPg2 = gVEPg2 + bb * xgVEPg2;
+      gVEEg1 = gVEEg1 + bb * xgVEEg1;
+      gVEEg2 = gVEEg2 + bb * xgVEEg2;
+      gsg = gsg + bb * xgsg;
+    }
+  ansE = 2.0 * (gTE + gVEC + gVEP) + 4.0 * gVEE * 0.5 + gTPg + gVPCg + gTEg1 +
+         gTEg3 + 2.0 * (gVEPg1 + gVECg1) + gTEg2 + gVEPg2 + gVECg2 +
+         2.0 * gVEEg1 * 0.5 + 2.0 * gVEEg2 * 0.5;
+  ansS = gsg;
+}
+
+// rxchfne/rxchfne_gam_2_OMP.f:2-530 (live terms :409-456)
+__device__ void xcalc_gam2_rx(const Prim* A, const Prim* B,
+                              const DevSystem& S, G3& st, double& ansE1,
+                              double& ansE2) {
+  const int ng = S.ngtg;
+  const double* b = S.bgem;
+  const double* gm = S.ggem;
+  Prim A321[3], B321[3];
+  perm3(A, 2, 1, 0, A321);
+  perm3(B, 2, 1, 0, B321);
+  double g[6], gVEPg2 = 0, gVEEg1 = 0, gVEEg2 = 0;
+  for (int ik = 0; ik < ng; ik++)
+    for (int il = 0; il < ng; il++) {
+      const double gk = gm[ik], gl = gm[il], bb = b[ik] * b[il];
+      gam6(g, A13, gk, B13, gl);
+      md::g3_setup(st, A321, B321, g, 0);
+      double xgVEPg2 = -md::underflow(md::g3_vee(st));
+      md::g3_setup(st, A, B, g, 0);
+      double xgVEEg1 = md::underflow(md::g3_vee(st));
+      gam6(g, A13, gk, B23, gl);
+      md::g3_setup(st, A, B, g, 0);
+      double xgVEEg2 = md::underflow(md::g3_vee(st));
+      gVEPg2 = gVEPg2 + bb * xgVEPg2;
+      gVEEg1 = gVEEg1 + bb * xgVEEg1;
+      gVEEg2 = gVEEg2 + bb * xgVEEg2;
+    }
+  ansE1 = gVEPg2 + gVEEg1;
+  ansE2 = gVEEg2;
+}
+
+// gam_3_OMP.f:617-984 xcalc_GAM3_MD.  Particles (e1, e2, e3, p).
+__device__ double xcalc_gam3(const Prim* A, const Prim* B, const DevSystem& S,
+                             G3& st, G4& s4) {
+  const int ng = S.ngtg, nat = S.nat;
+  const double* b = S.bgem;
+  const double* gm = S.ggem;
+  // particle-2/3 factors that do not depend on the geminal indices
+  const double yee = md::underflow(md::gfvee(A[1], A[2], B[1], B[2]));
+  double gVEE = 0.0;
+  for (int ik = 0; ik < ng; ik++) {
+    double xx = md::underflow(md::g2_xggs(A[0], A[3], B[0], B[3], gm[ik], 0.0));
+    gVEE = gVEE + (b[ik] * (xx * yee));
+  }
+  double xke = md::gfke(A[2], B[2], 1.0);
+  double Vc = 0.0;
+  for (int ia = 0; ia < nat; ia++)
+    Vc = Vc + (S.zan[ia] * md::gfvec(A[2], B[2], S.cat + 3 * ia));
+  const double xh = md::underflow(xke + (Vc * -1.0));
+  Prim A124[3] = {A[0], A[1], A[3]}, B124[3] = {B[0], B[1], B[3]};
+  md::g4_pairs(s4, A, B);
+  double gHEg = 0, gVEEg1 = 0, gVEEg2 = 0, g[6];
+  for (int ik = 0; ik < ng; ik++)
+    for (int il = 0; il < ng; il++) {
+      const double gk = gm[ik], gl = gm[il];
+      gam6(g, A13, gk, B23, gl);
+      md::g3_setup(st, A124, B124, g, 0);
+      double yy = md::underflow(md::g3_overlap(st));
+      double zz = md::underflow(md::g4_vep(s4, gk, gl));
+      double xgHEg = ((xh * yy) + (zz * -1.0));
+      double x2 = md::underflow(md::g2_xggs(A[0], A[3], B[0], B[3], gk, gl));
+      double xgVEEg1 = x2 * yee;
+      double xgVEEg2 = md::g4_vee(s4, gk, gl);
+      gHEg = gHEg + (b[ik] * b[il] * xgHEg);
+      gVEEg1 = gVEEg1 + (b[ik] * b[il] * xgVEEg1);
+      gVEEg2 = gVEEg2 + (b[ik] * b[il] * xgVEEg2);
+    }
+  return 2.0 * gVEE * 0.5 + gHEg + gVEEg1 * 0.5 + 4.0 * gVEEg2 * 0.5;
+}
+
+// ---- GAM_ee: thread per contracted (iec1,jec1,iec2,jec2) ------------------
+__global__ void __launch_bounds__(128)
+gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
+  const int ne = S.nebf;
+  const long long n4 = (long long)ne * ne * ne * ne;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n4;
+       t += (long long)gridDim.x * blockDim.x) {
+    // pack_4D(jec2, iec2, jec1, iec1) - 1 == t
+    long long r = t;
+    const int jc2 = (int)(r % ne); r /= ne;
+    const int ic2 = (int)(r % ne); r /= ne;
+    const int jc1 = (int)(r % ne); r /= ne;
+    const int ic1 = (int)r;
+    double acc = 0.0;
+    for (int i1 = S.kpestr[ic1]; i1 <= S.kpeend[ic1]; i1++)
+      for (int j1 = S.kpestr[jc1]; j1 <= S.kpeend[jc1]; j1++)
+        for (int i2 = S.kpestr[ic2]; i2 <= S.kpeend[ic2]; i2++)
+          for (int j2 = S.kpestr[jc2]; j2 <= S.kpeend[jc2]; j2++) {
+            const DevPrim &a1 = S.eprim[i1], &a2 = S.eprim[i2];
+            const DevPrim &b1 = S.eprim[j1], &b2 = S.eprim[j2];
+            double v = md::gfvee(to_prim(a1), to_prim(a2), to_prim(b1), to_prim(b2));
+            acc = acc + v * a1.coef * b1.coef * a2.coef * b2.coef;
+          }
+    gee[t] = acc;
+  }
+}
+
+// ---- gam_2 raw tensors: warp per contracted tuple --------------------------
+template <int RX>
+__global__ void __launch_bounds__(64)
+gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
+                double* __restrict__ x2, long long ntup) {
+  const int ne = S.nebf, np = S.npbf;
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (w >= ntup) return;
+  long long r = w;
+  const int jc2 = (int)(r % ne); r /= ne;
+  const int ic2 = (int)(r % ne); r /= ne;
+  const int jc1 = (int)(r % ne); r /= ne;
+  const int ic1 = (int)(r % ne); r /= ne;
+  const int jp = (int)(r % np);
+  const int ip = (int)(r / np);
+  const int s_i1 = S.kpestr[ic1], n_i1 = S.kpeend[ic1] - s_i1 + 1;
+  const int s_j1 = S.kpestr[jc1], n_j1 = S.kpeend[jc1] - s_j1 + 1;
+  const int s_i2 = S.kpestr[ic2], n_i2 = S.kpeend[ic2] - s_i2 + 1;
+  const int s_j2 = S.kpestr[jc2], n_j2 = S.kpeend[jc2] - s_j2 + 1;
+  const int nq = n_i1 * n_j1 * n_i2 * n_j2;
+  const DevPrim& pa = S.pprim[ip];
+  const DevPrim& pb = S.pprim[jp];
+  const double cp = pa.coef * pb.coef;
+  G3 st;
+  double o1 = 0.0, o2 = 0.0;
+  for (int q = lane; q < nq; q += 32) {
+    int qq = q;
+    const int j2 = s_j2 + qq % n_j2; qq /= n_j2;
+    const int i2 = s_i2 + qq % n_i2; qq /= n_i2;
+    const int j1 = s_j1 + qq % n_j1; qq /= n_j1;
+    const int i1 = s_i1 + qq;
+    Prim A[3] = {to_prim(S.eprim[i1]), to_prim(S.eprim[i2]), to_prim(pa)};
+    Prim B[3] = {to_prim(S.eprim[j1]), to_prim(S.eprim[j2]), to_prim(pb)};
+    double a1, a2;
+    if (RX) xcalc_gam2_rx(A, B, S, st, a1, a2);
+    else xcalc_gam2(A, B, S, st, a1, a2);
+    const double c = cp * S.eprim[i1].coef * S.eprim[j1].coef *
+                     S.eprim[i2].coef * S.eprim[j2].coef;
+    o1 = o1 + a1 * c;
+    o2 = o2 + a2 * c;
+  }
+  o1 = warp_sum(o1);
+  o2 = warp_sum(o2);
+  if (lane == 0) {
+    x1[w] = o1;
+    x2[w] = o2;
+  }
+}
+
+// In-place pair symmetrisation; the thread of the smaller packed index of
+// each {12, 21} pair writes both elements.
+__global__ void gam2_sym_kernel(int ne, int np, int rx, double* __restrict__ x1,
+                                double* __restrict__ x2, long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long r = t;
+    const int j2 = (int)(r % ne); r /= ne;
+    const int i2 = (int)(r % ne); r /= ne;
+    const int j1 = (int)(r % ne); r /= ne;
+    const int i1 = (int)(r % ne); r /= ne;
+    const long long pp = r;  // jp + np*ip
+    const long long u = j1 + (long long)ne * (i1 + (long long)ne * (j2 + (long long)ne * (i2 + (long long)ne * pp)));
+    if (u < t) continue;
+    const double a2 = x2[t], b2 = x2[u];
+    x2[t] = (a2 + b2) / 2.0;
+    x2[u] = (b2 + a2) / 2.0;
+    if (!rx) {
+      const double a1 = x1[t], b1 = x1[u];
+      x1[t] = (a1 + b1) / 2.0;
+      x1[u] = (b1 + a1) / 2.0;
+    }
+  }
+}
+
+// ---- gam_3 raw tensor: warp per contracted tuple ----------------------------
+__global__ void __launch_bounds__(64)
+gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long ntup) {
+  const int ne = S.nebf, np = S.npbf;
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (w >= ntup) return;
+  long long r = w;
+  int c[6];
+  for (int k = 5; k >= 0; k--) {
+    c[k] = (int)(r % ne);
+    r /= ne;
+  }
+  const int jp = (int)(r % np);
+  const int ip = (int)(r / np);
+  // c = (ic1, jc1, ic2, jc2, ic3, jc3)
+  int st0[6], cnt[6], nq = 1;
+  for (int k = 0; k < 6; k++) {
+    st0[k] = S.kpestr[c[k]];
+    cnt[k] = S.kpeend[c[k]] - st0[k] + 1;
+    nq *= cnt[k];
+  }
+  const DevPrim& pa = S.pprim[ip];
+  const DevPrim& pb = S.pprim[jp];
+  const double cp = pa.coef * pb.coef;
+  G3 st;
+  G4 s4;
+  double o = 0.0;
+  for (int q = lane; q < nq; q += 32) {
+    int qq = q, idx[6];
+    for (int k = 5; k >= 0; k--) {
+      idx[k] = st0[k] + qq % cnt[k];
+      qq /= cnt[k];
+    }
+    Prim A[4] = {to_prim(S.eprim[idx[0]]), to_prim(S.eprim[idx[2]]),
+                 to_prim(S.eprim[idx[4]]), to_prim(pa)};
+    Prim B[4] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
+                 to_prim(S.eprim[idx[5]]), to_prim(pb)};
+    double ans = xcalc_gam3(A, B, S, st, s4);
+    double cc = cp;
+    for (int k = 0; k < 6; k++) cc = cc * S.eprim[idx[k]].coef;
+    o = o + ans * cc;
+  }
+  o = warp_sum(o);
+  if (lane == 0) x3[w] = o;
+}
+
+// Six-permutation symmetrisation in place: each orbit is handled by the
+// tuple with the largest packed index (the reference's last writer), which
+// averages in its own permutation order and writes the whole orbit.
+__global__ void gam3_sym_kernel(int ne, int np, double* __restrict__ g,
+                                long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long r = t;
+    const int j3 = (int)(r % ne); r /= ne;
+    const int i3 = (int)(r % ne); r /= ne;
+    const int j2 = (int)(r % ne); r /= ne;
+    const int i2 = (int)(r % ne); r /= ne;
+    const int j1 = (int)(r % ne); r /= ne;
+    const int i1 = (int)(r % ne); r /= ne;
+    const long long pp = r;
+    auto idx = [&](int a, int b, int c, int d, int e, int f) -> long long {
+      return f + (long long)ne * (e + (long long)ne * (d + (long long)ne * (c +
+             (long long)ne * (b + (long long)ne * (a + (long long)ne * pp)))));
+    };
+    const long long a132 = idx(i1, j1, i3, j3, i2, j2);
+    const long long a213 = idx(i2, j2, i1, j1, i3, j3);
+    const long long a231 = idx(i2, j2, i3, j3, i1, j1);
+    const long long a312 = idx(i3, j3, i1, j1, i2, j2);
+    const long long a321 = idx(i3, j3, i2, j2, i1, j1);
+    if (a132 > t || a213 > t || a231 > t || a312 > t || a321 > t) continue;
+    const double xx = (g[t] + g[a132] + g[a213] + g[a231] + g[a312] + g[a321]) / 6.0;
+    g[t] = xx;
+    g[a132] = xx;
+    g[a213] = xx;
+    g[a231] = xx;
+    g[a312] = xx;
+    g[a321] = xx;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s) {
+  const long long n4 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf;
+  long long blocks = (n4 + 127) / 128;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  gam_ee_kernel<<<(unsigned)blocks, 128, 0, s>>>(sys, gee);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam2_raw(const DevSystem& sys, int rx, double* x1,
+                            double* x2, cudaStream_t s) {
+  const long long ntup = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
+                         sys.npbf * sys.npbf;
+  const long long threads = ntup * 32;
+  const unsigned blocks = (unsigned)((threads + 63) / 64);
+  if (rx) gam2_raw_kernel<1><<<blocks, 64, 0, s>>>(sys, x1, x2, ntup);
+  else gam2_raw_kernel<0><<<blocks, 64, 0, s>>>(sys, x1, x2, ntup);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,
+                                   double* x2, cudaStream_t s) {
+  const long long n = (long long)ne * ne * ne * ne * np * np;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  gam2_sym_kernel<<<(unsigned)blocks, 256, 0, s>>>(ne, np, rx, x1, x2, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3, cudaStream_t s) {
+  const long long n6 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
+                       sys.nebf * sys.nebf;
+  const long long ntup = n6 * sys.npbf * sys.npbf;
+  const long long threads = ntup * 32;
+  const unsigned blocks = (unsigned)((threads + 63) / 64);
+  gam3_raw_kernel<<<blocks, 64, 0, s>>>(sys, x3, ntup);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,
+                                   cudaStream_t s) {
+  const long long n = (long long)ne * ne * ne * ne * ne * ne * np * np;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  gam3_sym_kernel<<<(unsigned)blocks, 256, 0, s>>>(ne, np, g3, n);
+  return cudaGetLastError();
+}
+
+}  // namespace neoxc

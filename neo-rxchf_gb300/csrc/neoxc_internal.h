@@ -1,0 +1,103 @@
+// neoxc_internal.h -- internal launch interface of the GB300 engine.
+//
+// Every launcher takes DEVICE pointers, enqueues on the given stream and
+// returns a cudaError_t from the launch; none of them synchronises.
+// Index conventions follow the reference's packed arrays (pack_GAM.f):
+// a 0-based offset equals the Fortran packed index minus one.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace neoxc {
+
+// ---- device copy of the basis (driver arrays of xcneo_HYBRID.f) --------
+struct DevPrim {      // one primitive Cartesian Gaussian
+  double a;           // exponent
+  double c[3];        // centre (bohr)
+  double coef;        // contraction coefficient (AGEBFCC / AGNBFCC)
+  int l[3];           // (l,m,n)
+  int pad;
+};
+
+struct DevSystem {
+  int nebf, npebf, npbf, nat, ngtg;
+  double pmass;
+  const DevPrim* eprim;     // [npebf]
+  const DevPrim* pprim;     // [npbf]
+  const int* kpestr;        // [nebf] 0-based first primitive
+  const int* kpeend;        // [nebf] 0-based last primitive (inclusive)
+  const double* zan;        // [nat]
+  const double* cat;        // [3*nat]
+  const double* bgem;       // [ngtg]
+  const double* ggem;       // [ngtg]
+};
+
+// Largest per-Cartesian angular momentum supported by the MD kernels.
+constexpr int kMaxL = 2;
+constexpr int kMaxNG = 8;     // geminal terms
+constexpr int kMaxNat = 64;   // classical nuclei
+
+// Deterministic reduction of per-CTA Fock partials
+//   part[((ipjp*ne + i1)*nsub + s)*ne + j1]:
+//   fe(i1,j1) (+)= fe_scale * sum_ipjp DP * sum_s part,
+//   fp(ipjp)  (+)= sum_{i1,j1} DE * sum_s part,  E = sum_ipjp DP * fp-part.
+cudaError_t launch_fock_reduce(int ne, int np, int nsub, const double* part,
+                               const double* DE, const double* DP,
+                               double fe_scale, int accumulate, double* fe,
+                               double* fp, double* fp_tmp, double* E,
+                               cudaStream_t s);
+
+// ---- gam_4 (gam_4_OMP.f, gam4_DSCF_OMP.f, gam4_ICR_OMP.f) --------------
+constexpr int kGam4MaxNE = 32;
+size_t gam4_partial_doubles(int ne, int np);   // scratch the DSCF path uses
+cudaError_t launch_gam4_dscf(int ne, int np, const double* gee,
+                             const double* g2s, const double* DE,
+                             const double* DP, double* scratch,
+                             double* focke, double* fockp, double* E,
+                             cudaStream_t s);
+cudaError_t launch_gam4_icr(int ne, int np, const double* gee,
+                            const double* g2s, double* g4, cudaStream_t s);
+size_t eg4_partial_doubles(int ne, int np);
+cudaError_t launch_eg4icr(int ne, int np, const double* DE, const double* DP,
+                          const double* g4, double* scratch, double* focke,
+                          double* fockp, double* E, cudaStream_t s);
+
+// ---- in-core contractions (gam2_IC1_OMP.f, gam3_IC1_OMP.f, rxchfne) ----
+size_t eg3_partial_doubles(int ne, int np);
+cudaError_t launch_eg3ic1(int ne, int np, const double* DE, const double* DP,
+                          const double* g3, double* scratch, double* focke,
+                          double* fockp, double* E, cudaStream_t s);
+size_t eg2_partial_doubles(int ne, int np);
+cudaError_t launch_eg2ic1(int ne, int np, const double* DE, const double* DP,
+                          const double* g2, const double* g2s,
+                          double* scratch, double* FE, double* SE, double* FP,
+                          double* SP, double* E, double* S, cudaStream_t s);
+size_t omg2_partial_doubles(int ne, int np);
+// FAE / FP / FBE may be null (that output is skipped); E always written
+cudaError_t launch_rxchfne_omg2(int ne, int np, const double* DAE,
+                                const double* DBE, const double* DP,
+                                const double* g2, double* scratch, double* FAE,
+                                double* FP, double* FBE, double* E,
+                                cudaStream_t s);
+cudaError_t launch_xcfock_correction(int ne, int np, double S_total,
+                                     double H_expect, const double* se1,
+                                     const double* sp1, const double* se2,
+                                     const double* sp2, double* focke,
+                                     double* fockp, cudaStream_t s);
+
+// ---- integral builders (MD kernels) ------------------------------------
+cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s);
+cudaError_t launch_gam2_raw(const DevSystem& sys, int rxchfne, double* x1,
+                            double* x2, cudaStream_t s);
+cudaError_t launch_gam2_symmetrize(int ne, int np, int rxchfne, double* x1,
+                                   double* x2, cudaStream_t s);
+cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3,
+                            cudaStream_t s);
+cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,
+                                   cudaStream_t s);
+
+// ---- index maps on the device (pack_GAM.f) -----------------------------
+cudaError_t launch_index_fill(int kind, int ne, int np, int64_t count,
+                              int64_t* out, cudaStream_t s);
+
+}  // namespace neoxc

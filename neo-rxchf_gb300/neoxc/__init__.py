@@ -1,0 +1,328 @@
+"""neoxc -- host-side mirror of the NEO-RXCHF geminal-integral routines on
+the GB300 engine (``libneoxc_gb300.so``).
+
+Every function here calls the C-ABI declared in ``include/neoxc.h``; the
+names, argument meanings and output semantics follow the reference Fortran
+routines they replace (builders return fresh arrays, Fock contractions
+accumulate into the caller's matrices, energies are returned).  There is no
+CPU implementation behind this module: if the library is missing or no
+GB300 is usable, calls raise :class:`NeoxcError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+from .basis import NeoSystem  # noqa: F401  (re-export)
+
+__all__ = [
+    "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
+    "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "eg4icr", "eg3ic1", "eg2ic1",
+    "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
+    "rxchfne_omg2_fused", "xcfock_correction", "index_map",
+    "index_gam_2pk", "index_gam_3pk", "index_gam_4pk2", "pack_4d",
+]
+
+LIB_PATH = _build.LIB
+_lock = threading.Lock()
+_lib = None
+
+
+class NeoxcError(RuntimeError):
+    """Error status returned by the GB300 library (message from
+    neoxc_last_error)."""
+
+
+def _declare(L):
+    i64, d, vp = C.c_int64, C.c_double, C.c_void_p
+    I = C.c_int
+    sig = {
+        "neoxc_last_error": (C.c_char_p, []),
+        "neoxc_version": (I, []),
+        "neoxc_device_ok": (I, []),
+        "neoxc_pack_4d": (i64, [i64] * 7),
+        "neoxc_index_gam_2pk": (i64, [i64] * 8),
+        "neoxc_index_gam_3pk": (i64, [i64] * 10),
+        "neoxc_index_gam_4pk2": (i64, [i64] * 12),
+        "neoxc_index_map": (I, [i64, i64, i64, i64, vp]),
+        "neoxc_make_kpe": (I, [i64, i64, vp, vp, vp]),
+        "neoxc_calc_gam_ee": (I, [i64, i64, i64, vp, vp, vp, vp, vp, vp]),
+        "neoxc_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
+        "neoxc_gam3_ic1": (I, [i64] * 8 + [d] + [vp] * 16),
+        "neoxc_rxchfne_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
+        "neoxc_gam4_icr": (I, [i64] * 6 + [vp] * 3),
+        "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
+        "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
+        "neoxc_eg3ic1": (I, [i64] * 4 + [vp] * 6),
+        "neoxc_eg2ic1": (I, [i64] * 4 + [vp] * 10),
+        "neoxc_rxchfne_fae_omg2": (I, [i64] * 4 + [vp] * 6),
+        "neoxc_rxchfne_fp_omg2": (I, [i64] * 6 + [vp] * 6),
+        "neoxc_rxchfne_fbe_omg2": (I, [i64] * 6 + [vp] * 6),
+        "neoxc_rxchfne_omg2_fused": (I, [i64] * 2 + [vp] * 8),
+        "neoxc_xcfock_correction": (I, [i64, i64, d, d, d] + [vp] * 6),
+        "neoxc_dev_gam4_dscf": (I, [vp, i64, i64] + [vp] * 7),
+        "neoxc_dev_eg3ic1": (I, [vp, i64, i64] + [vp] * 6),
+        "neoxc_dev_eg2ic1": (I, [vp, i64, i64] + [vp] * 10),
+        "neoxc_dev_rxchfne_omg2": (I, [vp, i64, i64] + [vp] * 8),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib(build_if_missing: bool = False):
+    """Load libneoxc_gb300.so.  Raises NeoxcError when it is absent."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                if build_if_missing:
+                    _build.build()
+                else:
+                    raise NeoxcError(
+                        "libneoxc_gb300.so is not built (run "
+                        "`python -c 'import __graft_entry__ as g; g.build()'`); "
+                        "there is no CPU fallback")
+            L = C.CDLL(LIB_PATH)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = lib().neoxc_last_error()
+        raise NeoxcError("neoxc error %d: %s" % (rc, msg.decode() if msg else ""))
+
+
+def device_ok() -> bool:
+    return bool(lib().neoxc_device_ok())
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _fmat(a) -> np.ndarray:
+    """Column-major flat copy of a matrix (Fortran DE(n,n) layout)."""
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel(order="F"))
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ---- index maps (pack_GAM.f) --------------------------------------------
+def pack_4d(n1, n2, n3, i1, i2, i3, i4) -> int:
+    return int(lib().neoxc_pack_4d(n1, n2, n3, i1, i2, i3, i4))
+
+
+def index_gam_2pk(nebf, npbf, ip, jp, ie1, je1, ie2, je2) -> int:
+    return int(lib().neoxc_index_gam_2pk(nebf, npbf, ip, jp, ie1, je1, ie2, je2))
+
+
+def index_gam_3pk(nebf, npbf, ip, jp, ie1, je1, ie2, je2, ie3, je3) -> int:
+    return int(lib().neoxc_index_gam_3pk(nebf, npbf, ip, jp, ie1, je1, ie2, je2, ie3, je3))
+
+
+def index_gam_4pk2(nebf, npbf, ip, jp, ie1, je1, ie2, je2, ie3, je3, ie4, je4) -> int:
+    return int(lib().neoxc_index_gam_4pk2(nebf, npbf, ip, jp, ie1, je1, ie2, je2,
+                                          ie3, je3, ie4, je4))
+
+
+def index_map(kind: int, nebf: int, npbf: int, count: int | None = None) -> np.ndarray:
+    """Whole packed-index map evaluated on the GPU, in the reference's loop
+    order (kind 0: GAM_ee, 2/3/4: index_GAM_2PK/3PK/4PK2)."""
+    total = {0: nebf ** 4, 2: nebf ** 4 * npbf ** 2, 3: nebf ** 6 * npbf ** 2,
+             4: nebf ** 8 * npbf ** 2}[kind]
+    n = total if count is None else count
+    out = np.empty(n, np.int64)
+    _check(lib().neoxc_index_map(kind, nebf, npbf, n, _p(out)))
+    return out
+
+
+# ---- builders ---------------------------------------------------------------
+def _sysargs(s: NeoSystem):
+    keep = [s.cat_f, s.zan_f, s.bgem_f, s.ggem_f, s.KPESTR_f, s.KPEEND_f,
+            s.AMPEB2C_f, s.AGEBFCC_f, s.AGNBFCC_f, s.ELCEX_f, s.NUCEX_f,
+            s.ELCAM_f, s.NUCAM_f, s.ELCBFC_f, s.NUCBFC_f]
+    return keep, [_p(a) for a in keep]
+
+
+def calc_gam_ee(s: NeoSystem) -> np.ndarray:
+    """gam_ee.f calc_GAM_ee: contracted ERIs, packed pack_4D(je2,ie2,je1,ie1)."""
+    out = np.empty(s.ngee)
+    keep = [s.AMPEB2C_f, s.AGEBFCC_f, s.ELCEX_f, s.ELCAM_f, s.ELCBFC_f]
+    _check(lib().neoxc_calc_gam_ee(s.nebf, s.npebf, s.ngee, *[_p(a) for a in keep], _p(out)))
+    return out
+
+
+def gam2_ic1(s: NeoSystem, nchunks: int = 1):
+    """gam2_IC1_OMP.f GAM2_IC1 -> (GM2ICR, GM2sICR)."""
+    g, gs = np.empty(s.ng2), np.empty(s.ng2)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_gam2_ic1(nchunks, s.nebf, s.npebf, s.npbf, s.ng2, s.ng2prm,
+                                s.nat, s.ngtg, s.pmass, *ptrs, _p(g), _p(gs)))
+    return g, gs
+
+
+def rxchfne_gam2_ic1(s: NeoSystem, nchunks: int = 1):
+    """rxchfne_gam2_IC1_OMP.f RXCHFne_GAM2_IC1 -> (GM2ICR, GM2exICR)."""
+    g, gx = np.empty(s.ng2), np.empty(s.ng2)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_rxchfne_gam2_ic1(nchunks, s.nebf, s.npebf, s.npbf, s.ng2,
+                                        s.ng2prm, s.nat, s.ngtg, s.pmass, *ptrs,
+                                        _p(g), _p(gx)))
+    return g, gx
+
+
+def gam3_ic1(s: NeoSystem, nchunks: int = 1) -> np.ndarray:
+    """gam3_IC1_OMP.f GAM3_IC1 -> GM3ICR."""
+    g = np.empty(s.ng3)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_gam3_ic1(nchunks, s.nebf, s.npebf, s.npbf, s.ng3, s.ng3prm,
+                                s.nat, s.ngtg, s.pmass, *ptrs, _p(g)))
+    return g
+
+
+def gam4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:
+    """gam4_ICR_OMP.f GAM4_ICR -> GAM_4 (gam_4/16, packed index_GAM_4PK2)."""
+    g2, ge = _f64(gam_2s), _f64(gam_ee)
+    ng4 = ne ** 8 * np_ ** 2
+    out = np.empty(ng4)
+    _check(lib().neoxc_gam4_icr(nchunks, ne, np_, ne ** 4, ne ** 4 * np_ ** 2, ng4,
+                                _p(g2), _p(ge), _p(out)))
+    return out
+
+
+# ---- contractions ---------------------------------------------------------------
+def _fock_io(ne, np_, focke, fockp):
+    fe = np.zeros(ne * ne) if focke is None else _fmat(focke)
+    fp = np.zeros(np_ * np_) if fockp is None else _fmat(fockp)
+    return fe, fp
+
+
+def _fock_out(fe, fp, ne, np_):
+    return fe.reshape(ne, ne, order="F"), fp.reshape(np_, np_, order="F")
+
+
+def gam4_dscf(ne, np_, gam_ee, gam_2s, DE, DP, focke=None, fockp=None, nchunks=1):
+    """gam4_DSCF_OMP.f GAM4_DSCF: returns (focke + dF_e, fockp + dF_p, E_gam4)."""
+    ge, g2, de, dp = _f64(gam_ee), _f64(gam_2s), _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(ne, np_, focke, fockp)
+    E = np.zeros(1)
+    _check(lib().neoxc_gam4_dscf(nchunks, ne, np_, ne ** 4, ne ** 4 * np_ ** 2,
+                                 ne ** 8 * np_ ** 2, _p(ge), _p(g2), _p(de), _p(dp),
+                                 _p(fe), _p(fp), _p(E)))
+    return (*_fock_out(fe, fp, ne, np_), float(E[0]))
+
+
+def eg4icr(ne, np_, DE, DP, gm4, focke=None, fockp=None, nchunks=1):
+    """gam4_ICR_OMP.f EG4ICR."""
+    g, de, dp = _f64(gm4), _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(ne, np_, focke, fockp)
+    E = np.zeros(1)
+    _check(lib().neoxc_eg4icr(nchunks, ne, np_, len(g), _p(de), _p(dp), _p(g),
+                              _p(fe), _p(fp), _p(E)))
+    return (*_fock_out(fe, fp, ne, np_), float(E[0]))
+
+
+def eg3ic1(ne, np_, DE, DP, gm3, focke=None, fockp=None, nchunks=1):
+    """gam3_IC1_OMP.f EG3IC1."""
+    g, de, dp = _f64(gm3), _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(ne, np_, focke, fockp)
+    E = np.zeros(1)
+    _check(lib().neoxc_eg3ic1(nchunks, ne, np_, len(g), _p(de), _p(dp), _p(g),
+                              _p(fe), _p(fp), _p(E)))
+    return (*_fock_out(fe, fp, ne, np_), float(E[0]))
+
+
+def eg2ic1(ne, np_, DE, DP, gm2, gm2s, FE=None, FP=None, nchunks=1):
+    """gam2_IC1_OMP.f EG2IC1 -> (FE, SE, FP, SP, E_gam2, S_gam2)."""
+    g, gs, de, dp = _f64(gm2), _f64(gm2s), _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(ne, np_, FE, FP)
+    se, sp = np.zeros(ne * ne), np.zeros(np_ * np_)
+    E, S = np.zeros(1), np.zeros(1)
+    _check(lib().neoxc_eg2ic1(nchunks, ne, np_, len(g), _p(de), _p(dp), _p(g), _p(gs),
+                              _p(fe), _p(se), _p(fp), _p(sp), _p(E), _p(S)))
+    return (fe.reshape(ne, ne, order="F"), se.reshape(ne, ne, order="F"),
+            fp.reshape(np_, np_, order="F"), sp.reshape(np_, np_, order="F"),
+            float(E[0]), float(S[0]))
+
+
+def _omg2(fn, extra, ne, np_, DAE, DBE, DP, gm2, F, n):
+    g, da, db, dp = _f64(gm2), _fmat(DAE), _fmat(DBE), _fmat(DP)
+    f = np.zeros(n * n) if F is None else _fmat(F)
+    E = np.zeros(1)
+    _check(fn(1, ne, np_, len(g), *extra, _p(da), _p(db), _p(dp), _p(g), _p(f), _p(E)))
+    return f.reshape(n, n, order="F"), float(E[0])
+
+
+def rxchfne_fae_omg2(ne, np_, DAE, DBE, DP, gm2, FAE=None):
+    """rxchfne_omg2.f RXCHFne_FAE_OMG2 -> (FAE, E_AE_OMG2)."""
+    return _omg2(lib().neoxc_rxchfne_fae_omg2, (), ne, np_, DAE, DBE, DP, gm2, FAE, ne)
+
+
+def rxchfne_fp_omg2(ne, np_, DAE, DBE, DP, gm2, FP=None, NAE=1, NBE=1):
+    """rxchfne_omg2.f RXCHFne_FP_OMG2 -> (FP, E_P_OMG2)."""
+    return _omg2(lib().neoxc_rxchfne_fp_omg2, (NAE, NBE), ne, np_, DAE, DBE, DP, gm2, FP, np_)
+
+
+def rxchfne_fbe_omg2(ne, np_, DAE, DBE, DP, gm2, FBE=None, NAE=1, NBE=1):
+    """rxchfne_omg2.f RXCHFne_FBE_OMG2 -> (FBE, E_BE_OMG2)."""
+    return _omg2(lib().neoxc_rxchfne_fbe_omg2, (NAE, NBE), ne, np_, DAE, DBE, DP, gm2, FBE, ne)
+
+
+def rxchfne_omg2_fused(ne, np_, DAE, DBE, DP, gm2):
+    """One pass producing (FAE, FP, FBE, E_OMG2)."""
+    g, da, db, dp = _f64(gm2), _fmat(DAE), _fmat(DBE), _fmat(DP)
+    fa, fb, fp, E = np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(1)
+    _check(lib().neoxc_rxchfne_omg2_fused(ne, np_, _p(da), _p(db), _p(dp), _p(g),
+                                          _p(fa), _p(fp), _p(fb), _p(E)))
+    return (fa.reshape(ne, ne, order="F"), fp.reshape(np_, np_, order="F"),
+            fb.reshape(ne, ne, order="F"), float(E[0]))
+
+
+def xcfock_correction(ne, np_, E_total, S_total, H_expect, se1, sp1, se2, sp2,
+                      focke, fockp):
+    """xchf1_fock.f XCfock_correction -> corrected (focke, fockp)."""
+    a, b, c, d = _fmat(se1), _fmat(sp1), _fmat(se2), _fmat(sp2)
+    fe, fp = _fmat(focke), _fmat(fockp)
+    _check(lib().neoxc_xcfock_correction(ne, np_, E_total, S_total, H_expect, _p(a),
+                                         _p(b), _p(c), _p(d), _p(fe), _p(fp)))
+    return fe.reshape(ne, ne, order="F"), fp.reshape(np_, np_, order="F")
+
+
+# ---- device-resident variants (torch CUDA tensors) --------------------------------
+def _tptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def dev_gam4_dscf(stream, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_focke, d_fockp, d_E):
+    """Enqueue the fused gam_4 direct-SCF contraction on ``stream`` (a raw
+    cudaStream_t value); all arrays are torch float64 CUDA tensors."""
+    _check(lib().neoxc_dev_gam4_dscf(C.c_void_p(stream), ne, np_, _tptr(d_gee),
+                                     _tptr(d_g2s), _tptr(d_DE), _tptr(d_DP),
+                                     _tptr(d_focke), _tptr(d_fockp), _tptr(d_E)))
+
+
+def dev_eg3ic1(stream, ne, np_, d_DE, d_DP, d_g3, d_focke, d_fockp, d_E):
+    _check(lib().neoxc_dev_eg3ic1(C.c_void_p(stream), ne, np_, _tptr(d_DE), _tptr(d_DP),
+                                  _tptr(d_g3), _tptr(d_focke), _tptr(d_fockp), _tptr(d_E)))
+
+
+def dev_eg2ic1(stream, ne, np_, d_DE, d_DP, d_g2, d_g2s, d_FE, d_SE, d_FP, d_SP, d_E, d_S):
+    _check(lib().neoxc_dev_eg2ic1(C.c_void_p(stream), ne, np_, _tptr(d_DE), _tptr(d_DP),
+                                  _tptr(d_g2), _tptr(d_g2s), _tptr(d_FE), _tptr(d_SE),
+                                  _tptr(d_FP), _tptr(d_SP), _tptr(d_E), _tptr(d_S)))
+
+
+def dev_rxchfne_omg2(stream, ne, np_, d_DAE, d_DBE, d_DP, d_g2, d_FAE, d_FP, d_FBE, d_E):
+    _check(lib().neoxc_dev_rxchfne_omg2(C.c_void_p(stream), ne, np_, _tptr(d_DAE),
+                                        _tptr(d_DBE), _tptr(d_DP), _tptr(d_g2), _tptr(d_FAE),
+                                        _tptr(d_FP), _tptr(d_FBE), _tptr(d_E)))

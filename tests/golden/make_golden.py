@@ -1,0 +1,96 @@
+"""Generate the golden fixtures of the parity tests from the reference tree.
+
+Run in a container where the reference is mounted (it reads files only):
+
+    python tests/golden/make_golden.py /root/reference
+
+Writes, next to this script:
+  xchf_example.json   examples/xchf: input deck, initial MO guess
+                      (guessCE.inp), converged MOs (answer/FinalC*.dat) and
+                      the energy components printed in answer/XCHF.log for
+                      the initial guess and at convergence;
+  spot_check.json     CS_Integrals/Spot_Check/TEST_G{2,3,4}: the single-
+                      primitive inputs (first record block, as SCI.f:114-152
+                      reads them) and the MD values printed in each ``out``.
+Nothing at test time reads the reference tree; the tests use these files.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _components(log: str, header: str) -> dict:
+    i = log.index(header)
+    block = log[i:i + 2500]
+    out = {}
+    for key in ("E_NUC", "E_ECORE", "E_PCORE", "E_EP", "E_EE", "E_GAM1", "E_GAM2",
+                "E_GAM3", "E_GAM4", "S_TOTAL", "E_TOTAL"):
+        m = re.search(r"\b" + key + r"=\s*(-?[0-9.]+)", block)
+        out[key] = float(m.group(1))
+    return out
+
+
+def xchf_example(ref: str) -> dict:
+    d = os.path.join(ref, "examples", "xchf")
+    log = open(os.path.join(d, "answer", "XCHF.log")).read()
+    return {
+        "source": "examples/xchf (exam_xchf.inp, guessCE.inp, answer/)",
+        "inp": open(os.path.join(d, "exam_xchf.inp")).read(),
+        "guessCE": open(os.path.join(d, "guessCE.inp")).read(),
+        "finalCE": open(os.path.join(d, "answer", "FinalCE.dat")).read(),
+        "finalCP": open(os.path.join(d, "answer", "FinalCP.dat")).read(),
+        "initial": _components(log, "INITIAL GUESS ENERGETICS"),
+        "final": _components(log, "FINAL NEOXCHF ENERGY"),
+        "log_lines": {"initial": "XCHF.log:306-321", "final": "XCHF.log:335-350"},
+    }
+
+
+def _first_block(path: str):
+    rows = [l.split() for l in open(path).read().splitlines()]
+    k = 0
+    g1 = float(rows[k][0]); k += 1
+    g2 = float(rows[k][0]); k += 1
+    nbra = int(rows[k][0]); k += 1
+    bra = [[float(x) for x in rows[k + i][:7]] for i in range(nbra)]; k += nbra
+    nket = int(rows[k][0]); k += 1
+    ket = [[float(x) for x in rows[k + i][:7]] for i in range(nket)]; k += nket
+    cmat = [float(x) for x in rows[k][:3]]; k += 1
+    znuc = float(rows[k][0])
+    return {"gamma1": g1, "gamma2": g2, "bra": bra, "ket": ket, "C": cmat, "Z": znuc}
+
+
+def _md_values(out: str) -> dict:
+    i = out.index("MD VALUES")
+    j = out.find("VALUES", i + 10)
+    block = out[i:j if j > 0 else len(out)]
+    vals = {}
+    for m in re.finditer(r"^\s*([A-Za-z0-9]+)\s*=\s*(-?[0-9.]+(?:E[-+][0-9]+)?)\s*$", block, re.M):
+        vals[m.group(1)] = float(m.group(2))
+    return vals
+
+
+def spot_check(ref: str) -> dict:
+    base = os.path.join(ref, "source", "CS_Integrals", "Spot_Check")
+    res = {}
+    for t in ("TEST_G2", "TEST_G3", "TEST_G4"):
+        d = os.path.join(base, t)
+        res[t] = {"input": _first_block(os.path.join(d, "basis_definition.inp")),
+                  "md": _md_values(open(os.path.join(d, "out")).read()),
+                  "source": "source/CS_Integrals/Spot_Check/%s/{basis_definition.inp,out}" % t}
+    return res
+
+
+def main(ref: str):
+    with open(os.path.join(HERE, "xchf_example.json"), "w") as f:
+        json.dump(xchf_example(ref), f, indent=1)
+    with open(os.path.join(HERE, "spot_check.json"), "w") as f:
+        json.dump(spot_check(ref), f, indent=1)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,52 @@
+// md_host_check.cpp -- test helper: compiles the device integral math
+// (neo-rxchf_gb300/csrc/md_math.cuh) as plain C++ so the factorised MD
+// algorithm the GPU kernels run can be compared with the CPU oracle on any
+// machine.  Only the tests load this library.
+#include "../../neo-rxchf_gb300/csrc/md_math.cuh"
+
+using namespace neoxc::md;
+
+extern "C" {
+// same layout as the oracle's orc_prim
+struct HP { int l[3]; double a; double c[3]; };
+
+static Prim cv(const HP& h) {
+  Prim p;
+  p.a = h.a;
+  for (int d = 0; d < 3; d++) { p.l[d] = h.l[d]; p.c[d] = h.c[d]; }
+  return p;
+}
+
+double hc_g3(int kind, const HP* A, const HP* B, const double* gam,
+             const double* C, double xmass) {
+  Prim a[3], b[3];
+  for (int i = 0; i < 3; i++) { a[i] = cv(A[i]); b[i] = cv(B[i]); }
+  static thread_local G3 s;
+  g3_setup(s, a, b, gam, kind == 1 ? 2 : 0);
+  switch (kind) {
+    case 0: return g3_overlap(s);
+    case 1: return g3_ke(s, gam[4], xmass);
+    case 2: return g3_vxc(s, C);
+    default: return g3_vee(s);
+  }
+}
+
+double hc_g4(int kind, const HP* A, const HP* B, double g1, double g2) {
+  G4 s;
+  Prim a[4], b[4];
+  for (int i = 0; i < 4; i++) { a[i] = cv(A[i]); b[i] = cv(B[i]); }
+  g4_pairs(s, a, b);
+  return kind == 0 ? g4_vee(s, g1, g2) : g4_vep(s, g1, g2);
+}
+
+double hc_g2_xggs(const HP* A1, const HP* A2, const HP* B1, const HP* B2,
+                  double g1, double g2) {
+  return g2_xggs(cv(*A1), cv(*A2), cv(*B1), cv(*B2), g1, g2);
+}
+double hc_gfvee(const HP* A1, const HP* A2, const HP* B1, const HP* B2) {
+  return gfvee(cv(*A1), cv(*A2), cv(*B1), cv(*B2));
+}
+double hc_gfke(const HP* A, const HP* B, double m) { return gfke(cv(*A), cv(*B), m); }
+double hc_gfvec(const HP* A, const HP* B, const double* C) { return gfvec(cv(*A), cv(*B), C); }
+double hc_boys(int m, double T) { double F[64]; boys(m, T, F); return F[m]; }
+}

@@ -1,0 +1,249 @@
+"""GPU parity: every C-ABI entry point against the CPU oracle.
+
+Tolerances: integer index maps bit-exact; FP64 integral tensors within
+1e-10 relative (element-wise on significant elements, scale-relative on
+cancellation-dominated tiny ones); energies within 1e-10 relative.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import OracleTensors, assert_close_scaled, fmat
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-10
+
+
+def _system(seed, **kw):
+    from neoxc import basis
+    return basis.synthetic(seed=seed, **kw)
+
+
+def _dens(n, nocc, seed, prefac=2.0):
+    from neoxc import basis
+    return basis.random_density(n, nocc, seed, prefac)
+
+
+# ---------------------------------------------------------------- index maps
+@pytest.mark.parametrize("kind,ne,np_", [(0, 5, 1), (2, 4, 3), (3, 3, 2), (4, 2, 3)])
+def test_index_map_bit_exact(nx, orc, kind, ne, np_):
+    dev = nx.index_map(kind, ne, np_)
+    L = orc.lib()
+    ref = []
+    if kind == 0:
+        for i1 in range(1, ne + 1):
+            for j1 in range(1, ne + 1):
+                for i2 in range(1, ne + 1):
+                    for j2 in range(1, ne + 1):
+                        ref.append(L.orc_pack_4d(ne, ne, ne, j2, i2, j1, i1))
+    else:
+        import itertools
+        nidx = 2 * kind
+        fn = {2: L.orc_index_gam_2pk, 3: L.orc_index_gam_3pk, 4: L.orc_index_gam_4pk2}[kind]
+        for ip, jp in itertools.product(range(1, np_ + 1), repeat=2):
+            for e in itertools.product(range(1, ne + 1), repeat=nidx):
+                ref.append(fn(ne, np_, ip, jp, *e))
+    assert np.array_equal(dev, np.array(ref, np.int64))
+
+
+def test_index_map_int64_range(nx, orc):
+    """index_GAM_4PK2 at nebf=12, npbf=8 exceeds 2**31 (integer*8 path)."""
+    n = 12 ** 8 * 8 ** 2
+    head = nx.index_map(4, 12, 8, count=1 << 20)
+    assert head[0] == 1 and np.all(np.diff(head) == 1)
+    L = orc.lib()
+    assert L.orc_index_gam_4pk2(12, 8, 8, 8, 12, 12, 12, 12, 12, 12, 12, 12) == n
+    assert nx.index_gam_4pk2(12, 8, 8, 8, 12, 12, 12, 12, 12, 12, 12, 12) == n > 2 ** 31
+
+
+# ----------------------------------------------------------- gam_4 element path
+@pytest.mark.parametrize("seed,ne,np_", [(11, 3, 2), (12, 4, 1), (13, 2, 3), (14, 5, 2)])
+def test_gam4_dscf_icr_eg4(nx, orc, seed, ne, np_):
+    rng = np.random.default_rng(seed)
+    gee = rng.standard_normal(ne ** 4)
+    g2s = rng.standard_normal(ne ** 4 * np_ ** 2)
+    DE = _dens(ne, max(1, ne // 2), seed)
+    DP = _dens(np_, 1, seed + 1, 1.0)
+    L, O = orc.lib(), orc
+    # element-wise tensor (GAM4_ICR)
+    g4 = nx.gam4_icr(ne, np_, g2s, gee)
+    r4 = np.zeros(ne ** 8 * np_ ** 2)
+    L.orc_gam4_icr(ne, np_, O.ptr(g2s), O.ptr(gee), O.ptr(r4))
+    assert_close_scaled(g4, r4, RTOL, "GAM_4")
+    # fused DSCF contraction, accumulating into pre-filled Fock matrices
+    fe0, fp0 = rng.standard_normal((ne, ne)), rng.standard_normal((np_, np_))
+    fe, fp, E = nx.gam4_dscf(ne, np_, gee, g2s, DE, DP, fe0, fp0)
+    rfe, rfp, rE = fmat(fe0), fmat(fp0), np.zeros(1)
+    L.orc_gam4_dscf_range(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(fmat(DE)), O.ptr(fmat(DP)),
+                          0, ne ** 8 * np_ ** 2, O.ptr(rfe), O.ptr(rfp), O.ptr(rE))
+    assert E == pytest.approx(rE[0], rel=RTOL, abs=1e-12)
+    assert_close_scaled(fmat(fe), rfe, RTOL, "focke")
+    assert_close_scaled(fmat(fp), rfp, RTOL, "fockp")
+    # in-core contraction of the stored tensor (EG4ICR)
+    fe2, fp2, E2 = nx.eg4icr(ne, np_, DE, DP, g4, fe0, fp0)
+    assert E2 == pytest.approx(rE[0], rel=RTOL, abs=1e-12)
+    assert_close_scaled(fmat(fe2), rfe, RTOL, "focke (EG4ICR)")
+
+
+def test_gam4_dscf_deterministic(nx):
+    rng = np.random.default_rng(5)
+    ne, np_ = 6, 2
+    gee, g2s = rng.standard_normal(ne ** 4), rng.standard_normal(ne ** 4 * np_ ** 2)
+    DE, DP = _dens(ne, 3, 1), _dens(np_, 1, 2, 1.0)
+    a = nx.gam4_dscf(ne, np_, gee, g2s, DE, DP)
+    b = nx.gam4_dscf(ne, np_, gee, g2s, DE, DP)
+    assert a[2] == b[2]
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+# ------------------------------------------------------------ in-core contractions
+@pytest.mark.parametrize("seed,ne,np_", [(21, 3, 2), (22, 5, 1), (23, 4, 3)])
+def test_eg3ic1(nx, orc, seed, ne, np_):
+    rng = np.random.default_rng(seed)
+    g3 = rng.standard_normal(ne ** 6 * np_ ** 2)
+    DE, DP = _dens(ne, 2, seed), _dens(np_, 1, seed + 1, 1.0)
+    fe0, fp0 = rng.standard_normal((ne, ne)), rng.standard_normal((np_, np_))
+    fe, fp, E = nx.eg3ic1(ne, np_, DE, DP, g3, fe0, fp0)
+    O, L = orc, orc.lib()
+    rfe, rfp, rE = fmat(fe0), fmat(fp0), np.zeros(1)
+    L.orc_eg3ic1(ne, np_, O.ptr(fmat(DE)), O.ptr(fmat(DP)), O.ptr(g3), O.ptr(rfe), O.ptr(rfp),
+                 O.ptr(rE))
+    assert E == pytest.approx(rE[0], rel=RTOL, abs=1e-12)
+    assert_close_scaled(fmat(fe), rfe, RTOL, "focke")
+    assert_close_scaled(fmat(fp), rfp, RTOL, "fockp")
+
+
+@pytest.mark.parametrize("seed,ne,np_", [(31, 3, 2), (32, 6, 1), (33, 4, 3)])
+def test_eg2ic1(nx, orc, seed, ne, np_):
+    rng = np.random.default_rng(seed)
+    g2, g2s = rng.standard_normal(ne ** 4 * np_ ** 2), rng.standard_normal(ne ** 4 * np_ ** 2)
+    DE, DP = _dens(ne, 2, seed), _dens(np_, 1, seed + 1, 1.0)
+    FE0, FP0 = rng.standard_normal((ne, ne)), rng.standard_normal((np_, np_))
+    FE, SE, FP, SP, E, S = nx.eg2ic1(ne, np_, DE, DP, g2, g2s, FE0, FP0)
+    O, L = orc, orc.lib()
+    rFE, rSE, rFP, rSP = fmat(FE0), np.full(ne * ne, 7.0), fmat(FP0), np.full(np_ * np_, 7.0)
+    rE, rS = np.zeros(1), np.zeros(1)
+    L.orc_eg2ic1(ne, np_, O.ptr(fmat(DE)), O.ptr(fmat(DP)), O.ptr(g2), O.ptr(g2s), O.ptr(rFE),
+                 O.ptr(rSE), O.ptr(rFP), O.ptr(rSP), O.ptr(rE), O.ptr(rS))
+    assert E == pytest.approx(rE[0], rel=RTOL, abs=1e-12)
+    assert S == pytest.approx(rS[0], rel=RTOL, abs=1e-12)
+    for a, b, w in ((FE, rFE, "FE"), (SE, rSE, "SE"), (FP, rFP, "FP"), (SP, rSP, "SP")):
+        assert_close_scaled(fmat(a), b, RTOL, w)
+
+
+@pytest.mark.parametrize("seed,ne,np_", [(41, 3, 2), (42, 7, 1), (43, 5, 3)])
+def test_rxchfne_omg2(nx, orc, seed, ne, np_):
+    rng = np.random.default_rng(seed)
+    g2 = rng.standard_normal(ne ** 4 * np_ ** 2)
+    DAE, DBE = _dens(ne, 2, seed), _dens(ne, 1, seed + 7, 1.0)
+    DP = _dens(np_, 1, seed + 1, 1.0)
+    O, L = orc, orc.lib()
+    F0 = rng.standard_normal((ne, ne))
+    P0 = rng.standard_normal((np_, np_))
+    fae, e1 = nx.rxchfne_fae_omg2(ne, np_, DAE, DBE, DP, g2, F0)
+    fp, e2 = nx.rxchfne_fp_omg2(ne, np_, DAE, DBE, DP, g2, P0)
+    fbe, e3 = nx.rxchfne_fbe_omg2(ne, np_, DAE, DBE, DP, g2, F0)
+    args = [O.ptr(fmat(DAE)), O.ptr(fmat(DBE)), O.ptr(fmat(DP)), O.ptr(g2)]
+    r1, r2, r3 = fmat(F0), fmat(P0), fmat(F0)
+    E1, E2, E3 = np.zeros(1), np.zeros(1), np.zeros(1)
+    L.orc_rxchfne_fae_omg2(ne, np_, *args, O.ptr(r1), O.ptr(E1))
+    L.orc_rxchfne_fp_omg2(ne, np_, *args, O.ptr(r2), O.ptr(E2))
+    L.orc_rxchfne_fbe_omg2(ne, np_, *args, O.ptr(r3), O.ptr(E3))
+    assert_close_scaled(fmat(fae), r1, RTOL, "FAE")
+    assert_close_scaled(fmat(fp), r2, RTOL, "FP")
+    assert_close_scaled(fmat(fbe), r3, RTOL, "FBE")
+    for e, r in ((e1, E1), (e2, E2), (e3, E3)):
+        assert e == pytest.approx(r[0], rel=RTOL, abs=1e-12)
+    fa2, fp2, fb2, ef = nx.rxchfne_omg2_fused(ne, np_, DAE, DBE, DP, g2)
+    assert ef == pytest.approx(E1[0], rel=RTOL, abs=1e-12)
+    assert_close_scaled(fmat(fa2) + fmat(F0), r1, RTOL, "FAE fused")
+
+
+def test_xcfock_correction(nx, orc):
+    rng = np.random.default_rng(3)
+    ne, np_ = 5, 3
+    m = [rng.standard_normal(n * n) for n in (ne, np_, ne, np_, ne, np_)]
+    fe, fp = nx.xcfock_correction(ne, np_, -5.7, 170.97, -0.03, *[x.copy() for x in m])
+    O, L = orc, orc.lib()
+    rfe, rfp = m[4].copy(), m[5].copy()
+    L.orc_xcfock_correction(ne, np_, 170.97, -0.03, *[O.ptr(x) for x in m[:4]], O.ptr(rfe),
+                            O.ptr(rfp))
+    assert_close_scaled(fmat(fe), rfe, 1e-14, "focke")
+    assert_close_scaled(fmat(fp), rfp, 1e-14, "fockp")
+
+
+# ---------------------------------------------------------------- builders (MD)
+SMALL = [
+    dict(seed=101, nat=2, nebf=2, nprim=2, npbf=2, ngtg=2, lmax_e=1, lmax_p=1),
+    dict(seed=102, nat=3, nebf=3, nprim=1, npbf=1, ngtg=3, lmax_e=1, lmax_p=0),
+    dict(seed=103, nat=2, nebf=2, nprim=(1, 2), npbf=2, ngtg=2, lmax_e=2, lmax_p=2),
+]
+
+
+@pytest.mark.parametrize("kw", SMALL)
+def test_gam_ee(nx, orc, kw):
+    s = _system(**kw)
+    T = OracleTensors(orc, s)
+    assert_close_scaled(nx.calc_gam_ee(s), T.get("gee"), RTOL, "GAM_ee")
+
+
+@pytest.mark.parametrize("kw", SMALL)
+def test_gam2_ic1(nx, orc, kw):
+    s = _system(**kw)
+    T = OracleTensors(orc, s)
+    g2, g2s = nx.gam2_ic1(s)
+    assert_close_scaled(g2, T.get("g2"), RTOL, "GM2ICR")
+    assert_close_scaled(g2s, T.get("g2s"), RTOL, "GM2sICR")
+
+
+@pytest.mark.parametrize("kw", SMALL)
+def test_rxchfne_gam2_ic1(nx, orc, kw):
+    s = _system(**kw)
+    T = OracleTensors(orc, s)
+    g, gx = nx.rxchfne_gam2_ic1(s)
+    assert_close_scaled(g, T.get("rx2"), RTOL, "GM2ICR (RXCHF-ne)")
+    assert_close_scaled(gx, T.get("rx2ex"), RTOL, "GM2exICR")
+
+
+@pytest.mark.parametrize("kw", SMALL[:2])
+def test_gam3_ic1(nx, orc, kw):
+    s = _system(**kw)
+    T = OracleTensors(orc, s)
+    assert_close_scaled(nx.gam3_ic1(s), T.get("g3"), RTOL, "GM3ICR")
+
+
+def test_xchf_example_full_pipeline(nx, xchf, golden_xchf):
+    """examples/xchf end to end on the GPU: GAM_ee, GAM2_IC1, GAM3_IC1 and
+    the EG2/EG3/GAM4_DSCF contractions at the guessCE density reproduce
+    XCHF.log:313-315."""
+    s, DE, DP = xchf["sys"], xchf["DE0"], xchf["DP0"]
+    gee = nx.calc_gam_ee(s)
+    g2, g2s = nx.gam2_ic1(s)
+    g3 = nx.gam3_ic1(s)
+    ne, np_ = s.nebf, s.npbf
+    E2 = nx.eg2ic1(ne, np_, DE, DP, g2, g2s)[4]
+    E3 = nx.eg3ic1(ne, np_, DE, DP, g3)[2]
+    E4 = nx.gam4_dscf(ne, np_, gee, g2s, DE, DP)[2]
+    ref = golden_xchf["initial"]
+    assert abs(E2 - ref["E_GAM2"]) <= 6e-11
+    assert abs(E3 - ref["E_GAM3"]) <= 6e-11
+    assert abs(E4 - ref["E_GAM4"]) <= 6e-11
+
+
+# ------------------------------------------------------------------ error paths
+def test_unsupported_shapes_are_errors(nx):
+    rng = np.random.default_rng(0)
+    with pytest.raises(nx.NeoxcError, match="ne <= 32"):
+        nx.gam4_dscf(33, 1, np.zeros(33 ** 4), np.zeros(33 ** 4), np.eye(33), np.eye(1))
+    s = _system(seed=1, nat=1, nebf=1, nprim=1, npbf=1, ngtg=1, lmax_e=0, lmax_p=0)
+    s.ELCAM[0] = (2, 1, 0)
+    with pytest.raises(nx.NeoxcError, match="total l > 2"):
+        nx.gam2_ic1(s)
+    with pytest.raises(nx.NeoxcError, match="ng4"):
+        nx.lib()  # noqa: B018
+        import ctypes as C
+        a = np.zeros(16)
+        rc = nx.lib().neoxc_gam4_dscf(1, 2, 1, 16, 16, 17, *([a.ctypes.data_as(C.c_void_p)] * 7))
+        assert rc == 1
+        raise nx.NeoxcError(nx.lib().neoxc_last_error().decode())

@@ -1,0 +1,122 @@
+"""Pin the CPU oracle to the reference's own known answers.
+
+* CS_Integrals/Spot_Check/TEST_G{2,3,4}/out: single-primitive MD values
+  (mapping of gamma1/gamma2 to each term: DRIVER_G3.f:12-445,
+  DRIVER_G4.f:13-60, DRIVER_G2.f:11-40; Coulomb terms carry coul_sign*Z).
+* examples/xchf/answer/XCHF.log: E_GAM2, E_GAM3, E_GAM4 of one Fock build
+  at the initial guess (XCHF.log:306-321) and at convergence (:335-350).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import fmat
+
+
+def _prims(O, rows):
+    return O.prims([(int(r[0]), int(r[1]), int(r[2]), r[3], r[4], r[5], r[6]) for r in rows])
+
+
+def _gam(**kw):
+    g = np.zeros(6)
+    names = ["A12", "A13", "A23", "B12", "B13", "B23"]
+    for k, v in kw.items():
+        g[names.index(k)] = v
+    return g
+
+
+def test_spot_check_g3(orc, golden_spot):
+    O, L = orc, orc.lib()
+    t = golden_spot["TEST_G3"]
+    inp, md = t["input"], t["md"]
+    A, B = _prims(O, inp["bra"]), _prims(O, inp["ket"])
+    g1, g2 = inp["gamma1"], inp["gamma2"]
+    Cm, Z = np.array(inp["C"]), inp["Z"]
+    A312, B312 = O.prims([A[2], A[0], A[1]]), O.prims([B[2], B[0], B[1]])
+    A132, B132 = O.prims([A[0], A[2], A[1]]), O.prims([B[0], B[2], B[1]])
+    p = O.ptr
+    got = {
+        "xgSg": L.orc_g3_xggs(A, B, p(_gam(A13=g1, B23=g2))),
+        "xgTE": L.orc_g3_ke(A, B, p(_gam(A23=g1)), 1.0),
+        "xgTEg1": L.orc_g3_ke(A, B, p(_gam(A13=g1, B23=g2)), 1.0),
+        "xgTEg3": L.orc_g3_ke(A, B, p(_gam(A23=g1, B23=g2)), 1.0),
+        "xgTEg2": L.orc_g3_ke(A, B, p(_gam(A23=g1, B13=g2)), 1.0),
+        "xgTPg": L.orc_g3_ke(A312, B312, p(_gam(A12=g1, B13=g2)), 1836.0),
+        "xgVEC": -Z * L.orc_g3_xgvxcg(A, B, p(_gam(A23=g1)), p(Cm)),
+        "xgVPCg": Z * L.orc_g3_xgvxcg(A312, B312, p(_gam(A12=g1, B13=g2)), p(Cm)),
+        "xgVECg1": -Z * L.orc_g3_xgvxcg(A, B, p(_gam(A13=g1, B23=g2)), p(Cm)),
+        "xgVECg2": -Z * L.orc_g3_xgvxcg(A, B, p(_gam(A23=g1, B23=g2)), p(Cm)),
+        "xgVEP": -L.orc_g3_xgveeg(A132, B132, p(_gam(A23=g1))),
+        "xgVEE": L.orc_g3_xgveeg(A, B, p(_gam(A23=g1))),
+        "xgVEEg2": L.orc_g3_xgveeg(A, B, p(_gam(A13=g1, B23=g2))),
+        "xgVEEg1": L.orc_g3_xgveeg(A, B, p(_gam(A13=g1, B13=g2))),
+        "xgVEPg1": -L.orc_g3_xgveeg(A132, B132, p(_gam(A12=g1, B23=g2))),
+        "xgVEPg2": -L.orc_g3_xgveeg(A132, B132, p(_gam(A23=g1, B23=g2))),
+    }
+    assert set(got) == set(md)
+    for k, v in md.items():
+        # `out` prints 15 significant digits
+        assert got[k] == pytest.approx(v, rel=1e-12), k
+
+
+def test_spot_check_g4(orc, golden_spot):
+    O, L = orc, orc.lib()
+    t = golden_spot["TEST_G4"]
+    inp, md = t["input"], t["md"]
+    A, B = _prims(O, inp["bra"]), _prims(O, inp["ket"])
+    g1, g2 = inp["gamma1"], inp["gamma2"]
+    assert L.orc_g4_xgveeg(A, B, g1, g2) == pytest.approx(md["xgVEEg2"], rel=1e-12)
+    assert -L.orc_g4_xgvepg(A, B, g1, g2) == pytest.approx(md["xgVEPg"], rel=1e-12)
+
+
+def test_spot_check_g2(orc, golden_spot):
+    O, L = orc, orc.lib()
+    t = golden_spot["TEST_G2"]
+    inp, md = t["input"], t["md"]
+    A, B = _prims(O, inp["bra"]), _prims(O, inp["ket"])
+    x = L.orc_g2_xggs(C.byref(A[0]), C.byref(A[1]), C.byref(B[0]), C.byref(B[1]),
+                      inp["gamma1"], inp["gamma2"])
+    assert x == pytest.approx(md["XGGS"], rel=1e-12)
+
+
+def _energies(O, xchf, T, DE, DP, with_gam3=True):
+    s = xchf["sys"]
+    L = O.lib()
+    ne, np_ = s.nebf, s.npbf
+    de, dp = fmat(DE), fmat(DP)
+    FE, SE, FP, SP = (np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(np_ * np_),
+                      np.zeros(np_ * np_))
+    E2, S2 = np.zeros(1), np.zeros(1)
+    L.orc_eg2ic1(ne, np_, O.ptr(de), O.ptr(dp), O.ptr(T.get("g2")), O.ptr(T.get("g2s")),
+                 O.ptr(FE), O.ptr(SE), O.ptr(FP), O.ptr(SP), O.ptr(E2), O.ptr(S2))
+    fe, fp, E4 = np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(1)
+    L.orc_gam4_dscf(ne, np_, O.ptr(T.get("gee")), O.ptr(T.get("g2s")), O.ptr(de),
+                    O.ptr(dp), O.ptr(fe), O.ptr(fp), O.ptr(E4))
+    out = {"E_GAM2": E2[0], "E_GAM4": E4[0]}
+    if with_gam3:
+        E3 = np.zeros(1)
+        L.orc_eg3ic1(ne, np_, O.ptr(de), O.ptr(dp), O.ptr(T.get("g3")), O.ptr(fe),
+                     O.ptr(fp), O.ptr(E3))
+        out["E_GAM3"] = E3[0]
+    return out
+
+
+def test_xchf_initial_guess_energetics(orc, xchf, xchf_tensors, golden_xchf):
+    """One Fock build at the guessCE density reproduces XCHF.log:313-315 to
+    the 10 printed decimals."""
+    e = _energies(orc, xchf, xchf_tensors, xchf["DE0"], xchf["DP0"])
+    ref = golden_xchf["initial"]
+    for k in ("E_GAM2", "E_GAM3", "E_GAM4"):
+        assert abs(e[k] - ref[k]) <= 6e-11, (k, e[k], ref[k])
+
+
+def test_xchf_converged_energetics(orc, xchf, xchf_tensors, golden_xchf):
+    """At the converged MOs (FinalCE.dat / FinalCP.dat, 8 printed digits) the
+    components match XCHF.log:345-347 to the precision of those MOs."""
+    e = _energies(orc, xchf, xchf_tensors, xchf["DEf"], xchf["DPf"])
+    ref = golden_xchf["final"]
+    for k in ("E_GAM2", "E_GAM3", "E_GAM4"):
+        assert e[k] == pytest.approx(ref[k], rel=2e-7), (k, e[k], ref[k])
