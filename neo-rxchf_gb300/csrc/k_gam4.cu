@@ -176,7 +176,8 @@ gam4_kernel(int ne, int np, const double* __restrict__ gee,
   const int i1 = cta % ne; cta /= ne;
   const int jp = cta % np;
   const int ip = cta / np;
-  for (int k = threadIdx.x; k < n2; k += blockDim.x) sDE[k] = DE[k];
+  if (MODE == 0)  // the store mode (GAM4_ICR) has no density
+    for (int k = threadIdx.x; k < n2; k += blockDim.x) sDE[k] = DE[k];
   const int lanes_per_j1 = blockDim.x / ne;       // blockDim = ne*lanes
   const int j1 = threadIdx.x % ne;
   const int q0 = threadIdx.x / ne;
