@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""bench.py -- gam_4 integrals/s of the fused direct-SCF gam_4 Fock build.
+
+One step = one GAM4_DSCF Fock build (gam4_DSCF_OMP.f:2-320): every one of
+the ng4 = nebf^8 npbf^2 gam_4 elements is assembled from GAM_ee and GAM_2s
+(24 ket permutations x 6 pair products, gam_4_OMP.f:712-1192) and contracted
+with the electronic and nuclear densities into focke, fockp and E_gam4,
+without storing gam_4.  FP64 throughout.
+
+  value    device-resident inputs, K timed steps (CUDA events, barrier and
+           synchronize on both sides, L2 flushed between steps).
+  e2e      the public C-ABI call with HOST arrays (neoxc_gam4_dscf): the
+           host->device copies of GAM_ee/GAM_2s/DE/DP and the device->host
+           read of the Fock matrices and energy are inside the timed region.
+  roofline the gam_4 kernel against the FP64 FMA rate measured on the same
+           GPU by neoxc_probe_fp64 (the kernel is FP64-pipe bound; its DRAM
+           traffic is the two input tables).
+  cpu_baseline  the oracle's restatement of the reference loop on all host
+           cores over a bounded contiguous sample of the same tuples.
+
+--impl reference times that CPU implementation alone (all host threads),
+with the same metric and config.  With --gpus N (torchrun), every rank runs
+one independent replica of the workload (weak scaling); value is the total
+over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "neo-rxchf_gb300"))
+
+NEBF, NPBF, NGTG, NPRIM = 12, 8, 3, 3
+# FP64 operations of one element as evaluated (24 x 6 products accumulated
+# by FMA, 24 coefficient FMAs, the density-weight FMA): 2 FLOP per FMA.
+FLOP_PER_ELEMENT = 2 * (24 * 6 + 24 + 1)
+METRIC = "gam_4 integrals/s"
+UNIT = "integrals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nebf", type=int, default=NEBF)
+    ap.add_argument("--npbf", type=int, default=NPBF)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(ne, np_):
+    return {
+        "workload": ("XCHF RHF fused direct-SCF gam_4 Fock build (GAM4_DSCF): "
+                     "nebf=%d contracted electronic functions (%d primitives each), "
+                     "npbf=%d nuclear functions, NG=%d geminal terms" % (ne, NPRIM, np_, NGTG)),
+        "nebf": ne, "npbf": np_, "ng4_per_step": ne ** 8 * np_ ** 2,
+        "inputs": "GAM_ee (nebf^4) and GAM_2s (nebf^4 npbf^2) FP64 tables, DE, DP",
+        "l2": "flushed between timed steps (256 MiB device write)",
+        "parallelism": "replicas (one independent system per GPU)",
+    }
+
+
+def synthetic_inputs(ne, np_, seed=2024):
+    """Seeded tables with the layouts of GAM_ee / GAM_2s and densities from
+    two doubly occupied orbitals (the kernel's work is data independent)."""
+    from neoxc import basis
+    rng = np.random.Generator(np.random.PCG64(seed))
+    gee = rng.uniform(0.0, 1.0, ne ** 4)
+    g2s = rng.uniform(0.0, 1.0, ne ** 4 * np_ ** 2)
+    DE = basis.random_density(ne, 2, seed + 1, 2.0)
+    DP = basis.random_density(np_, 1, seed + 2, 1.0)
+    return gee, g2s, DE, DP
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(backend):
+    import torch.distributed as dist
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group(backend)
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return dist, ws, rank, local
+
+
+def replica_time(dist, ws, seconds, device=None):
+    """Max over ranks of each rank's timed seconds (replica runs)."""
+    if ws == 1:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(ne, np_, gee, g2s, DE, DP, target_s=12.0):
+    """Oracle restatement of the reference loop on all host threads over a
+    contiguous sample of the tuple space sized to about ``target_s``."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    L = O.lib()
+    de = np.ascontiguousarray(DE.ravel(order="F"))
+    dp = np.ascontiguousarray(DP.ravel(order="F"))
+    fe, fp, E = np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(1)
+    ng4 = ne ** 8 * np_ ** 2
+    n = min(ng4, 4_000_000)
+    t0 = time.perf_counter()
+    L.orc_gam4_dscf_sample(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(de), O.ptr(dp), 0, n,
+                           O.ptr(fe), O.ptr(fp), O.ptr(E))
+    dt = time.perf_counter() - t0
+    n2 = int(min(ng4, max(n, n * target_s / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    L.orc_gam4_dscf_sample(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(de), O.ptr(dp), 0, n2,
+                           O.ptr(fe), O.ptr(fp), O.ptr(E))
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt, "unit": UNIT, "cores": int(L.orc_num_threads()),
+            "kind": "port", "seconds": round(dt, 3),
+            "sample": "first %d of %d gam_4 elements in loop_map order (%.2e %%), "
+                      "oracle restatement of thread_gam4_DSCF with OpenMP" % (n2, ng4, 100.0 * n2 / ng4)}
+
+
+def read_traffic(ne, np_):
+    """Per-launch DRAM bytes of the gam_4 kernel from the committed ncu
+    summary (profiles/gam4_dscf_traffic.txt), scaled to this workload by
+    the table bytes it reads; None when no capture is recorded."""
+    p = os.path.join(ROOT, "profiles", "gam4_dscf_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    kv = {}
+    for ln in open(p):
+        if "=" in ln and not ln.startswith("#"):
+            k, v = ln.split("=", 1)
+            kv[k.strip()] = v.strip()
+    try:
+        cap_ne, cap_np = int(kv["nebf"]), int(kv["npbf"])
+        cap_bytes = float(kv["dram_bytes_per_launch"])
+    except (KeyError, ValueError):
+        return None
+    scale = (ne ** 4 * np_ ** 2 + ne ** 4) / (cap_ne ** 4 * cap_np ** 2 + cap_ne ** 4)
+    return cap_bytes * scale
+
+
+def run_reference(args):
+    dist, ws, rank, _ = dist_init("gloo")
+    if rank != 0:
+        return
+    ne, np_ = args.nebf, args.npbf
+    gee, g2s, DE, DP = synthetic_inputs(ne, np_)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    L = O.lib()
+    de = np.ascontiguousarray(DE.ravel(order="F"))
+    dp = np.ascontiguousarray(DP.ravel(order="F"))
+    ng4 = ne ** 8 * np_ ** 2
+    # size each step so that warm-up + timed steps take about two minutes
+    fe, fp, E = np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(1)
+    n = min(ng4, 4_000_000)
+    t0 = time.perf_counter()
+    L.orc_gam4_dscf_sample(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(de), O.ptr(dp), 0, n,
+                           O.ptr(fe), O.ptr(fp), O.ptr(E))
+    rate = n / (time.perf_counter() - t0)
+    per_step = int(min(ng4, max(n, rate * 120.0 / (args.steps + args.warmup))))
+    for _ in range(args.warmup):
+        L.orc_gam4_dscf_sample(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(de), O.ptr(dp), 0,
+                               per_step, O.ptr(fe), O.ptr(fp), O.ptr(E))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.orc_gam4_dscf_sample(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(de), O.ptr(dp), 0,
+                               per_step, O.ptr(fe), O.ptr(fp), O.ptr(E))
+    dt = time.perf_counter() - t0
+    value = per_step * args.steps / dt
+    cores = int(L.orc_num_threads())
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": workload_config(ne, np_),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "first %d of %d gam_4 elements per step (the reference "
+                                   "is Fortran and cannot be compiled here; the oracle "
+                                   "restates its loop)" % (per_step, ng4)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import neoxc
+    dist, ws, rank, local = dist_init("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    neoxc.lib()
+    if not neoxc.device_ok():
+        raise SystemExit("no usable GB300: " + neoxc.lib().neoxc_last_error().decode())
+    ne, np_ = args.nebf, args.npbf
+    ng4 = ne ** 8 * np_ ** 2
+    gee, g2s, DE, DP = synthetic_inputs(ne, np_)
+    f64 = torch.float64
+    d_gee = torch.tensor(gee, dtype=f64, device=dev)
+    d_g2s = torch.tensor(g2s, dtype=f64, device=dev)
+    d_DE = torch.tensor(np.ascontiguousarray(DE.ravel(order="F")), dtype=f64, device=dev)
+    d_DP = torch.tensor(np.ascontiguousarray(DP.ravel(order="F")), dtype=f64, device=dev)
+    d_fe = torch.zeros(ne * ne, dtype=f64, device=dev)
+    d_fp = torch.zeros(np_ * np_, dtype=f64, device=dev)
+    d_E = torch.zeros(1, dtype=f64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        neoxc.dev_gam4_dscf(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
+
+    peak = neoxc.probe_fp64_tflops()
+    for _ in range(max(args.warmup, 0)):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    total_s = t_start.elapsed_time(t_end) / 1e3
+    kern_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = replica_time(dist, ws, total_s, dev)
+    value = ws * ng4 * args.steps / total_s
+    # ---- e2e through the host-array C-ABI call
+    e2e_steps = max(1, min(args.steps, 2))
+    neoxc.gam4_dscf(ne, np_, gee, g2s, DE, DP)       # warm the host path
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        fe, fp, E = neoxc.gam4_dscf(ne, np_, gee, g2s, DE, DP)
+    e2e_s = replica_time(dist, ws, time.perf_counter() - t0, dev)
+    e2e = {"value": ws * ng4 * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * (ne ** 4 + ne ** 4 * np_ ** 2 + ne * ne + np_ * np_),
+           "d2h_bytes_per_step": 8 * (ne * ne + np_ * np_ + 1),
+           "api": "neoxc_gam4_dscf (host arrays)"}
+    if rank != 0:
+        return
+    mean_ms = float(np.mean(kern_ms))
+    achieved = FLOP_PER_ELEMENT * ng4 / (mean_ms * 1e-3) / 1e12
+    traffic = read_traffic(ne, np_)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded tables with the GAM_ee / GAM_2s layouts)",
+        "config": workload_config(ne, np_),
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_source": "neoxc_probe_fp64 on this GPU (measured DFMA rate); "
+                                    "MEASURED_PEAKS.json has no FP64 figure",
+                     "flop_per_element": FLOP_PER_ELEMENT,
+                     "kernel_ms_mean": mean_ms},
+    }
+    if not args.no_cpu_baseline and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(ne, np_, gee, g2s, DE, DP)
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

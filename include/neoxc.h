@@ -199,6 +199,11 @@ int neoxc_dev_rxchfne_omg2(void* stream, int64_t ne, int64_t np,
                            double* d_FAE, double* d_FP, double* d_FBE,
                            double* d_E);
 
+/* ---- diagnostics (no reference counterpart) --------------------------- */
+/* Sustained FP64 FMA throughput of the current device in TFLOP/s (2 FLOP
+ * per FMA), the denominator of the FP64 rooflines. */
+int neoxc_probe_fp64(double* tflops);
+
 /* ---- Fortran external-subroutine shims (all arguments by reference) --- */
 /* Same argument lists as the reference subroutines; on error they print a
  * message to stderr and record it for neoxc_last_error().  gam4_icr_ and

@@ -64,6 +64,7 @@ def _declare(L):
         "neoxc_rxchfne_fbe_omg2": (I, [i64] * 6 + [vp] * 6),
         "neoxc_rxchfne_omg2_fused": (I, [i64] * 2 + [vp] * 8),
         "neoxc_xcfock_correction": (I, [i64, i64, d, d, d] + [vp] * 6),
+        "neoxc_probe_fp64": (I, [vp]),
         "neoxc_dev_gam4_dscf": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_dev_eg3ic1": (I, [vp, i64, i64] + [vp] * 6),
         "neoxc_dev_eg2ic1": (I, [vp, i64, i64] + [vp] * 10),
@@ -102,6 +103,13 @@ def _check(rc: int):
 
 def device_ok() -> bool:
     return bool(lib().neoxc_device_ok())
+
+
+def probe_fp64_tflops() -> float:
+    """Measured FP64 FMA throughput of the current GPU (TFLOP/s)."""
+    v = np.zeros(1)
+    _check(lib().neoxc_probe_fp64(_p(v)))
+    return float(v[0])
 
 
 def _f64(a) -> np.ndarray:

@@ -864,3 +864,30 @@ void orc_density(int64_t nbf, int64_t nocc, double prefac, const double *C,
       D[i + nbf * j] = d;
     }
 }
+
+/* Bounded sample of GAM4_DSCF work: tuples [t0,t1) split over the OpenMP
+ * threads (thread_gam4_DSCF's parallel loop, gam4_DSCF_OMP.f:230-309);
+ * partial Fock matrices and energy are summed into the outputs.  Used as the
+ * timed CPU baseline. */
+void orc_gam4_dscf_sample(int64_t ne, int64_t np, const double *Gee,
+                          const double *G2s, const double *DE,
+                          const double *DP, int64_t t0, int64_t t1,
+                          double *focke, double *fockp, double *E) {
+  int nt = orc_num_threads();
+  double *xfe = (double *)calloc((size_t)(ne * ne * nt), sizeof(double));
+  double *xfp = (double *)calloc((size_t)(np * np * nt), sizeof(double));
+  double *Ep = (double *)calloc((size_t)nt, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < nt; c++) {
+    int64_t a, b;
+    orc_loop_size(t0, t1 - 1, nt, c, &a, &b);
+    orc_gam4_dscf_range(ne, np, Gee, G2s, DE, DP, a, b + 1, xfe + ne * ne * c,
+                        xfp + np * np * c, Ep + c);
+  }
+  for (int c = 0; c < nt; c++) {
+    *E += Ep[c];
+    for (int64_t k = 0; k < ne * ne; k++) focke[k] += xfe[ne * ne * c + k];
+    for (int64_t k = 0; k < np * np; k++) fockp[k] += xfp[np * np * c + k];
+  }
+  free(xfe); free(xfp); free(Ep);
+}

@@ -154,6 +154,10 @@ void orc_gam4_dscf_range(int64_t ne, int64_t np, const double *GAM_ee,
                          const double *GAM_2s, const double *DE,
                          const double *DP, int64_t t0, int64_t t1,
                          double *xfocke, double *xfockp, double *E_gam4);
+void orc_gam4_dscf_sample(int64_t ne, int64_t np, const double *GAM_ee,
+                          const double *GAM_2s, const double *DE,
+                          const double *DP, int64_t t0, int64_t t1,
+                          double *focke, double *fockp, double *E);
 void orc_eg4icr(int64_t ne, int64_t np, const double *DE, const double *DP,
                 const double *GM4, double *focke, double *fockp,
                 double *E_gam4);

@@ -113,6 +113,7 @@ def lib():
                 "orc_gam4_icr": (None, [i64, i64, vp, vp, vp]),
                 "orc_gam4_dscf": (None, [i64, i64, vp, vp, vp, vp, vp, vp, vp]),
                 "orc_gam4_dscf_range": (None, [i64, i64, vp, vp, vp, vp, i64, i64, vp, vp, vp]),
+                "orc_gam4_dscf_sample": (None, [i64, i64, vp, vp, vp, vp, i64, i64, vp, vp, vp]),
                 "orc_eg4icr": (None, [i64, i64, vp, vp, vp, vp, vp, vp]),
                 "orc_eg3ic1": (None, [i64, i64, vp, vp, vp, vp, vp, vp]),
                 "orc_eg2ic1": (None, [i64, i64] + [vp] * 10),
