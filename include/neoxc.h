@@ -184,6 +184,23 @@ int neoxc_dev_gam4_dscf(void* stream, int64_t ne, int64_t np,
                         const double* d_GAM_ee, const double* d_GAM_2s,
                         const double* d_DE, const double* d_DP,
                         double* d_focke, double* d_fockp, double* d_E_gam4);
+/* No counterpart in the reference.  Same computation as
+ * neoxc_dev_gam4_dscf, for callers that cannot allocate device memory
+ * (memory handed to their own pool, an SCF loop recorded once and
+ * replayed, a fixed memory budget): the call allocates nothing and uses a
+ * scratch array built into the library (264,192 doubles per GPU, held until
+ * the process exits).  Limit: npbf^2*nebf^3 + npbf^2 <= 264,192 (e.g.
+ * nebf=12/npbf=8 or nebf=16/npbf=8); larger systems return
+ * NEOXC_ERR_UNSUPPORTED.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls whose work overlaps on the GPU (e.g. on two streams at once) race;
+ * serialise them on one stream. */
+int neoxc_dev_gam4_dscf_noalloc(void* stream, int64_t ne, int64_t np,
+                                const double* d_GAM_ee,
+                                const double* d_GAM_2s, const double* d_DE,
+                                const double* d_DP, double* d_focke,
+                                double* d_fockp, double* d_E_gam4);
 int neoxc_dev_eg3ic1(void* stream, int64_t ne, int64_t np,
                      const double* d_DE, const double* d_DP,
                      const double* d_GM3ICR, double* d_focke,

@@ -234,6 +234,17 @@ int accumulate_back(double* host, const double* dev, int64_t n,
 
 }  // namespace
 
+// Records an error for neoxc_last_error() from other translation units.
+int neoxc::set_last_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
 extern "C" {
 
 const char* neoxc_last_error(void) { return g_err.c_str(); }

@@ -37,6 +37,9 @@ constexpr int kMaxL = 2;
 constexpr int kMaxNG = 8;     // geminal terms
 constexpr int kMaxNat = 64;   // classical nuclei
 
+// Record an error message for neoxc_last_error(); returns `code`.
+int set_last_error(int code, const char* fmt, ...);
+
 // Deterministic reduction of per-CTA Fock partials
 //   part[((ipjp*ne + i1)*nsub + s)*ne + j1]:
 //   fe(i1,j1) (+)= fe_scale * sum_ipjp DP * sum_s part,

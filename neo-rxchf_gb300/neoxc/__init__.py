@@ -66,6 +66,7 @@ def _declare(L):
         "neoxc_xcfock_correction": (I, [i64, i64, d, d, d] + [vp] * 6),
         "neoxc_probe_fp64": (I, [vp]),
         "neoxc_dev_gam4_dscf": (I, [vp, i64, i64] + [vp] * 7),
+        "neoxc_dev_gam4_dscf_noalloc": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_dev_eg3ic1": (I, [vp, i64, i64] + [vp] * 6),
         "neoxc_dev_eg2ic1": (I, [vp, i64, i64] + [vp] * 10),
         "neoxc_dev_rxchfne_omg2": (I, [vp, i64, i64] + [vp] * 8),
