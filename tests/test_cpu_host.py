@@ -1,0 +1,210 @@
+"""CPU tests: index maps, host logic, the device integral math compiled as
+host C++ against the oracle, and the C-ABI library's exported symbols and
+argument checks (no compute call needs a GPU here)."""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+# ---------------------------------------------------------------- index maps
+def _py_index(ne, np_, ip, jp, *e):
+    acc = (ip - 1)
+    acc = (jp - 1) + np_ * acc
+    for x in e:
+        acc = (x - 1) + ne * acc
+    return 1 + acc
+
+
+@pytest.mark.parametrize("ne,np_", [(1, 1), (2, 3), (3, 2), (4, 1)])
+def test_index_maps_are_the_loop_order(orc, ne, np_):
+    """index_GAM_2PK/3PK/4PK2 (pack_GAM.f:72-239) enumerate 1..N in the
+    reference's loop order (ip, jp, ie1, je1, ... last ket fastest)."""
+    L = orc.lib()
+    for k, fn in ((2, L.orc_index_gam_2pk), (3, L.orc_index_gam_3pk), (4, L.orc_index_gam_4pk2)):
+        if ne ** (2 * k) * np_ ** 2 > 70000:
+            continue
+        t = 0
+        for ip, jp in itertools.product(range(1, np_ + 1), repeat=2):
+            for e in itertools.product(range(1, ne + 1), repeat=2 * k):
+                t += 1
+                v = fn(ne, np_, ip, jp, *e)
+                assert v == t == _py_index(ne, np_, ip, jp, *e)
+
+
+def test_index_4pk2_is_int64(orc):
+    L = orc.lib()
+    big = L.orc_index_gam_4pk2(40, 20, 20, 20, *([40] * 8))
+    assert big == 40 ** 8 * 20 ** 2 > 2 ** 62 // 2 ** 20
+
+
+def test_loop_size_partition(orc):
+    """gam_2_OMP.f:1080-1095 loop_size splits [L1,L2] into contiguous,
+    covering, near-equal chunks (the multi-GPU range split)."""
+    L = orc.lib()
+    for n, parts in ((10, 3), (7, 7), (5, 8), (1000003, 16)):
+        got = []
+        for r in range(parts):
+            a, b = np.zeros(1, np.int64), np.zeros(1, np.int64)
+            L.orc_loop_size(1, n, parts, r, orc.ptr(a), orc.ptr(b))
+            got.append((int(a[0]), int(b[0])))
+        flat = [x for a, b in got for x in range(a, b + 1)]
+        assert flat == list(range(1, n + 1))
+        sizes = [b - a + 1 for a, b in got]
+        assert max(sizes) - min(sizes) <= 1
+
+
+# ---------------------------------------------------------------- basis logic
+def test_make_kpe_and_normalisation(orc, golden_xchf):
+    from neoxc import basis
+    s = basis.parse_inp(golden_xchf["inp"])
+    assert list(s.KPESTR) == [1, 4, 5, 8, 9, 12] and list(s.KPEEND) == [3, 4, 7, 8, 11, 12]
+    # normalised coefficients printed by the reference (XCHF.log, 6 decimals)
+    np.testing.assert_allclose(s.AGEBFCC[:4], [0.441353, 0.693497, 0.664184, 0.287167], atol=5e-7)
+    np.testing.assert_allclose(s.AGNBFCC, [2.077622], atol=5e-7)
+    # Python restatement == oracle restatement of ELCNORM3 / NUCNORM
+    L = orc.lib()
+    raw = basis.parse_inp.__globals__["_card_lines"](golden_xchf["inp"], "EBASIS", s.npebf)
+    coef = np.array([float(r[6]) for r in raw])
+    L.orc_elcnorm3(s.npebf, s.nebf, orc.ptr(s.AMPEB2C_f), orc.ptr(coef), orc.ptr(s.ELCEX_f),
+                   orc.ptr(s.ELCAM_f), orc.ptr(s.ELCBFC_f))
+    np.testing.assert_allclose(coef, s.AGEBFCC, rtol=1e-13)
+    kps, kpe = np.zeros(s.nebf, np.int64), np.zeros(s.nebf, np.int64)
+    L.orc_make_kpe(s.nebf, s.npebf, orc.ptr(s.AMPEB2C_f), orc.ptr(kps), orc.ptr(kpe))
+    assert np.array_equal(kps, s.KPESTR) and np.array_equal(kpe, s.KPEEND)
+
+
+def test_mo_reader_and_density(golden_xchf):
+    from neoxc import basis
+    vec = basis.read_mo_file(golden_xchf["guessCE"], 6)
+    assert vec[0, 0] == pytest.approx(0.402716176) and vec[5, 0] == pytest.approx(-1.68233830e-3)
+    D = basis.density(vec, 2, 2.0)
+    assert np.allclose(D, D.T)
+    assert D[0, 0] == pytest.approx(2 * (vec[0, 0] ** 2 + vec[0, 1] ** 2))
+
+
+def test_synthetic_is_seeded():
+    from neoxc import basis
+    a = basis.synthetic(seed=3, nebf=5, npbf=3)
+    b = basis.synthetic(seed=3, nebf=5, npbf=3)
+    assert np.array_equal(a.ELCEX, b.ELCEX) and np.array_equal(a.cat, b.cat)
+    assert a.npebf == 15 and a.ng2 == 5 ** 4 * 9
+
+
+# ------------------------------------- device integral math, host-compiled
+@pytest.fixture(scope="module")
+def hostcheck():
+    src = os.path.join(ROOT, "tests", "hostcheck", "md_host_check.cpp")
+    out = os.path.join(tempfile.mkdtemp(prefix="neoxc_hc_"), "libhc.so")
+    subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", src, "-o", out], check=True)
+    L = C.CDLL(out)
+    return L
+
+
+def test_md_math_matches_oracle(orc, hostcheck):
+    """The factorised MD evaluation the kernels run (md_math.cuh) against the
+    oracle's restatement of the reference loops, random s/p/d primitives."""
+    O, L, H = orc, orc.lib(), hostcheck
+    P = C.POINTER(O.Prim)
+    d = C.c_double
+    H.hc_g3.restype = d
+    H.hc_g3.argtypes = [C.c_int, P, P, C.c_void_p, C.c_void_p, d]
+    H.hc_g4.restype = d
+    H.hc_g4.argtypes = [C.c_int, P, P, d, d]
+    for f in ("hc_g2_xggs",):
+        getattr(H, f).restype = d
+        getattr(H, f).argtypes = [P, P, P, P, d, d]
+    H.hc_gfvee.restype = d
+    H.hc_gfvee.argtypes = [P, P, P, P]
+    H.hc_gfke.restype = d
+    H.hc_gfke.argtypes = [P, P, d]
+    H.hc_gfvec.restype = d
+    H.hc_gfvec.argtypes = [P, P, C.c_void_p]
+    rng = np.random.default_rng(1)
+    AMS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (1, 1, 0), (0, 2, 0),
+           (1, 0, 1), (0, 1, 1), (0, 0, 2)]
+
+    def rp():
+        l = AMS[rng.integers(0, len(AMS))]
+        return O.prim(*l, float(np.exp(rng.uniform(np.log(0.1), np.log(20)))),
+                      *rng.uniform(-1.5, 1.5, 3))
+
+    def check(a, b, what):
+        # relative on significant values, absolute floor for cancelled ones
+        assert abs(a - b) <= 1e-10 * abs(b) + 1e-14, (what, a, b)
+
+    for trial in range(25):
+        A = O.prims([rp() for _ in range(4)])
+        B = O.prims([rp() for _ in range(4)])
+        g = np.zeros(6)
+        for k in rng.choice(6, size=2, replace=False):
+            g[k] = float(np.exp(rng.uniform(np.log(0.5), np.log(20))))
+        Cm = rng.uniform(-1.5, 1.5, 3)
+        A3, B3 = O.prims([A[0], A[1], A[2]]), O.prims([B[0], B[1], B[2]])
+        check(H.hc_g3(0, A3, B3, O.ptr(g), O.ptr(Cm), 1.0), L.orc_g3_xggs(A3, B3, O.ptr(g)), "xggs")
+        gk = g.copy()
+        gk[3] = 0.0
+        check(H.hc_g3(1, A3, B3, O.ptr(gk), O.ptr(Cm), 1.0), L.orc_g3_ke(A3, B3, O.ptr(gk), 1.0), "ke")
+        check(H.hc_g3(2, A3, B3, O.ptr(g), O.ptr(Cm), 1.0),
+              L.orc_g3_xgvxcg(A3, B3, O.ptr(g), O.ptr(Cm)), "vxc")
+        check(H.hc_g3(3, A3, B3, O.ptr(g), O.ptr(Cm), 1.0), L.orc_g3_xgveeg(A3, B3, O.ptr(g)), "vee")
+        g1, g2 = g[g > 0][0], g[g > 0][1]
+        if trial < 10:
+            check(H.hc_g4(0, A, B, g1, g2), L.orc_g4_xgveeg(A, B, g1, g2), "g4vee")
+            check(H.hc_g4(1, A, B, g1, g2), L.orc_g4_xgvepg(A, B, g1, g2), "g4vep")
+        r = [C.byref(A[0]), C.byref(A[1]), C.byref(B[0]), C.byref(B[1])]
+        check(H.hc_g2_xggs(*r, g1, g2), L.orc_g2_xggs(*r, g1, g2), "g2")
+        check(H.hc_gfvee(*r), L.orc_gfvee(*r), "gfvee")
+        check(H.hc_gfke(r[0], r[2], 1.0), L.orc_gfke(r[0], r[2], 1.0), "gfke")
+        check(H.hc_gfvec(r[0], r[2], O.ptr(Cm)), L.orc_gfvec(r[0], r[2], O.ptr(Cm)), "gfvec")
+
+
+# ------------------------------------------------------- C-ABI library (no GPU)
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "neoxc.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"\b(?:int|int64_t|void|const char\*)\s+([a-z0-9_]+)\s*\(", txt)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    import neoxc
+    L = neoxc.lib(build_if_missing=True)
+    names = _header_symbols()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", neoxc.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    exported = set(ln.split()[-1] for ln in out.splitlines() if ln.strip())
+    assert set(names) <= exported
+
+
+def test_argument_checks_need_no_gpu():
+    """Size validation happens on the host before any device work, and a
+    shape outside the supported range is an error, never a CPU fallback."""
+    import neoxc
+    L = neoxc.lib(build_if_missing=True)
+    a = np.zeros(64)
+    p = a.ctypes.data_as(C.c_void_p)
+    # ng4 inconsistent with ne**8 np**2
+    assert L.neoxc_gam4_dscf(1, 2, 1, 16, 16, 17, *([p] * 7)) == 1
+    assert b"ng4" in L.neoxc_last_error()
+    # Nchunks must be >= 1 (the reference's NG4CHK)
+    assert L.neoxc_eg3ic1(0, 2, 1, 64, *([p] * 6)) == 1
+    # map kind outside {0,2,3,4}
+    assert L.neoxc_index_map(7, 2, 2, 4, p) == 1
+    # host index maps are plain arithmetic
+    assert L.neoxc_index_gam_2pk(3, 2, 2, 2, 3, 3, 3, 3) == 3 ** 4 * 4
+    # no device here: compute calls report a CUDA error instead of running
+    if not L.neoxc_device_ok():
+        assert b"CUDA" in L.neoxc_last_error() or b"device" in L.neoxc_last_error()
