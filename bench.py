@@ -39,9 +39,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "neo-rxchf_gb300"))
 
 NEBF, NPBF, NGTG, NPRIM = 12, 8, 3, 3
-# FP64 operations of one element as evaluated (24 x 6 products accumulated
-# by FMA, 24 coefficient FMAs, the density-weight FMA): 2 FLOP per FMA.
-FLOP_PER_ELEMENT = 2 * (24 * 6 + 24 + 1)
+# FP64 operations of one element as the kernel evaluates it: 42 products
+# accumulated by FMA (the factored form of the 24 x 6 products of
+# symm_gam4), 4 operations combining the coefficient classes and 1 scaling,
+# the density weight (2 multiplies) and its FMA; 2 FLOP per FMA.
+FLOP_PER_ELEMENT = 2 * 42 + 7 + 1 + 2 + 2
 METRIC = "gam_4 integrals/s"
 UNIT = "integrals/s"
 

@@ -13,8 +13,9 @@
 //
 // Layout: one CTA per (ip,jp,ie1,ie2).  For each (ie3,ie4) the CTA stages
 // the twelve ne x ne slices of GAM_2s / GAM_ee that the 24 permutations of
-// that bra can touch in shared memory, then every thread evaluates ket
-// tuples (je1 fixed per thread, je2..je4 strided).  The Fock/energy
+// that bra can touch, plus their transformed copies (see gam4_elem_f), in
+// shared memory; every thread then evaluates ket tuples (je1 fixed per
+// thread, je2..je4 strided) with 42 FP64 products per element.  The Fock/energy
 // contraction is fused (the direct-SCF path never writes gam_4), and
 // per-CTA partial sums are reduced deterministically by a second kernel.
 #include "neoxc_internal.h"
@@ -22,71 +23,6 @@
 namespace neoxc {
 namespace {
 
-// Permutations of symm_gam4 (gam_4_OMP.f:756-803): ket slot feeding bra
-// position m (2 bits per position), and the coefficients of :833-856.
-// Written as switch functions so that, once the element loops are
-// unrolled, every lookup folds to an immediate.
-__device__ __forceinline__ int perm_code(int p) {
-  switch (p) {
-    case 0: return 228;
-    case 1: return 225;
-    case 2: return 210;
-    case 3: return 216;
-    case 4: return 201;
-    case 5: return 198;
-    case 6: return 135;
-    case 7: return 141;
-    case 8: return 156;
-    case 9: return 147;
-    case 10: return 177;
-    case 11: return 180;
-    case 12: return 120;
-    case 13: return 114;
-    case 14: return 99;
-    case 15: return 108;
-    case 16: return 78;
-    case 17: return 75;
-    case 18: return 27;
-    case 19: return 30;
-    case 20: return 45;
-    case 21: return 39;
-    case 22: return 54;
-    case 23: return 57;
-    default: return 0;
-  }
-}
-__device__ __forceinline__ int perm_of(int p, int m) {
-  return (perm_code(p) >> (2 * m)) & 3;
-}
-__device__ __forceinline__ double coef_of(int p) {
-  switch (p) {
-    case 0: return 16.0;
-    case 1: return -8.0;
-    case 2: return 4.0;
-    case 3: return -8.0;
-    case 4: return 4.0;
-    case 5: return -8.0;
-    case 6: return 4.0;
-    case 7: return -2.0;
-    case 8: return 4.0;
-    case 9: return -2.0;
-    case 10: return 4.0;
-    case 11: return -8.0;
-    case 12: return 4.0;
-    case 13: return -2.0;
-    case 14: return 4.0;
-    case 15: return -8.0;
-    case 16: return 4.0;
-    case 17: return -2.0;
-    case 18: return 4.0;
-    case 19: return -2.0;
-    case 20: return 4.0;
-    case 21: return -8.0;
-    case 22: return 4.0;
-    case 23: return -2.0;
-    default: return 0.0;
-  }
-}
 // pair splits: GS(a,b) * EE(c,d) (calc_GAM_4_integral x1..x6); split q
 // packs (a,b,c,d) in 2-bit fields.
 __device__ __forceinline__ int split_of(int q, int f) {
@@ -133,29 +69,107 @@ __device__ void stage_tables(int ne, int np, int ip, int jp, const int* i,
   }
 }
 
-// gam_4 element for ket offsets jn[m] = je_m*ne, jv[m] = je_m.
-__device__ __forceinline__ double gam4_elem(const double* __restrict__ sGS,
-                                            const double* __restrict__ sEE,
-                                            const int* jn, const int* jv,
-                                            int n2) {
-  double acc = 0.0;
-#pragma unroll
-  for (int p = 0; p < 24; p++) {
-    double x = 0.0;
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-      const int a = split_of(q, 0), b = split_of(q, 1);
-      const int c = split_of(q, 2), d = split_of(q, 3);
-      const int sg = pair_slot(a, b), se = pair_slot(c, d);
-      const int ka = perm_of(p, a), kb = perm_of(p, b);
-      const int kc = perm_of(p, c), kd = perm_of(p, d);
-      double gs = sGS[sg * n2 + jn[ka] + jv[kb]];
-      double ee = sEE[se * n2 + jn[kc] + jv[kd]];
-      x = fma(ee, gs, x);
-    }
-    acc = fma(coef_of(p), x, acc);
+// ---- factored element (42 products instead of 144) ------------------------
+// For each pair split q = (ab|cd) and each choice of the two kets that land
+// on the Coulomb pair (c,d), the four ket orderings of the two pairs carry
+// coefficients c_sigma that form a 2x2 block.  With T = X - X^T/2 applied to
+// the split's GAM_ee slice (X = EE_q) and GAM_2s slice (X = GS_q), 30 of
+// the 36 blocks are one product T_E * T_G times -8, 4 or 16, and the
+// remaining 6 (the kets of the pair (a,b) sent to (c,d) and vice versa)
+// need one extra raw product E * G times 3.  The element is then
+//   gam4 = (-8 A + 4 B + 16 C + 3 D) / 192,
+// the same value as the sum over the 24 permutations of symm_gam4 up to
+// rounding.  Term t packs (split q, raw flag, ket slots of the E factor,
+// ket slots of the G factor, coefficient class).
+__device__ __forceinline__ int fterm(int t) {
+  switch (t) {
+    case 0: return 7744;  // split 0 T E(J0,J1) G(J2,J3) class 1
+    case 1: return 15128;  // split 0 raw E(J1,J0) G(J3,J2) class 3
+    case 2: return 1824;  // split 0 T E(J2,J0) G(J3,J1) class 0
+    case 3: return 1728;  // split 0 T E(J0,J3) G(J2,J1) class 0
+    case 4: return 3168;  // split 0 T E(J2,J1) G(J0,J3) class 0
+    case 5: return 2256;  // split 0 T E(J1,J3) G(J0,J2) class 0
+    case 6: return 9440;  // split 0 T E(J2,J3) G(J0,J1) class 2
+    case 7: return 2833;  // split 1 T E(J1,J0) G(J3,J2) class 0
+    case 8: return 7553;  // split 1 T E(J0,J2) G(J1,J3) class 1
+    case 9: return 14121;  // split 1 raw E(J2,J0) G(J3,J1) class 3
+    case 10: return 2497;  // split 1 T E(J0,J3) G(J1,J2) class 0
+    case 11: return 3217;  // split 1 T E(J1,J2) G(J0,J3) class 0
+    case 12: return 10449;  // split 1 T E(J1,J3) G(J0,J2) class 2
+    case 13: return 1249;  // split 1 T E(J2,J3) G(J0,J1) class 0
+    case 14: return 3602;  // split 2 T E(J1,J0) G(J2,J3) class 0
+    case 15: return 3458;  // split 2 T E(J0,J2) G(J1,J3) class 0
+    case 16: return 6594;  // split 2 T E(J0,J3) G(J1,J2) class 1
+    case 17: return 13882;  // split 2 raw E(J3,J0) G(J2,J1) class 3
+    case 18: return 11410;  // split 2 T E(J1,J2) G(J0,J3) class 2
+    case 19: return 2258;  // split 2 T E(J1,J3) G(J0,J2) class 0
+    case 20: return 1202;  // split 2 T E(J3,J2) G(J0,J1) class 0
+    case 21: return 2883;  // split 3 T E(J0,J1) G(J3,J2) class 0
+    case 22: return 3459;  // split 3 T E(J0,J2) G(J1,J3) class 0
+    case 23: return 10691;  // split 3 T E(J0,J3) G(J1,J2) class 2
+    case 24: return 7315;  // split 3 T E(J1,J2) G(J0,J3) class 1
+    case 25: return 13163;  // split 3 raw E(J2,J1) G(J3,J0) class 3
+    case 26: return 2259;  // split 3 T E(J1,J3) G(J0,J2) class 0
+    case 27: return 483;  // split 3 T E(J2,J3) G(J1,J0) class 0
+    case 28: return 3652;  // split 4 T E(J0,J1) G(J2,J3) class 0
+    case 29: return 11652;  // split 4 T E(J0,J2) G(J1,J3) class 2
+    case 30: return 2500;  // split 4 T E(J0,J3) G(J1,J2) class 0
+    case 31: return 3220;  // split 4 T E(J1,J2) G(J0,J3) class 0
+    case 32: return 6356;  // split 4 T E(J1,J3) G(J0,J2) class 1
+    case 33: return 12924;  // split 4 raw E(J3,J1) G(J2,J0) class 3
+    case 34: return 436;  // split 4 T E(J3,J2) G(J1,J0) class 0
+    case 35: return 11845;  // split 5 T E(J0,J1) G(J2,J3) class 2
+    case 36: return 3461;  // split 5 T E(J0,J2) G(J1,J3) class 0
+    case 37: return 1733;  // split 5 T E(J0,J3) G(J2,J1) class 0
+    case 38: return 3173;  // split 5 T E(J2,J1) G(J0,J3) class 0
+    case 39: return 629;  // split 5 T E(J3,J1) G(J2,J0) class 0
+    case 40: return 5349;  // split 5 T E(J2,J3) G(J0,J1) class 1
+    case 41: return 12733;  // split 5 raw E(J3,J2) G(J1,J0) class 3
+    default: return 0;
   }
-  return acc * (1.0 / 192.0);   // 1/16 * 1/6 * 1/2
+}
+
+// Per-split tables from the staged slot tables: TE_q = E_q - E_q^T/2 and
+// TG_q = G_q - G_q^T/2 (E_q = EE slot (c,d), G_q = GS slot (a,b) of split q).
+__device__ void stage_transformed(int ne, const double* __restrict__ sGS,
+                                  const double* __restrict__ sEE, double* sTG,
+                                  double* sTE) {
+  const int n2 = ne * ne;
+  for (int k = threadIdx.x; k < 6 * n2; k += blockDim.x) {
+    const int q = k / n2, r = k - q * n2, x = r / ne, y = r - x * ne;
+    const int sg = pair_slot(split_of(q, 0), split_of(q, 1));
+    const int se = pair_slot(split_of(q, 2), split_of(q, 3));
+    sTG[k] = fma(-0.5, sGS[sg * n2 + y * ne + x], sGS[sg * n2 + r]);
+    sTE[k] = fma(-0.5, sEE[se * n2 + y * ne + x], sEE[se * n2 + r]);
+  }
+}
+
+__device__ __forceinline__ double gam4_elem_f(const double* __restrict__ sGS,
+                                              const double* __restrict__ sEE,
+                                              const double* __restrict__ sTG,
+                                              const double* __restrict__ sTE,
+                                              const int* jn, const int* jv,
+                                              int n2) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+  for (int t = 0; t < 42; t++) {
+    const int code = fterm(t);
+    const int q = code & 7, raw = (code >> 3) & 1;
+    const int e0 = (code >> 4) & 3, e1 = (code >> 6) & 3;
+    const int g0 = (code >> 8) & 3, g1 = (code >> 10) & 3;
+    const int cl = (code >> 12) & 3;
+    const double* Et = raw ? sEE + pair_slot(split_of(q, 2), split_of(q, 3)) * n2
+                           : sTE + q * n2;
+    const double* Gt = raw ? sGS + pair_slot(split_of(q, 0), split_of(q, 1)) * n2
+                           : sTG + q * n2;
+    const double x = Et[jn[e0] + jv[e1]];
+    const double y = Gt[jn[g0] + jv[g1]];
+    if (cl == 0) a0 = fma(x, y, a0);
+    else if (cl == 1) a1 = fma(x, y, a1);
+    else if (cl == 2) a2 = fma(x, y, a2);
+    else a3 = fma(x, y, a3);
+  }
+  return (-8.0 * a0 + 4.0 * a1 + 16.0 * a2 + 3.0 * a3) * (1.0 / 192.0);
 }
 
 // mode 0: fused DSCF contraction; mode 1: store gam4 (GAM4_ICR)
@@ -169,7 +183,9 @@ gam4_kernel(int ne, int np, const double* __restrict__ gee,
   const int n2 = ne * ne;
   double* sGS = smem;
   double* sEE = smem + 6 * n2;
-  double* sDE = smem + 12 * n2;
+  double* sTG = smem + 12 * n2;
+  double* sTE = smem + 18 * n2;
+  double* sDE = smem + 24 * n2;
   double* sred = sDE + n2;
   int cta = blockIdx.x;
   const int i2 = cta % ne; cta /= ne;
@@ -191,11 +207,13 @@ gam4_kernel(int ne, int np, const double* __restrict__ gee,
       __syncthreads();
       stage_tables(ne, np, ip, jp, ibra, gee, g2s, sGS, sEE);
       __syncthreads();
+      stage_transformed(ne, sGS, sEE, sTG, sTE);
+      __syncthreads();
       for (int q = q0; q < n3; q += lanes_per_j1) {
         const int j2 = q / n2, r = q - j2 * n2, j3 = r / ne, j4 = r - j3 * ne;
         int jv[4] = {j1, j2, j3, j4};
         int jn[4] = {j1 * ne, j2 * ne, j3 * ne, j4 * ne};
-        double g = gam4_elem(sGS, sEE, jn, jv, n2);
+        double g = gam4_elem_f(sGS, sEE, sTG, sTE, jn, jv, n2);
         if (MODE == 0) {
           // DE is column-major DE(i,j) = DE[i + ne*j]
           double w = sDE[i2 + ne * j2] * sDE[i3 + ne * j3] * sDE[i4 + ne * j4];
@@ -224,7 +242,22 @@ gam4_kernel(int ne, int np, const double* __restrict__ gee,
 
 int gam4_block(int ne) { return ne * (256 / ne); }
 size_t gam4_smem(int ne, int bs) {
-  return sizeof(double) * (size_t)(13 * ne * ne + bs);
+  return sizeof(double) * (size_t)(25 * ne * ne + bs);
+}
+
+template <int MODE>
+cudaError_t launch_gam4_kernel(int ne, int np, const double* gee,
+                               const double* g2s, const double* DE,
+                               const double* DP, double* part, double* g4,
+                               cudaStream_t s) {
+  const int bs = gam4_block(ne);
+  const size_t smem = gam4_smem(ne, bs);
+  cudaError_t e = cudaFuncSetAttribute(gam4_kernel<MODE>,
+      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  gam4_kernel<MODE><<<(unsigned)(np * np * ne * ne), bs, smem, s>>>(
+      ne, np, gee, g2s, DE, DP, part, g4);
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -238,15 +271,8 @@ cudaError_t launch_gam4_dscf(int ne, int np, const double* gee,
                              const double* DP, double* scratch, double* focke,
                              double* fockp, double* E, cudaStream_t s) {
   if (ne < 1 || ne > kGam4MaxNE || np < 1) return cudaErrorInvalidValue;
-  const int bs = gam4_block(ne);
-  const size_t smem = gam4_smem(ne, bs);
-  cudaError_t e = cudaFuncSetAttribute(gam4_kernel<0>,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const unsigned grid = (unsigned)(np * np * ne * ne);
-  gam4_kernel<0><<<grid, bs, smem, s>>>(ne, np, gee, g2s, DE, DP, scratch,
-                                        nullptr);
-  e = cudaGetLastError();
+  cudaError_t e = launch_gam4_kernel<0>(ne, np, gee, g2s, DE, DP, scratch,
+                                        nullptr, s);
   if (e != cudaSuccess) return e;
   double* fp_tmp = scratch + (size_t)np * np * ne * ne * ne;
   return launch_fock_reduce(ne, np, ne, scratch, DE, DP, 4.0, 1, focke, fockp,
@@ -256,14 +282,8 @@ cudaError_t launch_gam4_dscf(int ne, int np, const double* gee,
 cudaError_t launch_gam4_icr(int ne, int np, const double* gee,
                             const double* g2s, double* g4, cudaStream_t s) {
   if (ne < 1 || ne > kGam4MaxNE || np < 1) return cudaErrorInvalidValue;
-  const int bs = gam4_block(ne);
-  const size_t smem = gam4_smem(ne, bs);
-  cudaError_t e = cudaFuncSetAttribute(gam4_kernel<1>,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  gam4_kernel<1><<<(unsigned)(np * np * ne * ne), bs, smem, s>>>(
-      ne, np, gee, g2s, nullptr, nullptr, nullptr, g4);
-  return cudaGetLastError();
+  return launch_gam4_kernel<1>(ne, np, gee, g2s, nullptr, nullptr, nullptr,
+                               g4, s);
 }
 
 // ---- EG4ICR: stream GM4ICR once (HBM-bound) ----------------------------

@@ -51,7 +51,7 @@ cudaError_t launch_fock_reduce(int ne, int np, int nsub, const double* part,
                                cudaStream_t s);
 
 // ---- gam_4 (gam_4_OMP.f, gam4_DSCF_OMP.f, gam4_ICR_OMP.f) --------------
-constexpr int kGam4MaxNE = 32;
+constexpr int kGam4MaxNE = 24;   // shared-memory tables: 25*ne^2 doubles
 size_t gam4_partial_doubles(int ne, int np);   // scratch the DSCF path uses
 cudaError_t launch_gam4_dscf(int ne, int np, const double* gee,
                              const double* g2s, const double* DE,

@@ -234,8 +234,8 @@ def test_xchf_example_full_pipeline(nx, xchf, golden_xchf):
 # ------------------------------------------------------------------ error paths
 def test_unsupported_shapes_are_errors(nx):
     rng = np.random.default_rng(0)
-    with pytest.raises(nx.NeoxcError, match="ne <= 32"):
-        nx.gam4_dscf(33, 1, np.zeros(33 ** 4), np.zeros(33 ** 4), np.eye(33), np.eye(1))
+    with pytest.raises(nx.NeoxcError, match="ne <= 24"):
+        nx.gam4_dscf(25, 1, np.zeros(25 ** 4), np.zeros(25 ** 4), np.eye(25), np.eye(1))
     s = _system(seed=1, nat=1, nebf=1, nprim=1, npbf=1, ngtg=1, lmax_e=0, lmax_p=0)
     s.ELCAM[0] = (2, 1, 0)
     with pytest.raises(nx.NeoxcError, match="total l > 2"):
