@@ -101,6 +101,37 @@ int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
                    const int64_t* NUCAM, const double* ELCBFC,
                    const double* NUCBFC, double* GM3ICR);
 
+/* gam3_DSCF_OMP.f:2-137 GAM3_DSCF: builds gam_3 one proton pair at a time
+ * and contracts it on the fly; focke, fockp accumulate (add2fock), E_gam3
+ * overwritten.  Limit: nebf <= 20. */
+int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                    int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
+                    double pmass, const double* cat, const double* zan,
+                    const double* bcoef1, const double* gamma1,
+                    const int64_t* KPESTR, const int64_t* KPEEND,
+                    const int64_t* AMPEB2C, const double* AGEBFCC,
+                    const double* AGNBFCC, const double* ELCEX,
+                    const double* NUCEX, const int64_t* ELCAM,
+                    const int64_t* NUCAM, const double* ELCBFC,
+                    const double* NUCBFC, const double* DE, const double* DP,
+                    double* focke, double* fockp, double* E_gam3);
+
+/* gam2_DSCF_OMP.f:2-140 GAM2_DSCF: builds gam_2 / gam_2s one proton pair at
+ * a time; focke, fockp, se2, sp2 accumulate (add2fock), E_gam2 and S_gam2
+ * overwritten. */
+int neoxc_gam2_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                    int64_t ng2, int64_t ng2prm, int64_t nat, int64_t ngtg1,
+                    double pmass, const double* cat, const double* zan,
+                    const double* bcoef1, const double* gamma1,
+                    const int64_t* KPESTR, const int64_t* KPEEND,
+                    const int64_t* AMPEB2C, const double* AGEBFCC,
+                    const double* AGNBFCC, const double* ELCEX,
+                    const double* NUCEX, const int64_t* ELCAM,
+                    const int64_t* NUCAM, const double* ELCBFC,
+                    const double* NUCBFC, const double* DE, const double* DP,
+                    double* focke, double* fockp, double* se2, double* sp2,
+                    double* E_gam2, double* S_gam2);
+
 /* rxchfne/rxchfne_gam2_IC1_OMP.f:2-243 RXCHFne_GAM2_IC1 -> GM2ICR (raw),
  * GM2exICR (pair-averaged exchange term) */
 int neoxc_rxchfne_gam2_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf,
@@ -269,6 +300,31 @@ void gam3_ic1_(const int64_t* Nchunks, const int64_t* nebf,
                const double* NUCEX, const int64_t* ELCAM,
                const int64_t* NUCAM, const double* ELCBFC,
                const double* NUCBFC, double* GM3ICR);
+void gam3_dscf_(const int64_t* Nchunks, const int64_t* nebf,
+                const int64_t* npebf, const int64_t* npbf, const int64_t* ng3,
+                const int64_t* ng3prm, const int64_t* nat,
+                const int64_t* ngtg1, const double* pmass, const double* cat,
+                const double* zan, const double* bcoef1, const double* gamma1,
+                const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC,
+                const double* AGNBFCC, const double* ELCEX,
+                const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC,
+                const double* NUCBFC, const double* DE, const double* DP,
+                double* focke, double* fockp, double* E_gam3);
+void gam2_dscf_(const int64_t* Nchunks, const int64_t* nebf,
+                const int64_t* npebf, const int64_t* npbf, const int64_t* ng2,
+                const int64_t* ng2prm, const int64_t* nat,
+                const int64_t* ngtg1, const double* pmass, const double* cat,
+                const double* zan, const double* bcoef1, const double* gamma1,
+                const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC,
+                const double* AGNBFCC, const double* ELCEX,
+                const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC,
+                const double* NUCBFC, const double* DE, const double* DP,
+                double* focke, double* fockp, double* se2, double* sp2,
+                double* E_gam2, double* S_gam2);
 void rxchfne_gam2_ic1_(const int64_t* Nchunks, const int64_t* nebf,
                        const int64_t* npebf, const int64_t* npbf,
                        const int64_t* ng2, const int64_t* ng2prm,

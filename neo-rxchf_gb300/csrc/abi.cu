@@ -753,4 +753,134 @@ int neoxc_xcfock_correction(int64_t ne, int64_t np, double E_total,
   return finish(s);
 }
 
+// ---- direct-SCF builders: slice by proton pair, never hold the tensor --------
+// gam3_DSCF_OMP.f:2-137 GAM3_DSCF.  For each proton pair (ip,jp) the raw
+// gam_3 slice (nebf^6 doubles) is built, six-permutation symmetrised in place
+// and contracted into per-CTA partials; one reduction gives the Fock
+// matrices (accumulated) and E_gam3 (overwritten).  Nchunks (the reference's
+// NG3CHK) is accepted and validated; the slicing is by proton pair.
+int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                    int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
+                    double pmass, const double* cat, const double* zan,
+                    const double* bcoef1, const double* gamma1,
+                    const int64_t* KPESTR, const int64_t* KPEEND,
+                    const int64_t* AMPEB2C, const double* AGEBFCC,
+                    const double* AGNBFCC, const double* ELCEX,
+                    const double* NUCEX, const int64_t* ELCAM,
+                    const int64_t* NUCAM, const double* ELCBFC,
+                    const double* NUCBFC, const double* DE, const double* DP,
+                    double* focke, double* fockp, double* E_gam3) {
+  (void)AMPEB2C;
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  const int64_t n6 = nebf * nebf * nebf * nebf * nebf * nebf;
+  RC(need(ng3 == n6 * npbf * npbf, "ng3 == nebf**6 * npbf**2"));
+  RC(need(ng3prm == npebf * npebf * npebf * npebf * npebf * npebf * npbf * npbf,
+          "ng3prm"));
+  RC(need(DE && DP && focke && fockp && E_gam3, "pointers"));
+  if (nebf > 20) return set_err(NEOXC_ERR_UNSUPPORTED, "GAM3_DSCF: nebf <= 20");
+  cudaStream_t s;
+  RC(get_stream(&s));
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
+                  gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
+                  NUCAM, ELCBFC, NUCBFC));
+  const int ne = (int)nebf, np = (int)npbf;
+  DBuf slice, part, dde, ddp, dfe, dfp, dE;
+  RC(dalloc(slice, sizeof(double) * n6, s));
+  RC(dalloc(part, sizeof(double) * eg3_partial_doubles(ne, np), s));
+  RC(upload(dde, DE, sizeof(double) * nebf * nebf, s));
+  RC(upload(ddp, DP, sizeof(double) * npbf * npbf, s));
+  RC(dalloc(dfe, sizeof(double) * nebf * nebf, s));
+  RC(dalloc(dfp, sizeof(double) * npbf * npbf, s));
+  RC(dalloc(dE, sizeof(double), s));
+  CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * nebf * nebf, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * npbf * npbf, s));
+  for (int64_t pp = 0; pp < npbf * npbf; pp++) {
+    CU(launch_gam3_raw_range(u.d, pp * n6, n6, slice.as<double>(), s));
+    CU(launch_gam3_symmetrize(ne, 1, slice.as<double>(), s));
+    CU(launch_eg3_partials(ne, np, pp, 1, dde.as<double>(), slice.as<double>(),
+                           part.as<double>(), s));
+  }
+  const size_t nparts = (size_t)np * np * ne * ne * ne * ne;
+  CU(launch_fock_reduce(ne, np, ne * ne, part.as<double>(), dde.as<double>(),
+                        ddp.as<double>(), 3.0, 1, dfe.as<double>(),
+                        dfp.as<double>(), part.as<double>() + nparts,
+                        dE.as<double>(), s));
+  RC(accumulate_back(focke, dfe.as<double>(), nebf * nebf, s));
+  RC(accumulate_back(fockp, dfp.as<double>(), npbf * npbf, s));
+  CU(cudaMemcpyAsync(E_gam3, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+// gam2_DSCF_OMP.f:2-140 GAM2_DSCF: focke, fockp, se2, sp2 accumulate (the
+// reference's add2fock); E_gam2, S_gam2 overwritten.
+int neoxc_gam2_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                    int64_t ng2, int64_t ng2prm, int64_t nat, int64_t ngtg1,
+                    double pmass, const double* cat, const double* zan,
+                    const double* bcoef1, const double* gamma1,
+                    const int64_t* KPESTR, const int64_t* KPEEND,
+                    const int64_t* AMPEB2C, const double* AGEBFCC,
+                    const double* AGNBFCC, const double* ELCEX,
+                    const double* NUCEX, const int64_t* ELCAM,
+                    const int64_t* NUCAM, const double* ELCBFC,
+                    const double* NUCBFC, const double* DE, const double* DP,
+                    double* focke, double* fockp, double* se2, double* sp2,
+                    double* E_gam2, double* S_gam2) {
+  (void)AMPEB2C;
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  const int64_t n4 = nebf * nebf * nebf * nebf;
+  RC(need(ng2 == n4 * npbf * npbf, "ng2 == nebf**4 * npbf**2"));
+  RC(need(ng2prm == npebf * npebf * npebf * npebf * npbf * npbf, "ng2prm"));
+  RC(need(DE && DP && focke && fockp && se2 && sp2 && E_gam2 && S_gam2,
+          "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
+                  gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
+                  NUCAM, ELCBFC, NUCBFC));
+  const int ne = (int)nebf, np = (int)npbf;
+  const size_t npart = (size_t)np * np * ne * ne * ne;
+  DBuf s1, s2, part, dde, ddp, dfe, dfp, dse, dsp, dE;
+  RC(dalloc(s1, sizeof(double) * n4, s));
+  RC(dalloc(s2, sizeof(double) * n4, s));
+  RC(dalloc(part, sizeof(double) * (2 * npart + 2 * np * np), s));
+  RC(upload(dde, DE, sizeof(double) * nebf * nebf, s));
+  RC(upload(ddp, DP, sizeof(double) * npbf * npbf, s));
+  RC(dalloc(dfe, sizeof(double) * nebf * nebf, s));
+  RC(dalloc(dfp, sizeof(double) * npbf * npbf, s));
+  RC(dalloc(dse, sizeof(double) * nebf * nebf, s));
+  RC(dalloc(dsp, sizeof(double) * npbf * npbf, s));
+  RC(dalloc(dE, 2 * sizeof(double), s));
+  for (DBuf* b : {&dfe, &dse}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * nebf * nebf, s));
+  for (DBuf* b : {&dfp, &dsp}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * npbf * npbf, s));
+  double* pv = part.as<double>();
+  double* ps = pv + npart;
+  double* ftmp = ps + npart;
+  for (int64_t pp = 0; pp < npbf * npbf; pp++) {
+    CU(launch_gam2_raw_range(u.d, 0, pp * n4, n4, s1.as<double>(),
+                             s2.as<double>(), s));
+    CU(launch_gam2_symmetrize(ne, 1, 0, s1.as<double>(), s2.as<double>(), s));
+    CU(launch_eg2_partials(ne, np, pp, 1, dde.as<double>(), s1.as<double>(),
+                           s2.as<double>(), pv, ps, s));
+  }
+  CU(launch_fock_reduce(ne, np, ne, pv, dde.as<double>(), ddp.as<double>(), 2.0,
+                        1, dfe.as<double>(), dfp.as<double>(), ftmp,
+                        dE.as<double>(), s));
+  CU(launch_fock_reduce(ne, np, ne, ps, dde.as<double>(), ddp.as<double>(), 1.0,
+                        1, dse.as<double>(), dsp.as<double>(), ftmp + np * np,
+                        dE.as<double>() + 1, s));
+  RC(accumulate_back(focke, dfe.as<double>(), nebf * nebf, s));
+  RC(accumulate_back(fockp, dfp.as<double>(), npbf * npbf, s));
+  RC(accumulate_back(se2, dse.as<double>(), nebf * nebf, s));
+  RC(accumulate_back(sp2, dsp.as<double>(), npbf * npbf, s));
+  double e2[2];
+  CU(cudaMemcpyAsync(e2, dE.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RC(finish(s));
+  *E_gam2 = e2[0];
+  *S_gam2 = e2[1];
+  return NEOXC_OK;
+}
+
 }  // extern "C"
+

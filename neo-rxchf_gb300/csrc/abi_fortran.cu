@@ -156,6 +156,47 @@ void gam3_ic1_(const int64_t* Nchunks, const int64_t* nebf,
                         NUCAM, ELCBFC, NUCBFC, GM3ICR));
 }
 
+void gam3_dscf_(const int64_t* Nchunks, const int64_t* nebf,
+                const int64_t* npebf, const int64_t* npbf, const int64_t* ng3,
+                const int64_t* ng3prm, const int64_t* nat,
+                const int64_t* ngtg1, const double* pmass, const double* cat,
+                const double* zan, const double* bcoef1, const double* gamma1,
+                const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC,
+                const double* AGNBFCC, const double* ELCEX,
+                const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC,
+                const double* NUCBFC, const double* DE, const double* DP,
+                double* focke, double* fockp, double* E_gam3) {
+  report("gam3_dscf",
+         neoxc_gam3_dscf(*Nchunks, *nebf, *npebf, *npbf, *ng3, *ng3prm, *nat,
+                         *ngtg1, *pmass, cat, zan, bcoef1, gamma1, KPESTR,
+                         KPEEND, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
+                         ELCAM, NUCAM, ELCBFC, NUCBFC, DE, DP, focke, fockp,
+                         E_gam3));
+}
+
+void gam2_dscf_(const int64_t* Nchunks, const int64_t* nebf,
+                const int64_t* npebf, const int64_t* npbf, const int64_t* ng2,
+                const int64_t* ng2prm, const int64_t* nat,
+                const int64_t* ngtg1, const double* pmass, const double* cat,
+                const double* zan, const double* bcoef1, const double* gamma1,
+                const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC,
+                const double* AGNBFCC, const double* ELCEX,
+                const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC,
+                const double* NUCBFC, const double* DE, const double* DP,
+                double* focke, double* fockp, double* se2, double* sp2,
+                double* E_gam2, double* S_gam2) {
+  report("gam2_dscf",
+         neoxc_gam2_dscf(*Nchunks, *nebf, *npebf, *npbf, *ng2, *ng2prm, *nat,
+                         *ngtg1, *pmass, cat, zan, bcoef1, gamma1, KPESTR,
+                         KPEEND, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
+                         ELCAM, NUCAM, ELCBFC, NUCBFC, DE, DP, focke, fockp,
+                         se2, sp2, E_gam2, S_gam2));
+}
+
 void rxchfne_gam2_ic1_(const int64_t* Nchunks, const int64_t* nebf,
                        const int64_t* npebf, const int64_t* npbf,
                        const int64_t* ng2, const int64_t* ng2prm,

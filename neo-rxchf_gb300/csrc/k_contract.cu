@@ -95,7 +95,8 @@ namespace {
 // forms GAM3 for its (j1,j2,j3) from the six ket permutations.
 __global__ void __launch_bounds__(256)
 eg3_kernel(int ne, int np, const double* __restrict__ DE,
-           const double* __restrict__ g3, double* __restrict__ part) {
+           const double* __restrict__ g3, double* __restrict__ part,
+           long long ipjp0) {
   extern __shared__ double sm[];
   const int n2 = ne * ne, n3 = n2 * ne;
   double* sG = sm;           // [x][y][z] = G3(i1,x,i2,y,i3,z)
@@ -105,7 +106,7 @@ eg3_kernel(int ne, int np, const double* __restrict__ DE,
   const int i3 = cta % ne; cta /= ne;
   const int i2 = cta % ne; cta /= ne;
   const int i1 = cta % ne; cta /= ne;
-  const long long ipjp = cta;
+  const long long ipjp = cta;   // relative to the slice g3 points at
   for (int k = threadIdx.x; k < n2; k += blockDim.x) sDE[k] = DE[k];
   // index_GAM_3PK(ip,jp,i1,x,i2,y,i3,z)-1 = z + ne*(i3 + ne*(y + ne*(i2 +
   //   ne*(x + ne*(i1 + ne*ipjp)))))
@@ -135,7 +136,7 @@ eg3_kernel(int ne, int np, const double* __restrict__ DE,
   if ((int)threadIdx.x < ne) {
     double s = 0.0;
     for (int t = threadIdx.x; t < (int)blockDim.x; t += ne) s += sred[t];
-    part[(size_t)blockIdx.x * ne + threadIdx.x] = s;
+    part[((size_t)blockIdx.x + (size_t)ipjp0 * n3) * ne + threadIdx.x] = s;
   }
 }
 
@@ -144,7 +145,8 @@ eg3_kernel(int ne, int np, const double* __restrict__ DE,
 __global__ void eg2_kernel(int ne, int np, const double* __restrict__ DE,
                            const double* __restrict__ g2,
                            const double* __restrict__ g2s,
-                           double* __restrict__ pv, double* __restrict__ ps) {
+                           double* __restrict__ pv, double* __restrict__ ps,
+                           long long ipjp0) {
   int cta = blockIdx.x;
   const int i2 = cta % ne; cta /= ne;
   const int i1 = cta % ne; cta /= ne;
@@ -162,8 +164,9 @@ __global__ void eg2_kernel(int ne, int np, const double* __restrict__ DE,
       av = fma(d, v, av);
       as = fma(d, vs, as);
     }
-    pv[(size_t)blockIdx.x * ne + j1] = av;
-    ps[(size_t)blockIdx.x * ne + j1] = as;
+    const size_t c = (size_t)blockIdx.x + (size_t)ipjp0 * ne * ne;
+    pv[c * ne + j1] = av;
+    ps[c * ne + j1] = as;
   }
 }
 
@@ -329,19 +332,28 @@ size_t eg3_partial_doubles(int ne, int np) {
   return (size_t)np * np * ne * ne * ne * ne + (size_t)np * np;
 }
 
-cudaError_t launch_eg3ic1(int ne, int np, const double* DE, const double* DP,
-                          const double* g3, double* scratch, double* focke,
-                          double* fockp, double* E, cudaStream_t s) {
+cudaError_t launch_eg3_partials(int ne, int np, long long ipjp0,
+                                long long nipjp, const double* DE,
+                                const double* g3_slice, double* part,
+                                cudaStream_t s) {
   if (ne < 1 || ne > 20 || np < 1) return cudaErrorInvalidValue;
   const int bs = ne * (256 / ne);
   const size_t smem = sizeof(double) * ((size_t)ne * ne * ne + ne * ne + bs);
   cudaError_t e = cudaFuncSetAttribute(eg3_kernel,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const long long grid = (long long)np * np * ne * ne * ne;
-  eg3_kernel<<<(unsigned)grid, bs, smem, s>>>(ne, np, DE, g3, scratch);
-  e = cudaGetLastError();
+  const long long grid = nipjp * ne * ne * ne;
+  eg3_kernel<<<(unsigned)grid, bs, smem, s>>>(ne, np, DE, g3_slice, part, ipjp0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eg3ic1(int ne, int np, const double* DE, const double* DP,
+                          const double* g3, double* scratch, double* focke,
+                          double* fockp, double* E, cudaStream_t s) {
+  cudaError_t e = launch_eg3_partials(ne, np, 0, (long long)np * np, DE, g3,
+                                      scratch, s);
   if (e != cudaSuccess) return e;
+  const long long grid = (long long)np * np * ne * ne * ne;
   double* fp_tmp = scratch + (size_t)grid * ne;
   return launch_fock_reduce(ne, np, ne * ne, scratch, DE, DP, 3.0, 1, focke,
                             fockp, fp_tmp, E, s);
@@ -361,7 +373,7 @@ cudaError_t launch_eg2ic1(int ne, int np, const double* DE, const double* DP,
   double* ps = scratch + npart;
   double* ftmp = scratch + 2 * npart;
   eg2_kernel<<<(unsigned)(np * np * ne * ne), 32, 0, s>>>(ne, np, DE, g2, g2s,
-                                                          pv, ps);
+                                                          pv, ps, 0);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // FE, FP accumulate (add2fock); SE, SP are overwritten (:379-381)
@@ -369,6 +381,17 @@ cudaError_t launch_eg2ic1(int ne, int np, const double* DE, const double* DP,
   if (e != cudaSuccess) return e;
   return launch_fock_reduce(ne, np, ne, ps, DE, DP, 1.0, 0, SE, SP,
                             ftmp + np * np, S, s);
+}
+
+cudaError_t launch_eg2_partials(int ne, int np, long long ipjp0,
+                                long long nipjp, const double* DE,
+                                const double* g2_slice,
+                                const double* g2s_slice, double* pv,
+                                double* ps, cudaStream_t s) {
+  if (ne < 1 || np < 1 || nipjp < 1) return cudaErrorInvalidValue;
+  eg2_kernel<<<(unsigned)(nipjp * ne * ne), 32, 0, s>>>(
+      ne, np, DE, g2_slice, g2s_slice, pv, ps, ipjp0);
+  return cudaGetLastError();
 }
 
 size_t omg2_partial_doubles(int ne, int np) {

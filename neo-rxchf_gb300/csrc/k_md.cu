@@ -250,12 +250,12 @@ gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
 template <int RX>
 __global__ void __launch_bounds__(64)
 gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
-                double* __restrict__ x2, long long ntup) {
+                double* __restrict__ x2, long long t0, long long ntup) {
   const int ne = S.nebf, np = S.npbf;
   const int lane = threadIdx.x & 31;
   const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   if (w >= ntup) return;
-  long long r = w;
+  long long r = w + t0;   // packed index - 1 of the tuple; outputs from t0
   const int jc2 = (int)(r % ne); r /= ne;
   const int ic2 = (int)(r % ne); r /= ne;
   const int jc1 = (int)(r % ne); r /= ne;
@@ -323,12 +323,13 @@ __global__ void gam2_sym_kernel(int ne, int np, int rx, double* __restrict__ x1,
 
 // ---- gam_3 raw tensor: warp per contracted tuple ----------------------------
 __global__ void __launch_bounds__(64)
-gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long ntup) {
+gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
+                long long ntup) {
   const int ne = S.nebf, np = S.npbf;
   const int lane = threadIdx.x & 31;
   const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   if (w >= ntup) return;
-  long long r = w;
+  long long r = w + t0;   // packed index - 1 of the tuple; outputs from t0
   int c[6];
   for (int k = 5; k >= 0; k--) {
     c[k] = (int)(r % ne);
@@ -413,15 +414,22 @@ cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
+                                  long long ntup, double* x1, double* x2,
+                                  cudaStream_t s) {
+  const long long threads = ntup * 32;
+  const unsigned blocks = (unsigned)((threads + 63) / 64);
+  if (ntup <= 0) return cudaSuccess;
+  if (rx) gam2_raw_kernel<1><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
+  else gam2_raw_kernel<0><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rx, double* x1,
                             double* x2, cudaStream_t s) {
   const long long ntup = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
                          sys.npbf * sys.npbf;
-  const long long threads = ntup * 32;
-  const unsigned blocks = (unsigned)((threads + 63) / 64);
-  if (rx) gam2_raw_kernel<1><<<blocks, 64, 0, s>>>(sys, x1, x2, ntup);
-  else gam2_raw_kernel<0><<<blocks, 64, 0, s>>>(sys, x1, x2, ntup);
-  return cudaGetLastError();
+  return launch_gam2_raw_range(sys, rx, 0, ntup, x1, x2, s);
 }
 
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,
@@ -433,14 +441,19 @@ cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,
   return cudaGetLastError();
 }
 
+cudaError_t launch_gam3_raw_range(const DevSystem& sys, long long t0,
+                                  long long ntup, double* x3, cudaStream_t s) {
+  const long long threads = ntup * 32;
+  const unsigned blocks = (unsigned)((threads + 63) / 64);
+  if (ntup <= 0) return cudaSuccess;
+  gam3_raw_kernel<<<blocks, 64, 0, s>>>(sys, x3, t0, ntup);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3, cudaStream_t s) {
   const long long n6 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
                        sys.nebf * sys.nebf;
-  const long long ntup = n6 * sys.npbf * sys.npbf;
-  const long long threads = ntup * 32;
-  const unsigned blocks = (unsigned)((threads + 63) / 64);
-  gam3_raw_kernel<<<blocks, 64, 0, s>>>(sys, x3, ntup);
-  return cudaGetLastError();
+  return launch_gam3_raw_range(sys, 0, n6 * sys.npbf * sys.npbf, x3, s);
 }
 
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,

@@ -88,8 +88,27 @@ cudaError_t launch_xcfock_correction(int ne, int np, double S_total,
                                      const double* sp2, double* focke,
                                      double* fockp, cudaStream_t s);
 
+// Partial sums of one proton-pair slice [ipjp0, ipjp0+nipjp) of the
+// contraction; the slice pointer addresses the slice's first element and the
+// partials land at their global positions (direct-SCF slicing).
+cudaError_t launch_eg3_partials(int ne, int np, long long ipjp0,
+                                long long nipjp, const double* DE,
+                                const double* g3_slice, double* part,
+                                cudaStream_t s);
+cudaError_t launch_eg2_partials(int ne, int np, long long ipjp0,
+                                long long nipjp, const double* DE,
+                                const double* g2_slice,
+                                const double* g2s_slice, double* pv,
+                                double* ps, cudaStream_t s);
+
 // ---- integral builders (MD kernels) ------------------------------------
 cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s);
+// tuples [t0, t0+ntup) of the packed index space, written from x[0]
+cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
+                                  long long ntup, double* x1, double* x2,
+                                  cudaStream_t s);
+cudaError_t launch_gam3_raw_range(const DevSystem& sys, long long t0,
+                                  long long ntup, double* x3, cudaStream_t s);
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rxchfne, double* x1,
                             double* x2, cudaStream_t s);
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rxchfne, double* x1,

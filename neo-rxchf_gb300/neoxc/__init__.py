@@ -21,7 +21,8 @@ from .basis import NeoSystem  # noqa: F401  (re-export)
 
 __all__ = [
     "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
-    "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "eg4icr", "eg3ic1", "eg2ic1",
+    "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam3_dscf", "gam2_dscf",
+    "eg4icr", "eg3ic1", "eg2ic1",
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
     "index_gam_2pk", "index_gam_3pk", "index_gam_4pk2", "pack_4d",
@@ -54,6 +55,8 @@ def _declare(L):
         "neoxc_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
         "neoxc_gam3_ic1": (I, [i64] * 8 + [d] + [vp] * 16),
         "neoxc_rxchfne_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
+        "neoxc_gam3_dscf": (I, [i64] * 8 + [d] + [vp] * 20),
+        "neoxc_gam2_dscf": (I, [i64] * 8 + [d] + [vp] * 23),
         "neoxc_gam4_icr": (I, [i64] * 6 + [vp] * 3),
         "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
         "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
@@ -199,6 +202,35 @@ def gam3_ic1(s: NeoSystem, nchunks: int = 1) -> np.ndarray:
     return g
 
 
+def gam3_dscf(s: NeoSystem, DE, DP, focke=None, fockp=None, nchunks: int = 1):
+    """gam3_DSCF_OMP.f GAM3_DSCF: returns (focke + dF_e, fockp + dF_p, E_gam3)."""
+    de, dp = _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(s.nebf, s.npbf, focke, fockp)
+    E = np.zeros(1)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_gam3_dscf(nchunks, s.nebf, s.npebf, s.npbf, s.ng3, s.ng3prm,
+                                 s.nat, s.ngtg, s.pmass, *ptrs, _p(de), _p(dp),
+                                 _p(fe), _p(fp), _p(E)))
+    return (*_fock_out(fe, fp, s.nebf, s.npbf), float(E[0]))
+
+
+def gam2_dscf(s: NeoSystem, DE, DP, focke=None, fockp=None, se2=None, sp2=None,
+              nchunks: int = 1):
+    """gam2_DSCF_OMP.f GAM2_DSCF -> (focke, fockp, se2, sp2, E_gam2, S_gam2);
+    the four matrices accumulate into the given ones (zeros when None)."""
+    ne, np_ = s.nebf, s.npbf
+    de, dp = _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(ne, np_, focke, fockp)
+    se, sp = _fock_io(ne, np_, se2, sp2)
+    E, S = np.zeros(1), np.zeros(1)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_gam2_dscf(nchunks, ne, s.npebf, np_, s.ng2, s.ng2prm,
+                                 s.nat, s.ngtg, s.pmass, *ptrs, _p(de), _p(dp),
+                                 _p(fe), _p(fp), _p(se), _p(sp), _p(E), _p(S)))
+    return (*_fock_out(fe, fp, ne, np_), *_fock_out(se, sp, ne, np_),
+            float(E[0]), float(S[0]))
+
+
 def gam4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:
     """gam4_ICR_OMP.f GAM4_ICR -> GAM_4 (gam_4/16, packed index_GAM_4PK2)."""
     g2, ge = _f64(gam_2s), _f64(gam_ee)
@@ -211,8 +243,8 @@ def gam4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:
 
 # ---- contractions ---------------------------------------------------------------
 def _fock_io(ne, np_, focke, fockp):
-    fe = np.zeros(ne * ne) if focke is None else _fmat(focke)
-    fp = np.zeros(np_ * np_) if fockp is None else _fmat(fockp)
+    fe = np.zeros(ne * ne) if focke is None else _fmat(focke).copy()
+    fp = np.zeros(np_ * np_) if fockp is None else _fmat(fockp).copy()
     return fe, fp
 
 

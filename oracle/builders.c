@@ -891,3 +891,139 @@ void orc_gam4_dscf_sample(int64_t ne, int64_t np, const double *Gee,
   }
   free(xfe); free(xfp); free(Ep);
 }
+
+/* ---- direct-SCF builders ------------------------------------------------ */
+#define DEo(i, j) DE[((i) - 1) + ne * ((j) - 1)]
+#define DPo(i, j) DP[((i) - 1) + np * ((j) - 1)]
+
+/* gam2_DSCF_OMP.f:330-559 contract_omega2 (direct): the pair-symmetrised
+ * OMG2/OMG2s of one contracted tuple, half*(OMG2_12 + OMG2_21). */
+static void contract_omega2_direct(const orc_system *s, int64_t ip, int64_t jp,
+                                   int64_t iec1, int64_t jec1, int64_t iec2,
+                                   int64_t jec2, double *O, double *Os) {
+  double o12 = 0.0, o21 = 0.0, s12 = 0.0, s21 = 0.0;
+  orc_prim A[3], B[3], A2[3], B2[3];
+  p_prim(s, ip, &A[2]);
+  p_prim(s, jp, &B[2]);
+  double cip = s->AGNBFCC[ip - 1], cjp = s->AGNBFCC[jp - 1];
+  for (int64_t ie1 = s->KPESTR[iec1 - 1]; ie1 <= s->KPEEND[iec1 - 1]; ie1++)
+  for (int64_t je1 = s->KPESTR[jec1 - 1]; je1 <= s->KPEEND[jec1 - 1]; je1++)
+  for (int64_t ie2 = s->KPESTR[iec2 - 1]; ie2 <= s->KPEEND[iec2 - 1]; ie2++)
+  for (int64_t je2 = s->KPESTR[jec2 - 1]; je2 <= s->KPEEND[jec2 - 1]; je2++) {
+    e_prim(s, ie1, &A[0]); e_prim(s, ie2, &A[1]);
+    e_prim(s, je1, &B[0]); e_prim(s, je2, &B[1]);
+    A2[0] = A[1]; A2[1] = A[0]; A2[2] = A[2];
+    B2[0] = B[1]; B2[1] = B[0]; B2[2] = B[2];
+    double c = cip * cjp * s->AGEBFCC[ie1 - 1] * s->AGEBFCC[je1 - 1] *
+               s->AGEBFCC[ie2 - 1] * s->AGEBFCC[je2 - 1];
+    double aE, aS;
+    orc_xcalc_gam2(A, B, s, &aE, &aS);
+    o12 = o12 + aE * c;
+    s12 = s12 + aS * c;
+    orc_xcalc_gam2(A2, B2, s, &aE, &aS);
+    o21 = o21 + aE * c;
+    s21 = s21 + aS * c;
+  }
+  *O = 0.5 * (o12 + o21);
+  *Os = 0.5 * (s12 + s21);
+}
+
+/* gam2_DSCF_OMP.f:2-140 GAM2_DSCF and :143-327 thread_gam2: focke, fockp,
+ * se2, sp2 accumulate (add2fock); E_gam2, S_gam2 overwritten.  Threads
+ * split the tuples like the reference's OpenMP loop (array reductions). */
+void orc_gam2_dscf(const orc_system *s, const double *DE, const double *DP,
+                   double *focke, double *fockp, double *se2, double *sp2,
+                   double *E_gam2, double *S_gam2) {
+  const int64_t ne = s->nebf, np = s->npbf;
+  const int64_t dims[6] = {np, np, ne, ne, ne, ne};
+  int64_t ng2 = ne * ne * ne * ne * np * np;
+  double e = 0.0, sg = 0.0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : e, sg) \
+    reduction(+ : focke[0 : ne * ne], se2[0 : ne * ne])             \
+    reduction(+ : fockp[0 : np * np], sp2[0 : np * np])
+  for (int64_t t = 0; t < ng2; t++) {
+    int64_t x[6];
+    decode(t, 6, dims, x);
+    int64_t ip = x[0], jp = x[1], i1 = x[2], j1 = x[3], i2 = x[4], j2 = x[5];
+    double o12, s12, o21, s21;
+    contract_omega2_direct(s, ip, jp, i1, j1, i2, j2, &o12, &s12);
+    contract_omega2_direct(s, ip, jp, i1, j2, i2, j1, &o21, &s21);
+    double g = o12 - 0.5 * o21, gs = s12 - 0.5 * s21;
+    focke[(i1 - 1) + ne * (j1 - 1)] += DPo(ip, jp) * DEo(i2, j2) * 2.0 * g;
+    fockp[(ip - 1) + np * (jp - 1)] += DEo(i1, j1) * DEo(i2, j2) * g;
+    e = e + DEo(i1, j1) * DEo(i2, j2) * DPo(ip, jp) * g;
+    se2[(i1 - 1) + ne * (j1 - 1)] += DPo(ip, jp) * DEo(i2, j2) * gs;
+    sp2[(ip - 1) + np * (jp - 1)] += DEo(i1, j1) * DEo(i2, j2) * gs;
+    sg = sg + DEo(i1, j1) * DEo(i2, j2) * DPo(ip, jp) * gs;
+  }
+  *E_gam2 = e;
+  *S_gam2 = sg;
+}
+
+/* gam3_DSCF_OMP.f:367-717 contract_omega3 (direct): the six particle
+ * orderings of one contracted tuple evaluated and averaged. */
+static double contract_omega3_direct(const orc_system *s, int64_t ip,
+                                     int64_t jp, int64_t iec1, int64_t jec1,
+                                     int64_t iec2, int64_t jec2, int64_t iec3,
+                                     int64_t jec3) {
+  static const int ord[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2},
+                                {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  double o[6] = {0, 0, 0, 0, 0, 0};
+  orc_prim A[4], B[4], PA[4], PB[4];
+  p_prim(s, ip, &A[3]);
+  p_prim(s, jp, &B[3]);
+  double cip = s->AGNBFCC[ip - 1], cjp = s->AGNBFCC[jp - 1];
+  const int64_t *KS = s->KPESTR, *KE = s->KPEEND;
+  const double *C = s->AGEBFCC;
+  for (int64_t ie1 = KS[iec1 - 1]; ie1 <= KE[iec1 - 1]; ie1++)
+  for (int64_t je1 = KS[jec1 - 1]; je1 <= KE[jec1 - 1]; je1++)
+  for (int64_t ie2 = KS[iec2 - 1]; ie2 <= KE[iec2 - 1]; ie2++)
+  for (int64_t je2 = KS[jec2 - 1]; je2 <= KE[jec2 - 1]; je2++)
+  for (int64_t ie3 = KS[iec3 - 1]; ie3 <= KE[iec3 - 1]; ie3++)
+  for (int64_t je3 = KS[jec3 - 1]; je3 <= KE[jec3 - 1]; je3++) {
+    e_prim(s, ie1, &A[0]); e_prim(s, ie2, &A[1]); e_prim(s, ie3, &A[2]);
+    e_prim(s, je1, &B[0]); e_prim(s, je2, &B[1]); e_prim(s, je3, &B[2]);
+    double c = cip * cjp * C[ie1 - 1] * C[je1 - 1] * C[ie2 - 1] * C[je2 - 1] *
+               C[ie3 - 1] * C[je3 - 1];
+    for (int k = 0; k < 6; k++) {
+      for (int m = 0; m < 3; m++) { PA[m] = A[ord[k][m]]; PB[m] = B[ord[k][m]]; }
+      PA[3] = A[3];
+      PB[3] = B[3];
+      o[k] = o[k] + orc_xcalc_gam3(PA, PB, s) * c;
+    }
+  }
+  return (o[0] + o[1] + o[2] + o[3] + o[4] + o[5]) / 6.0;
+}
+
+/* gam3_DSCF_OMP.f:2-137 GAM3_DSCF and :140-364 thread_gam3: Fock
+ * accumulate, E overwritten (OpenMP array reductions over the tuples). */
+void orc_gam3_dscf(const orc_system *s, const double *DE, const double *DP,
+                   double *focke, double *fockp, double *E_gam3) {
+  const int64_t ne = s->nebf, np = s->npbf;
+  const int64_t dims[8] = {np, np, ne, ne, ne, ne, ne, ne};
+  int64_t ng3 = ne * ne * ne * ne * ne * ne * np * np;
+  double e = 0.0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : e) \
+    reduction(+ : focke[0 : ne * ne], fockp[0 : np * np])
+  for (int64_t t = 0; t < ng3; t++) {
+    int64_t x[8];
+    decode(t, 8, dims, x);
+    int64_t ip = x[0], jp = x[1], i1 = x[2], j1 = x[3], i2 = x[4], j2 = x[5],
+            i3 = x[6], j3 = x[7];
+    double o123 = contract_omega3_direct(s, ip, jp, i1, j1, i2, j2, i3, j3);
+    double o213 = contract_omega3_direct(s, ip, jp, i1, j2, i2, j1, i3, j3);
+    double o312 = contract_omega3_direct(s, ip, jp, i1, j3, i2, j1, i3, j2);
+    double o132 = contract_omega3_direct(s, ip, jp, i1, j1, i2, j3, i3, j2);
+    double o231 = contract_omega3_direct(s, ip, jp, i1, j2, i2, j3, i3, j1);
+    double o321 = contract_omega3_direct(s, ip, jp, i1, j3, i2, j2, i3, j1);
+    double g = 8.0 * o123 - 4.0 * o213 + 2.0 * o312 - 4.0 * o132 +
+               2.0 * o231 - 4.0 * o321;
+    g = g / 8.0;
+    focke[(i1 - 1) + ne * (j1 - 1)] += DPo(ip, jp) * DEo(i2, j2) * DEo(i3, j3) * 3.0 * g;
+    fockp[(ip - 1) + np * (jp - 1)] += DEo(i1, j1) * DEo(i2, j2) * DEo(i3, j3) * g;
+    e = e + DEo(i1, j1) * DEo(i2, j2) * DEo(i3, j3) * DPo(ip, jp) * g;
+  }
+  *E_gam3 = e;
+}
+#undef DEo
+#undef DPo

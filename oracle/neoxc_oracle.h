@@ -181,6 +181,13 @@ void orc_xcfock_correction(int64_t ne, int64_t np, double S_total,
                            const double *sp1, const double *se2,
                            const double *sp2, double *focke, double *fockp);
 
+/* direct-SCF variants (gam2_DSCF_OMP.f, gam3_DSCF_OMP.f) */
+void orc_gam2_dscf(const orc_system *s, const double *DE, const double *DP,
+                   double *focke, double *fockp, double *se2, double *sp2,
+                   double *E_gam2, double *S_gam2);
+void orc_gam3_dscf(const orc_system *s, const double *DE, const double *DP,
+                   double *focke, double *fockp, double *E_gam3);
+
 /* density from MO coefficients (GAM_IO.f read_elec_density) */
 void orc_density(int64_t nbf, int64_t nocc, double prefac, const double *C,
                  double *D);

@@ -122,6 +122,8 @@ def lib():
                 "orc_rxchfne_fbe_omg2": (None, [i64, i64] + [vp] * 6),
                 "orc_xcfock_correction": (None, [i64, i64, d, d] + [vp] * 6),
                 "orc_density": (None, [i64, i64, d, vp, vp]),
+                "orc_gam2_dscf": (None, [vp] + [vp] * 8),
+                "orc_gam3_dscf": (None, [vp] + [vp] * 5),
                 "orc_num_threads": (C.c_int, []),
             }
             for name, (res, args) in sig.items():

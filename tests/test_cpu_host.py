@@ -189,6 +189,34 @@ def test_library_exports_every_declared_symbol():
     assert set(names) <= exported
 
 
+def _header_arg_counts():
+    txt = open(os.path.join(ROOT, "include", "neoxc.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(?:int|int64_t|void|const char\*)\s+([a-z0-9_]+)\s*\(([^)]*)\)",
+                         txt):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header():
+    """Every ctypes prototype the Python mirror sets has the parameter count
+    that include/neoxc.h declares (a mismatch would pass garbage over the
+    C-ABI)."""
+    import neoxc
+    L = neoxc.lib(build_if_missing=True)
+    want = _header_arg_counts()
+    checked = 0
+    for name, n in want.items():
+        f = getattr(L, name)
+        if f.argtypes is None:
+            continue
+        assert len(f.argtypes) == n, (name, len(f.argtypes), n)
+        checked += 1
+    assert checked >= 30
+
+
 def test_argument_checks_need_no_gpu():
     """Size validation happens on the host before any device work, and a
     shape outside the supported range is an error, never a CPU fallback."""

@@ -213,6 +213,80 @@ def test_gam3_ic1(nx, orc, kw):
     assert_close_scaled(nx.gam3_ic1(s), T.get("g3"), RTOL, "GM3ICR")
 
 
+# Direct-SCF builders.  Every case is checked against the oracle's in-core
+# pipeline (GAM3_IC1 + EG3IC1, GAM2_IC1 + EG2IC1); the tiny cases (one
+# primitive per contracted function) also against the oracle's restatement of
+# the direct loops, which re-evaluates every particle ordering of every tuple.
+DSCF_CASES = [
+    (True, dict(seed=113, nat=2, nebf=2, nprim=1, npbf=2, ngtg=2, lmax_e=1, lmax_p=1)),
+    (False, dict(seed=111, nat=2, nebf=3, nprim=1, npbf=2, ngtg=2, lmax_e=1, lmax_p=1)),
+    (False, dict(seed=112, nat=2, nebf=2, nprim=(1, 2), npbf=3, ngtg=2, lmax_e=2, lmax_p=1)),
+]
+
+
+def _dscf_inputs(kw, n_extra):
+    s = _system(**kw)
+    ne, np_ = s.nebf, s.npbf
+    rng = np.random.default_rng(kw["seed"] + 7)
+    DE, DP = _dens(ne, 2, kw["seed"]), _dens(np_, 1, kw["seed"] + 1, 1.0)
+    m0 = [rng.standard_normal((n, n)) for n in (ne, np_, ne, np_)[:n_extra]]
+    return s, ne, np_, DE, DP, m0
+
+
+def _close_e(got, want, what):
+    assert abs(got - want) <= RTOL * max(1.0, abs(want)), (what, got, want)
+
+
+@pytest.mark.parametrize("direct,kw", DSCF_CASES)
+def test_gam3_dscf(nx, orc, direct, kw):
+    """GAM3_DSCF (proton-pair slices built and contracted on the fly):
+    focke/fockp accumulate into pre-filled matrices, E_gam3 overwritten."""
+    s, ne, np_, DE, DP, m0 = _dscf_inputs(kw, 2)
+    fe, fp, E = nx.gam3_dscf(s, DE, DP, *m0)
+    L, T = orc.lib(), OracleTensors(orc, s)
+    rfe, rfp, rE = m0[0].ravel("F").copy(), m0[1].ravel("F").copy(), np.zeros(1)
+    L.orc_eg3ic1(ne, np_, orc.ptr(fmat(DE)), orc.ptr(fmat(DP)), orc.ptr(T.get("g3")),
+                 orc.ptr(rfe), orc.ptr(rfp), orc.ptr(rE))
+    assert_close_scaled(fe.ravel("F"), rfe, RTOL, "focke (GAM3_DSCF vs in-core)")
+    assert_close_scaled(fp.ravel("F"), rfp, RTOL, "fockp (GAM3_DSCF vs in-core)")
+    _close_e(E, rE[0], "E_gam3")
+    if direct:
+        dfe, dfp, dE = m0[0].ravel("F").copy(), m0[1].ravel("F").copy(), np.zeros(1)
+        L.orc_gam3_dscf(T.h.ref, orc.ptr(fmat(DE)), orc.ptr(fmat(DP)),
+                        orc.ptr(dfe), orc.ptr(dfp), orc.ptr(dE))
+        assert_close_scaled(fe.ravel("F"), dfe, RTOL, "focke (direct oracle)")
+        assert_close_scaled(fp.ravel("F"), dfp, RTOL, "fockp (direct oracle)")
+        _close_e(E, dE[0], "E_gam3 (direct oracle)")
+
+
+@pytest.mark.parametrize("direct,kw", DSCF_CASES)
+def test_gam2_dscf(nx, orc, direct, kw):
+    """GAM2_DSCF: focke/fockp/se2/sp2 accumulate, E_gam2/S_gam2 overwritten."""
+    s, ne, np_, DE, DP, m0 = _dscf_inputs(kw, 4)
+    out = nx.gam2_dscf(s, DE, DP, *m0)
+    L, T = orc.lib(), OracleTensors(orc, s)
+    fe, fp = m0[0].ravel("F").copy(), m0[1].ravel("F").copy()
+    se, sp, E, S = np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(1), np.zeros(1)
+    L.orc_eg2ic1(ne, np_, orc.ptr(fmat(DE)), orc.ptr(fmat(DP)), orc.ptr(T.get("g2")),
+                 orc.ptr(T.get("g2s")), orc.ptr(fe), orc.ptr(se), orc.ptr(fp),
+                 orc.ptr(sp), orc.ptr(E), orc.ptr(S))
+    ref = [fe, fp, m0[2].ravel("F") + se, m0[3].ravel("F") + sp]
+    names = ("focke", "fockp", "se2", "sp2")
+    for got, want, name in zip(out[:4], ref, names):
+        assert_close_scaled(got.ravel("F"), want, RTOL, name + " (GAM2_DSCF vs in-core)")
+    _close_e(out[4], E[0], "E_gam2")
+    _close_e(out[5], S[0], "S_gam2")
+    if direct:
+        d = [m.ravel("F").copy() for m in m0]
+        dE, dS = np.zeros(1), np.zeros(1)
+        L.orc_gam2_dscf(T.h.ref, orc.ptr(fmat(DE)), orc.ptr(fmat(DP)),
+                        *[orc.ptr(x) for x in d], orc.ptr(dE), orc.ptr(dS))
+        for got, want, name in zip(out[:4], d, names):
+            assert_close_scaled(got.ravel("F"), want, RTOL, name + " (direct oracle)")
+        _close_e(out[4], dE[0], "E_gam2 (direct oracle)")
+        _close_e(out[5], dS[0], "S_gam2 (direct oracle)")
+
+
 def test_xchf_example_full_pipeline(nx, xchf, golden_xchf):
     """examples/xchf end to end on the GPU: GAM_ee, GAM2_IC1, GAM3_IC1 and
     the EG2/EG3/GAM4_DSCF contractions at the guessCE density reproduce

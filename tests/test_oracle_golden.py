@@ -120,3 +120,34 @@ def test_xchf_converged_energetics(orc, xchf, xchf_tensors, golden_xchf):
     ref = golden_xchf["final"]
     for k in ("E_GAM2", "E_GAM3", "E_GAM4"):
         assert e[k] == pytest.approx(ref[k], rel=2e-7), (k, e[k], ref[k])
+
+
+def test_direct_restatement_matches_in_core(orc):
+    """The oracle's direct-SCF loops (gam2_DSCF_OMP.f, gam3_DSCF_OMP.f), which
+    evaluate every particle ordering of every tuple, agree with its in-core
+    pipeline (GAM2_IC1/GAM3_IC1 tensors contracted by EG2IC1/EG3IC1)."""
+    from neoxc import basis
+    s = basis.synthetic(seed=113, nat=2, nebf=2, nprim=1, npbf=2, ngtg=2, lmax_e=1, lmax_p=1)
+    ne, np_ = s.nebf, s.npbf
+    L, h = orc.lib(), orc.SystemHandle(s)
+    DE = fmat(basis.random_density(ne, 2, 113, 2.0))
+    DP = fmat(basis.random_density(np_, 1, 114, 1.0))
+    g2, g2s, g3 = np.zeros(s.ng2), np.zeros(s.ng2), np.zeros(s.ng3)
+    L.orc_gam2_ic1(h.ref, orc.ptr(g2), orc.ptr(g2s))
+    L.orc_gam3_ic1(h.ref, orc.ptr(g3))
+    m = lambda n: np.zeros(n * n)  # noqa: E731
+    ic2 = [m(ne), m(ne), m(np_), m(np_), np.zeros(1), np.zeros(1)]
+    L.orc_eg2ic1(ne, np_, orc.ptr(DE), orc.ptr(DP), orc.ptr(g2), orc.ptr(g2s),
+                 *[orc.ptr(x) for x in ic2])
+    d2 = [m(ne), m(np_), m(ne), m(np_), np.zeros(1), np.zeros(1)]
+    L.orc_gam2_dscf(h.ref, orc.ptr(DE), orc.ptr(DP), *[orc.ptr(x) for x in d2])
+    # EG2IC1 order: FE, SE, FP, SP, E, S; GAM2_DSCF order: focke, fockp, se2, sp2, E, S
+    for a, b in zip(d2, [ic2[0], ic2[2], ic2[1], ic2[3], ic2[4], ic2[5]]):
+        assert np.allclose(a, b, rtol=1e-11, atol=1e-14 * max(1.0, np.abs(b).max()))
+    ic3 = [m(ne), m(np_), np.zeros(1)]
+    L.orc_eg3ic1(ne, np_, orc.ptr(DE), orc.ptr(DP), orc.ptr(g3), *[orc.ptr(x) for x in ic3])
+    d3 = [m(ne), m(np_), np.zeros(1)]
+    L.orc_gam3_dscf(h.ref, orc.ptr(DE), orc.ptr(DP), *[orc.ptr(x) for x in d3])
+    for a, b in zip(d3, ic3):
+        assert np.allclose(a, b, rtol=1e-11, atol=1e-14 * max(1.0, np.abs(b).max()))
+    assert abs(d2[4][0]) > 1e-3 and abs(d3[2][0]) > 1e-6
