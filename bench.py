@@ -17,6 +17,10 @@ without storing gam_4.  FP64 throughout.
            traffic is the two input tables).
   cpu_baseline  the oracle's restatement of the reference loop on all host
            cores over a bounded contiguous sample of the same tuples.
+  factored the factorised Fock build (same focke/fockp/E for the
+           pair-symmetric tables the reference produces, O(nebf^4 npbf^2 +
+           nebf^5) work) at this shape and at nebf=60/npbf=24, labelled
+           separately; its "equivalent" rate is ng4 / time.
 
 --impl reference times that CPU implementation alone (all host threads),
 with the same metric and config.  With --gpus N (torchrun), every rank runs
@@ -73,12 +77,16 @@ def workload_config(ne, np_):
 
 
 def synthetic_inputs(ne, np_, seed=2024):
-    """Seeded tables with the layouts of GAM_ee / GAM_2s and densities from
-    two doubly occupied orbitals (the kernel's work is data independent)."""
+    """Seeded tables with the layouts and the pair-exchange symmetry of
+    GAM_ee ((ab|cd) = (cd|ab)) and GAM_2s (gs(p;ab;cd) = gs(p;cd;ab), the
+    GAM2_IC1 symmetrisation), and densities from two doubly occupied
+    orbitals (the element kernel's work is data independent)."""
     from neoxc import basis
     rng = np.random.Generator(np.random.PCG64(seed))
-    gee = rng.uniform(0.0, 1.0, ne ** 4)
-    g2s = rng.uniform(0.0, 1.0, ne ** 4 * np_ ** 2)
+    ee = rng.uniform(0.0, 1.0, (ne,) * 4)
+    gee = np.ascontiguousarray((0.5 * (ee + ee.transpose(2, 3, 0, 1))).ravel())
+    gs = rng.uniform(0.0, 1.0, (np_, np_) + (ne,) * 4)
+    g2s = np.ascontiguousarray((0.5 * (gs + gs.transpose(0, 1, 4, 5, 2, 3))).ravel())
     DE = basis.random_density(ne, 2, seed + 1, 2.0)
     DP = basis.random_density(np_, 1, seed + 2, 1.0)
     return gee, g2s, DE, DP
@@ -250,6 +258,97 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+FACTORED_LARGE = (60, 24)   # nebf, npbf of the mixed-precision XCHF shape
+FACTORED_LAUNCHES = 14      # kernels of one factorised build (k_gam4f.cu)
+
+
+def time_factored(neoxc, torch, dev, stream, ne, np_, d_gee, d_g2s, d_DE, d_DP,
+                  warmup=2, steps=5):
+    f64 = torch.float64
+    d_fe = torch.zeros(ne * ne, dtype=f64, device=dev)
+    d_fp = torch.zeros(np_ * np_, dtype=f64, device=dev)
+    d_E = torch.zeros(1, dtype=f64, device=dev)
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        neoxc.dev_gam4_fock_factored(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
+    torch.cuda.synchronize(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        neoxc.dev_gam4_fock_factored(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    return a.elapsed_time(b) / steps, float(d_E.item())
+
+
+def factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
+                     d_gee, d_g2s, d_DE, d_DP, elem_ms, elem_E):
+    """The factorised gam_4 Fock build (k_gam4f.cu): same focke/fockp/E as
+    GAM4_DSCF for pair-symmetric tables at O(nebf^4 npbf^2 + nebf^5) work.
+    Reported beside the element-wise number, not instead of it."""
+    ms, E = time_factored(neoxc, torch, dev, stream, ne, np_, d_gee, d_g2s, d_DE, d_DP)
+    t0 = time.perf_counter()
+    n_e2e = 5
+    for _ in range(n_e2e):
+        neoxc.gam4_fock_factored(ne, np_, gee, g2s, DE, DP)
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / n_e2e
+    out = {"api": "neoxc_dev_gam4_fock_factored (device), neoxc_gam4_fock_factored (host arrays)",
+           "nebf": ne, "npbf": np_, "ms_per_build": ms, "e2e_ms_per_build": e2e_ms,
+           "equivalent_gam4_integrals_per_s": ne ** 8 * np_ ** 2 / (ms * 1e-3),
+           "speedup_vs_element_kernel": elem_ms / ms,
+           "E_rel_diff_vs_element_kernel": abs(E - elem_E) / max(abs(elem_E), 1e-300),
+           "kernel_launches_per_build": FACTORED_LAUNCHES}
+    # the larger XCHF shape: tables generated on the device (60 GB of GAM_2s)
+    nl, pl = FACTORED_LARGE
+    n4 = nl ** 4
+    need = 8 * (n4 * pl * pl + 9 * n4)
+    free, _ = torch.cuda.mem_get_info(dev)
+    if free < 1.2 * need:
+        out["large"] = {"nebf": nl, "npbf": pl, "skipped": "needs %.1f GB free" % (need / 1e9)}
+        return out
+    f64 = torch.float64
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2025)
+    lg2s = torch.empty(n4 * pl * pl, dtype=f64, device=dev)
+    for p in range(pl * pl):
+        t = torch.rand((nl,) * 4, generator=gen, dtype=f64, device=dev)
+        lg2s[p * n4:(p + 1) * n4].view((nl,) * 4).copy_(0.5 * (t + t.permute(2, 3, 0, 1)))
+        del t
+    t = torch.rand((nl,) * 4, generator=gen, dtype=f64, device=dev)
+    lgee = (0.5 * (t + t.permute(2, 3, 0, 1))).contiguous().view(-1)
+    del t
+    from neoxc import basis
+    lDE = torch.tensor(np.ascontiguousarray(basis.random_density(nl, 5, 11, 2.0).ravel(order="F")),
+                       dtype=f64, device=dev)
+    lDP = torch.tensor(np.ascontiguousarray(basis.random_density(pl, 1, 12, 1.0).ravel(order="F")),
+                       dtype=f64, device=dev)
+    lms, lE = time_factored(neoxc, torch, dev, stream, nl, pl, lgee, lg2s, lDE, lDP)
+    table_bytes = 8 * n4 * pl * pl
+    # GAM_2s is read twice (G = DP.GAM_2s, fockp = GAM_2s.W): the HBM floor
+    hbm_bytes = 2 * table_bytes
+    peak = read_hbm_peak()
+    out["large"] = {"nebf": nl, "npbf": pl, "ms_per_build": lms,
+                    "equivalent_gam4_integrals_per_s": nl ** 8 * pl * pl / (lms * 1e-3),
+                    "GAM_2s_GB": table_bytes / 1e9,
+                    "roofline": {"bound": "hbm", "algorithmic_bytes": hbm_bytes,
+                                 "achieved": hbm_bytes / (lms * 1e-3) / 1e9, "unit": "GB/s",
+                                 "peak": peak,
+                                 "frac": (hbm_bytes / (lms * 1e-3) / 1e9) / peak if peak else None,
+                                 "note": "whole build timed; bytes = the two passes over GAM_2s"},
+                    "E": lE}
+    del lg2s, lgee
+    torch.cuda.empty_cache()
+    return out
+
+
+def read_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -348,6 +447,8 @@ def main():
                      "flop_per_element": FLOP_PER_ELEMENT,
                      "kernel_ms_mean": mean_ms},
     }
+    line["factored"] = factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
+                                        d_gee, d_g2s, d_DE, d_DP, mean_ms, float(d_E.item()))
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(ne, np_, gee, g2s, DE, DP)
     print(json.dumps(line), flush=True)

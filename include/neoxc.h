@@ -247,6 +247,27 @@ int neoxc_dev_rxchfne_omg2(void* stream, int64_t ne, int64_t np,
                            double* d_FAE, double* d_FP, double* d_FBE,
                            double* d_E);
 
+/* ---- factorised gam_4 Fock build (no routine of its own in the reference) --
+ * Same focke, fockp (accumulated) and E_gam4 (overwritten) as GAM4_DSCF
+ * (gam4_DSCF_OMP.f:2-320, element gam_4_OMP.f:712-1192) for pair-symmetric
+ * tables: gs(p;ab;cd) = gs(p;cd;ab) and (ab|cd) = (cd|ab), which the
+ * reference's GAM2_IC1 (gam2_IC1_OMP.f:141-176) and calc_GAM_ee produce.
+ * Work O(ne^4 np^2 + ne^5) instead of O(ne^8 np^2).  Limits: ne <= 64,
+ * np <= 255.  The host-array entry checks the symmetry (relative 1e-12)
+ * and returns NEOXC_ERR_ARG without computing when it fails; the device
+ * entry does not check.  gam4_dscf_ uses this path when the environment
+ * variable NEOXC_GAM4_FACTORED is "1". */
+int neoxc_gam4_fock_factored(int64_t ne, int64_t np, int64_t ngee,
+                             int64_t ng2, const double* GAM_ee,
+                             const double* GAM_2s, const double* DE,
+                             const double* DP, double* focke, double* fockp,
+                             double* E_gam4);
+int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
+                                 const double* d_GAM_ee,
+                                 const double* d_GAM_2s, const double* d_DE,
+                                 const double* d_DP, double* d_focke,
+                                 double* d_fockp, double* d_E_gam4);
+
 /* ---- diagnostics (no reference counterpart) --------------------------- */
 /* Sustained FP64 FMA throughput of the current device in TFLOP/s (2 FLOP
  * per FMA), the denominator of the FP64 rooflines. */

@@ -525,6 +525,81 @@ int neoxc_gam4_dscf(int64_t NG4CHK, int64_t ne, int64_t np, int64_t ngee,
   return finish(s);
 }
 
+// ---- factorised gam_4 Fock build ----------------------------------------------
+int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
+                                 const double* d_gee, const double* d_g2s,
+                                 const double* d_DE, const double* d_DP,
+                                 double* d_focke, double* d_fockp,
+                                 double* d_E) {
+  RC(need(ne >= 1 && np >= 1, "sizes"));
+  if (ne > kGam4FactMaxNE || np > 255)
+    return set_err(NEOXC_ERR_UNSUPPORTED,
+                   "factorised gam_4 Fock build: ne <= %d, np <= 255",
+                   kGam4FactMaxNE);
+  cudaStream_t s = (cudaStream_t)stream;
+  DBuf scr;
+  RC(dalloc(scr, sizeof(double) * gam4f_scratch_doubles((int)ne, (int)np), s));
+  CU(launch_gam4_factored((int)ne, (int)np, d_gee, d_g2s, d_DE, d_DP,
+                          scr.as<double>(), d_focke, d_fockp, d_E, 1, s));
+  return NEOXC_OK;
+}
+
+int neoxc_gam4_fock_factored(int64_t ne, int64_t np, int64_t ngee,
+                             int64_t ng2, const double* GAM_ee,
+                             const double* GAM_2s, const double* DE,
+                             const double* DP, double* focke, double* fockp,
+                             double* E_gam4) {
+  RC(need(ne >= 1 && np >= 1, "sizes"));
+  if (ne > kGam4FactMaxNE || np > 255)
+    return set_err(NEOXC_ERR_UNSUPPORTED,
+                   "factorised gam_4 Fock build: ne <= %d, np <= 255",
+                   kGam4FactMaxNE);
+  RC(need(ngee == ne * ne * ne * ne, "ngee == ne**4"));
+  RC(need(ng2 == ngee * np * np, "ng2 == ne**4 np**2"));
+  RC(need(GAM_ee && GAM_2s && DE && DP && focke && fockp && E_gam4, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dee, dg2, dde, ddp, dfe, dfp, dE, dchk;
+  RC(upload(dee, GAM_ee, sizeof(double) * ngee, s));
+  RC(upload(dg2, GAM_2s, sizeof(double) * ng2, s));
+  // The factorisation holds for pair-symmetric tables (what GAM2_IC1 and
+  // calc_GAM_ee produce); refuse others instead of returning a different sum.
+  RC(dalloc(dchk, sizeof(double) * 4 * 152 * 16, s));
+  int grid = 0;
+  CU(launch_pair_symmetry_check((int)ne, (int)np, dee.as<double>(),
+                                dg2.as<double>(), dchk.as<double>(), &grid, s));
+  std::vector<double> chk(4 * (size_t)grid);
+  CU(cudaMemcpyAsync(chk.data(), dchk.p, sizeof(double) * chk.size(),
+                     cudaMemcpyDeviceToHost, s));
+  RC(finish(s));
+  double m[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int g = 0; g < grid; g++)
+    for (int k = 0; k < 4; k++) m[k] = chk[4 * g + k] > m[k] ? chk[4 * g + k] : m[k];
+  if (m[0] > 1e-12 * m[1])
+    return set_err(NEOXC_ERR_ARG,
+                   "factorised gam_4: GAM_ee is not symmetric under pair exchange "
+                   "(max |(ab|cd)-(cd|ab)| = %.3e, max |(ab|cd)| = %.3e)", m[0], m[1]);
+  if (m[2] > 1e-12 * m[3])
+    return set_err(NEOXC_ERR_ARG,
+                   "factorised gam_4: GAM_2s is not pair-symmetric (max "
+                   "|gs(p;ab;cd)-gs(p;cd;ab)| = %.3e, max |gs| = %.3e)", m[2], m[3]);
+  RC(upload(dde, DE, sizeof(double) * ne * ne, s));
+  RC(upload(ddp, DP, sizeof(double) * np * np, s));
+  RC(dalloc(dfe, sizeof(double) * ne * ne, s));
+  RC(dalloc(dfp, sizeof(double) * np * np, s));
+  RC(dalloc(dE, sizeof(double), s));
+  CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * ne * ne, s));
+  CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * np * np, s));
+  RC(neoxc_dev_gam4_fock_factored(s, ne, np, dee.as<double>(), dg2.as<double>(),
+                                  dde.as<double>(), ddp.as<double>(),
+                                  dfe.as<double>(), dfp.as<double>(),
+                                  dE.as<double>()));
+  RC(accumulate_back(focke, dfe.as<double>(), ne * ne, s));
+  RC(accumulate_back(fockp, dfp.as<double>(), np * np, s));
+  CU(cudaMemcpyAsync(E_gam4, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
 int neoxc_eg4icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ng4,
                  const double* DE, const double* DP, const double* GM4ICR,
                  double* focke, double* fockp, double* E_gam4) {

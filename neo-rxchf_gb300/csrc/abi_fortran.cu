@@ -67,6 +67,8 @@ extern "C" {
 
 // gam4_DSCF_OMP.f:2-3 GAM4_DSCF(NG4CHK,ne,np,ngee,ng2,ng4,DE,DP,focke,
 // fockp,E_gam4); GAM_ee.ufm / GAM_2s.ufm read as in :46-47.
+// NEOXC_GAM4_FACTORED=1 selects the factorised Fock build (same results for
+// the pair-symmetric tables the reference writes, O(ne^4 np^2 + ne^5)).
 void gam4_dscf_(const int64_t* NG4CHK, const int64_t* ne, const int64_t* np,
                 const int64_t* ngee, const int64_t* ng2, const int64_t* ng4,
                 const double* DE, const double* DP, double* focke,
@@ -74,6 +76,13 @@ void gam4_dscf_(const int64_t* NG4CHK, const int64_t* ne, const int64_t* np,
   std::vector<double> gee, g2s;
   if (!read_ufm("GAM_ee.ufm", *ngee, gee) || !read_ufm("GAM_2s.ufm", *ng2, g2s)) {
     std::fprintf(stderr, "neoxc: gam4_dscf: cannot read GAM_ee.ufm/GAM_2s.ufm\n");
+    return;
+  }
+  const char* fac = std::getenv("NEOXC_GAM4_FACTORED");
+  if (fac && std::strcmp(fac, "1") == 0) {
+    report("gam4_dscf (factorised)",
+           neoxc_gam4_fock_factored(*ne, *np, *ngee, *ng2, gee.data(),
+                                    g2s.data(), DE, DP, focke, fockp, E_gam4));
     return;
   }
   report("gam4_dscf", neoxc_gam4_dscf(*NG4CHK, *ne, *np, *ngee, *ng2, *ng4,

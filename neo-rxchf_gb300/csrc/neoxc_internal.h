@@ -65,6 +65,23 @@ cudaError_t launch_eg4icr(int ne, int np, const double* DE, const double* DP,
                           const double* g4, double* scratch, double* focke,
                           double* fockp, double* E, cudaStream_t s);
 
+// Factorised gam_4 Fock build (k_gam4f.cu): same focke/fockp/E as
+// launch_gam4_dscf for pair-symmetric GAM_ee / GAM_2s, at O(ne^4 np^2 + ne^5).
+// accumulate = 1 adds into focke/fockp; E is always overwritten.
+constexpr int kGam4FactMaxNE = 64;
+size_t gam4f_scratch_doubles(int ne, int np);
+cudaError_t launch_gam4_factored(int ne, int np, const double* gee,
+                                 const double* g2s, const double* DE,
+                                 const double* DP, double* scratch,
+                                 double* focke, double* fockp, double* E,
+                                 int accumulate, cudaStream_t s);
+// Largest |T - T^swap| and |T| over GAM_ee (t=0) and GAM_2s (t=1), where
+// ^swap exchanges the two electron pairs; per-CTA maxima in out[4*grid],
+// returns the grid size used in *grid.
+cudaError_t launch_pair_symmetry_check(int ne, int np, const double* gee,
+                                       const double* g2s, double* out,
+                                       int* grid, cudaStream_t s);
+
 // ---- in-core contractions (gam2_IC1_OMP.f, gam3_IC1_OMP.f, rxchfne) ----
 size_t eg3_partial_doubles(int ne, int np);
 cudaError_t launch_eg3ic1(int ne, int np, const double* DE, const double* DP,

@@ -21,7 +21,8 @@ from .basis import NeoSystem  # noqa: F401  (re-export)
 
 __all__ = [
     "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
-    "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam3_dscf", "gam2_dscf",
+    "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam4_fock_factored",
+    "gam3_dscf", "gam2_dscf",
     "eg4icr", "eg3ic1", "eg2ic1",
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
@@ -59,6 +60,8 @@ def _declare(L):
         "neoxc_gam2_dscf": (I, [i64] * 8 + [d] + [vp] * 23),
         "neoxc_gam4_icr": (I, [i64] * 6 + [vp] * 3),
         "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
+        "neoxc_gam4_fock_factored": (I, [i64] * 4 + [vp] * 7),
+        "neoxc_dev_gam4_fock_factored": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg3ic1": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg2ic1": (I, [i64] * 4 + [vp] * 10),
@@ -263,6 +266,17 @@ def gam4_dscf(ne, np_, gam_ee, gam_2s, DE, DP, focke=None, fockp=None, nchunks=1
     return (*_fock_out(fe, fp, ne, np_), float(E[0]))
 
 
+def gam4_fock_factored(ne, np_, gam_ee, gam_2s, DE, DP, focke=None, fockp=None):
+    """Factorised GAM4_DSCF Fock build (pair-symmetric tables): returns
+    (focke + dF_e, fockp + dF_p, E_gam4)."""
+    ge, g2, de, dp = _f64(gam_ee), _f64(gam_2s), _fmat(DE), _fmat(DP)
+    fe, fp = _fock_io(ne, np_, focke, fockp)
+    E = np.zeros(1)
+    _check(lib().neoxc_gam4_fock_factored(ne, np_, ne ** 4, ne ** 4 * np_ ** 2, _p(ge),
+                                          _p(g2), _p(de), _p(dp), _p(fe), _p(fp), _p(E)))
+    return (*_fock_out(fe, fp, ne, np_), float(E[0]))
+
+
 def eg4icr(ne, np_, DE, DP, gm4, focke=None, fockp=None, nchunks=1):
     """gam4_ICR_OMP.f EG4ICR."""
     g, de, dp = _f64(gm4), _fmat(DE), _fmat(DP)
@@ -350,6 +364,14 @@ def dev_gam4_dscf(stream, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_focke, d_fockp, d
     _check(lib().neoxc_dev_gam4_dscf(C.c_void_p(stream), ne, np_, _tptr(d_gee),
                                      _tptr(d_g2s), _tptr(d_DE), _tptr(d_DP),
                                      _tptr(d_focke), _tptr(d_fockp), _tptr(d_E)))
+
+
+def dev_gam4_fock_factored(stream, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_focke, d_fockp, d_E):
+    """Enqueue the factorised gam_4 Fock build on ``stream`` (pair-symmetric
+    tables, not checked); all arrays are torch float64 CUDA tensors."""
+    _check(lib().neoxc_dev_gam4_fock_factored(C.c_void_p(stream), ne, np_, _tptr(d_gee),
+                                              _tptr(d_g2s), _tptr(d_DE), _tptr(d_DP),
+                                              _tptr(d_focke), _tptr(d_fockp), _tptr(d_E)))
 
 
 def dev_eg3ic1(stream, ne, np_, d_DE, d_DP, d_g3, d_focke, d_fockp, d_E):

@@ -86,6 +86,95 @@ def test_gam4_dscf_icr_eg4(nx, orc, seed, ne, np_):
     assert_close_scaled(fmat(fe2), rfe, RTOL, "focke (EG4ICR)")
 
 
+# ------------------------------------------------- factorised gam_4 Fock build
+def _pair_symmetric_tables(rng, ne, np_):
+    """Random tables with the symmetry of the reference's inputs:
+    gs(p; ab; cd) = gs(p; cd; ab) (GAM2_IC1 pair symmetrisation) and
+    (ab|cd) = (cd|ab) (ERIs)."""
+    gs = rng.standard_normal((np_, np_, ne, ne, ne, ne))
+    gs = 0.5 * (gs + gs.transpose(0, 1, 4, 5, 2, 3))
+    ee = rng.standard_normal((ne,) * 4)
+    ee = 0.5 * (ee + ee.transpose(2, 3, 0, 1))
+    return np.ascontiguousarray(ee.ravel()), np.ascontiguousarray(gs.ravel())
+
+
+@pytest.mark.parametrize("seed,ne,np_", [(51, 3, 2), (52, 4, 1), (53, 5, 2), (54, 2, 3)])
+def test_gam4_fock_factored_vs_oracle(nx, orc, seed, ne, np_):
+    """The factorised build reproduces the oracle's element-wise GAM4_DSCF
+    (all ne^8 np^2 elements) on pair-symmetric tables, accumulating into
+    pre-filled Fock matrices."""
+    rng = np.random.default_rng(seed)
+    gee, g2s = _pair_symmetric_tables(rng, ne, np_)
+    DE, DP = _dens(ne, max(2, ne // 2), seed), _dens(np_, 1, seed + 1, 1.0)
+    fe0, fp0 = rng.standard_normal((ne, ne)), rng.standard_normal((np_, np_))
+    fe, fp, E = nx.gam4_fock_factored(ne, np_, gee, g2s, DE, DP, fe0, fp0)
+    O, L = orc, orc.lib()
+    rfe, rfp, rE = fmat(fe0), fmat(fp0), np.zeros(1)
+    L.orc_gam4_dscf_range(ne, np_, O.ptr(gee), O.ptr(g2s), O.ptr(fmat(DE)), O.ptr(fmat(DP)),
+                          0, ne ** 8 * np_ ** 2, O.ptr(rfe), O.ptr(rfp), O.ptr(rE))
+    assert E == pytest.approx(rE[0], rel=RTOL, abs=1e-12)
+    assert_close_scaled(fmat(fe), rfe, RTOL, "focke (factorised)")
+    assert_close_scaled(fmat(fp), rfp, RTOL, "fockp (factorised)")
+
+
+@pytest.mark.parametrize("ne,np_", [(8, 3), (12, 2)])
+def test_gam4_fock_factored_vs_element_kernel(nx, ne, np_):
+    """Against the GPU element-wise kernel at sizes beyond the oracle's reach;
+    the two sum ~1e9-1e10 terms in different orders, so the check is against
+    the matrices' scale."""
+    rng = np.random.default_rng(60 + ne)
+    gee, g2s = _pair_symmetric_tables(rng, ne, np_)
+    DE, DP = _dens(ne, 3, ne), _dens(np_, 1, ne + 1, 1.0)
+    a = nx.gam4_fock_factored(ne, np_, gee, g2s, DE, DP)
+    b = nx.gam4_dscf(ne, np_, gee, g2s, DE, DP)
+    for x, y, w in ((a[0], b[0], "focke"), (a[1], b[1], "fockp")):
+        scale = np.abs(y).max()
+        assert np.abs(x - y).max() <= 1e-10 * scale, w
+    assert a[2] == pytest.approx(b[2], rel=1e-10)
+
+
+def test_gam4_fock_factored_xchf_example(nx, xchf, golden_xchf):
+    """examples/xchf through the factorised build: GAM_ee and GAM_2s from the
+    GPU builders at the guessCE density give E_GAM4 of XCHF.log:315."""
+    s, DE, DP = xchf["sys"], xchf["DE0"], xchf["DP0"]
+    gee = nx.calc_gam_ee(s)
+    _, g2s = nx.gam2_ic1(s)
+    E4 = nx.gam4_fock_factored(s.nebf, s.npbf, gee, g2s, DE, DP)[2]
+    assert abs(E4 - golden_xchf["initial"]["E_GAM4"]) <= 6e-11
+
+
+def test_gam4_fock_factored_properties_large(nx):
+    """nebf=40, npbf=6: E is linear in DP and quartic in DE, E = sum DP fockp,
+    and sum DE focke = 4 E (focke is dE/dDE)."""
+    ne, np_ = 40, 6
+    rng = np.random.default_rng(7)
+    gee, g2s = _pair_symmetric_tables(rng, ne, np_)
+    DE, DP = _dens(ne, 5, 8), _dens(np_, 1, 9, 1.0)
+    fe, fp, E = nx.gam4_fock_factored(ne, np_, gee, g2s, DE, DP)
+    assert np.isfinite(E) and abs(E) > 0
+    assert float((DP * fp).sum()) == pytest.approx(E, rel=1e-12)
+    E2 = nx.gam4_fock_factored(ne, np_, gee, g2s, DE, 2.0 * DP)[2]
+    assert E2 == pytest.approx(2.0 * E, rel=1e-12)
+    E3 = nx.gam4_fock_factored(ne, np_, gee, g2s, 0.5 * DE, DP)[2]
+    assert E3 == pytest.approx(E / 16.0, rel=1e-12)
+    # focke is dE/dDE: DE-weighted trace gives 4 E (degree-4 homogeneity)
+    assert float((DE * fe).sum()) == pytest.approx(4.0 * E, rel=1e-10)
+
+
+def test_gam4_fock_factored_rejects_asymmetric_tables(nx):
+    rng = np.random.default_rng(3)
+    ne, np_ = 3, 2
+    gee, g2s = _pair_symmetric_tables(rng, ne, np_)
+    bad = g2s.copy()
+    bad[5] += 1e-3
+    with pytest.raises(nx.NeoxcError, match="GAM_2s is not pair-symmetric"):
+        nx.gam4_fock_factored(ne, np_, gee, bad, np.eye(ne), np.eye(np_))
+    bad = gee.copy()
+    bad[7] += 1e-3
+    with pytest.raises(nx.NeoxcError, match="GAM_ee is not symmetric"):
+        nx.gam4_fock_factored(ne, np_, bad, g2s, np.eye(ne), np.eye(np_))
+
+
 def test_gam4_dscf_deterministic(nx):
     rng = np.random.default_rng(5)
     ne, np_ = 6, 2
