@@ -268,6 +268,41 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
                                  const double* d_DP, double* d_focke,
                                  double* d_fockp, double* d_E_gam4);
 
+/* ---- XCHF RHF SCF on the device ----------------------------------------------
+ * xchf1_independent/xcscf.f:2-658 xcscf (the plain Roothaan branch; SOSCF is
+ * not provided) with xchf1_fock.f:2-361 as the Fock build: builds every
+ * integral on the GPU (overlaps and core Hamiltonians, pure_ovlap.f and
+ * gam_epcore.f; GAM_ep, gam_ep.f; GAM_1/GAM_1s, gam_1_OMP.f; GAM_ee,
+ * gam_ee.f; GM2ICR/GM2sICR and GM3ICR in core), then iterates: Fock build
+ * -> ROOTHAN for the nucleus (state nucst) -> Fock build -> ROOTHAN for the
+ * electrons, until max|dDE| < 1e-6 (and max|dDP| < 1e-4 when npbf > 1), as
+ * xcscf does.  gam_4 uses the factorised Fock build unless
+ * NEOXC_SCF_GAM4_ELEMENT selects the element-wise GAM4_DSCF.
+ *   DE (in: initial electronic density, e.g. from guessCE; out: converged)
+ *   DP (in: initial nuclear density unless NEOXC_SCF_GUESS_PROT; out)
+ *   E_init[16], E_final[16]: energy slots 0 E_total 1 E_nuc 2 E_ecore
+ *     3 E_pcore 4 E_ep 5 E_ee 6 E_gam1 7 E_gam2 8 E_gam3 9 E_gam4 10 S_total
+ *     11 S_gam1 12 S_gam2 13 H_expect 14 max|dDE| 15 max|dDP| of the first
+ *     and of the last Fock build ("INITIAL GUESS" / final energetics).
+ *   history[4*maxit] (may be NULL): per iteration E_total, its change,
+ *     max|dDE|, max|dDP|.
+ *   niter, converged: iterations run and 1 when the thresholds were met.
+ * Limits: nebf, npbf <= 64; with gam_3 (nelec > 2) nebf <= 20. */
+#define NEOXC_SCF_GUESS_PROT 1     /* DP from the nuclear core Hamiltonian */
+#define NEOXC_SCF_GAM4_ELEMENT 4   /* element-wise GAM4_DSCF for gam_4     */
+int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
+                   int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
+                   const double* cat, const double* zan, const double* bcoef1,
+                   const double* gamma1, const int64_t* KPESTR,
+                   const int64_t* KPEEND, const int64_t* AMPEB2C,
+                   const double* AGEBFCC, const double* AGNBFCC,
+                   const double* ELCEX, const double* NUCEX,
+                   const int64_t* ELCAM, const int64_t* NUCAM,
+                   const double* ELCBFC, const double* NUCBFC, int64_t options,
+                   int64_t maxit, double* DE, double* DP, double* E_init,
+                   double* E_final, double* history, int64_t* niter,
+                   int64_t* converged);
+
 /* ---- diagnostics (no reference counterpart) --------------------------- */
 /* Sustained FP64 FMA throughput of the current device in TFLOP/s (2 FLOP
  * per FMA), the denominator of the FP64 rooflines. */

@@ -7,7 +7,9 @@
 // compute path: if CUDA is unusable the call returns NEOXC_ERR_CUDA.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -957,5 +959,197 @@ int neoxc_gam2_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   return NEOXC_OK;
 }
 
-}  // extern "C"
+// ---- XCHF RHF SCF on the device (xchf1_independent/xcscf.f:2-658) ----------
+// class_nuc_rep.f:2-45
+static double nuc_rep(int64_t nat, const double* zan, const double* cat) {
+  double E = 0.0;
+  for (int64_t i = 1; i < nat; i++)
+    for (int64_t j = 0; j < i; j++) {
+      double R2 = 0.0;
+      for (int k = 0; k < 3; k++) {
+        const double d = cat[3 * i + k] - cat[3 * j + k];
+        R2 = R2 + d * d;
+      }
+      if (R2 != 0.0) E = E + zan[i] * zan[j] / sqrt(R2);
+    }
+  return E;
+}
 
+int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
+                   int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
+                   const double* cat, const double* zan, const double* bcoef1,
+                   const double* gamma1, const int64_t* KPESTR,
+                   const int64_t* KPEEND, const int64_t* AMPEB2C,
+                   const double* AGEBFCC, const double* AGNBFCC,
+                   const double* ELCEX, const double* NUCEX,
+                   const int64_t* ELCAM, const int64_t* NUCAM,
+                   const double* ELCBFC, const double* NUCBFC, int64_t options,
+                   int64_t maxit, double* DE, double* DP, double* E_init,
+                   double* E_final, double* history, int64_t* niter,
+                   int64_t* converged) {
+  (void)AMPEB2C;
+  RC(need(nelec >= 1 && maxit >= 1, "nelec >= 1, maxit >= 1"));
+  RC(need(nucst >= 1 && nucst <= npbf, "1 <= nucst <= npbf"));
+  RC(need(DE && DP && E_init && E_final && niter && converged, "pointers"));
+  RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_GAM4_ELEMENT)) == 0,
+          "options"));
+  if (nebf > kScfMaxN || npbf > kScfMaxN)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "XCHF SCF: nebf, npbf <= %d", kScfMaxN);
+  const bool elem4 = (options & NEOXC_SCF_GAM4_ELEMENT) != 0;
+  if (nelec > 2 && nebf > 20)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "XCHF SCF with gam_3: nebf <= 20");
+  if (nelec > 2 && elem4 && nebf > kGam4MaxNE)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "element-wise gam_4: nebf <= %d", kGam4MaxNE);
+  cudaStream_t s;
+  RC(get_stream(&s));
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
+                  gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
+                  NUCAM, ELCBFC, NUCBFC));
+  const int ne = (int)nebf, np = (int)npbf;
+  const size_t e2 = (size_t)ne * ne, p2 = (size_t)np * np;
+  const size_t ng1 = e2 * p2, ng2 = e2 * e2 * p2;
+  const size_t ng3 = nelec > 2 ? e2 * e2 * e2 * p2 : 0;
+  // integrals
+  DBuf Se, Sp, Hce, Hcp, Gep, G1, G1s, Gee, G2, G2s, G3;
+  RC(dalloc(Se, sizeof(double) * e2, s));
+  RC(dalloc(Sp, sizeof(double) * p2, s));
+  RC(dalloc(Hce, sizeof(double) * e2, s));
+  RC(dalloc(Hcp, sizeof(double) * p2, s));
+  RC(dalloc(Gep, sizeof(double) * ng1, s));
+  RC(dalloc(G1, sizeof(double) * ng1, s));
+  RC(dalloc(G1s, sizeof(double) * ng1, s));
+  RC(dalloc(Gee, sizeof(double) * e2 * e2, s));
+  RC(dalloc(G2, sizeof(double) * (nelec > 1 ? ng2 : 1), s));
+  RC(dalloc(G2s, sizeof(double) * (nelec > 1 ? ng2 : 1), s));
+  RC(dalloc(G3, sizeof(double) * (ng3 ? ng3 : 1), s));
+  CU(launch_scf_onebody(u.d, Se.as<double>(), Sp.as<double>(), Hce.as<double>(),
+                        Hcp.as<double>(), s));
+  CU(launch_gam_ep(u.d, Gep.as<double>(), s));
+  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s));
+  CU(launch_gam_ee(u.d, Gee.as<double>(), s));
+  if (nelec > 1) {
+    CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s));
+    CU(launch_gam2_symmetrize(ne, np, 0, G2.as<double>(), G2s.as<double>(), s));
+  }
+  if (nelec > 2) {
+    CU(launch_gam3_raw(u.d, G3.as<double>(), s));
+    CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
+  }
+  // SCF state
+  DBuf dDE, dDP, DE0, DP0, fe, fp, se1, sp1, se2, sp2, Xe, Xp, en, part, scr, st;
+  RC(upload(dDE, DE, sizeof(double) * e2, s));
+  RC(dalloc(dDP, sizeof(double) * p2, s));
+  RC(dalloc(DE0, sizeof(double) * e2, s));
+  RC(dalloc(DP0, sizeof(double) * p2, s));
+  for (DBuf* b : {&fe, &se1, &se2}) RC(dalloc(*b, sizeof(double) * e2, s));
+  for (DBuf* b : {&fp, &sp1, &sp2}) RC(dalloc(*b, sizeof(double) * p2, s));
+  RC(dalloc(Xe, sizeof(double) * e2, s));
+  RC(dalloc(Xp, sizeof(double) * p2, s));
+  RC(dalloc(en, sizeof(double) * kScfSlots, s));
+  RC(dalloc(part, sizeof(double) * scf_fock1_part_doubles(ne, np), s));
+  size_t nscr = 1;
+  if (nelec > 1) nscr = std::max(nscr, eg2_partial_doubles(ne, np));
+  if (nelec > 2) {
+    nscr = std::max(nscr, eg3_partial_doubles(ne, np));
+    nscr = std::max(nscr, elem4 ? gam4_partial_doubles(ne, np)
+                                : gam4f_scratch_doubles(ne, np));
+  }
+  RC(dalloc(scr, sizeof(double) * nscr, s));
+  RC(dalloc(st, sizeof(int) * 4, s));
+  CU(cudaMemsetAsync(DE0.p, 0, sizeof(double) * e2, s));
+  CU(cudaMemsetAsync(DP0.p, 0, sizeof(double) * p2, s));
+  CU(cudaMemsetAsync(se2.p, 0, sizeof(double) * e2, s));
+  CU(cudaMemsetAsync(sp2.p, 0, sizeof(double) * p2, s));
+  CU(cudaMemsetAsync(st.p, 0, sizeof(int) * 4, s));
+  CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kScfSlots, s));
+  const double Enuc = nuc_rep(nat, zan, cat);
+  CU(cudaMemcpyAsync(en.as<double>() + 1, &Enuc, sizeof(double),
+                     cudaMemcpyHostToDevice, s));
+  int* sts = st.as<int>();
+  CU(launch_inv_sqrt(ne, Se.as<double>(), Xe.as<double>(), sts + 0, s));
+  CU(launch_inv_sqrt(np, Sp.as<double>(), Xp.as<double>(), sts + 1, s));
+  const int noccE = nelec > 1 ? (int)(nelec / 2) : 1;
+  const double prefE = nelec > 1 ? 2.0 : 1.0;
+  if (options & NEOXC_SCF_GUESS_PROT) {
+    // guess_prot (xcscf.f:683-716): diagonalise the nuclear core Hamiltonian
+    CU(launch_roothan(np, Hcp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1,
+                      1.0, dDP.as<double>(), nullptr, nullptr, sts + 3, s));
+  } else {
+    CU(cudaMemcpyAsync(dDP.p, DP, sizeof(double) * p2, cudaMemcpyHostToDevice, s));
+  }
+  double* d_en = en.as<double>();
+  auto fock_build = [&]() -> int {
+    CU(launch_scf_fock1(ne, np, (int)nelec, Hce.as<double>(), Hcp.as<double>(),
+                        Gep.as<double>(), G1.as<double>(), G1s.as<double>(),
+                        Gee.as<double>(), dDE.as<double>(), dDP.as<double>(),
+                        fe.as<double>(), fp.as<double>(), se1.as<double>(),
+                        sp1.as<double>(), part.as<double>(), d_en, s));
+    if (nelec > 1)
+      CU(launch_eg2ic1(ne, np, dDE.as<double>(), dDP.as<double>(), G2.as<double>(),
+                       G2s.as<double>(), scr.as<double>(), fe.as<double>(),
+                       se2.as<double>(), fp.as<double>(), sp2.as<double>(),
+                       d_en + 7, d_en + 12, s));
+    if (nelec > 2) {
+      CU(launch_eg3ic1(ne, np, dDE.as<double>(), dDP.as<double>(), G3.as<double>(),
+                       scr.as<double>(), fe.as<double>(), fp.as<double>(),
+                       d_en + 8, s));
+      if (elem4)
+        CU(launch_gam4_dscf(ne, np, Gee.as<double>(), G2s.as<double>(),
+                            dDE.as<double>(), dDP.as<double>(), scr.as<double>(),
+                            fe.as<double>(), fp.as<double>(), d_en + 9, s));
+      else
+        CU(launch_gam4_factored(ne, np, Gee.as<double>(), G2s.as<double>(),
+                                dDE.as<double>(), dDP.as<double>(),
+                                scr.as<double>(), fe.as<double>(),
+                                fp.as<double>(), d_en + 9, 1, s));
+    }
+    CU(launch_scf_assemble(ne, np, d_en, se1.as<double>(), sp1.as<double>(),
+                           se2.as<double>(), sp2.as<double>(), fe.as<double>(),
+                           fp.as<double>(), s));
+    return NEOXC_OK;
+  };
+  const double tolE = 1.0e-6, tolP = 1.0e-4;   // xcscf.f TOLE, TOLP
+  double Eold = 0.0;
+  int64_t it = 0;
+  bool done = false;
+  for (it = 1; it <= maxit && !done; it++) {
+    RC(fock_build());
+    if (it == 1) {
+      CU(cudaMemcpyAsync(E_init, d_en, sizeof(double) * kScfSlots,
+                         cudaMemcpyDeviceToHost, s));
+    }
+    CU(launch_roothan(np, fp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
+                      dDP.as<double>(), nullptr, nullptr, sts + 1, s));
+    RC(fock_build());
+    CU(launch_roothan(ne, fe.as<double>(), Xe.as<double>(), 0, noccE, prefE,
+                      dDE.as<double>(), nullptr, nullptr, sts + 0, s));
+    CU(launch_dendif(ne, np, dDE.as<double>(), DE0.as<double>(), dDP.as<double>(),
+                     DP0.as<double>(), d_en, s));
+    double h[kScfSlots];
+    int hs[4];
+    CU(cudaMemcpyAsync(h, d_en, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    RC(finish(s));
+    for (int k = 0; k < 4; k++)
+      if (hs[k] > 40)
+        return set_err(NEOXC_ERR_CUDA, "ROOTHAN: Jacobi eigensolver did not converge");
+    if (history) {
+      history[4 * (it - 1) + 0] = h[0];
+      history[4 * (it - 1) + 1] = h[0] - Eold;
+      history[4 * (it - 1) + 2] = h[14];
+      history[4 * (it - 1) + 3] = h[15];
+    }
+    Eold = h[0];
+    for (int k = 0; k < kScfSlots; k++) E_final[k] = h[k];
+    done = npbf > 1 ? (h[14] < tolE && h[15] < tolP) : (h[14] < tolE);
+    if (done) *niter = it;
+  }
+  if (!done) *niter = maxit;
+  *converged = done ? 1 : 0;
+  CU(cudaMemcpyAsync(DE, dDE.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(DP, dDP.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+}  // extern "C"

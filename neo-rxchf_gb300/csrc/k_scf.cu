@@ -1,0 +1,619 @@
+// k_scf.cu -- device side of the XCHF RHF SCF (xchf1_independent/xcscf.f,
+// xchf1_fock.f) for sm_103a: the one- and two-particle integrals besides
+// gam_2/3/4, the Fock/energy assembly, ROOTHAN with a block-parallel Jacobi
+// eigensolver, and the density-change check.  Every kernel takes device
+// pointers; energies and convergence scalars live in a device array so an
+// SCF iteration needs no host round trip except the final 3-scalar read.
+//
+// Device energy slots (en[]):
+//   0 E_total 1 E_nuc 2 E_ecore 3 E_pcore 4 E_ep 5 E_ee 6 E_gam1 7 E_gam2
+//   8 E_gam3 9 E_gam4 10 S_total 11 S_gam1 12 S_gam2 13 H_expect
+//   14 max|DE-DE0| 15 max|DP-DP0|
+// Matrices (DE, DP, focke, fockp, se*, sp*, S, X) are column-major like the
+// reference's Fortran arrays; the core matrices keep pack_2D order
+// ([i][j] = GAM_ecore(pack_2D(n,j,i))) and GAM_ep / GAM_1 / GAM_1s keep
+// pack_4D(nebf,nebf,npbf, je,ie,jp,ip) order, i.e. C-order [ip][jp][ie][je].
+#include "md_math.cuh"
+#include "neoxc_internal.h"
+
+namespace neoxc {
+namespace {
+
+using md::Prim;
+
+__device__ __forceinline__ Prim to_prim(const DevPrim& p) {
+  Prim r;
+  r.a = p.a;
+  for (int d = 0; d < 3; d++) {
+    r.c[d] = p.c[d];
+    r.l[d] = p.l[d];
+  }
+  return r;
+}
+
+__device__ __forceinline__ double gfovlap(const Prim& A, const Prim& B) {
+  double s = 1.0;
+  for (int d = 0; d < 3; d++) s *= md::ovl1d(A.l[d], A.a, A.c[d], B.l[d], B.a, B.c[d]);
+  return s;
+}
+
+// gam_epcore.f:200-270 xcalc_GAM_epcore
+__device__ __noinline__ double xcalc_epcore(const Prim& A, const Prim& B,
+                                            const DevSystem& S, double xmass,
+                                            double coul_sign) {
+  const double ke = md::gfke(A, B, xmass);
+  double v = 0.0;
+  for (int k = 0; k < S.nat; k++) {
+    const double C[3] = {S.cat[3 * k], S.cat[3 * k + 1], S.cat[3 * k + 2]};
+    v = v + coul_sign * S.zan[k] * md::gfvec(A, B, C);
+  }
+  return ke + v;
+}
+
+// ---- overlaps and core Hamiltonians (pure_ovlap.f, gam_epcore.f) ----------
+// t < ne^2: electronic pair (i,j); then np^2 nuclear pairs.  Sums over the
+// primitive pairs in the reference's order (bra primitive outer).
+__global__ void onebody_kernel(DevSystem S, double* __restrict__ Se,
+                               double* __restrict__ Sp, double* __restrict__ Hce,
+                               double* __restrict__ Hcp) {
+  const int ne = S.nebf, np = S.npbf;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ne * ne) {
+    const int i = t / ne, j = t - i * ne;
+    double so = 0.0, h = 0.0;
+    for (int a = S.kpestr[i]; a <= S.kpeend[i]; a++)
+      for (int b = S.kpestr[j]; b <= S.kpeend[j]; b++) {
+        const Prim A = to_prim(S.eprim[a]), B = to_prim(S.eprim[b]);
+        const double c = S.eprim[a].coef, d = S.eprim[b].coef;
+        so = so + gfovlap(A, B) * c * d;
+        h = h + xcalc_epcore(A, B, S, 1.0, -1.0) * c * d;
+      }
+    Se[i * ne + j] = so;   // pack_2D(ne, j, i) order; symmetric
+    Hce[i * ne + j] = h;
+  } else if (t < ne * ne + np * np) {
+    const int k = t - ne * ne, p = k / np, q = k - p * np;
+    const Prim A = to_prim(S.pprim[p]), B = to_prim(S.pprim[q]);
+    const double c = S.pprim[p].coef, d = S.pprim[q].coef;
+    Sp[p * np + q] = gfovlap(A, B) * c * d;
+    Hcp[p * np + q] = xcalc_epcore(A, B, S, S.pmass, 1.0) * c * d;
+  }
+}
+
+// ---- GAM_ep (gam_ep.f:2-219): -(e p | e' p'), C-order [ip][jp][ie][je] ----
+__global__ void gam_ep_kernel(DevSystem S, double* __restrict__ Gep) {
+  const int ne = S.nebf, np = S.npbf;
+  const int total = np * np * ne * ne;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int r = t;
+  const int je = r % ne; r /= ne;
+  const int ie = r % ne; r /= ne;
+  const int jp = r % np; r /= np;
+  const int ip = r;
+  const Prim P1 = to_prim(S.pprim[ip]), P2 = to_prim(S.pprim[jp]);
+  const double cp = S.pprim[ip].coef, cq = S.pprim[jp].coef;
+  double acc = 0.0;
+  for (int a = S.kpestr[ie]; a <= S.kpeend[ie]; a++)
+    for (int b = S.kpestr[je]; b <= S.kpeend[je]; b++) {
+      const double v = -md::gfvee(to_prim(S.eprim[a]), P1, to_prim(S.eprim[b]), P2);
+      acc = acc + v * cp * cq * S.eprim[a].coef * S.eprim[b].coef;
+    }
+  Gep[t] = acc;
+}
+
+// ---- gam_1 (gam_1_OMP.f:398-836 xcalc_GAM1_MD) -----------------------------
+// A = (e, p), B = (e', p'); returns ansE, ansS.
+__device__ __noinline__ void xcalc_gam1(const Prim* A, const Prim* B,
+                                        const DevSystem& S, double* ansE,
+                                        double* ansS) {
+  const double zero = 0.0, one = 1.0, pmass = S.pmass;
+  double tegx = zero, tpgx = zero, texg = zero, tpxg = zero, tegg = zero,
+         tpgg = zero, VCEGX = zero, VCEGG = zero, VCPGX = zero, VCPGG = zero,
+         VMGX = zero, VMGG = zero;
+  for (int k = 0; k < S.ngtg; k++) {
+    const double GV = S.ggem[k], BV = S.bgem[k];
+    tegx = tegx + BV * md::pgike1(A[0], A[1], B[0], B[1], GV, zero, one);
+    tpgx = tpgx + BV * md::pgike1(A[1], A[0], B[1], B[0], GV, zero, pmass);
+    double ve = zero, vp = zero;
+    for (int c = 0; c < S.nat; c++) {
+      const double C[3] = {S.cat[3 * c], S.cat[3 * c + 1], S.cat[3 * c + 2]};
+      ve = md::g2_xggvec(A[0], A[1], B[0], B[1], GV, zero, C) * S.zan[c] + ve;
+      vp = md::g2_xggvec(A[1], A[0], B[1], B[0], GV, zero, C) * S.zan[c] + vp;
+    }
+    const double vm = md::g2_xggvee(A[0], A[1], B[0], B[1], GV, zero);
+    VCEGX = VCEGX + BV * ve;
+    VCPGX = VCPGX + BV * vp;
+    VMGX = VMGX + BV * vm;
+    texg = texg + BV * md::pgike1(A[0], A[1], B[0], B[1], zero, GV, one);
+    tpxg = tpxg + BV * md::pgike1(A[1], A[0], B[1], B[0], zero, GV, pmass);
+    for (int l = 0; l < S.ngtg; l++) {
+      const double GW = S.ggem[l], BW = S.bgem[l];
+      tegg = tegg + BV * BW * md::pgike1(A[0], A[1], B[0], B[1], GV, GW, one);
+      tpgg = tpgg + BV * BW * md::pgike1(A[1], A[0], B[1], B[0], GV, GW, pmass);
+      double vee = zero, vpp = zero;
+      for (int c = 0; c < S.nat; c++) {
+        const double C[3] = {S.cat[3 * c], S.cat[3 * c + 1], S.cat[3 * c + 2]};
+        vee = md::g2_xggvec(A[0], A[1], B[0], B[1], GV, GW, C) * S.zan[c] + vee;
+        vpp = md::g2_xggvec(A[1], A[0], B[1], B[0], GV, GW, C) * S.zan[c] + vpp;
+      }
+      const double vmm = md::g2_xggvee(A[0], A[1], B[0], B[1], GV, GW);
+      VCEGG = VCEGG + BV * BW * vee;
+      VCPGG = VCPGG + BV * BW * vpp;
+      VMGG = VMGG + BV * BW * vmm;
+    }
+  }
+  const double TE = tegx + texg + tegg, TP = tpgx + tpxg + tpgg;
+  const double VCE = 2.0 * VCEGX + VCEGG, VCP = 2.0 * VCPGX + VCPGG;
+  const double VMX = 2.0 * VMGX + VMGG;
+  *ansE = TE + TP - VCE + VCP - VMX;
+  double OGX = zero, OGG = zero;
+  for (int k = 0; k < S.ngtg; k++) {
+    const double GV = S.ggem[k], BV = S.bgem[k];
+    OGX = OGX + BV * md::g2_xggs(A[0], A[1], B[0], B[1], GV, zero);
+    for (int l = 0; l < S.ngtg; l++)
+      OGG = OGG + BV * S.bgem[l] * md::g2_xggs(A[0], A[1], B[0], B[1], GV, S.ggem[l]);
+  }
+  *ansS = 2.0 * OGX + OGG;
+}
+
+// One warp per contracted (ip, jp, ie, je); lanes take primitive pairs and
+// the warp sums them in a fixed shuffle order (deterministic).
+__global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
+                            double* __restrict__ G1s) {
+  const int ne = S.nebf, np = S.npbf;
+  const int total = np * np * ne * ne;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (w >= total) return;
+  int r = w;
+  const int je = r % ne; r /= ne;
+  const int ie = r % ne; r /= ne;
+  const int jp = r % np; r /= np;
+  const int ip = r;
+  const int na = S.kpeend[ie] - S.kpestr[ie] + 1;
+  const int nb = S.kpeend[je] - S.kpestr[je] + 1;
+  double e = 0.0, sv = 0.0;
+  for (int k = lane; k < na * nb; k += 32) {
+    const int a = S.kpestr[ie] + k / nb, b = S.kpestr[je] + k % nb;
+    Prim A[2], B[2];
+    A[0] = to_prim(S.eprim[a]);
+    A[1] = to_prim(S.pprim[ip]);
+    B[0] = to_prim(S.eprim[b]);
+    B[1] = to_prim(S.pprim[jp]);
+    double aE, aS;
+    xcalc_gam1(A, B, S, &aE, &aS);
+    const double cip = S.pprim[ip].coef, cjp = S.pprim[jp].coef;
+    const double cie = S.eprim[a].coef, cje = S.eprim[b].coef;
+    e = e + aE * cip * cjp * cie * cje;
+    sv = sv + aS * cip * cjp * cie * cje;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_down_sync(0xffffffffu, e, o);
+    sv += __shfl_down_sync(0xffffffffu, sv, o);
+  }
+  if (lane == 0) {
+    G1[w] = e;
+    G1s[w] = sv;
+  }
+}
+
+// ---- one-body part of xchf1_fock (E_from_GAM_ecore/pcore/ep/ee/1, S_from_GAM_1s)
+// t < ne^2 : electronic (i,j);  ne^2 <= t < ne^2+np^2 : nuclear (p,q).
+// part[c*nt + t]: c = 0 E_ecore, 1 E_pcore, 2 E_ep, 3 E_ee, 4 E_gam1, 5 S_gam1.
+__global__ void fock1_kernel(int ne, int np, int nelec,
+                             const double* __restrict__ Hce,
+                             const double* __restrict__ Hcp,
+                             const double* __restrict__ Gep,
+                             const double* __restrict__ G1,
+                             const double* __restrict__ G1s,
+                             const double* __restrict__ Gee,
+                             const double* __restrict__ DE,
+                             const double* __restrict__ DP,
+                             double* __restrict__ focke, double* __restrict__ fockp,
+                             double* __restrict__ se1, double* __restrict__ sp1,
+                             double* __restrict__ part) {
+  const int nt = ne * ne + np * np;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const int n2 = ne * ne;
+  double e[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (t < n2) {
+    const int i = t / ne, j = t - i * ne;
+    const double fc = Hce[i * ne + j];
+    double fep = 0.0, fg1 = 0.0, s1 = 0.0;
+    for (int p = 0; p < np; p++)
+      for (int q = 0; q < np; q++) {
+        const double dp = DP[p + np * q];
+        const long long o = ((long long)(p * np + q) * ne + i) * ne + j;
+        fep = fep + dp * Gep[o];
+        fg1 = fg1 + dp * G1[o];
+        s1 = s1 + dp * G1s[o];
+      }
+    double fee = 0.0;
+    if (nelec > 1) {
+      for (int k = 0; k < ne; k++)
+        for (int l = 0; l < ne; l++) {
+          const double v1 = Gee[(((long long)i * ne + j) * ne + k) * ne + l];
+          const double v2 = Gee[(((long long)i * ne + l) * ne + k) * ne + j];
+          fee = fee + 2.0 * DE[k + ne * l] * ((v1 - 0.5 * v2) * 0.5);
+        }
+    }
+    focke[i + ne * j] = fc + fep + fee + fg1;
+    se1[i + ne * j] = s1;
+    const double d = DE[i + ne * j];
+    e[0] = d * fc;
+    e[2] = d * fep;
+    e[3] = d * (0.5 * fee);
+    e[4] = d * fg1;
+    e[5] = d * s1;
+  } else {
+    const int k = t - n2, p = k / np, q = k - p * np;
+    const double fc = Hcp[p * np + q];
+    double fep = 0.0, fg1 = 0.0, s1 = 0.0;
+    for (int i = 0; i < ne; i++)
+      for (int j = 0; j < ne; j++) {
+        const double de = DE[i + ne * j];
+        const long long o = ((long long)(p * np + q) * ne + i) * ne + j;
+        fep = fep + de * Gep[o];
+        fg1 = fg1 + de * G1[o];
+        s1 = s1 + de * G1s[o];
+      }
+    fockp[p + np * q] = fc + fep + fg1;
+    sp1[p + np * q] = s1;
+    e[1] = DP[p + np * q] * fc;
+  }
+  for (int c = 0; c < 6; c++) part[(long long)c * nt + t] = e[c];
+}
+
+__device__ double block_sum(double v, double* sw) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sw[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int k = 0; k < (int)(blockDim.x + 31) / 32; k++) r += sw[k];
+  return r;   // every thread gets the same value
+}
+
+// en[2..6], en[11] from the partials; the later slots (gam_2..4) are zeroed
+// here and filled by their contractions when the electron count has them.
+__global__ void fock1_energy_kernel(int nt, const double* __restrict__ part,
+                                    double* __restrict__ en) {
+  __shared__ double sw[32];
+  const int slot[6] = {2, 3, 4, 5, 6, 11};
+  for (int c = 0; c < 6; c++) {
+    double v = 0.0;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) v += part[(long long)c * nt + t];
+    const double s = block_sum(v, sw);
+    if (threadIdx.x == 0) en[slot[c]] = s;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) en[7] = en[8] = en[9] = en[12] = 0.0;
+}
+
+// S_total, E_total, H_expect (xchf1_fock.f:311-319) and XCfock_correction
+// (:728-783), from the device energy slots.
+__global__ void assemble_kernel(int ne, int np, double* __restrict__ en,
+                                const double* __restrict__ se1,
+                                const double* __restrict__ sp1,
+                                const double* __restrict__ se2,
+                                const double* __restrict__ sp2,
+                                double* __restrict__ focke,
+                                double* __restrict__ fockp) {
+  __shared__ double sS, sH;
+  if (threadIdx.x == 0) {
+    const double S_total = 1.0 + en[11] + en[12];
+    const double psi = (en[2] + en[3] + en[4] + en[5] + en[6] + en[7] + en[8] + en[9]) / S_total;
+    en[0] = psi + en[1];
+    en[10] = S_total;
+    en[13] = psi / S_total;
+    sS = S_total;
+    sH = psi / S_total;
+  }
+  __syncthreads();
+  const double one = 1.0, two = 2.0, S = sS, H = sH;
+  for (int k = threadIdx.x; k < ne * ne; k += blockDim.x)
+    focke[k] = (one / S) * focke[k] - H * (se1[k] + two * se2[k]);
+  for (int k = threadIdx.x; k < np * np; k += blockDim.x)
+    fockp[k] = (one / S) * fockp[k] - H * (sp1[k] + sp2[k]);
+}
+
+// ---- symmetric eigensolver: cyclic Jacobi with round-robin pairing ------------
+// A (row-major n x n, symmetric) and V in shared memory; on return A is
+// diagonal to working precision and V holds the eigenvectors as columns.
+// Sweeps are bounded; *sweeps_out = sweeps used (kJacobiMaxSweeps + 1 when
+// the off-diagonal norm did not converge).
+constexpr int kJacobiMaxSweeps = 40;
+
+__device__ int jacobi_eig(int n, double* A, double* V, double* rc, double* rs,
+                          int* rp, int* rq, double* sw) {
+  const int m = (n + 1) & ~1;   // pad to even with a dummy index n
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x)
+    V[k] = (k / n == k % n) ? 1.0 : 0.0;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < kJacobiMaxSweeps; sweep++) {
+    // convergence: off-diagonal vs diagonal squared norms
+    double off = 0.0, dia = 0.0;
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+      const double a = A[k];
+      if (k / n == k % n) dia += a * a;
+      else off += a * a;
+    }
+    off = block_sum(off, sw);
+    __syncthreads();
+    dia = block_sum(dia, sw);
+    __syncthreads();
+    if (off <= 1e-30 * dia || off == 0.0) break;
+    for (int step = 0; step < m - 1; step++) {
+      // round robin: slot 0 fixed, the other m-1 rotate
+      for (int k = threadIdx.x; k < m / 2; k += blockDim.x) {
+        const int a = (k == 0) ? 0 : 1 + (k - 1 + step) % (m - 1);
+        const int b = 1 + (m - 2 - k + step) % (m - 1);
+        int p = a < b ? a : b, q = a < b ? b : a;
+        double c = 1.0, s = 0.0;
+        if (q < n) {
+          const double apq = A[p * n + q];
+          if (apq != 0.0) {
+            const double th = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+            const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            s = t * c;
+          }
+        } else {
+          p = q = -1;   // pair with the dummy index: no rotation
+        }
+        rp[k] = p;
+        rq[k] = q;
+        rc[k] = c;
+        rs[k] = s;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int e = threadIdx.x; e < (m / 2) * n; e += blockDim.x) {
+        const int k = e / n, j = e - k * n, p = rp[k], q = rq[k];
+        if (p < 0) continue;
+        const double c = rc[k], s = rs[k];
+        const double apj = A[p * n + j], aqj = A[q * n + j];
+        A[p * n + j] = c * apj - s * aqj;
+        A[q * n + j] = s * apj + c * aqj;
+      }
+      __syncthreads();
+      // columns: A <- A J, V <- V J
+      for (int e = threadIdx.x; e < (m / 2) * n; e += blockDim.x) {
+        const int k = e / n, i = e - k * n, p = rp[k], q = rq[k];
+        if (p < 0) continue;
+        const double c = rc[k], s = rs[k];
+        const double aip = A[i * n + p], aiq = A[i * n + q];
+        A[i * n + p] = c * aip - s * aiq;
+        A[i * n + q] = s * aip + c * aiq;
+        const double vip = V[i * n + p], viq = V[i * n + q];
+        V[i * n + p] = c * vip - s * viq;
+        V[i * n + q] = s * vip + c * viq;
+      }
+      __syncthreads();
+    }
+  }
+  return sweep < kJacobiMaxSweeps ? sweep : kJacobiMaxSweeps + 1;
+}
+
+struct EigSmem {
+  double *A, *V, *T, *rc, *rs, *sw;
+  int *rp, *rq, *rank;
+};
+__device__ EigSmem carve(int n, double* base) {
+  EigSmem m;
+  m.A = base;
+  m.V = m.A + n * n;
+  m.T = m.V + n * n;
+  m.rc = m.T + n * n;
+  m.rs = m.rc + 64;
+  m.sw = m.rs + 64;
+  m.rp = (int*)(m.sw + 32);
+  m.rq = m.rp + 64;
+  m.rank = m.rq + 64;
+  return m;
+}
+size_t eig_smem_bytes(int n) {
+  return sizeof(double) * (3 * (size_t)n * n + 64 + 64 + 32) + sizeof(int) * (64 * 3);
+}
+
+// X = S^{-1/2} = U diag(1/sqrt(w)) U^T (xcscf.f:766-838 in ROOTHAN).
+// S, X column-major (symmetric).  status[0] = Jacobi sweeps (> max: failed).
+__global__ void inv_sqrt_kernel(int n, const double* __restrict__ S,
+                                double* __restrict__ X, int* status) {
+  extern __shared__ double smem[];
+  EigSmem m = carve(n, smem);
+  // RS reads the lower triangle: use it for both halves
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;
+    m.A[k] = i >= j ? S[i + n * j] : S[j + n * i];
+  }
+  __syncthreads();
+  const int sw = jacobi_eig(n, m.A, m.V, m.rc, m.rs, m.rp, m.rq, m.sw);
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;
+    double acc = 0.0;
+    for (int l = 0; l < n; l++)
+      acc += m.V[i * n + l] * (1.0 / sqrt(m.A[l * n + l])) * m.V[j * n + l];
+    X[i + n * j] = acc;
+  }
+  if (threadIdx.x == 0) status[0] = sw;
+}
+
+// ROOTHAN (xcscf.f:766-953): F' = X^T F X, eigenvectors V (ascending
+// eigenvalues), C = X V, D = prefac sum_{k=first}^{first+nocc-1} C_k C_k^T.
+// evals[n] (ascending) and C (column-major, sorted) written when non-null.
+__global__ void roothan_kernel(int n, const double* __restrict__ F,
+                               const double* __restrict__ X, int first, int nocc,
+                               double prefac, double* __restrict__ D,
+                               double* __restrict__ evals,
+                               double* __restrict__ Cout, int* status) {
+  extern __shared__ double smem[];
+  EigSmem m = carve(n, smem);
+  // T = F X  (row-major T[i][j])
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;
+    double acc = 0.0;
+    for (int l = 0; l < n; l++) acc += F[i + n * l] * X[l + n * j];
+    m.T[k] = acc;
+  }
+  __syncthreads();
+  // A = X^T T, lower triangle mirrored (RS reads the lower triangle)
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;
+    const int r = i >= j ? i : j, c = i >= j ? j : i;
+    double acc = 0.0;
+    for (int l = 0; l < n; l++) acc += X[l + n * r] * m.T[l * n + c];
+    m.A[k] = acc;
+  }
+  __syncthreads();
+  const int sw = jacobi_eig(n, m.A, m.V, m.rc, m.rs, m.rp, m.rq, m.sw);
+  // ascending order: rank of each eigenvalue (ties by index)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double w = m.A[i * n + i];
+    int r = 0;
+    for (int j = 0; j < n; j++) {
+      const double v = m.A[j * n + j];
+      r += (v < w) || (v == w && j < i);
+    }
+    m.rank[r] = i;   // rank -> eigen index
+  }
+  __syncthreads();
+  // C = X V in sorted order (T reused, row-major T[i][k])
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, k = e - i * n, col = m.rank[k];
+    double acc = 0.0;
+    for (int l = 0; l < n; l++) acc += X[i + n * l] * m.V[l * n + col];
+    m.T[e] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;
+    double acc = 0.0;
+    for (int k = first; k < first + nocc; k++) acc += prefac * m.T[i * n + k] * m.T[j * n + k];
+    D[i + n * j] = acc;
+    if (Cout) Cout[i + n * j] = m.T[e];
+  }
+  if (evals)
+    for (int k = threadIdx.x; k < n; k += blockDim.x) evals[k] = m.A[m.rank[k] * (n + 1)];
+  if (threadIdx.x == 0) status[0] = sw;
+}
+
+// DENDIF + COPYDEN (xcscf.f:719-764) for both particles: en[14], en[15].
+__global__ void dendif_kernel(int ne, int np, const double* __restrict__ DE,
+                              double* __restrict__ DE0,
+                              const double* __restrict__ DP,
+                              double* __restrict__ DP0, double* __restrict__ en) {
+  __shared__ double sw[32];
+  for (int which = 0; which < 2; which++) {
+    const int n = which ? np : ne;
+    const double* D = which ? DP : DE;
+    double* D0 = which ? DP0 : DE0;
+    double mx = 0.0;
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+      mx = fmax(mx, fabs(D0[k] - D[k]));
+      D0[k] = D[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sw[w] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double r = 0.0;
+      for (int k = 0; k < (int)(blockDim.x + 31) / 32; k++) r = fmax(r, sw[k]);
+      en[14 + which] = r;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_scf_onebody(const DevSystem& S, double* Se, double* Sp,
+                               double* Hce, double* Hcp, cudaStream_t s) {
+  const int n = S.nebf * S.nebf + S.npbf * S.npbf;
+  onebody_kernel<<<(n + 127) / 128, 128, 0, s>>>(S, Se, Sp, Hce, Hcp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam_ep(const DevSystem& S, double* Gep, cudaStream_t s) {
+  const int n = S.npbf * S.npbf * S.nebf * S.nebf;
+  gam_ep_kernel<<<(n + 127) / 128, 128, 0, s>>>(S, Gep);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam1(const DevSystem& S, double* G1, double* G1s,
+                        cudaStream_t s) {
+  const long long warps = (long long)S.npbf * S.npbf * S.nebf * S.nebf;
+  const long long blocks = (warps * 32 + 127) / 128;
+  gam1_kernel<<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s);
+  return cudaGetLastError();
+}
+
+size_t scf_fock1_part_doubles(int ne, int np) {
+  return 6 * ((size_t)ne * ne + (size_t)np * np);
+}
+
+cudaError_t launch_scf_fock1(int ne, int np, int nelec, const double* Hce,
+                             const double* Hcp, const double* Gep,
+                             const double* G1, const double* G1s,
+                             const double* Gee, const double* DE,
+                             const double* DP, double* focke, double* fockp,
+                             double* se1, double* sp1, double* part, double* en,
+                             cudaStream_t s) {
+  const int nt = ne * ne + np * np;
+  fock1_kernel<<<(nt + 127) / 128, 128, 0, s>>>(ne, np, nelec, Hce, Hcp, Gep, G1,
+                                                G1s, Gee, DE, DP, focke, fockp,
+                                                se1, sp1, part);
+  fock1_energy_kernel<<<1, 256, 0, s>>>(nt, part, en);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scf_assemble(int ne, int np, double* en, const double* se1,
+                                const double* sp1, const double* se2,
+                                const double* sp2, double* focke,
+                                double* fockp, cudaStream_t s) {
+  assemble_kernel<<<1, 256, 0, s>>>(ne, np, en, se1, sp1, se2, sp2, focke, fockp);
+  return cudaGetLastError();
+}
+
+static cudaError_t eig_attr(const void* fn, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+cudaError_t launch_inv_sqrt(int n, const double* S, double* X, int* status,
+                            cudaStream_t s) {
+  if (n < 1 || n > kScfMaxN) return cudaErrorInvalidValue;
+  const size_t smem = eig_smem_bytes(n);
+  cudaError_t e = eig_attr((const void*)inv_sqrt_kernel, smem);
+  if (e != cudaSuccess) return e;
+  inv_sqrt_kernel<<<1, 256, smem, s>>>(n, S, X, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
+                           int nocc, double prefac, double* D, double* evals,
+                           double* C, int* status, cudaStream_t s) {
+  if (n < 1 || n > kScfMaxN || first < 0 || nocc < 1 || first + nocc > n)
+    return cudaErrorInvalidValue;
+  const size_t smem = eig_smem_bytes(n);
+  cudaError_t e = eig_attr((const void*)roothan_kernel, smem);
+  if (e != cudaSuccess) return e;
+  roothan_kernel<<<1, 256, smem, s>>>(n, F, X, first, nocc, prefac, D, evals, C,
+                                      status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dendif(int ne, int np, const double* DE, double* DE0,
+                          const double* DP, double* DP0, double* en,
+                          cudaStream_t s) {
+  dendif_kernel<<<1, 256, 0, s>>>(ne, np, DE, DE0, DP, DP0, en);
+  return cudaGetLastError();
+}
+
+}  // namespace neoxc

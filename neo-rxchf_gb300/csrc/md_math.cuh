@@ -711,6 +711,177 @@ NX_BIG double gfvee(const Prim& A1, const Prim& A2, const Prim& B1,
                             beta, Rv);
 }
 
+// ======================================================================
+// two-particle geminal kernels of gam_1 (XC1_G2_MD.f, g2.f)
+
+// d^N/dx^N exp(-q (x - B)^2) at x = A for N = 0..nmax (common.f gdel_x)
+NX_HD void gauss_derivs(int nmax, double q, double u /* A - B */, double* g) {
+  g[0] = exp(-q * u * u);
+  for (int N = 1; N <= nmax; N++)
+    g[N] = -2.0 * q * u * g[N - 1] - (N > 1 ? 2.0 * q * (N - 1) * g[N - 2] : 0.0);
+}
+
+// G2_MD_xggvec (XC1_G2_MD.f:190-624): attraction of particle 1 to the point
+// C for the pairs (A1,B1), (A2,B2) coupled by exp(-(gamma1+gamma2) r12^2).
+// Per direction W[n] folds the Hermite coefficients, the binomial split
+// between the Gaussian and Coulomb parts and the powers of -DC1 / -DC2 of
+// g2_dhermite_vec; R_tuv is taken about C - S as in g2_vec_prefactors.
+NX_BIG double g2_xggvec(const Prim& A1, const Prim& A2, const Prim& B1,
+                       const Prim& B2, double gamma1, double gamma2,
+                       const double* C) {
+  const double G = gamma1 + gamma2;
+  Pair p1, p2;
+  gauss_pair(A1, B1, p1);
+  gauss_pair(A2, B2, p2);
+  const double P1 = p1.p, P2 = p2.p;
+  const double s = (P1 * P2 + P1 * G + P2 * G) / (P2 + G);
+  const double alpha = s;
+  const double x = kPiT / (P2 + G);
+  const double c1 = pow(x, 1.5) * 2.0 * kPiT / s;
+  const double xx = P1 * P2 + P1 * G + P2 * G;
+  const double qP = (P1 * P2 * G) / xx;
+  const double DC1 = (P1 * P2 + P1 * G) / xx, DC2 = (P2 * G) / xx;
+  double RCS[3], R2 = 0.0;
+  double W[3][LTOT + 1];
+  int n[3];
+  for (int d = 0; d < 3; d++) {
+    const double Sm = ((P1 * P2 + P1 * G) * p1.P[d] + P2 * G * p2.P[d]) / xx;
+    RCS[d] = C[d] - Sm;
+    R2 += RCS[d] * RCS[d];
+    double E1[2 * LP + 1], E2[2 * LP + 1], gd[4 * LP + 1];
+    const int l1 = A1.l[d] + B1.l[d], l2 = A2.l[d] + B2.l[d];
+    hermite_e(A1.l[d], B1.l[d], p1.K[d], A1.a, B1.a, P1, p1.q, p1.Q[d], E1);
+    hermite_e(A2.l[d], B2.l[d], p2.K[d], A2.a, B2.a, P2, p2.q, p2.Q[d], E2);
+    gauss_derivs(l1 + l2, qP, p1.P[d] - p2.P[d], gd);
+    double pw1[2 * LP + 1], pw2[2 * LP + 1];
+    pw1[0] = pw2[0] = 1.0;
+    for (int k = 1; k <= 2 * LP; k++) {
+      pw1[k] = pw1[k - 1] * -DC1;
+      pw2[k] = pw2[k - 1] * -DC2;
+    }
+    for (int k = 0; k <= l1 + l2; k++) W[d][k] = 0.0;
+    for (int t1 = 0; t1 <= l1; t1++)
+      for (int t2 = 0; t2 <= l2; t2++) {
+        const double e = E1[t1] * E2[t2];
+        for (int b1 = 0; b1 <= t1; b1++)
+          for (int b2 = 0; b2 <= t2; b2++) {
+            const double sg = ((t2 - b2) & 1) ? -1.0 : 1.0;
+            W[d][b1 + b2] += e * binom(t1, b1) * binom(t2, b2) * sg * pw1[b1] *
+                             pw2[b2] * gd[(t1 - b1) + (t2 - b2)];
+          }
+      }
+    n[d] = l1 + l2;
+  }
+  return c1 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], alpha * R2,
+                          alpha, RCS);
+}
+
+// G2_MD_xggvee (XC1_G2_MD.f:630-960): 1/|r1 - r2| between the two
+// geminal-coupled particles (g2_ee_prefactors, g2_dhermite_vee).
+NX_BIG double g2_xggvee(const Prim& A1, const Prim& A2, const Prim& B1,
+                       const Prim& B2, double gamma1, double gamma2) {
+  const double G = gamma1 + gamma2;
+  Pair p1, p2;
+  gauss_pair(A1, B1, p1);
+  gauss_pair(A2, B2, p2);
+  const double P1 = p1.p, P2 = p2.p;
+  const double xx = P1 * P2 + P1 * G + P2 * G;
+  const double c0 = (2.0 * pow(kPiT, 2.5)) / (xx * sqrt(P1 + P2));
+  const double qP = (P1 * P2 * G) / xx;
+  const double alpha = (P1 * P1 * P2 * P2) / (xx * (P1 + P2));
+  double X[3], R2 = 0.0;
+  double W[3][LTOT + 1];
+  int n[3];
+  for (int d = 0; d < 3; d++) {
+    X[d] = p1.P[d] - p2.P[d];
+    R2 += X[d] * X[d];
+    double E1[2 * LP + 1], E2[2 * LP + 1], gd[4 * LP + 1];
+    const int l1 = A1.l[d] + B1.l[d], l2 = A2.l[d] + B2.l[d];
+    hermite_e(A1.l[d], B1.l[d], p1.K[d], A1.a, B1.a, P1, p1.q, p1.Q[d], E1);
+    hermite_e(A2.l[d], B2.l[d], p2.K[d], A2.a, B2.a, P2, p2.q, p2.Q[d], E2);
+    gauss_derivs(l1 + l2, qP, X[d], gd);
+    for (int k = 0; k <= l1 + l2; k++) W[d][k] = 0.0;
+    for (int t1 = 0; t1 <= l1; t1++)
+      for (int t2 = 0; t2 <= l2; t2++) {
+        const double e = E1[t1] * E2[t2] * ((t2 & 1) ? -1.0 : 1.0);
+        const int N = t1 + t2;
+        for (int b = 0; b <= N; b++) W[d][b] += e * binom(N, b) * gd[N - b];
+      }
+    n[d] = l1 + l2;
+  }
+  return c0 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], alpha * R2,
+                          alpha, X);
+}
+
+// pgiovlap_1D (g2.f:915-1009) with pgi_hint0_1D (:200-234, whose pi is
+// 3.141592650): 1-D overlap of two particles coupled by
+// exp(-(gamA+gamB) x12^2).
+NX_BIG double pgi_ovl1d(int I1, double a1, double A1, int I2, double a2,
+                       double A2, int L1, double b1, double B1, int L2,
+                       double b2, double B2, double gam) {
+  const double p1 = a1 + b1, q1 = (a1 * b1) / (a1 + b1), Q1 = A1 - B1;
+  const double p2 = a2 + b2, q2 = (a2 * b2) / (a2 + b2), Q2 = A2 - B2;
+  const double Pm1 = (a1 * A1 + b1 * B1) / (a1 + b1);
+  const double Pm2 = (a2 * A2 + b2 * B2) / (a2 + b2);
+  double E1[2 * TMX + 1], E2[2 * TMX + 1], gd[2 * TMX + 1];
+  hermite_e(I1, L1, exp(-q1 * Q1 * Q1), a1, b1, p1, q1, Q1, E1);
+  hermite_e(I2, L2, exp(-q2 * Q2 * Q2), a2, b2, p2, q2, Q2, E2);
+  const double s = (p1 * p2) + (p1 * gam) + (p2 * gam);
+  const double q = (p1 * p2 * gam) / s;
+  const double PI = 3.141592650;
+  const double pre = sqrt(PI * PI / s);
+  gauss_derivs(I1 + L1 + I2 + L2, q, Pm1 - Pm2, gd);
+  double acc = 0.0;
+  for (int t1 = 0; t1 <= I1 + L1; t1++)
+    for (int t2 = 0; t2 <= I2 + L2; t2++)
+      acc += E1[t1] * E2[t2] * (((t2 & 1) ? -1.0 : 1.0) * pre * gd[t1 + t2]);
+  return acc;
+}
+
+// pgi_Lapx1 (g2.f:655-765) with pgi_calcS2 / pgi_calcS3 (:768-911)
+NX_BIG double pgi_lapx1(int I1, double a1, double A1, int I2, double a2,
+                       double A2, int L1, double b1, double B1, int L2,
+                       double b2, double B2, double gA, double gB) {
+  const double g = gA + gB;
+#define OV(l1s, l2s) pgi_ovl1d(I1, a1, A1, I2, a2, A2, (l1s), b1, B1, (l2s), b2, B2, g)
+  const double X12 = B1 - B2;
+  const double d1 = (L1 - 1 >= 0) ? (double)(L1 * (L1 - 1)) : 0.0;
+  const double d2 = -2.0 * b1 * (double)((2 * L1) + 1);
+  const double d3 = 4.0 * b1 * b1;
+  const double c1 = (double)L1, c2 = -2.0 * b1;
+  const double p1 = (L1 - 2 >= 0) ? OV(L1 - 2, L2) : 0.0;
+  const double p2 = OV(L1, L2);
+  const double p3 = OV(L1 + 2, L2);
+  const double W1 = (d1 * p1) + (d2 * p2) + (d3 * p3);
+  // calcS2(L) = OV(L+1, L2) - OV(L, L2+1) + X12 OV(L, L2)
+  const double q1 = (L1 - 1 >= 0) ? OV(L1, L2) - OV(L1 - 1, L2 + 1) + (X12 * OV(L1 - 1, L2)) : 0.0;
+  const double q2 = OV(L1 + 2, L2) - OV(L1 + 1, L2 + 1) + (X12 * OV(L1 + 1, L2));
+  const double W2 = -2.0 * gB * ((c1 * q1) + (c2 * q2));
+  const double t1 = p2;
+  const double t2 = OV(L1 + 2, L2) + OV(L1, L2 + 2) + (X12 * X12 * p2) -
+                    (2.0 * OV(L1 + 1, L2 + 1)) - (2.0 * X12 * OV(L1, L2 + 1)) +
+                    (2.0 * X12 * OV(L1 + 1, L2));
+  const double W3 = (-2.0 * gB * t1) + (4.0 * gB * gB * t2);
+#undef OV
+  return W1 + (2.0 * W2) + W3;
+}
+
+// pgike1 (g2.f:545-651): kinetic energy of particle 1 (mass xmass) for the
+// geminal-coupled pairs (A1,B1), (A2,B2); geminal exponents gA (bra), gB (ket).
+NX_BIG double pgike1(const Prim& A1, const Prim& A2, const Prim& B1,
+                    const Prim& B2, double gA, double gB, double xmass) {
+  double S[3], T[3];
+  for (int d = 0; d < 3; d++) {
+    S[d] = pgi_ovl1d(A1.l[d], A1.a, A1.c[d], A2.l[d], A2.a, A2.c[d], B1.l[d],
+                     B1.a, B1.c[d], B2.l[d], B2.a, B2.c[d], gA + gB);
+    const double dd = pgi_lapx1(A1.l[d], A1.a, A1.c[d], A2.l[d], A2.a,
+                                A2.c[d], B1.l[d], B1.a, B1.c[d], B2.l[d],
+                                B2.a, B2.c[d], gA, gB);
+    T[d] = -dd * 0.50 / xmass;
+  }
+  return (T[0] * S[1] * S[2]) + (S[0] * T[1] * S[2]) + (S[0] * S[1] * T[2]);
+}
+
 NX_HD double underflow(double x) { return fabs(x) < 1.0e-100 ? 0.0 : x; }
 
 }  // namespace md

@@ -135,6 +135,38 @@ cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3,
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,
                                    cudaStream_t s);
 
+// ---- XCHF SCF (k_scf.cu): xcscf.f, xchf1_fock.f ---------------------------
+// Device energy slots: 0 E_total 1 E_nuc 2 E_ecore 3 E_pcore 4 E_ep 5 E_ee
+// 6 E_gam1 7 E_gam2 8 E_gam3 9 E_gam4 10 S_total 11 S_gam1 12 S_gam2
+// 13 H_expect 14 max|dDE| 15 max|dDP|.
+constexpr int kScfMaxN = 64;   // one-CTA Jacobi eigensolver (3 n^2 doubles)
+constexpr int kScfSlots = 16;
+cudaError_t launch_scf_onebody(const DevSystem& sys, double* Se, double* Sp,
+                               double* Hce, double* Hcp, cudaStream_t s);
+cudaError_t launch_gam_ep(const DevSystem& sys, double* Gep, cudaStream_t s);
+cudaError_t launch_gam1(const DevSystem& sys, double* G1, double* G1s,
+                        cudaStream_t s);
+size_t scf_fock1_part_doubles(int ne, int np);
+cudaError_t launch_scf_fock1(int ne, int np, int nelec, const double* Hce,
+                             const double* Hcp, const double* Gep,
+                             const double* G1, const double* G1s,
+                             const double* Gee, const double* DE,
+                             const double* DP, double* focke, double* fockp,
+                             double* se1, double* sp1, double* part, double* en,
+                             cudaStream_t s);
+cudaError_t launch_scf_assemble(int ne, int np, double* en, const double* se1,
+                                const double* sp1, const double* se2,
+                                const double* sp2, double* focke,
+                                double* fockp, cudaStream_t s);
+cudaError_t launch_inv_sqrt(int n, const double* S, double* X, int* status,
+                            cudaStream_t s);
+cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
+                           int nocc, double prefac, double* D, double* evals,
+                           double* C, int* status, cudaStream_t s);
+cudaError_t launch_dendif(int ne, int np, const double* DE, double* DE0,
+                          const double* DP, double* DP0, double* en,
+                          cudaStream_t s);
+
 // ---- index maps on the device (pack_GAM.f) -----------------------------
 cudaError_t launch_index_fill(int kind, int ne, int np, int64_t count,
                               int64_t* out, cudaStream_t s);

@@ -22,7 +22,7 @@ from .basis import NeoSystem  # noqa: F401  (re-export)
 __all__ = [
     "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
     "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam4_fock_factored",
-    "gam3_dscf", "gam2_dscf",
+    "gam3_dscf", "gam2_dscf", "xchf_scf", "SCF_SLOTS",
     "eg4icr", "eg3ic1", "eg2ic1",
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
@@ -61,6 +61,7 @@ def _declare(L):
         "neoxc_gam4_icr": (I, [i64] * 6 + [vp] * 3),
         "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
         "neoxc_gam4_fock_factored": (I, [i64] * 4 + [vp] * 7),
+        "neoxc_xchf_scf": (I, [i64] * 7 + [d] + [vp] * 15 + [i64, i64] + [vp] * 7),
         "neoxc_dev_gam4_fock_factored": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg3ic1": (I, [i64] * 4 + [vp] * 6),
@@ -232,6 +233,35 @@ def gam2_dscf(s: NeoSystem, DE, DP, focke=None, fockp=None, se2=None, sp2=None,
                                  _p(fe), _p(fp), _p(se), _p(sp), _p(E), _p(S)))
     return (*_fock_out(fe, fp, ne, np_), *_fock_out(se, sp, ne, np_),
             float(E[0]), float(S[0]))
+
+
+SCF_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_gam1", "E_gam2",
+             "E_gam3", "E_gam4", "S_total", "S_gam1", "S_gam2", "H_expect", "dDE", "dDP")
+
+
+def xchf_scf(s: NeoSystem, DE, DP=None, nucst=None, maxit: int = 100,
+             gam4_element: bool = False):
+    """xcscf.f XCHF RHF SCF on the GPU (plain Roothaan).  DE: initial
+    electronic density; DP: initial nuclear density, or None for the
+    core-Hamiltonian guess (guess_prot).  Returns a dict with the initial and
+    final energetics (SCF_SLOTS names), the per-iteration history, the
+    converged densities, the iteration count and the convergence flag."""
+    ne, np_ = s.nebf, s.npbf
+    opts = (1 if DP is None else 0) | (4 if gam4_element else 0)
+    de = _fmat(DE).copy()
+    dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
+    Ei, Ef = np.zeros(16), np.zeros(16)
+    hist = np.zeros(4 * maxit)
+    nit, conv = np.zeros(1, np.int64), np.zeros(1, np.int64)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_xchf_scf(s.nelec, s.nucst if nucst is None else nucst, ne, s.npebf,
+                                np_, s.nat, s.ngtg, s.pmass, *ptrs, opts, maxit, _p(de),
+                                _p(dp), _p(Ei), _p(Ef), _p(hist), _p(nit), _p(conv)))
+    n = int(nit[0])
+    return {"initial": dict(zip(SCF_SLOTS, Ei.tolist())),
+            "final": dict(zip(SCF_SLOTS, Ef.tolist())),
+            "history": hist[:4 * n].reshape(n, 4), "niter": n, "converged": bool(conv[0]),
+            "DE": de.reshape(ne, ne, order="F"), "DP": dp.reshape(np_, np_, order="F")}
 
 
 def gam4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:

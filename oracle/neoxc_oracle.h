@@ -188,6 +188,26 @@ void orc_gam2_dscf(const orc_system *s, const double *DE, const double *DP,
 void orc_gam3_dscf(const orc_system *s, const double *DE, const double *DP,
                    double *focke, double *fockp, double *E_gam3);
 
+/* two-particle geminal kernels of gam_1 (XC1_G2_MD.f, g2.f) */
+double orc_g2_xggvec(const orc_prim *A1, const orc_prim *A2,
+                     const orc_prim *B1, const orc_prim *B2, double gamma1,
+                     double gamma2, const double *C);
+double orc_g2_xggvee(const orc_prim *A1, const orc_prim *A2,
+                     const orc_prim *B1, const orc_prim *B2, double gamma1,
+                     double gamma2);
+double orc_pgike1(const orc_prim *A1, const orc_prim *A2, const orc_prim *B1,
+                  const orc_prim *B2, double gamA, double gamB, double xmass1,
+                  double *sval);
+
+/* XCHF SCF integrals (scf.c) */
+void orc_overlaps(const orc_system *s, double *Se, double *Sp);
+void orc_gam_epcore(const orc_system *s, double *Gecore, double *Gpcore);
+void orc_gam_ep(const orc_system *s, double *Gep);
+void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
+                    double *ansE, double *ansS);
+void orc_gam1(const orc_system *s, double *G1, double *G1s);
+double orc_nuc_rep(const orc_system *s);
+
 /* density from MO coefficients (GAM_IO.f read_elec_density) */
 void orc_density(int64_t nbf, int64_t nocc, double prefac, const double *C,
                  double *D);

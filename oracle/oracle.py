@@ -1,7 +1,7 @@
 """ctypes binding for the CPU oracle (test infrastructure only).
 
 The oracle restates the NEO-RXCHF integral and contraction arithmetic on
-the CPU (``prim.c``, ``builders.c``).  Only the tests, the smoke check and
+the CPU (``prim.c``, ``builders.c``, ``scf.c``).  Only the tests, the smoke check and
 the CPU-baseline leg of ``bench.py`` load it; the product never does.
 """
 from __future__ import annotations
@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libneoxc_oracle.so")
-SOURCES = ["prim.c", "builders.c"]
+SOURCES = ["prim.c", "builders.c", "scf.c"]
 _lock = threading.Lock()
 _lib = None
 
@@ -82,6 +82,9 @@ def lib():
                 "orc_gfvec": (d, [P, P, vp]),
                 "orc_gfvee": (d, [P, P, P, P]),
                 "orc_g2_xggs": (d, [P, P, P, P, d, d]),
+                "orc_g2_xggvec": (d, [P, P, P, P, d, d, vp]),
+                "orc_g2_xggvee": (d, [P, P, P, P, d, d]),
+                "orc_pgike1": (d, [P, P, P, P, d, d, d, vp]),
                 "orc_g3_xggs": (d, [P, P, vp]),
                 "orc_g3_ke": (d, [P, P, vp, d]),
                 "orc_g3_xgvxcg": (d, [P, P, vp, vp]),
@@ -124,6 +127,11 @@ def lib():
                 "orc_density": (None, [i64, i64, d, vp, vp]),
                 "orc_gam2_dscf": (None, [vp] + [vp] * 8),
                 "orc_gam3_dscf": (None, [vp] + [vp] * 5),
+                "orc_overlaps": (None, [vp] * 3),
+                "orc_gam_epcore": (None, [vp] * 3),
+                "orc_gam_ep": (None, [vp] * 2),
+                "orc_gam1": (None, [vp] * 3),
+                "orc_nuc_rep": (C.c_double, [vp]),
                 "orc_num_threads": (C.c_int, []),
             }
             for name, (res, args) in sig.items():

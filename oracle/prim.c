@@ -993,3 +993,248 @@ double orc_gfvee(const orc_prim *A1, const orc_prim *A2, const orc_prim *B1,
   }
   return xsum;
 }
+
+/* ---- two-particle geminal kernels used by gam_1 (XC1_G2_MD.f, g2.f) ------- */
+
+/* XC1_G2_MD.f:383-461 g2_vec_prefactors and :465-624 g2_dhermite_vec,
+ * summed as G2_MD_xggvec (:190-378): Coulomb attraction of particle 1 to the
+ * point C between geminal-correlated particles (A1,B1) and (A2,B2). */
+double orc_g2_xggvec(const orc_prim *A1, const orc_prim *A2,
+                     const orc_prim *B1, const orc_prim *B2, double gamma1,
+                     double gamma2, const double *C) {
+  double GAM = gamma1 + gamma2;
+  double K1[3], q1, P1, Pm1[3], Q1[3], K2[3], q2, P2, Pm2[3], Q2[3];
+  gauss_prod(A1->a, B1->a, A1->c, B1->c, K1, &q1, &P1, Pm1, Q1);
+  gauss_prod(A2->a, B2->a, A2->c, B2->c, K2, &q2, &P2, Pm2, Q2);
+  double E1[3][24], E2[3][24];
+  for (int d = 0; d < 3; d++) {
+    orc_ghec(A1->l[d], B1->l[d], K1[d], A1->a, B1->a, P1, q1, Q1[d], E1[d]);
+    orc_ghec(A2->l[d], B2->l[d], K2[d], A2->a, B2->a, P2, q2, Q2[d], E2[d]);
+  }
+  /* g2_vec_prefactors */
+  double s = (P1 * P2 + P1 * GAM + P2 * GAM) / (P2 + GAM);
+  double alpha = s;
+  double c1 = pow(PI_T / (P2 + GAM), 3.0 / 2.0) * 2.0 * PI_T / s;
+  double xx = P1 * P2 + P1 * GAM + P2 * GAM;
+  double Sm[3], RCS[3];
+  for (int d = 0; d < 3; d++)
+    Sm[d] = ((P1 * P2 + P1 * GAM) * Pm1[d] + P2 * GAM * Pm2[d]) / xx;
+  for (int d = 0; d < 3; d++) RCS[d] = C[d] - Sm[d];
+  double R2CS = RCS[0] * RCS[0] + RCS[1] * RCS[1] + RCS[2] * RCS[2];
+  double expT = alpha * R2CS;
+  double qP = (P1 * P2 * GAM) / xx;
+  double DC1 = (P1 * P2 + P1 * GAM) / xx;
+  double DC2 = (P2 * GAM) / xx;
+  double out = 0.0;
+  for (int t1 = 0; t1 <= A1->l[0] + B1->l[0]; t1++)
+  for (int u1 = 0; u1 <= A1->l[1] + B1->l[1]; u1++)
+  for (int v1 = 0; v1 <= A1->l[2] + B1->l[2]; v1++)
+  for (int t2 = 0; t2 <= A2->l[0] + B2->l[0]; t2++)
+  for (int u2 = 0; u2 <= A2->l[1] + B2->l[1]; u2++)
+  for (int v2 = 0; v2 <= A2->l[2] + B2->l[2]; v2++) {
+    /* g2_dhermite_vec */
+    double Dgf = 0.0;
+    for (int xb1 = 0; xb1 <= t1; xb1++) {
+      int ax1 = t1 - xb1;
+      double a1 = cbinom(t1, xb1);
+      for (int yb1 = 0; yb1 <= u1; yb1++) {
+        int ay1 = u1 - yb1;
+        double a2 = cbinom(u1, yb1);
+        for (int zb1 = 0; zb1 <= v1; zb1++) {
+          int az1 = v1 - zb1;
+          double a3 = cbinom(v1, zb1);
+          for (int xb2 = 0; xb2 <= t2; xb2++) {
+            int ax2 = t2 - xb2;
+            double b1 = cbinom(t2, xb2);
+            for (int yb2 = 0; yb2 <= u2; yb2++) {
+              int ay2 = u2 - yb2;
+              double b2 = cbinom(u2, yb2);
+              for (int zb2 = 0; zb2 <= v2; zb2++) {
+                int az2 = v2 - zb2;
+                double b3 = cbinom(v2, zb2);
+                double C1 = ipow(-1.0, ax2 + ay2 + az2);
+                double C2 = ipow(-DC1, xb1 + yb1 + zb1);
+                double C3 = ipow(-DC2, xb2 + yb2 + zb2);
+                double dgx = orc_gdel_x(ax1 + ax2, Pm1[0], qP, Pm2[0]);
+                double dgy = orc_gdel_x(ay1 + ay2, Pm1[1], qP, Pm2[1]);
+                double dgz = orc_gdel_x(az1 + az2, Pm1[2], qP, Pm2[2]);
+                double dgxyz = dgx * dgy * dgz;
+                int nLim = xb1 + yb1 + zb1 + xb2 + yb2 + zb2;
+                double dfxyz = orc_rtuv(xb1 + xb2, yb1 + yb2, zb1 + zb2, nLim,
+                                        expT, alpha, RCS[0], RCS[1], RCS[2]);
+                Dgf = Dgf + a1 * a2 * a3 * b1 * b2 * b3 * C1 * C2 * C3 *
+                                dgxyz * dfxyz;
+              }
+            }
+          }
+        }
+      }
+    }
+    double ans = c1 * E1[0][t1] * E2[0][t2] * E1[1][u1] * E2[1][u2] *
+                 E1[2][v1] * E2[2][v2] * Dgf;
+    out = out + ans;
+  }
+  return out;
+}
+
+/* XC1_G2_MD.f:801-859 g2_ee_prefactors and :863-960 g2_dhermite_vee,
+ * summed as G2_MD_xggvee (:630-796): Coulomb repulsion between the two
+ * geminal-correlated particles. */
+double orc_g2_xggvee(const orc_prim *A1, const orc_prim *A2,
+                     const orc_prim *B1, const orc_prim *B2, double gamma1,
+                     double gamma2) {
+  double GAM = gamma1 + gamma2;
+  double K1[3], q1, P1, Pm1[3], Q1[3], K2[3], q2, P2, Pm2[3], Q2[3];
+  gauss_prod(A1->a, B1->a, A1->c, B1->c, K1, &q1, &P1, Pm1, Q1);
+  gauss_prod(A2->a, B2->a, A2->c, B2->c, K2, &q2, &P2, Pm2, Q2);
+  double E1[3][24], E2[3][24];
+  for (int d = 0; d < 3; d++) {
+    orc_ghec(A1->l[d], B1->l[d], K1[d], A1->a, B1->a, P1, q1, Q1[d], E1[d]);
+    orc_ghec(A2->l[d], B2->l[d], K2[d], A2->a, B2->a, P2, q2, Q2[d], E2[d]);
+  }
+  /* g2_ee_prefactors */
+  double xx = P1 * P2 + P1 * GAM + P2 * GAM;
+  double c0 = (2.0 * pow(PI_T, 5.0 / 2.0)) / (xx * sqrt(P1 + P2));
+  double qP = (P1 * P2 * GAM) / (P1 * P2 + P1 * GAM + P2 * GAM);
+  double alpha = (P1 * P1 * P2 * P2) / (xx * (P1 + P2));
+  double X[3];
+  for (int d = 0; d < 3; d++) X[d] = Pm1[d] - Pm2[d];
+  double R2 = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
+  double expT = alpha * R2;
+  double out = 0.0;
+  for (int t1 = 0; t1 <= A1->l[0] + B1->l[0]; t1++)
+  for (int u1 = 0; u1 <= A1->l[1] + B1->l[1]; u1++)
+  for (int v1 = 0; v1 <= A1->l[2] + B1->l[2]; v1++)
+  for (int t2 = 0; t2 <= A2->l[0] + B2->l[0]; t2++)
+  for (int u2 = 0; u2 <= A2->l[1] + B2->l[1]; u2++)
+  for (int v2 = 0; v2 <= A2->l[2] + B2->l[2]; v2++) {
+    double c2 = pow(-1.0, (double)(t2 + u2 + v2));
+    int Nt = t1 + t2, Nu = u1 + u2, Nv = v1 + v2;
+    /* g2_dhermite_vee */
+    double Dgf = 0.0;
+    for (int xb1 = 0; xb1 <= Nt; xb1++) {
+      int argx = Nt - xb1;
+      double bx = cbinom(Nt, xb1);
+      for (int yb1 = 0; yb1 <= Nu; yb1++) {
+        int argy = Nu - yb1;
+        double by = cbinom(Nu, yb1);
+        for (int zb1 = 0; zb1 <= Nv; zb1++) {
+          int argz = Nv - zb1;
+          double bz = cbinom(Nv, zb1);
+          double dgx = orc_gdel_x(argx, Pm1[0], qP, Pm2[0]);
+          double dgy = orc_gdel_x(argy, Pm1[1], qP, Pm2[1]);
+          double dgz = orc_gdel_x(argz, Pm1[2], qP, Pm2[2]);
+          double dgxyz = dgx * dgy * dgz;
+          int nLim = xb1 + yb1 + zb1;
+          double dfxyz =
+              orc_rtuv(xb1, yb1, zb1, nLim, expT, alpha, X[0], X[1], X[2]);
+          Dgf = Dgf + bx * by * bz * dgxyz * dfxyz;
+        }
+      }
+    }
+    double ans = c0 * c2 * E1[0][t1] * E2[0][t2] * E1[1][u1] * E2[1][u2] *
+                 E1[2][v1] * E2[2][v2] * Dgf;
+    out = out + ans;
+  }
+  return out;
+}
+
+/* g2.f:200-234 pgi_hint0_1D (pi truncated to 3.141592650 there) */
+static double pgi_hint0_1d(int it1, int it2, double p1, double p2,
+                           double gamma, double P1, double P2) {
+  const double PI = 3.141592650;
+  double coe1 = ipow(-1.0, it2);
+  double s = (p1 * p2) + (p1 * gamma) + (p2 * gamma);
+  double q = (p1 * p2 * gamma) / s;
+  double gd0 = orc_gdel_x(it1 + it2, P1, q, P2);
+  return coe1 * sqrt(PI * PI / s) * gd0;
+}
+
+/* g2.f:915-1009 pgiovlap_1D: 1-D overlap of two particles coupled by the
+ * geminal exp(-(gamA+gamB) x12^2) */
+static double pgiovlap_1d(int I1, double alp1, double A1, int I2, double alp2,
+                          double A2, int L1, double beta1, double B1, int L2,
+                          double beta2, double B2, double gamA, double gamB) {
+  double gamma = gamA + gamB;
+  double p1, q1, P1, Q1, K1, ex1[24];
+  double p2, q2, P2, Q2, K2, ex2[24];
+  omega1d(I1, L1, alp1, beta1, A1, B1, &p1, &q1, &P1, &Q1, &K1, ex1);
+  omega1d(I2, L2, alp2, beta2, A2, B2, &p2, &q2, &P2, &Q2, &K2, ex2);
+  double xsum = 0.0;
+  for (int it1 = 0; it1 <= I1 + L1; it1++)
+    for (int it2 = 0; it2 <= I2 + L2; it2++) {
+      double herm = pgi_hint0_1d(it1, it2, p1, p2, gamma, P1, P2);
+      xsum = xsum + (ex1[it1] * ex2[it2] * herm);
+    }
+  return xsum;
+}
+
+/* g2.f:768-825 pgi_calcS2 */
+static double pgi_calcs2(int I1, double alp1, double A1, int I2, double alp2,
+                         double A2, int L1, double beta1, double B1, int L2,
+                         double beta2, double B2, double gA, double gB) {
+  double p1 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1 + 1, beta1, B1, L2, beta2, B2, gA, gB);
+  double p2 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2 + 1, beta2, B2, gA, gB);
+  double p3 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2, beta2, B2, gA, gB);
+  return p1 - p2 + ((B1 - B2) * p3);
+}
+
+/* g2.f:829-911 pgi_calcS3 */
+static double pgi_calcs3(int I1, double alp1, double A1, int I2, double alp2,
+                         double A2, int L1, double beta1, double B1, int L2,
+                         double beta2, double B2, double gA, double gB) {
+  double X12 = B1 - B2;
+  double p1 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1 + 2, beta1, B1, L2, beta2, B2, gA, gB);
+  double p2 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2 + 2, beta2, B2, gA, gB);
+  double p3 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2, beta2, B2, gA, gB);
+  double p4 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1 + 1, beta1, B1, L2 + 1, beta2, B2, gA, gB);
+  double p5 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2 + 1, beta2, B2, gA, gB);
+  double p6 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1 + 1, beta1, B1, L2, beta2, B2, gA, gB);
+  return p1 + p2 + (X12 * X12 * p3) - (2.0 * p4) - (2.0 * X12 * p5) +
+         (2.0 * X12 * p6);
+}
+
+/* g2.f:655-765 pgi_Lapx1: 1-D Laplacian of particle 1 with the geminal */
+static double pgi_lapx1(int I1, double alp1, double A1, int I2, double alp2,
+                        double A2, int L1, double beta1, double B1, int L2,
+                        double beta2, double B2, double gA, double gB) {
+  double d1 = 0.0, c1, c2, p1 = 0.0, p2, p3, q1 = 0.0, q2, t1, t2;
+  if (L1 - 1 >= 0) d1 = (double)(L1 * (L1 - 1));
+  double d2 = -2.0 * beta1 * (double)((2 * L1) + 1);
+  double d3 = 4.0 * beta1 * beta1;
+  c1 = (double)L1;
+  c2 = -2.0 * beta1;
+  if (L1 - 2 >= 0)
+    p1 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1 - 2, beta1, B1, L2, beta2, B2, gA, gB);
+  p2 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2, beta2, B2, gA, gB);
+  p3 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1 + 2, beta1, B1, L2, beta2, B2, gA, gB);
+  double W1 = (d1 * p1) + (d2 * p2) + (d3 * p3);
+  if (L1 - 1 >= 0)
+    q1 = pgi_calcs2(I1, alp1, A1, I2, alp2, A2, L1 - 1, beta1, B1, L2, beta2, B2, gA, gB);
+  q2 = pgi_calcs2(I1, alp1, A1, I2, alp2, A2, L1 + 1, beta1, B1, L2, beta2, B2, gA, gB);
+  double W2 = -2.0 * gB * ((c1 * q1) + (c2 * q2));
+  t1 = pgiovlap_1d(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2, beta2, B2, gA, gB);
+  t2 = pgi_calcs3(I1, alp1, A1, I2, alp2, A2, L1, beta1, B1, L2, beta2, B2, gA, gB);
+  double W3 = (-2.0 * gB * t1) + (4.0 * gB * gB * t2);
+  return W1 + (2.0 * W2) + W3;
+}
+
+/* g2.f:545-651 pgike1: kinetic energy of particle 1 (mass xmass1) between
+ * geminal-correlated pairs; also returns the overlap Sx Sy Sz in *sval. */
+double orc_pgike1(const orc_prim *A1, const orc_prim *A2, const orc_prim *B1,
+                  const orc_prim *B2, double gamA, double gamB, double xmass1,
+                  double *sval) {
+  double S[3], T[3];
+  for (int d = 0; d < 3; d++)
+    S[d] = pgiovlap_1d(A1->l[d], A1->a, A1->c[d], A2->l[d], A2->a, A2->c[d],
+                       B1->l[d], B1->a, B1->c[d], B2->l[d], B2->a, B2->c[d],
+                       gamA, gamB);
+  for (int d = 0; d < 3; d++) {
+    double dd = pgi_lapx1(A1->l[d], A1->a, A1->c[d], A2->l[d], A2->a, A2->c[d],
+                          B1->l[d], B1->a, B1->c[d], B2->l[d], B2->a, B2->c[d],
+                          gamA, gamB);
+    T[d] = -dd * 0.50 / xmass1;
+  }
+  if (sval) *sval = S[0] * S[1] * S[2];
+  return (T[0] * S[1] * S[2]) + (S[0] * T[1] * S[2]) + (S[0] * S[1] * T[2]);
+}

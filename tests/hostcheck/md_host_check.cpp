@@ -43,6 +43,18 @@ double hc_g2_xggs(const HP* A1, const HP* A2, const HP* B1, const HP* B2,
                   double g1, double g2) {
   return g2_xggs(cv(*A1), cv(*A2), cv(*B1), cv(*B2), g1, g2);
 }
+double hc_g2_xggvec(const HP* A1, const HP* A2, const HP* B1, const HP* B2,
+                    double g1, double g2, const double* C) {
+  return g2_xggvec(cv(*A1), cv(*A2), cv(*B1), cv(*B2), g1, g2, C);
+}
+double hc_g2_xggvee(const HP* A1, const HP* A2, const HP* B1, const HP* B2,
+                    double g1, double g2) {
+  return g2_xggvee(cv(*A1), cv(*A2), cv(*B1), cv(*B2), g1, g2);
+}
+double hc_pgike1(const HP* A1, const HP* A2, const HP* B1, const HP* B2,
+                 double gA, double gB, double m) {
+  return pgike1(cv(*A1), cv(*A2), cv(*B1), cv(*B2), gA, gB, m);
+}
 double hc_gfvee(const HP* A1, const HP* A2, const HP* B1, const HP* B2) {
   return gfvee(cv(*A1), cv(*A2), cv(*B1), cv(*B2));
 }

@@ -120,9 +120,13 @@ def test_md_math_matches_oracle(orc, hostcheck):
     H.hc_g3.argtypes = [C.c_int, P, P, C.c_void_p, C.c_void_p, d]
     H.hc_g4.restype = d
     H.hc_g4.argtypes = [C.c_int, P, P, d, d]
-    for f in ("hc_g2_xggs",):
+    for f in ("hc_g2_xggs", "hc_g2_xggvee"):
         getattr(H, f).restype = d
         getattr(H, f).argtypes = [P, P, P, P, d, d]
+    H.hc_g2_xggvec.restype = d
+    H.hc_g2_xggvec.argtypes = [P, P, P, P, d, d, C.c_void_p]
+    H.hc_pgike1.restype = d
+    H.hc_pgike1.argtypes = [P, P, P, P, d, d, d]
     H.hc_gfvee.restype = d
     H.hc_gfvee.argtypes = [P, P, P, P]
     H.hc_gfke.restype = d
@@ -163,6 +167,14 @@ def test_md_math_matches_oracle(orc, hostcheck):
             check(H.hc_g4(1, A, B, g1, g2), L.orc_g4_xgvepg(A, B, g1, g2), "g4vep")
         r = [C.byref(A[0]), C.byref(A[1]), C.byref(B[0]), C.byref(B[1])]
         check(H.hc_g2_xggs(*r, g1, g2), L.orc_g2_xggs(*r, g1, g2), "g2")
+        # gam_1 kernels (XC1_G2_MD.f, g2.f), with one geminal exponent zero as
+        # in xcalc_GAM1_MD and with both set
+        for ga, gb in ((g1, 0.0), (0.0, g1), (g1, g2)):
+            check(H.hc_g2_xggvec(*r, ga, gb, O.ptr(Cm)),
+                  L.orc_g2_xggvec(*r, ga, gb, O.ptr(Cm)), "g2vec")
+            check(H.hc_g2_xggvee(*r, ga, gb), L.orc_g2_xggvee(*r, ga, gb), "g2vee")
+            check(H.hc_pgike1(*r, ga, gb, 1836.0), L.orc_pgike1(*r, ga, gb, 1836.0, None),
+                  "pgike1")
         check(H.hc_gfvee(*r), L.orc_gfvee(*r), "gfvee")
         check(H.hc_gfke(r[0], r[2], 1.0), L.orc_gfke(r[0], r[2], 1.0), "gfke")
         check(H.hc_gfvec(r[0], r[2], O.ptr(Cm)), L.orc_gfvec(r[0], r[2], O.ptr(Cm)), "gfvec")

@@ -151,3 +151,32 @@ def test_direct_restatement_matches_in_core(orc):
     for a, b in zip(d3, ic3):
         assert np.allclose(a, b, rtol=1e-11, atol=1e-14 * max(1.0, np.abs(b).max()))
     assert abs(d2[4][0]) > 1e-3 and abs(d3[2][0]) > 1e-6
+
+
+def test_xchf_scf_oracle_pinned(xchf, golden_xchf):
+    """The oracle's XCHF SCF (xcscf.f plain Roothaan over its own integrals:
+    overlaps, core Hamiltonians, GAM_ep, GAM_1/GAM_1s, GAM_ee, gam_2, gam_3,
+    gam_4) reproduces examples/xchf: every initial-guess component of
+    XCHF.log:306-321 to the printed 10 decimals, and the converged total
+    energy of XCHF.log:335 (the reference converged with SOSCF; the plain
+    Roothaan sequence reaches the same stationary point)."""
+    import xchf_scf as X
+    s = xchf["sys"]
+    ints = X.XchfIntegrals(s)
+    hist, r, DE, DP, ok = X.xchf_scf(ints, xchf["DE0"])
+    init = hist[0][1]
+    ref = golden_xchf["initial"]
+    for k in ("E_NUC", "E_ECORE", "E_PCORE", "E_EP", "E_EE", "E_GAM1", "E_GAM2", "E_GAM3",
+              "E_GAM4", "S_TOTAL", "E_TOTAL"):
+        mine = {"E_NUC": "E_nuc", "E_ECORE": "E_ecore", "E_PCORE": "E_pcore", "E_EP": "E_ep",
+                "E_EE": "E_ee", "E_GAM1": "E_gam1", "E_GAM2": "E_gam2", "E_GAM3": "E_gam3",
+                "E_GAM4": "E_gam4", "S_TOTAL": "S_total", "E_TOTAL": "E_total"}[k]
+        assert abs(init[mine] - ref[k]) <= 6e-11, (k, init[mine], ref[k])
+    assert ok
+    # iteration 2 precedes the reference's first SOSCF step: same number
+    assert abs(hist[2][1] - (-5.7737887409)) <= 6e-11
+    fin = golden_xchf["final"]
+    assert abs(r["E_total"] - fin["E_TOTAL"]) <= 1e-9
+    for k, mine in (("E_ECORE", "E_ecore"), ("E_EP", "E_ep"), ("E_GAM1", "E_gam1"),
+                    ("E_GAM2", "E_gam2"), ("S_TOTAL", "S_total")):
+        assert abs(r[mine] - fin[k]) <= 1e-5 * max(1.0, abs(fin[k])), k
