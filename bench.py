@@ -341,6 +341,65 @@ def factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
     return out
 
 
+def scf_section(neoxc, with_cpu: bool):
+    """XCHF RHF SCF solves/s on the reference's examples/xchf system (inputs
+    from the committed fixture tests/golden/xchf_example.json: exam_xchf.inp
+    and guessCE.inp), through neoxc_xchf_scf with host arrays: every integral
+    (overlaps, core, GAM_ep, GAM_1, GAM_ee, gam_2, gam_3) is built on the GPU
+    and the Roothaan loop (plain, as xcscf.f, and with DIIS) runs there.  The
+    converged energy is compared with XCHF.log's."""
+    from neoxc import basis
+    with open(os.path.join(ROOT, "tests", "golden", "xchf_example.json")) as f:
+        g = json.load(f)
+    s = basis.parse_inp(g["inp"], name="examples/xchf")
+    DE = basis.density(basis.read_mo_file(g["guessCE"], s.nebf), s.nelec // 2, 2.0)
+    E_log = g["final"]["E_TOTAL"]
+    out = {"workload": "examples/xchf XCHF RHF (nebf=%d, npebf=%d, npbf=%d, NG=%d, nelec=%d), "
+                       "guessCE start, core-Hamiltonian proton guess" % (
+                           s.nebf, s.npebf, s.npbf, s.ngtg, s.nelec),
+           "api": "neoxc_xchf_scf (host arrays; integrals and SCF on the GPU)"}
+    neoxc.xchf_scf(s, DE, maxit=3)   # warm-up (module load, allocator)
+    for name, diis in (("roothan", False), ("diis", True)):
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = neoxc.xchf_scf(s, DE, diis=diis)
+        dt = (time.perf_counter() - t0) / reps
+        t1 = time.perf_counter()
+        neoxc.xchf_scf(s, DE, maxit=1, diis=diis)
+        dt1 = time.perf_counter() - t1
+        out[name] = {"solves_per_s": 1.0 / dt, "ms_per_solve": 1e3 * dt,
+                     "iterations": r["niter"], "converged": r["converged"],
+                     "ms_integrals_plus_first_iteration": 1e3 * dt1,
+                     "ms_per_iteration": 1e3 * (dt - dt1) / max(1, r["niter"] - 1),
+                     "E_total": r["final"]["E_total"],
+                     "E_err_vs_log": r["final"]["E_total"] - E_log}
+    if with_cpu:
+        out["cpu_baseline"] = scf_cpu_baseline(s, DE, out["roothan"]["iterations"])
+    return out
+
+
+def scf_cpu_baseline(s, DE, niter):
+    """The oracle's restatement (C integrals with OpenMP + numpy xcscf) of the
+    same solve: integrals timed in full, the Roothaan loop timed over 3
+    iterations and scaled to the GPU run's iteration count."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import xchf_scf as X
+    O.build()
+    t0 = time.perf_counter()
+    ints = X.XchfIntegrals(s)
+    t_int = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    X.xchf_scf(ints, DE, maxit=3)
+    t_it = (time.perf_counter() - t1) / 3
+    total = t_int + niter * t_it
+    return {"solves_per_s": 1.0 / total, "unit": "SCF solves/s", "kind": "port",
+            "cores": int(O.lib().orc_num_threads()),
+            "sample": "integrals in full (%.1f s) + 3 of %d Roothaan iterations "
+                      "(%.2f s each), scaled" % (t_int, niter, t_it)}
+
+
 def read_hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -449,6 +508,7 @@ def main():
     }
     line["factored"] = factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
                                         d_gee, d_g2s, d_DE, d_DP, mean_ms, float(d_E.item()))
+    line["scf"] = scf_section(neoxc, not args.no_cpu_baseline and ws == 1)
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(ne, np_, gee, g2s, DE, DP)
     print(json.dumps(line), flush=True)

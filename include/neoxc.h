@@ -278,6 +278,9 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
  * electrons, until max|dDE| < 1e-6 (and max|dDP| < 1e-4 when npbf > 1), as
  * xcscf does.  gam_4 uses the factorised Fock build unless
  * NEOXC_SCF_GAM4_ELEMENT selects the element-wise GAM4_DSCF.
+ * NEOXC_SCF_DIIS (no reference counterpart) extrapolates the electronic Fock
+ * matrix over the last 8 iterations (error F DE S - S DE F) before ROOTHAN:
+ * same converged state in fewer iterations.
  *   DE (in: initial electronic density, e.g. from guessCE; out: converged)
  *   DP (in: initial nuclear density unless NEOXC_SCF_GUESS_PROT; out)
  *   E_init[16], E_final[16]: energy slots 0 E_total 1 E_nuc 2 E_ecore
@@ -289,6 +292,7 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
  *   niter, converged: iterations run and 1 when the thresholds were met.
  * Limits: nebf, npbf <= 64; with gam_3 (nelec > 2) nebf <= 20. */
 #define NEOXC_SCF_GUESS_PROT 1     /* DP from the nuclear core Hamiltonian */
+#define NEOXC_SCF_DIIS 2           /* Pulay DIIS on the electronic Fock (new) */
 #define NEOXC_SCF_GAM4_ELEMENT 4   /* element-wise GAM4_DSCF for gam_4     */
 int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,

@@ -991,7 +991,8 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   RC(need(nelec >= 1 && maxit >= 1, "nelec >= 1, maxit >= 1"));
   RC(need(nucst >= 1 && nucst <= npbf, "1 <= nucst <= npbf"));
   RC(need(DE && DP && E_init && E_final && niter && converged, "pointers"));
-  RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_GAM4_ELEMENT)) == 0,
+  RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_DIIS |
+                                NEOXC_SCF_GAM4_ELEMENT)) == 0,
           "options"));
   if (nebf > kScfMaxN || npbf > kScfMaxN)
     return set_err(NEOXC_ERR_UNSUPPORTED, "XCHF SCF: nebf, npbf <= %d", kScfMaxN);
@@ -1056,12 +1057,16 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                                 : gam4f_scratch_doubles(ne, np));
   }
   RC(dalloc(scr, sizeof(double) * nscr, s));
-  RC(dalloc(st, sizeof(int) * 4, s));
+  RC(dalloc(st, sizeof(int) * 8, s));
+  const bool diis = (options & NEOXC_SCF_DIIS) != 0;
+  DBuf dwork;
+  RC(dalloc(dwork, sizeof(double) * (diis ? diis_doubles(ne) : 1), s));
+  if (diis) CU(cudaMemsetAsync(dwork.p, 0, sizeof(double) * diis_doubles(ne), s));
   CU(cudaMemsetAsync(DE0.p, 0, sizeof(double) * e2, s));
   CU(cudaMemsetAsync(DP0.p, 0, sizeof(double) * p2, s));
   CU(cudaMemsetAsync(se2.p, 0, sizeof(double) * e2, s));
   CU(cudaMemsetAsync(sp2.p, 0, sizeof(double) * p2, s));
-  CU(cudaMemsetAsync(st.p, 0, sizeof(int) * 4, s));
+  CU(cudaMemsetAsync(st.p, 0, sizeof(int) * 8, s));
   CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kScfSlots, s));
   const double Enuc = nuc_rep(nat, zan, cat);
   CU(cudaMemcpyAsync(en.as<double>() + 1, &Enuc, sizeof(double),
@@ -1122,6 +1127,9 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
     CU(launch_roothan(np, fp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
                       dDP.as<double>(), nullptr, nullptr, sts + 1, s));
     RC(fock_build());
+    if (diis)
+      CU(launch_diis(ne, fe.as<double>(), dDE.as<double>(), Se.as<double>(),
+                     dwork.as<double>(), sts + 4, nullptr, s));
     CU(launch_roothan(ne, fe.as<double>(), Xe.as<double>(), 0, noccE, prefE,
                       dDE.as<double>(), nullptr, nullptr, sts + 0, s));
     CU(launch_dendif(ne, np, dDE.as<double>(), DE0.as<double>(), dDP.as<double>(),

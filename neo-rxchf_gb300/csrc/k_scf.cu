@@ -530,6 +530,137 @@ __global__ void dendif_kernel(int ne, int np, const double* __restrict__ DE,
   }
 }
 
+// ---- DIIS (Pulay) extrapolation of the electronic Fock matrix ------------------
+// Not in the reference (xcscf.f iterates plain Roothaan or SOSCF).  One CTA:
+// error e = F D S - S D F (= M - M^T with M = F D S for symmetric F, D, S),
+// stored with F in a ring of kDiisMax slots; B_ij = <e_i, e_j>; the Pulay
+// system [B -1; -1 0][c; l] = [0; -1] is solved by Gaussian elimination with
+// partial pivoting; F <- sum_i c_i F_i.  state[0] = vectors held, state[1] =
+// next slot.  With fewer than two vectors, or a singular system, F is left
+// unchanged.  err_out (optional) receives max|e|.
+constexpr int kDiisMax = 8;
+
+__global__ void diis_kernel(int n, double* __restrict__ F,
+                            const double* __restrict__ D,
+                            const double* __restrict__ S, double* __restrict__ Fh,
+                            double* __restrict__ Eh, double* __restrict__ B,
+                            int* __restrict__ state, double* __restrict__ err_out) {
+  extern __shared__ double sm[];
+  double* T = sm;            // F D
+  double* M = sm + n * n;    // F D S
+  __shared__ double sw[32];
+  __shared__ double coef[kDiisMax + 1];
+  __shared__ int s_cnt, s_slot, s_ok;
+  const int nn = n * n;
+  if (threadIdx.x == 0) {
+    s_cnt = state[0];
+    s_slot = state[1];
+  }
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;   // T[i][j]
+    double acc = 0.0;
+    for (int l = 0; l < n; l++) acc += F[i + n * l] * D[l + n * j];
+    T[k] = acc;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;
+    double acc = 0.0;
+    for (int l = 0; l < n; l++) acc += T[i * n + l] * S[l + n * j];
+    M[k] = acc;
+  }
+  __syncthreads();
+  const int slot = s_slot;
+  double* e = Eh + (size_t)slot * nn;
+  double* f = Fh + (size_t)slot * nn;
+  double emax = 0.0;
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+    const int i = k / n, j = k - i * n;
+    const double v = M[i * n + j] - M[j * n + i];
+    e[i + n * j] = v;
+    f[k] = F[k];
+    emax = fmax(emax, fabs(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) emax = fmax(emax, __shfl_down_sync(0xffffffffu, emax, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x / 32] = emax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int k = 0; k < (int)(blockDim.x + 31) / 32; k++) r = fmax(r, sw[k]);
+    if (err_out) *err_out = r;
+  }
+  __syncthreads();
+  const int cnt = s_cnt + 1 < kDiisMax ? s_cnt + 1 : kDiisMax;
+  // new row of B: <e_slot, e_j> for the occupied slots
+  for (int j = 0; j < cnt; j++) {
+    const double* ej = Eh + (size_t)j * nn;
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) acc += e[k] * ej[k];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x / 32] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double r = 0.0;
+      for (int k = 0; k < (int)(blockDim.x + 31) / 32; k++) r += sw[k];
+      B[slot * kDiisMax + j] = r;
+      B[j * kDiisMax + slot] = r;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    state[0] = cnt;
+    state[1] = (slot + 1) % kDiisMax;
+    s_ok = 0;
+    if (cnt >= 2) {
+      const int m = cnt + 1;
+      double A[(kDiisMax + 1) * (kDiisMax + 2)];
+      const int w = m + 1;
+      for (int i = 0; i < cnt; i++) {
+        for (int j = 0; j < cnt; j++) A[i * w + j] = B[i * kDiisMax + j];
+        A[i * w + cnt] = -1.0;
+        A[i * w + m] = 0.0;
+      }
+      for (int j = 0; j < cnt; j++) A[cnt * w + j] = -1.0;
+      A[cnt * w + cnt] = 0.0;
+      A[cnt * w + m] = -1.0;
+      double scale = 0.0;
+      for (int i = 0; i < cnt; i++) scale = fmax(scale, fabs(B[i * kDiisMax + i]));
+      bool ok = scale > 0.0;
+      for (int c = 0; c < m && ok; c++) {
+        int piv = c;
+        for (int r = c + 1; r < m; r++)
+          if (fabs(A[r * w + c]) > fabs(A[piv * w + c])) piv = r;
+        if (fabs(A[piv * w + c]) < 1e-14 * fmax(scale, 1.0)) { ok = false; break; }
+        if (piv != c)
+          for (int k = 0; k <= m; k++) {
+            const double t = A[c * w + k];
+            A[c * w + k] = A[piv * w + k];
+            A[piv * w + k] = t;
+          }
+        for (int r = 0; r < m; r++) {
+          if (r == c) continue;
+          const double fct = A[r * w + c] / A[c * w + c];
+          for (int k = c; k <= m; k++) A[r * w + k] -= fct * A[c * w + k];
+        }
+      }
+      if (ok) {
+        for (int i = 0; i < cnt; i++) coef[i] = A[i * w + m] / A[i * w + i];
+        s_ok = 1;
+      }
+    }
+  }
+  __syncthreads();
+  if (s_ok) {
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+      double acc = 0.0;
+      for (int i = 0; i < cnt; i++) acc += coef[i] * Fh[(size_t)i * nn + k];
+      F[k] = acc;
+    }
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_scf_onebody(const DevSystem& S, double* Se, double* Sp,
@@ -606,6 +737,23 @@ cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
   if (e != cudaSuccess) return e;
   roothan_kernel<<<1, 256, smem, s>>>(n, F, X, first, nocc, prefac, D, evals, C,
                                       status);
+  return cudaGetLastError();
+}
+
+size_t diis_doubles(int n) {
+  return 2 * (size_t)kDiisMax * n * n + (size_t)kDiisMax * kDiisMax;
+}
+
+cudaError_t launch_diis(int n, double* F, const double* D, const double* S,
+                        double* work, int* state, double* err, cudaStream_t s) {
+  if (n < 1 || n > kScfMaxN) return cudaErrorInvalidValue;
+  const size_t smem = sizeof(double) * 2 * (size_t)n * n;
+  cudaError_t e = eig_attr((const void*)diis_kernel, smem);
+  if (e != cudaSuccess) return e;
+  double* Fh = work;
+  double* Eh = Fh + (size_t)kDiisMax * n * n;
+  double* B = Eh + (size_t)kDiisMax * n * n;
+  diis_kernel<<<1, 256, smem, s>>>(n, F, D, S, Fh, Eh, B, state, err);
   return cudaGetLastError();
 }
 

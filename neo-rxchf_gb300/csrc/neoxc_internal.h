@@ -166,6 +166,11 @@ cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
 cudaError_t launch_dendif(int ne, int np, const double* DE, double* DE0,
                           const double* DP, double* DP0, double* en,
                           cudaStream_t s);
+// Pulay DIIS on F (in place) with error F D S - S D F; work = diis_doubles(n)
+// (zeroed before the first call), state[2] = {0, 0} initially.
+size_t diis_doubles(int n);
+cudaError_t launch_diis(int n, double* F, const double* D, const double* S,
+                        double* work, int* state, double* err, cudaStream_t s);
 
 // ---- index maps on the device (pack_GAM.f) -----------------------------
 cudaError_t launch_index_fill(int kind, int ne, int np, int64_t count,

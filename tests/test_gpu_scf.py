@@ -89,3 +89,14 @@ def test_synthetic_scf_matches_oracle(nx, orc, kw):
     if ok:
         assert g["niter"] == len(hist) - 1
         assert abs(g["final"]["E_total"] - r["E_total"]) <= 1e-9
+
+
+def test_diis_converges_to_same_state_faster(nx, xchf, xchf_gpu_scf, golden_xchf):
+    """Pulay DIIS on the electronic Fock matrix (no reference counterpart):
+    same converged energy, fewer iterations than plain Roothaan."""
+    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], diis=True)
+    assert r["converged"]
+    assert r["niter"] < xchf_gpu_scf["niter"]
+    assert abs(r["final"]["E_total"] - golden_xchf["final"]["E_TOTAL"]) <= 1e-9
+    assert abs(r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]) <= 1e-9
+    assert np.abs(r["DE"] - xchf_gpu_scf["DE"]).max() <= 1e-5
