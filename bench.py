@@ -359,14 +359,16 @@ def scf_section(neoxc, with_cpu: bool):
                            s.nebf, s.npebf, s.npbf, s.ngtg, s.nelec),
            "api": "neoxc_xchf_scf (host arrays; integrals and SCF on the GPU)"}
     neoxc.xchf_scf(s, DE, maxit=3)   # warm-up (module load, allocator)
-    for name, diis in (("roothan", False), ("diis", True)):
+    E_fp64 = None
+    for name, diis, mixed in (("roothan", False, False), ("diis", True, False),
+                              ("diis_mixed", True, True)):
         reps = 3
         t0 = time.perf_counter()
         for _ in range(reps):
-            r = neoxc.xchf_scf(s, DE, diis=diis)
+            r = neoxc.xchf_scf(s, DE, diis=diis, mixed=mixed)
         dt = (time.perf_counter() - t0) / reps
         t1 = time.perf_counter()
-        neoxc.xchf_scf(s, DE, maxit=1, diis=diis)
+        neoxc.xchf_scf(s, DE, maxit=1, diis=diis, mixed=mixed)
         dt1 = time.perf_counter() - t1
         out[name] = {"solves_per_s": 1.0 / dt, "ms_per_solve": 1e3 * dt,
                      "iterations": r["niter"], "converged": r["converged"],
@@ -374,6 +376,11 @@ def scf_section(neoxc, with_cpu: bool):
                      "ms_per_iteration": 1e3 * (dt - dt1) / max(1, r["niter"] - 1),
                      "E_total": r["final"]["E_total"],
                      "E_err_vs_log": r["final"]["E_total"] - E_log}
+        if mixed:
+            out[name]["E_err_vs_fp64_Eh"] = r["final"]["E_total"] - E_fp64
+            out[name]["precision"] = "gam_3 MD integrals FP32 (Boys FP64), sums FP64"
+        else:
+            E_fp64 = r["final"]["E_total"]
     if with_cpu:
         out["cpu_baseline"] = scf_cpu_baseline(s, DE, out["roothan"]["iterations"])
     return out

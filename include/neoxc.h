@@ -281,6 +281,9 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
  * NEOXC_SCF_DIIS (no reference counterpart) extrapolates the electronic Fock
  * matrix over the last 8 iterations (error F DE S - S DE F) before ROOTHAN:
  * same converged state in fewer iterations.
+ * NEOXC_SCF_MIXED (no reference counterpart) evaluates the gam_3 primitive
+ * integrals with FP32 McMurchie-Davidson recursions (FP64 Boys function,
+ * FP64 sums over primitives and geminal pairs); everything else stays FP64.
  *   DE (in: initial electronic density, e.g. from guessCE; out: converged)
  *   DP (in: initial nuclear density unless NEOXC_SCF_GUESS_PROT; out)
  *   E_init[16], E_final[16]: energy slots 0 E_total 1 E_nuc 2 E_ecore
@@ -294,6 +297,7 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
 #define NEOXC_SCF_GUESS_PROT 1     /* DP from the nuclear core Hamiltonian */
 #define NEOXC_SCF_DIIS 2           /* Pulay DIIS on the electronic Fock (new) */
 #define NEOXC_SCF_GAM4_ELEMENT 4   /* element-wise GAM4_DSCF for gam_4     */
+#define NEOXC_SCF_MIXED 8          /* gam_3 MD integrals in FP32 (new)     */
 int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
                    const double* cat, const double* zan, const double* bcoef1,

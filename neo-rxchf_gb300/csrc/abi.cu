@@ -992,8 +992,9 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   RC(need(nucst >= 1 && nucst <= npbf, "1 <= nucst <= npbf"));
   RC(need(DE && DP && E_init && E_final && niter && converged, "pointers"));
   RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_DIIS |
-                                NEOXC_SCF_GAM4_ELEMENT)) == 0,
+                                NEOXC_SCF_GAM4_ELEMENT | NEOXC_SCF_MIXED)) == 0,
           "options"));
+  const int mixed = (options & NEOXC_SCF_MIXED) ? 1 : 0;
   if (nebf > kScfMaxN || npbf > kScfMaxN)
     return set_err(NEOXC_ERR_UNSUPPORTED, "XCHF SCF: nebf, npbf <= %d", kScfMaxN);
   const bool elem4 = (options & NEOXC_SCF_GAM4_ELEMENT) != 0;
@@ -1034,7 +1035,7 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
     CU(launch_gam2_symmetrize(ne, np, 0, G2.as<double>(), G2s.as<double>(), s));
   }
   if (nelec > 2) {
-    CU(launch_gam3_raw(u.d, G3.as<double>(), s));
+    CU(launch_gam3_raw(u.d, G3.as<double>(), s, mixed));
     CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
   }
   // SCF state

@@ -20,7 +20,10 @@
 // per-primitive integrand with the factorised MD kernels of md_math.cuh,
 // re-using one Boys'-lemma/derivative setup for every integral that shares
 // a particle order and geminal assignment.
+#include <type_traits>
+
 #include "md_math.cuh"
+#include "md_math32.cuh"
 #include "neoxc_internal.h"
 
 namespace neoxc {
@@ -219,6 +222,65 @@ __device__ double xcalc_gam3(const Prim* A, const Prim* B, const DevSystem& S,
   return 2.0 * gVEE * 0.5 + gHEg + gVEEg1 * 0.5 + 4.0 * gVEEg2 * 0.5;
 }
 
+// Mixed precision: the same integrand with the MD integrals in FP32
+// (md_math32.cuh; Boys function in FP64) and every product with the geminal
+// coefficients and every sum over geminal pairs in FP64.  No reference
+// counterpart: an option of the SCF driver whose energy error against the
+// FP64 path is measured.
+__device__ double xcalc_gam3_f32(const md32::Prim* A, const md32::Prim* B,
+                                 const DevSystem& S, md32::G3& st,
+                                 md32::G4& s4) {
+  const int ng = S.ngtg, nat = S.nat;
+  const double* b = S.bgem;
+  const double* gm = S.ggem;
+  const double yee = (double)md32::gfvee(A[1], A[2], B[1], B[2]);
+  double gVEE = 0.0;
+  for (int ik = 0; ik < ng; ik++) {
+    double xx = (double)md32::g2_xggs(A[0], A[3], B[0], B[3], (float)gm[ik], 0.0f);
+    gVEE = gVEE + (b[ik] * (xx * yee));
+  }
+  double xke = (double)md32::gfke(A[2], B[2], 1.0f);
+  double Vc = 0.0;
+  for (int ia = 0; ia < nat; ia++) {
+    const float C[3] = {(float)S.cat[3 * ia], (float)S.cat[3 * ia + 1],
+                        (float)S.cat[3 * ia + 2]};
+    Vc = Vc + (S.zan[ia] * (double)md32::gfvec(A[2], B[2], C));
+  }
+  const double xh = md::underflow(xke + (Vc * -1.0));
+  md32::Prim A124[3] = {A[0], A[1], A[3]}, B124[3] = {B[0], B[1], B[3]};
+  md32::g4_pairs(s4, A, B);
+  double gHEg = 0, gVEEg1 = 0, gVEEg2 = 0;
+  float g[6];
+  for (int ik = 0; ik < ng; ik++)
+    for (int il = 0; il < ng; il++) {
+      const float gk = (float)gm[ik], gl = (float)gm[il];
+      for (int k = 0; k < 6; k++) g[k] = 0.0f;
+      g[A13] = gk;
+      g[B23] = gl;
+      md32::g3_setup(st, A124, B124, g, 0);
+      double yy = (double)md32::g3_overlap(st);
+      double zz = (double)md32::g4_vep(s4, gk, gl);
+      double xgHEg = ((xh * yy) + (zz * -1.0));
+      double x2 = (double)md32::g2_xggs(A[0], A[3], B[0], B[3], gk, gl);
+      double xgVEEg1 = x2 * yee;
+      double xgVEEg2 = (double)md32::g4_vee(s4, gk, gl);
+      gHEg = gHEg + (b[ik] * b[il] * xgHEg);
+      gVEEg1 = gVEEg1 + (b[ik] * b[il] * xgVEEg1);
+      gVEEg2 = gVEEg2 + (b[ik] * b[il] * xgVEEg2);
+    }
+  return 2.0 * gVEE * 0.5 + gHEg + gVEEg1 * 0.5 + 4.0 * gVEEg2 * 0.5;
+}
+
+__device__ __forceinline__ md32::Prim to_prim32(const DevPrim& d) {
+  md32::Prim p;
+  p.a = (float)d.a;
+  for (int k = 0; k < 3; k++) {
+    p.c[k] = (float)d.c[k];
+    p.l[k] = d.l[k];
+  }
+  return p;
+}
+
 // ---- GAM_ee: thread per contracted (iec1,jec1,iec2,jec2) ------------------
 __global__ void __launch_bounds__(128)
 gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
@@ -322,6 +384,7 @@ __global__ void gam2_sym_kernel(int ne, int np, int rx, double* __restrict__ x1,
 }
 
 // ---- gam_3 raw tensor: warp per contracted tuple ----------------------------
+template <bool F32>
 __global__ void __launch_bounds__(64)
 gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
                 long long ntup) {
@@ -347,8 +410,8 @@ gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
   const DevPrim& pa = S.pprim[ip];
   const DevPrim& pb = S.pprim[jp];
   const double cp = pa.coef * pb.coef;
-  G3 st;
-  G4 s4;
+  typename std::conditional<F32, md32::G3, G3>::type st;
+  typename std::conditional<F32, md32::G4, G4>::type s4;
   double o = 0.0;
   for (int q = lane; q < nq; q += 32) {
     int qq = q, idx[6];
@@ -356,11 +419,20 @@ gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
       idx[k] = st0[k] + qq % cnt[k];
       qq /= cnt[k];
     }
-    Prim A[4] = {to_prim(S.eprim[idx[0]]), to_prim(S.eprim[idx[2]]),
-                 to_prim(S.eprim[idx[4]]), to_prim(pa)};
-    Prim B[4] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
-                 to_prim(S.eprim[idx[5]]), to_prim(pb)};
-    double ans = xcalc_gam3(A, B, S, st, s4);
+    double ans;
+    if constexpr (F32) {
+      md32::Prim A[4] = {to_prim32(S.eprim[idx[0]]), to_prim32(S.eprim[idx[2]]),
+                         to_prim32(S.eprim[idx[4]]), to_prim32(pa)};
+      md32::Prim B[4] = {to_prim32(S.eprim[idx[1]]), to_prim32(S.eprim[idx[3]]),
+                         to_prim32(S.eprim[idx[5]]), to_prim32(pb)};
+      ans = xcalc_gam3_f32(A, B, S, st, s4);
+    } else {
+      Prim A[4] = {to_prim(S.eprim[idx[0]]), to_prim(S.eprim[idx[2]]),
+                   to_prim(S.eprim[idx[4]]), to_prim(pa)};
+      Prim B[4] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
+                   to_prim(S.eprim[idx[5]]), to_prim(pb)};
+      ans = xcalc_gam3(A, B, S, st, s4);
+    }
     double cc = cp;
     for (int k = 0; k < 6; k++) cc = cc * S.eprim[idx[k]].coef;
     o = o + ans * cc;
@@ -442,18 +514,21 @@ cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,
 }
 
 cudaError_t launch_gam3_raw_range(const DevSystem& sys, long long t0,
-                                  long long ntup, double* x3, cudaStream_t s) {
+                                  long long ntup, double* x3, cudaStream_t s,
+                                  int fp32) {
   const long long threads = ntup * 32;
   const unsigned blocks = (unsigned)((threads + 63) / 64);
   if (ntup <= 0) return cudaSuccess;
-  gam3_raw_kernel<<<blocks, 64, 0, s>>>(sys, x3, t0, ntup);
+  if (fp32) gam3_raw_kernel<true><<<blocks, 64, 0, s>>>(sys, x3, t0, ntup);
+  else gam3_raw_kernel<false><<<blocks, 64, 0, s>>>(sys, x3, t0, ntup);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3, cudaStream_t s) {
+cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3, cudaStream_t s,
+                            int fp32) {
   const long long n6 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
                        sys.nebf * sys.nebf;
-  return launch_gam3_raw_range(sys, 0, n6 * sys.npbf * sys.npbf, x3, s);
+  return launch_gam3_raw_range(sys, 0, n6 * sys.npbf * sys.npbf, x3, s, fp32);
 }
 
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,

@@ -100,3 +100,13 @@ def test_diis_converges_to_same_state_faster(nx, xchf, xchf_gpu_scf, golden_xchf
     assert abs(r["final"]["E_total"] - golden_xchf["final"]["E_TOTAL"]) <= 1e-9
     assert abs(r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]) <= 1e-9
     assert np.abs(r["DE"] - xchf_gpu_scf["DE"]).max() <= 1e-5
+
+
+def test_mixed_precision_gam3_energy_error(nx, xchf, xchf_gpu_scf):
+    """FP32 MD for the gam_3 integrals (FP64 Boys and sums): the converged
+    total energy stays within 1 microhartree of the FP64 path."""
+    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], mixed=True)
+    assert r["converged"]
+    err = r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]
+    print("mixed-precision E error (Eh):", err)
+    assert abs(err) <= 1e-6
