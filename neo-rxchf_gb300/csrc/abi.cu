@@ -992,9 +992,11 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   RC(need(nucst >= 1 && nucst <= npbf, "1 <= nucst <= npbf"));
   RC(need(DE && DP && E_init && E_final && niter && converged, "pointers"));
   RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_DIIS |
-                                NEOXC_SCF_GAM4_ELEMENT | NEOXC_SCF_MIXED)) == 0,
+                                NEOXC_SCF_GAM4_ELEMENT | NEOXC_SCF_MIXED |
+                                NEOXC_SCF_MIXED_GAM2)) == 0,
           "options"));
   const int mixed = (options & NEOXC_SCF_MIXED) ? 1 : 0;
+  const int mixed_gam2 = (options & NEOXC_SCF_MIXED_GAM2) ? 1 : 0;
   if (nebf > kScfMaxN || npbf > kScfMaxN)
     return set_err(NEOXC_ERR_UNSUPPORTED, "XCHF SCF: nebf, npbf <= %d", kScfMaxN);
   const bool elem4 = (options & NEOXC_SCF_GAM4_ELEMENT) != 0;
@@ -1031,7 +1033,8 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s));
   CU(launch_gam_ee(u.d, Gee.as<double>(), s));
   if (nelec > 1) {
-    CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s));
+    CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s,
+                       mixed_gam2));
     CU(launch_gam2_symmetrize(ne, np, 0, G2.as<double>(), G2s.as<double>(), s));
   }
   if (nelec > 2) {

@@ -6,7 +6,7 @@
 //   gam2_CONV_OMP.f:388-579 (contract_omega2_conv),
 //   gam2_IC1_OMP.f:214-337 (thread_gam2_IC1)     -> gam2_raw_kernel
 //   rxchfne/rxchfne_gam_2_OMP.f:2-530,
-//   rxchfne/rxchfne_gam2_IC1_OMP.f:245-340       -> gam2_raw_kernel<RX>
+//   rxchfne/rxchfne_gam2_IC1_OMP.f:245-340       -> gam2_raw_kernel<RX, F32>
 //   gam2_IC1_OMP.f:136-185, rxchfne_gam2_IC1_OMP.f:184-201
 //                                                -> gam2_sym_kernel
 //   gam_3_OMP.f:617-984 (xcalc_GAM3_MD),
@@ -48,44 +48,55 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-__device__ __forceinline__ void gam6(double* g, int slot_a, double va,
-                                     int slot_b, double vb) {
-  for (int k = 0; k < 6; k++) g[k] = 0.0;
+template <class R>
+__device__ __forceinline__ void gam6(R* g, int slot_a, R va, int slot_b, R vb) {
+  for (int k = 0; k < 6; k++) g[k] = R(0.0);
   if (slot_a >= 0) g[slot_a] = va;
   if (slot_b >= 0) g[slot_b] = vb;
 }
 enum { A12 = 0, A13, A23, B12, B13, B23 };
 
-__device__ __forceinline__ void perm3(const Prim* X, int a, int b, int c,
-                                      Prim* Y) {
+template <class P>
+__device__ __forceinline__ void perm3(const P* X, int a, int b, int c, P* Y) {
   Y[0] = X[a];
   Y[1] = X[b];
   Y[2] = X[c];
 }
 
-// gam_2_OMP.f:546-1077 xcalc_GAM2_MD.  Particles (e1, e2, p).
-__device__ void xcalc_gam2(const Prim* A, const Prim* B, const DevSystem& S,
-                           G3& st, double& ansE, double& ansS) {
+// gam_2_OMP.f:546-1077 xcalc_GAM2_MD.  Particles (e1, e2, p).  P is md::Prim
+// (FP64 integrals) or md32::Prim (FP32 integrals of the mixed path); the
+// integral calls resolve to md:: / md32:: by argument-dependent lookup and
+// every sum over geminal terms is FP64 in both.
+template <class P, class G3T>
+__device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
+                           G3T& st, double& ansE, double& ansS) {
+  using R = typename std::remove_cv<decltype(P::a)>::type;
   const int ng = S.ngtg, nat = S.nat;
   const double* b = S.bgem;
   const double* gm = S.ggem;
-  Prim A132[3], B132[3], A312[3], B312[3];
+  P A132[3], B132[3], A312[3], B312[3];
   perm3(A, 0, 2, 1, A132);
   perm3(B, 0, 2, 1, B132);
   perm3(A, 2, 0, 1, A312);
   perm3(B, 2, 0, 1, B312);
-  double g[6];
+  R g[6];
+  const R zero = R(0.0), one = R(1.0);
+  // centre of classical nucleus ia in the working precision
+  auto vxc = [&](int ia) {
+    const R C3[3] = {(R)S.cat[3 * ia], (R)S.cat[3 * ia + 1], (R)S.cat[3 * ia + 2]};
+    return md::underflow((double)g3_vxc(st, C3));
+  };
   double gTE = 0, gVEC = 0, gVEE = 0, gVEP = 0;
   for (int ik = 0; ik < ng; ik++) {
-    gam6(g, A23, gm[ik], -1, 0.0);
-    md::g3_setup(st, A, B, g, 2);
-    double xgTE = md::g3_ke(st, 0.0, 1.0);
+    gam6(g, A23, (R)gm[ik], -1, zero);
+    g3_setup(st, A, B, g, 2);
+    double xgTE = (double)g3_ke(st, zero, one);
     double xgVEC = 0.0;
     for (int ia = 0; ia < nat; ia++)
-      xgVEC = xgVEC - S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
-    double xgVEE = md::underflow(md::g3_vee(st));
-    md::g3_setup(st, A132, B132, g, 0);
-    double xgVEP = -md::underflow(md::g3_vee(st));
+      xgVEC = xgVEC - S.zan[ia] * vxc(ia);
+    double xgVEE = md::underflow((double)g3_vee(st));
+    g3_setup(st, A132, B132, g, 0);
+    double xgVEP = -md::underflow((double)g3_vee(st));
     gTE = gTE + b[ik] * xgTE;
     gVEC = gVEC + b[ik] * xgVEC;
     gVEP = gVEP + b[ik] * xgVEP;
@@ -95,45 +106,46 @@ __device__ void xcalc_gam2(const Prim* A, const Prim* B, const DevSystem& S,
          gVECg2 = 0, gVEPg1 = 0, gVEPg2 = 0, gVEEg1 = 0, gVEEg2 = 0, gsg = 0;
   for (int ik = 0; ik < ng; ik++)
     for (int il = 0; il < ng; il++) {
-      const double gk = gm[ik], gl = gm[il], bb = b[ik] * b[il];
+      const R gk = (R)gm[ik], gl = (R)gm[il];
+      const double bb = b[ik] * b[il];
       // order (p, e1, e2): gA12 = g(p,e1), gB13 = g(p,e2)
       gam6(g, A12, gk, B13, gl);
-      md::g3_setup(st, A312, B312, g, 2);
-      double xgTPg = md::g3_ke(st, gl, S.pmass);
+      g3_setup(st, A312, B312, g, 2);
+      double xgTPg = (double)g3_ke(st, gl, (R)S.pmass);
       double xgVPCg = 0.0;
       for (int ia = 0; ia < nat; ia++)
-        xgVPCg = xgVPCg + S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
+        xgVPCg = xgVPCg + S.zan[ia] * vxc(ia);
       // order (e1, e2, p): A13, B23
       gam6(g, A13, gk, B23, gl);
-      md::g3_setup(st, A, B, g, 2);
-      double xgTEg1 = md::g3_ke(st, 0.0, 1.0);
+      g3_setup(st, A, B, g, 2);
+      double xgTEg1 = (double)g3_ke(st, zero, one);
       double xgVECg1 = 0.0;
       for (int ia = 0; ia < nat; ia++)
-        xgVECg1 = xgVECg1 - S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
-      double xgVEEg2 = md::underflow(md::g3_vee(st));
-      double xgsg = md::g3_overlap(st);
+        xgVECg1 = xgVECg1 - S.zan[ia] * vxc(ia);
+      double xgVEEg2 = md::underflow((double)g3_vee(st));
+      double xgsg = (double)g3_overlap(st);
       // A23, B13
       gam6(g, A23, gk, B13, gl);
-      md::g3_setup(st, A, B, g, 2);
-      double xgTEg2 = md::g3_ke(st, gl, 1.0);
+      g3_setup(st, A, B, g, 2);
+      double xgTEg2 = (double)g3_ke(st, gl, one);
       // A23, B23
       gam6(g, A23, gk, B23, gl);
-      md::g3_setup(st, A, B, g, 2);
-      double xgTEg3 = md::g3_ke(st, 0.0, 1.0);
+      g3_setup(st, A, B, g, 2);
+      double xgTEg3 = (double)g3_ke(st, zero, one);
       double xgVECg2 = 0.0;
       for (int ia = 0; ia < nat; ia++)
-        xgVECg2 = xgVECg2 - S.zan[ia] * md::underflow(md::g3_vxc(st, S.cat + 3 * ia));
+        xgVECg2 = xgVECg2 - S.zan[ia] * vxc(ia);
       // A13, B13
       gam6(g, A13, gk, B13, gl);
-      md::g3_setup(st, A, B, g, 0);
-      double xgVEEg1 = md::underflow(md::g3_vee(st));
+      g3_setup(st, A, B, g, 0);
+      double xgVEEg1 = md::underflow((double)g3_vee(st));
       // order (e1, p, e2): A12 B23 and A23 B23
       gam6(g, A12, gk, B23, gl);
-      md::g3_setup(st, A132, B132, g, 0);
-      double xgVEPg1 = -md::underflow(md::g3_vee(st));
+      g3_setup(st, A132, B132, g, 0);
+      double xgVEPg1 = -md::underflow((double)g3_vee(st));
       gam6(g, A23, gk, B23, gl);
-      md::g3_setup(st, A132, B132, g, 0);
-      double xgVEPg2 = -md::underflow(md::g3_vee(st));
+      g3_setup(st, A132, B132, g, 0);
+      double xgVEPg2 = -md::underflow((double)g3_vee(st));
       gTPg = gTPg + bb * xgTPg;
       gTEg1 = gTEg1 + bb * xgTEg1;
       gTEg2 = gTEg2 + bb * xgTEg2;
@@ -309,7 +321,7 @@ gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
 }
 
 // ---- gam_2 raw tensors: warp per contracted tuple --------------------------
-template <int RX>
+template <int RX, bool F32>
 __global__ void __launch_bounds__(64)
 gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
                 double* __restrict__ x2, long long t0, long long ntup) {
@@ -332,7 +344,7 @@ gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
   const DevPrim& pa = S.pprim[ip];
   const DevPrim& pb = S.pprim[jp];
   const double cp = pa.coef * pb.coef;
-  G3 st;
+  typename std::conditional<F32, md32::G3, G3>::type st;
   double o1 = 0.0, o2 = 0.0;
   for (int q = lane; q < nq; q += 32) {
     int qq = q;
@@ -340,11 +352,17 @@ gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
     const int i2 = s_i2 + qq % n_i2; qq /= n_i2;
     const int j1 = s_j1 + qq % n_j1; qq /= n_j1;
     const int i1 = s_i1 + qq;
-    Prim A[3] = {to_prim(S.eprim[i1]), to_prim(S.eprim[i2]), to_prim(pa)};
-    Prim B[3] = {to_prim(S.eprim[j1]), to_prim(S.eprim[j2]), to_prim(pb)};
     double a1, a2;
-    if (RX) xcalc_gam2_rx(A, B, S, st, a1, a2);
-    else xcalc_gam2(A, B, S, st, a1, a2);
+    if constexpr (F32) {
+      md32::Prim A[3] = {to_prim32(S.eprim[i1]), to_prim32(S.eprim[i2]), to_prim32(pa)};
+      md32::Prim B[3] = {to_prim32(S.eprim[j1]), to_prim32(S.eprim[j2]), to_prim32(pb)};
+      xcalc_gam2(A, B, S, st, a1, a2);
+    } else {
+      Prim A[3] = {to_prim(S.eprim[i1]), to_prim(S.eprim[i2]), to_prim(pa)};
+      Prim B[3] = {to_prim(S.eprim[j1]), to_prim(S.eprim[j2]), to_prim(pb)};
+      if (RX) xcalc_gam2_rx(A, B, S, st, a1, a2);
+      else xcalc_gam2(A, B, S, st, a1, a2);
+    }
     const double c = cp * S.eprim[i1].coef * S.eprim[j1].coef *
                      S.eprim[i2].coef * S.eprim[j2].coef;
     o1 = o1 + a1 * c;
@@ -488,20 +506,22 @@ cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s) {
 
 cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
                                   long long ntup, double* x1, double* x2,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, int fp32) {
   const long long threads = ntup * 32;
   const unsigned blocks = (unsigned)((threads + 63) / 64);
   if (ntup <= 0) return cudaSuccess;
-  if (rx) gam2_raw_kernel<1><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
-  else gam2_raw_kernel<0><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
+  if (rx && fp32) return cudaErrorInvalidValue;   // FP32 path: XCHF gam_2 only
+  if (rx) gam2_raw_kernel<1, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
+  else if (fp32) gam2_raw_kernel<0, true><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
+  else gam2_raw_kernel<0, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rx, double* x1,
-                            double* x2, cudaStream_t s) {
+                            double* x2, cudaStream_t s, int fp32) {
   const long long ntup = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
                          sys.npbf * sys.npbf;
-  return launch_gam2_raw_range(sys, rx, 0, ntup, x1, x2, s);
+  return launch_gam2_raw_range(sys, rx, 0, ntup, x1, x2, s, fp32);
 }
 
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,

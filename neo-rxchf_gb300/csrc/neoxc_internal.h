@@ -123,13 +123,13 @@ cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s);
 // tuples [t0, t0+ntup) of the packed index space, written from x[0]
 cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
                                   long long ntup, double* x1, double* x2,
-                                  cudaStream_t s);
+                                  cudaStream_t s, int fp32 = 0);
 // fp32 = 1: MD integrals in FP32 (md_math32.cuh), sums in FP64 (mixed path)
 cudaError_t launch_gam3_raw_range(const DevSystem& sys, long long t0,
                                   long long ntup, double* x3, cudaStream_t s,
                                   int fp32 = 0);
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rxchfne, double* x1,
-                            double* x2, cudaStream_t s);
+                            double* x2, cudaStream_t s, int fp32 = 0);
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rxchfne, double* x1,
                                    double* x2, cudaStream_t s);
 cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3,
