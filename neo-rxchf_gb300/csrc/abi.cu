@@ -447,9 +447,11 @@ int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan,
                   bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX,
                   NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC));
-  DBuf d;
+  DBuf d, aux;
   RC(dalloc(d, sizeof(double) * ng3, s));
-  CU(launch_gam3_raw(u.d, d.as<double>(), s));
+  RC(dalloc(aux, sizeof(double) * gam3_aux_doubles((int)nebf, (int)npbf), s));
+  CU(launch_gam3_aux(u.d, aux.as<double>(), s));
+  CU(launch_gam3_raw(u.d, aux.as<double>(), d.as<double>(), s));
   CU(launch_gam3_symmetrize((int)nebf, (int)npbf, d.as<double>(), s));
   CU(cudaMemcpyAsync(GM3ICR, d.p, sizeof(double) * ng3, cudaMemcpyDeviceToHost,
                      s));
@@ -862,9 +864,11 @@ int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
                   gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
                   NUCAM, ELCBFC, NUCBFC));
   const int ne = (int)nebf, np = (int)npbf;
-  DBuf slice, part, dde, ddp, dfe, dfp, dE;
+  DBuf slice, part, dde, ddp, dfe, dfp, dE, aux;
   RC(dalloc(slice, sizeof(double) * n6, s));
   RC(dalloc(part, sizeof(double) * eg3_partial_doubles(ne, np), s));
+  RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
+  CU(launch_gam3_aux(u.d, aux.as<double>(), s));
   RC(upload(dde, DE, sizeof(double) * nebf * nebf, s));
   RC(upload(ddp, DP, sizeof(double) * npbf * npbf, s));
   RC(dalloc(dfe, sizeof(double) * nebf * nebf, s));
@@ -873,7 +877,8 @@ int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * nebf * nebf, s));
   CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * npbf * npbf, s));
   for (int64_t pp = 0; pp < npbf * npbf; pp++) {
-    CU(launch_gam3_raw_range(u.d, pp * n6, n6, slice.as<double>(), s));
+    CU(launch_gam3_raw_range(u.d, aux.as<double>(), pp * n6, n6,
+                             slice.as<double>(), s));
     CU(launch_gam3_symmetrize(ne, 1, slice.as<double>(), s));
     CU(launch_eg3_partials(ne, np, pp, 1, dde.as<double>(), slice.as<double>(),
                            part.as<double>(), s));
@@ -1038,7 +1043,10 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
     CU(launch_gam2_symmetrize(ne, np, 0, G2.as<double>(), G2s.as<double>(), s));
   }
   if (nelec > 2) {
-    CU(launch_gam3_raw(u.d, G3.as<double>(), s, mixed));
+    DBuf aux;
+    RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
+    CU(launch_gam3_aux(u.d, aux.as<double>(), s));
+    CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed));
     CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
   }
   // SCF state

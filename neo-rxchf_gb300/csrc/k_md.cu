@@ -195,92 +195,37 @@ __device__ void xcalc_gam2_rx(const Prim* A, const Prim* B,
   ansE2 = gVEEg2;
 }
 
-// gam_3_OMP.f:617-984 xcalc_GAM3_MD.  Particles (e1, e2, e3, p).
-__device__ double xcalc_gam3(const Prim* A, const Prim* B, const DevSystem& S,
-                             G3& st, G4& s4) {
-  const int ng = S.ngtg, nat = S.nat;
+// gam_3_OMP.f:617-984 xcalc_GAM3_MD, particles (e1, e2, e3, p):
+//   ans = gVEE + gHEg + gVEEg1/2 + 2 gVEEg2 (:964) with
+//   gVEE   = sum_k b_k G2xggs(e1,p; g_k, 0) (e2 e2'|e3 e3')            (:720-753)
+//   gHEg   = sum_kl b_k b_l [h(e3) G3xggs(e1,e2,p; g_k, g_l) - G4Vep]    (:760-872)
+//   gVEEg1 = sum_kl b_k b_l G2xggs(e1,p; g_k, g_l) (e2 e2'|e3 e3')      (:877-902)
+//   gVEEg2 = sum_kl b_k b_l G4Vee                                      (:907-930)
+// with h(e3) the electronic core Hamiltonian.  Three of the terms are
+// products of factors on disjoint particles, so their contracted sums are
+// built once as small tensors (W1(p,e1) x GAM_ee(e2,e3) and
+// W3(p,e1,e2) x Hcore(e3), gam3_aux) instead of per primitive 8-tuple; the
+// primitive loop keeps only the four-particle Coulomb integrals:
+//   g4part = sum_kl b_k b_l (2 G4Vee - G4Vep).
+template <class G4T, class P>
+__device__ double gam3_g4part(const P* A, const P* B, const DevSystem& S,
+                              G4T& s4) {
+  using R = typename std::remove_cv<decltype(P::a)>::type;
+  const int ng = S.ngtg;
   const double* b = S.bgem;
   const double* gm = S.ggem;
-  // particle-2/3 factors that do not depend on the geminal indices
-  const double yee = md::underflow(md::gfvee(A[1], A[2], B[1], B[2]));
-  double gVEE = 0.0;
-  for (int ik = 0; ik < ng; ik++) {
-    double xx = md::underflow(md::g2_xggs(A[0], A[3], B[0], B[3], gm[ik], 0.0));
-    gVEE = gVEE + (b[ik] * (xx * yee));
-  }
-  double xke = md::gfke(A[2], B[2], 1.0);
-  double Vc = 0.0;
-  for (int ia = 0; ia < nat; ia++)
-    Vc = Vc + (S.zan[ia] * md::gfvec(A[2], B[2], S.cat + 3 * ia));
-  const double xh = md::underflow(xke + (Vc * -1.0));
-  Prim A124[3] = {A[0], A[1], A[3]}, B124[3] = {B[0], B[1], B[3]};
-  md::g4_pairs(s4, A, B);
-  double gHEg = 0, gVEEg1 = 0, gVEEg2 = 0, g[6];
+  g4_pairs(s4, A, B);
+  double zsum = 0.0, vsum = 0.0;
   for (int ik = 0; ik < ng; ik++)
     for (int il = 0; il < ng; il++) {
-      const double gk = gm[ik], gl = gm[il];
-      gam6(g, A13, gk, B23, gl);
-      md::g3_setup(st, A124, B124, g, 0);
-      double yy = md::underflow(md::g3_overlap(st));
-      double zz = md::underflow(md::g4_vep(s4, gk, gl));
-      double xgHEg = ((xh * yy) + (zz * -1.0));
-      double x2 = md::underflow(md::g2_xggs(A[0], A[3], B[0], B[3], gk, gl));
-      double xgVEEg1 = x2 * yee;
-      double xgVEEg2 = md::g4_vee(s4, gk, gl);
-      gHEg = gHEg + (b[ik] * b[il] * xgHEg);
-      gVEEg1 = gVEEg1 + (b[ik] * b[il] * xgVEEg1);
-      gVEEg2 = gVEEg2 + (b[ik] * b[il] * xgVEEg2);
+      const R gk = (R)gm[ik], gl = (R)gm[il];
+      const double bb = b[ik] * b[il];
+      const double zz = md::underflow((double)g4_vep(s4, gk, gl));
+      const double vv = (double)g4_vee(s4, gk, gl);
+      zsum = zsum + bb * zz;
+      vsum = vsum + bb * vv;
     }
-  return 2.0 * gVEE * 0.5 + gHEg + gVEEg1 * 0.5 + 4.0 * gVEEg2 * 0.5;
-}
-
-// Mixed precision: the same integrand with the MD integrals in FP32
-// (md_math32.cuh; Boys function in FP64) and every product with the geminal
-// coefficients and every sum over geminal pairs in FP64.  No reference
-// counterpart: an option of the SCF driver whose energy error against the
-// FP64 path is measured.
-__device__ double xcalc_gam3_f32(const md32::Prim* A, const md32::Prim* B,
-                                 const DevSystem& S, md32::G3& st,
-                                 md32::G4& s4) {
-  const int ng = S.ngtg, nat = S.nat;
-  const double* b = S.bgem;
-  const double* gm = S.ggem;
-  const double yee = (double)md32::gfvee(A[1], A[2], B[1], B[2]);
-  double gVEE = 0.0;
-  for (int ik = 0; ik < ng; ik++) {
-    double xx = (double)md32::g2_xggs(A[0], A[3], B[0], B[3], (float)gm[ik], 0.0f);
-    gVEE = gVEE + (b[ik] * (xx * yee));
-  }
-  double xke = (double)md32::gfke(A[2], B[2], 1.0f);
-  double Vc = 0.0;
-  for (int ia = 0; ia < nat; ia++) {
-    const float C[3] = {(float)S.cat[3 * ia], (float)S.cat[3 * ia + 1],
-                        (float)S.cat[3 * ia + 2]};
-    Vc = Vc + (S.zan[ia] * (double)md32::gfvec(A[2], B[2], C));
-  }
-  const double xh = md::underflow(xke + (Vc * -1.0));
-  md32::Prim A124[3] = {A[0], A[1], A[3]}, B124[3] = {B[0], B[1], B[3]};
-  md32::g4_pairs(s4, A, B);
-  double gHEg = 0, gVEEg1 = 0, gVEEg2 = 0;
-  float g[6];
-  for (int ik = 0; ik < ng; ik++)
-    for (int il = 0; il < ng; il++) {
-      const float gk = (float)gm[ik], gl = (float)gm[il];
-      for (int k = 0; k < 6; k++) g[k] = 0.0f;
-      g[A13] = gk;
-      g[B23] = gl;
-      md32::g3_setup(st, A124, B124, g, 0);
-      double yy = (double)md32::g3_overlap(st);
-      double zz = (double)md32::g4_vep(s4, gk, gl);
-      double xgHEg = ((xh * yy) + (zz * -1.0));
-      double x2 = (double)md32::g2_xggs(A[0], A[3], B[0], B[3], gk, gl);
-      double xgVEEg1 = x2 * yee;
-      double xgVEEg2 = (double)md32::g4_vee(s4, gk, gl);
-      gHEg = gHEg + (b[ik] * b[il] * xgHEg);
-      gVEEg1 = gVEEg1 + (b[ik] * b[il] * xgVEEg1);
-      gVEEg2 = gVEEg2 + (b[ik] * b[il] * xgVEEg2);
-    }
-  return 2.0 * gVEE * 0.5 + gHEg + gVEEg1 * 0.5 + 4.0 * gVEEg2 * 0.5;
+  return 2.0 * vsum - zsum;
 }
 
 __device__ __forceinline__ md32::Prim to_prim32(const DevPrim& d) {
@@ -401,11 +346,114 @@ __global__ void gam2_sym_kernel(int ne, int np, int rx, double* __restrict__ x1,
   }
 }
 
+// ---- separable gam_3 factors (contracted, FP64) ---------------------------
+// W1[ip][jp][i1][j1] = sum_prims c c c_p c_p' [sum_k b_k G2xggs(g_k,0)
+//                       + 1/2 sum_kl b_k b_l G2xggs(g_k,g_l)]       (e1, p)
+__global__ void gam3_w1_kernel(DevSystem S, double* __restrict__ W1) {
+  const int ne = S.nebf, np = S.npbf;
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (w >= (long long)np * np * ne * ne) return;
+  long long r = w;
+  const int j1 = (int)(r % ne); r /= ne;
+  const int i1 = (int)(r % ne); r /= ne;
+  const int jp = (int)(r % np);
+  const int ip = (int)(r / np);
+  const int s1 = S.kpestr[i1], n1 = S.kpeend[i1] - s1 + 1;
+  const int s2 = S.kpestr[j1], n2 = S.kpeend[j1] - s2 + 1;
+  const Prim P1 = to_prim(S.pprim[ip]), P2 = to_prim(S.pprim[jp]);
+  double o = 0.0;
+  for (int q = lane; q < n1 * n2; q += 32) {
+    const int a = s1 + q / n2, bq = s2 + q % n2;
+    const Prim A = to_prim(S.eprim[a]), B = to_prim(S.eprim[bq]);
+    double v = 0.0;
+    for (int k = 0; k < S.ngtg; k++)
+      v = v + S.bgem[k] * md::underflow(md::g2_xggs(A, P1, B, P2, S.ggem[k], 0.0));
+    double v2 = 0.0;
+    for (int k = 0; k < S.ngtg; k++)
+      for (int l = 0; l < S.ngtg; l++)
+        v2 = v2 + S.bgem[k] * S.bgem[l] *
+                      md::underflow(md::g2_xggs(A, P1, B, P2, S.ggem[k], S.ggem[l]));
+    o = o + (v + 0.5 * v2) * (S.eprim[a].coef * S.eprim[bq].coef *
+                              S.pprim[ip].coef * S.pprim[jp].coef);
+  }
+  o = warp_sum(o);
+  if (lane == 0) W1[w] = o;
+}
+
+// W3[ip][jp][i1][j1][i2][j2] = sum_prims c^6 sum_kl b_k b_l
+//                              G3xggs(e1,e2,p; A13 = g_k, B23 = g_l)
+__global__ void __launch_bounds__(64)
+gam3_w3_kernel(DevSystem S, double* __restrict__ W3) {
+  const int ne = S.nebf, np = S.npbf;
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (w >= (long long)np * np * ne * ne * ne * ne) return;
+  long long r = w;
+  int c[4];
+  for (int k = 3; k >= 0; k--) {
+    c[k] = (int)(r % ne);
+    r /= ne;
+  }
+  const int jp = (int)(r % np);
+  const int ip = (int)(r / np);
+  int st0[4], cnt[4], nq = 1;
+  for (int k = 0; k < 4; k++) {
+    st0[k] = S.kpestr[c[k]];
+    cnt[k] = S.kpeend[c[k]] - st0[k] + 1;
+    nq *= cnt[k];
+  }
+  G3 st;
+  double o = 0.0, g[6];
+  for (int q = lane; q < nq; q += 32) {
+    int qq = q, idx[4];
+    for (int k = 3; k >= 0; k--) {
+      idx[k] = st0[k] + qq % cnt[k];
+      qq /= cnt[k];
+    }
+    const Prim A[3] = {to_prim(S.eprim[idx[0]]), to_prim(S.eprim[idx[2]]),
+                       to_prim(S.pprim[ip])};
+    const Prim B[3] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
+                       to_prim(S.pprim[jp])};
+    double v = 0.0;
+    for (int k = 0; k < S.ngtg; k++)
+      for (int l = 0; l < S.ngtg; l++) {
+        gam6(g, A13, S.ggem[k], B23, S.ggem[l]);
+        md::g3_setup(st, A, B, g, 0);
+        v = v + S.bgem[k] * S.bgem[l] * md::underflow(md::g3_overlap(st));
+      }
+    double cc = S.pprim[ip].coef * S.pprim[jp].coef;
+    for (int k = 0; k < 4; k++) cc = cc * S.eprim[idx[k]].coef;
+    o = o + v * cc;
+  }
+  o = warp_sum(o);
+  if (lane == 0) W3[w] = o;
+}
+
+// Hcore[i][j] = sum_prims c c [T - sum_C Z V_C]  (xcalc_GAM3_MD's h(e3))
+__global__ void gam3_hcore_kernel(DevSystem S, double* __restrict__ Hc) {
+  const int ne = S.nebf;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ne * ne) return;
+  const int i = t / ne, j = t - i * ne;
+  double h = 0.0;
+  for (int a = S.kpestr[i]; a <= S.kpeend[i]; a++)
+    for (int bq = S.kpestr[j]; bq <= S.kpeend[j]; bq++) {
+      const Prim A = to_prim(S.eprim[a]), B = to_prim(S.eprim[bq]);
+      const double xke = md::gfke(A, B, 1.0);
+      double Vc = 0.0;
+      for (int ia = 0; ia < S.nat; ia++)
+        Vc = Vc + (S.zan[ia] * md::gfvec(A, B, S.cat + 3 * ia));
+      h = h + (xke + (Vc * -1.0)) * (S.eprim[a].coef * S.eprim[bq].coef);
+    }
+  Hc[t] = h;
+}
+
 // ---- gam_3 raw tensor: warp per contracted tuple ----------------------------
 template <bool F32>
 __global__ void __launch_bounds__(64)
-gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
-                long long ntup) {
+gam3_raw_kernel(DevSystem S, const double* __restrict__ aux,
+                double* __restrict__ x3, long long t0, long long ntup) {
   const int ne = S.nebf, np = S.npbf;
   const int lane = threadIdx.x & 31;
   const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -428,7 +476,6 @@ gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
   const DevPrim& pa = S.pprim[ip];
   const DevPrim& pb = S.pprim[jp];
   const double cp = pa.coef * pb.coef;
-  typename std::conditional<F32, md32::G3, G3>::type st;
   typename std::conditional<F32, md32::G4, G4>::type s4;
   double o = 0.0;
   for (int q = lane; q < nq; q += 32) {
@@ -443,20 +490,33 @@ gam3_raw_kernel(DevSystem S, double* __restrict__ x3, long long t0,
                          to_prim32(S.eprim[idx[4]]), to_prim32(pa)};
       md32::Prim B[4] = {to_prim32(S.eprim[idx[1]]), to_prim32(S.eprim[idx[3]]),
                          to_prim32(S.eprim[idx[5]]), to_prim32(pb)};
-      ans = xcalc_gam3_f32(A, B, S, st, s4);
+      ans = gam3_g4part(A, B, S, s4);
     } else {
       Prim A[4] = {to_prim(S.eprim[idx[0]]), to_prim(S.eprim[idx[2]]),
                    to_prim(S.eprim[idx[4]]), to_prim(pa)};
       Prim B[4] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
                    to_prim(S.eprim[idx[5]]), to_prim(pb)};
-      ans = xcalc_gam3(A, B, S, st, s4);
+      ans = gam3_g4part(A, B, S, s4);
     }
     double cc = cp;
     for (int k = 0; k < 6; k++) cc = cc * S.eprim[idx[k]].coef;
     o = o + ans * cc;
   }
   o = warp_sum(o);
-  if (lane == 0) x3[w] = o;
+  if (lane == 0) {
+    // separable terms: W1(p,e1) GAM_ee(e2,e3) + W3(p,e1,e2) Hcore(e3)
+    const long long n2 = (long long)ne * ne, n4 = n2 * n2;
+    const double* gee = aux;
+    const double* hc = gee + n4;
+    const double* W1 = hc + n2;
+    const double* W3 = W1 + (long long)np * np * n2;
+    const long long pp = (long long)ip * np + jp;
+    const double w1 = W1[(pp * ne + c[0]) * ne + c[1]];
+    const double w3 = W3[(((pp * ne + c[0]) * ne + c[1]) * ne + c[2]) * ne + c[3]];
+    const double ee = gee[((c[2] * (long long)ne + c[3]) * ne + c[4]) * ne + c[5]];
+    const double h = hc[c[4] * ne + c[5]];
+    x3[w] = o + w1 * ee + w3 * h;
+  }
 }
 
 // Six-permutation symmetrisation in place: each orbit is handled by the
@@ -533,22 +593,43 @@ cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,
   return cudaGetLastError();
 }
 
-cudaError_t launch_gam3_raw_range(const DevSystem& sys, long long t0,
-                                  long long ntup, double* x3, cudaStream_t s,
-                                  int fp32) {
-  const long long threads = ntup * 32;
-  const unsigned blocks = (unsigned)((threads + 63) / 64);
-  if (ntup <= 0) return cudaSuccess;
-  if (fp32) gam3_raw_kernel<true><<<blocks, 64, 0, s>>>(sys, x3, t0, ntup);
-  else gam3_raw_kernel<false><<<blocks, 64, 0, s>>>(sys, x3, t0, ntup);
+size_t gam3_aux_doubles(int ne, int np) {
+  const size_t n2 = (size_t)ne * ne;
+  return n2 * n2 + n2 + (size_t)np * np * n2 + (size_t)np * np * n2 * n2;
+}
+
+cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s) {
+  const int ne = sys.nebf, np = sys.npbf;
+  const long long n2 = (long long)ne * ne, n4 = n2 * n2;
+  double* gee = aux;
+  double* hc = gee + n4;
+  double* W1 = hc + n2;
+  double* W3 = W1 + (long long)np * np * n2;
+  cudaError_t e = launch_gam_ee(sys, gee, s);
+  if (e != cudaSuccess) return e;
+  gam3_hcore_kernel<<<(unsigned)((n2 + 127) / 128), 128, 0, s>>>(sys, hc);
+  const long long w1 = (long long)np * np * n2, w3 = w1 * n2;
+  gam3_w1_kernel<<<(unsigned)((w1 * 32 + 127) / 128), 128, 0, s>>>(sys, W1);
+  gam3_w3_kernel<<<(unsigned)((w3 * 32 + 63) / 64), 64, 0, s>>>(sys, W3);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3, cudaStream_t s,
-                            int fp32) {
+cudaError_t launch_gam3_raw_range(const DevSystem& sys, const double* aux,
+                                  long long t0, long long ntup, double* x3,
+                                  cudaStream_t s, int fp32) {
+  const long long threads = ntup * 32;
+  const unsigned blocks = (unsigned)((threads + 63) / 64);
+  if (ntup <= 0) return cudaSuccess;
+  if (fp32) gam3_raw_kernel<true><<<blocks, 64, 0, s>>>(sys, aux, x3, t0, ntup);
+  else gam3_raw_kernel<false><<<blocks, 64, 0, s>>>(sys, aux, x3, t0, ntup);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gam3_raw(const DevSystem& sys, const double* aux, double* x3,
+                            cudaStream_t s, int fp32) {
   const long long n6 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
                        sys.nebf * sys.nebf;
-  return launch_gam3_raw_range(sys, 0, n6 * sys.npbf * sys.npbf, x3, s, fp32);
+  return launch_gam3_raw_range(sys, aux, 0, n6 * sys.npbf * sys.npbf, x3, s, fp32);
 }
 
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,

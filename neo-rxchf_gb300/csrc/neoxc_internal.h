@@ -124,15 +124,20 @@ cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s);
 cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
                                   long long ntup, double* x1, double* x2,
                                   cudaStream_t s, int fp32 = 0);
-// fp32 = 1: MD integrals in FP32 (md_math32.cuh), sums in FP64 (mixed path)
-cudaError_t launch_gam3_raw_range(const DevSystem& sys, long long t0,
-                                  long long ntup, double* x3, cudaStream_t s,
-                                  int fp32 = 0);
+// gam_3 raw tensor = W1(p,e1) GAM_ee(e2,e3) + W3(p,e1,e2) Hcore(e3) + the
+// primitive sum of the four-particle terms.  aux (gam3_aux_doubles) holds
+// GAM_ee, Hcore, W1, W3 from launch_gam3_aux (FP64).  fp32 = 1: the
+// four-particle integrals in FP32 (md_math32.cuh), sums in FP64 (mixed path).
+size_t gam3_aux_doubles(int ne, int np);
+cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s);
+cudaError_t launch_gam3_raw_range(const DevSystem& sys, const double* aux,
+                                  long long t0, long long ntup, double* x3,
+                                  cudaStream_t s, int fp32 = 0);
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rxchfne, double* x1,
                             double* x2, cudaStream_t s, int fp32 = 0);
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rxchfne, double* x1,
                                    double* x2, cudaStream_t s);
-cudaError_t launch_gam3_raw(const DevSystem& sys, double* x3,
+cudaError_t launch_gam3_raw(const DevSystem& sys, const double* aux, double* x3,
                             cudaStream_t s, int fp32 = 0);
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,
                                    cudaStream_t s);
