@@ -361,14 +361,14 @@ def scf_section(neoxc, with_cpu: bool):
     neoxc.xchf_scf(s, DE, maxit=3)   # warm-up (module load, allocator)
     E_fp64 = None
     for name, diis, mixed in (("roothan", False, False), ("diis", True, False),
-                              ("diis_mixed", True, 1), ("diis_mixed_gam2", True, 2)):
+                              ("diis_mixed_gam3", True, "gam3"), ("diis_mixed", True, True)):
         reps = 3
         t0 = time.perf_counter()
         for _ in range(reps):
-            r = neoxc.xchf_scf(s, DE, diis=diis, mixed=bool(mixed), mixed_gam2=mixed == 2)
+            r = neoxc.xchf_scf(s, DE, diis=diis, mixed=mixed)
         dt = (time.perf_counter() - t0) / reps
         t1 = time.perf_counter()
-        neoxc.xchf_scf(s, DE, maxit=1, diis=diis, mixed=bool(mixed), mixed_gam2=mixed == 2)
+        neoxc.xchf_scf(s, DE, maxit=1, diis=diis, mixed=mixed)
         dt1 = time.perf_counter() - t1
         out[name] = {"solves_per_s": 1.0 / dt, "ms_per_solve": 1e3 * dt,
                      "iterations": r["niter"], "converged": r["converged"],
@@ -378,8 +378,10 @@ def scf_section(neoxc, with_cpu: bool):
                      "E_err_vs_log": r["final"]["E_total"] - E_log}
         if mixed:
             out[name]["E_err_vs_fp64_Eh"] = r["final"]["E_total"] - E_fp64
-            out[name]["precision"] = ("gam_3%s MD integrals FP32 (Boys FP64), sums FP64"
-                                      % (" and gam_2" if mixed == 2 else ""))
+            out[name]["precision"] = ("%s MD integrals FP32, sums over primitives and "
+                                      "geminal terms FP64; one-body, GAM_ee, contractions, "
+                                      "Fock assembly and diagonalisation FP64"
+                                      % ("gam_3" if mixed == "gam3" else "gam_1, gam_2, gam_3"))
         else:
             E_fp64 = r["final"]["E_total"]
     if with_cpu:

@@ -1035,7 +1035,7 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   CU(launch_scf_onebody(u.d, Se.as<double>(), Sp.as<double>(), Hce.as<double>(),
                         Hcp.as<double>(), s));
   CU(launch_gam_ep(u.d, Gep.as<double>(), s));
-  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s));
+  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, mixed_gam2));
   CU(launch_gam_ee(u.d, Gee.as<double>(), s));
   if (nelec > 1) {
     CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s,
@@ -1045,7 +1045,8 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   if (nelec > 2) {
     DBuf aux;
     RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
-    CU(launch_gam3_aux(u.d, aux.as<double>(), s));
+    // GAM_ee and the core Hamiltonian (Hce, pack_2D order) are already built
+    CU(launch_gam3_aux(u.d, aux.as<double>(), s, Gee.as<double>(), Hce.as<double>()));
     CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed));
     CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
   }

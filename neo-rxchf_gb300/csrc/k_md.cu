@@ -598,16 +598,23 @@ size_t gam3_aux_doubles(int ne, int np) {
   return n2 * n2 + n2 + (size_t)np * np * n2 + (size_t)np * np * n2 * n2;
 }
 
-cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s) {
+cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s,
+                            const double* gee_in, const double* hc_in) {
   const int ne = sys.nebf, np = sys.npbf;
   const long long n2 = (long long)ne * ne, n4 = n2 * n2;
   double* gee = aux;
   double* hc = gee + n4;
   double* W1 = hc + n2;
   double* W3 = W1 + (long long)np * np * n2;
-  cudaError_t e = launch_gam_ee(sys, gee, s);
+  cudaError_t e = gee_in ? cudaMemcpyAsync(gee, gee_in, sizeof(double) * n4,
+                                           cudaMemcpyDeviceToDevice, s)
+                         : launch_gam_ee(sys, gee, s);
   if (e != cudaSuccess) return e;
-  gam3_hcore_kernel<<<(unsigned)((n2 + 127) / 128), 128, 0, s>>>(sys, hc);
+  if (hc_in)
+    e = cudaMemcpyAsync(hc, hc_in, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s);
+  else
+    gam3_hcore_kernel<<<(unsigned)((n2 + 127) / 128), 128, 0, s>>>(sys, hc);
+  if (e != cudaSuccess) return e;
   const long long w1 = (long long)np * np * n2, w3 = w1 * n2;
   gam3_w1_kernel<<<(unsigned)((w1 * 32 + 127) / 128), 128, 0, s>>>(sys, W1);
   gam3_w3_kernel<<<(unsigned)((w3 * 32 + 63) / 64), 64, 0, s>>>(sys, W3);

@@ -13,7 +13,10 @@
 // reference's Fortran arrays; the core matrices keep pack_2D order
 // ([i][j] = GAM_ecore(pack_2D(n,j,i))) and GAM_ep / GAM_1 / GAM_1s keep
 // pack_4D(nebf,nebf,npbf, je,ie,jp,ip) order, i.e. C-order [ip][jp][ie][je].
+#include <type_traits>
+
 #include "md_math.cuh"
+#include "md_math32.cuh"
 #include "neoxc_internal.h"
 
 namespace neoxc {
@@ -102,41 +105,47 @@ __global__ void gam_ep_kernel(DevSystem S, double* __restrict__ Gep) {
 }
 
 // ---- gam_1 (gam_1_OMP.f:398-836 xcalc_GAM1_MD) -----------------------------
-// A = (e, p), B = (e', p'); returns ansE, ansS.
-__device__ __noinline__ void xcalc_gam1(const Prim* A, const Prim* B,
+// A = (e, p), B = (e', p'); returns ansE, ansS.  P is md::Prim (FP64) or
+// md32::Prim (FP32 integrals, mixed path); the integral calls resolve by
+// argument-dependent lookup and every geminal/atom sum is FP64.
+template <class P>
+__device__ __noinline__ void xcalc_gam1(const P* A, const P* B,
                                         const DevSystem& S, double* ansE,
                                         double* ansS) {
-  const double zero = 0.0, one = 1.0, pmass = S.pmass;
-  double tegx = zero, tpgx = zero, texg = zero, tpxg = zero, tegg = zero,
-         tpgg = zero, VCEGX = zero, VCEGG = zero, VCPGX = zero, VCPGG = zero,
-         VMGX = zero, VMGG = zero;
+  using R = typename std::remove_cv<decltype(P::a)>::type;
+  const R zero = R(0.0), one = R(1.0), pmass = (R)S.pmass;
+  double tegx = 0.0, tpgx = 0.0, texg = 0.0, tpxg = 0.0, tegg = 0.0,
+         tpgg = 0.0, VCEGX = 0.0, VCEGG = 0.0, VCPGX = 0.0, VCPGG = 0.0,
+         VMGX = 0.0, VMGG = 0.0;
   for (int k = 0; k < S.ngtg; k++) {
-    const double GV = S.ggem[k], BV = S.bgem[k];
-    tegx = tegx + BV * md::pgike1(A[0], A[1], B[0], B[1], GV, zero, one);
-    tpgx = tpgx + BV * md::pgike1(A[1], A[0], B[1], B[0], GV, zero, pmass);
-    double ve = zero, vp = zero;
+    const R GV = (R)S.ggem[k];
+    const double BV = S.bgem[k];
+    tegx = tegx + BV * (double)pgike1(A[0], A[1], B[0], B[1], GV, zero, one);
+    tpgx = tpgx + BV * (double)pgike1(A[1], A[0], B[1], B[0], GV, zero, pmass);
+    double ve = 0.0, vp = 0.0;
     for (int c = 0; c < S.nat; c++) {
-      const double C[3] = {S.cat[3 * c], S.cat[3 * c + 1], S.cat[3 * c + 2]};
-      ve = md::g2_xggvec(A[0], A[1], B[0], B[1], GV, zero, C) * S.zan[c] + ve;
-      vp = md::g2_xggvec(A[1], A[0], B[1], B[0], GV, zero, C) * S.zan[c] + vp;
+      const R C[3] = {(R)S.cat[3 * c], (R)S.cat[3 * c + 1], (R)S.cat[3 * c + 2]};
+      ve = (double)g2_xggvec(A[0], A[1], B[0], B[1], GV, zero, C) * S.zan[c] + ve;
+      vp = (double)g2_xggvec(A[1], A[0], B[1], B[0], GV, zero, C) * S.zan[c] + vp;
     }
-    const double vm = md::g2_xggvee(A[0], A[1], B[0], B[1], GV, zero);
+    const double vm = (double)g2_xggvee(A[0], A[1], B[0], B[1], GV, zero);
     VCEGX = VCEGX + BV * ve;
     VCPGX = VCPGX + BV * vp;
     VMGX = VMGX + BV * vm;
-    texg = texg + BV * md::pgike1(A[0], A[1], B[0], B[1], zero, GV, one);
-    tpxg = tpxg + BV * md::pgike1(A[1], A[0], B[1], B[0], zero, GV, pmass);
+    texg = texg + BV * (double)pgike1(A[0], A[1], B[0], B[1], zero, GV, one);
+    tpxg = tpxg + BV * (double)pgike1(A[1], A[0], B[1], B[0], zero, GV, pmass);
     for (int l = 0; l < S.ngtg; l++) {
-      const double GW = S.ggem[l], BW = S.bgem[l];
-      tegg = tegg + BV * BW * md::pgike1(A[0], A[1], B[0], B[1], GV, GW, one);
-      tpgg = tpgg + BV * BW * md::pgike1(A[1], A[0], B[1], B[0], GV, GW, pmass);
-      double vee = zero, vpp = zero;
+      const R GW = (R)S.ggem[l];
+      const double BW = S.bgem[l];
+      tegg = tegg + BV * BW * (double)pgike1(A[0], A[1], B[0], B[1], GV, GW, one);
+      tpgg = tpgg + BV * BW * (double)pgike1(A[1], A[0], B[1], B[0], GV, GW, pmass);
+      double vee = 0.0, vpp = 0.0;
       for (int c = 0; c < S.nat; c++) {
-        const double C[3] = {S.cat[3 * c], S.cat[3 * c + 1], S.cat[3 * c + 2]};
-        vee = md::g2_xggvec(A[0], A[1], B[0], B[1], GV, GW, C) * S.zan[c] + vee;
-        vpp = md::g2_xggvec(A[1], A[0], B[1], B[0], GV, GW, C) * S.zan[c] + vpp;
+        const R C[3] = {(R)S.cat[3 * c], (R)S.cat[3 * c + 1], (R)S.cat[3 * c + 2]};
+        vee = (double)g2_xggvec(A[0], A[1], B[0], B[1], GV, GW, C) * S.zan[c] + vee;
+        vpp = (double)g2_xggvec(A[1], A[0], B[1], B[0], GV, GW, C) * S.zan[c] + vpp;
       }
-      const double vmm = md::g2_xggvee(A[0], A[1], B[0], B[1], GV, GW);
+      const double vmm = (double)g2_xggvee(A[0], A[1], B[0], B[1], GV, GW);
       VCEGG = VCEGG + BV * BW * vee;
       VCPGG = VCPGG + BV * BW * vpp;
       VMGG = VMGG + BV * BW * vmm;
@@ -146,18 +155,31 @@ __device__ __noinline__ void xcalc_gam1(const Prim* A, const Prim* B,
   const double VCE = 2.0 * VCEGX + VCEGG, VCP = 2.0 * VCPGX + VCPGG;
   const double VMX = 2.0 * VMGX + VMGG;
   *ansE = TE + TP - VCE + VCP - VMX;
-  double OGX = zero, OGG = zero;
+  double OGX = 0.0, OGG = 0.0;
   for (int k = 0; k < S.ngtg; k++) {
-    const double GV = S.ggem[k], BV = S.bgem[k];
-    OGX = OGX + BV * md::g2_xggs(A[0], A[1], B[0], B[1], GV, zero);
+    const R GV = (R)S.ggem[k];
+    const double BV = S.bgem[k];
+    OGX = OGX + BV * (double)g2_xggs(A[0], A[1], B[0], B[1], GV, zero);
     for (int l = 0; l < S.ngtg; l++)
-      OGG = OGG + BV * S.bgem[l] * md::g2_xggs(A[0], A[1], B[0], B[1], GV, S.ggem[l]);
+      OGG = OGG + BV * S.bgem[l] *
+                      (double)g2_xggs(A[0], A[1], B[0], B[1], GV, (R)S.ggem[l]);
   }
   *ansS = 2.0 * OGX + OGG;
 }
 
+__device__ __forceinline__ md32::Prim to_prim32(const DevPrim& p) {
+  md32::Prim r;
+  r.a = (float)p.a;
+  for (int d = 0; d < 3; d++) {
+    r.c[d] = (float)p.c[d];
+    r.l[d] = p.l[d];
+  }
+  return r;
+}
+
 // One warp per contracted (ip, jp, ie, je); lanes take primitive pairs and
 // the warp sums them in a fixed shuffle order (deterministic).
+template <bool F32>
 __global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
                             double* __restrict__ G1s) {
   const int ne = S.nebf, np = S.npbf;
@@ -175,13 +197,16 @@ __global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
   double e = 0.0, sv = 0.0;
   for (int k = lane; k < na * nb; k += 32) {
     const int a = S.kpestr[ie] + k / nb, b = S.kpestr[je] + k % nb;
-    Prim A[2], B[2];
-    A[0] = to_prim(S.eprim[a]);
-    A[1] = to_prim(S.pprim[ip]);
-    B[0] = to_prim(S.eprim[b]);
-    B[1] = to_prim(S.pprim[jp]);
     double aE, aS;
-    xcalc_gam1(A, B, S, &aE, &aS);
+    if constexpr (F32) {
+      md32::Prim A[2] = {to_prim32(S.eprim[a]), to_prim32(S.pprim[ip])};
+      md32::Prim B[2] = {to_prim32(S.eprim[b]), to_prim32(S.pprim[jp])};
+      xcalc_gam1(A, B, S, &aE, &aS);
+    } else {
+      Prim A[2] = {to_prim(S.eprim[a]), to_prim(S.pprim[ip])};
+      Prim B[2] = {to_prim(S.eprim[b]), to_prim(S.pprim[jp])};
+      xcalc_gam1(A, B, S, &aE, &aS);
+    }
     const double cip = S.pprim[ip].coef, cjp = S.pprim[jp].coef;
     const double cie = S.eprim[a].coef, cje = S.eprim[b].coef;
     e = e + aE * cip * cjp * cie * cje;
@@ -677,10 +702,11 @@ cudaError_t launch_gam_ep(const DevSystem& S, double* Gep, cudaStream_t s) {
 }
 
 cudaError_t launch_gam1(const DevSystem& S, double* G1, double* G1s,
-                        cudaStream_t s) {
+                        cudaStream_t s, int fp32) {
   const long long warps = (long long)S.npbf * S.npbf * S.nebf * S.nebf;
   const long long blocks = (warps * 32 + 127) / 128;
-  gam1_kernel<<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s);
+  if (fp32) gam1_kernel<true><<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s);
+  else gam1_kernel<false><<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s);
   return cudaGetLastError();
 }
 

@@ -129,7 +129,11 @@ cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
 // GAM_ee, Hcore, W1, W3 from launch_gam3_aux (FP64).  fp32 = 1: the
 // four-particle integrals in FP32 (md_math32.cuh), sums in FP64 (mixed path).
 size_t gam3_aux_doubles(int ne, int np);
-cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s);
+// gee_in / hc_in (optional, device): GAM_ee and Hcore already built by the
+// caller (C-order [i][j][k][l] and [i][j]); copied instead of recomputed.
+cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s,
+                            const double* gee_in = nullptr,
+                            const double* hc_in = nullptr);
 cudaError_t launch_gam3_raw_range(const DevSystem& sys, const double* aux,
                                   long long t0, long long ntup, double* x3,
                                   cudaStream_t s, int fp32 = 0);
@@ -152,7 +156,7 @@ cudaError_t launch_scf_onebody(const DevSystem& sys, double* Se, double* Sp,
                                double* Hce, double* Hcp, cudaStream_t s);
 cudaError_t launch_gam_ep(const DevSystem& sys, double* Gep, cudaStream_t s);
 cudaError_t launch_gam1(const DevSystem& sys, double* G1, double* G1s,
-                        cudaStream_t s);
+                        cudaStream_t s, int fp32 = 0);
 size_t scf_fock1_part_doubles(int ne, int np);
 cudaError_t launch_scf_fock1(int ne, int np, int nelec, const double* Hce,
                              const double* Hcp, const double* Gep,

@@ -105,18 +105,18 @@ def test_diis_converges_to_same_state_faster(nx, xchf, xchf_gpu_scf, golden_xchf
 def test_mixed_precision_gam3_energy_error(nx, xchf, xchf_gpu_scf):
     """FP32 MD for the gam_3 integrals (FP64 Boys and sums): the converged
     total energy stays within 1 microhartree of the FP64 path."""
-    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], mixed=True)
+    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], mixed="gam3")
     assert r["converged"]
     err = r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]
-    print("mixed-precision E error (Eh):", err)
+    print("mixed-precision (gam_3) E error (Eh):", err)
     assert abs(err) <= 1e-6
 
 
-def test_mixed_precision_gam2_gam3_energy_error(nx, xchf, xchf_gpu_scf):
-    """FP32 MD for both gam_2 and gam_3 (FP64 Boys and sums): the converged
-    total energy error against the FP64 path is reported and bounded."""
-    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], mixed=True, mixed_gam2=True, diis=True)
+def test_mixed_precision_all_geminal_energy_error(nx, xchf, xchf_gpu_scf):
+    """FP32 MD for gam_1, gam_2 and gam_3 (FP64 sums), with DIIS: the
+    converged total energy is within 1 microhartree of the FP64 path."""
+    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], mixed=True, diis=True)
     assert r["converged"]
     err = r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]
-    print("mixed-precision (gam_2 + gam_3) E error (Eh):", err)
+    print("mixed-precision (gam_1 + gam_2 + gam_3) E error (Eh):", err)
     assert abs(err) <= 1e-6
