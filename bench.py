@@ -384,8 +384,29 @@ def scf_section(neoxc, with_cpu: bool):
                                       % ("gam_3" if mixed == "gam3" else "gam_1, gam_2, gam_3"))
         else:
             E_fp64 = r["final"]["E_total"]
+    out["batch"] = scf_batch_section(neoxc, s, DE)
     if with_cpu:
         out["cpu_baseline"] = scf_cpu_baseline(s, DE, out["roothan"]["iterations"])
+    return out
+
+
+def scf_batch_section(neoxc, s, DE, njobs=48):
+    """A proton-position scan (proton basis centre displaced uniformly within
+    +-0.5 bohr, seeded) of njobs independent solves through
+    neoxc_xchf_scf_batch: solves/s with one worker stream and with eight."""
+    from neoxc import basis
+    systems = basis.proton_scan(s, njobs, 0.5, seed=11)
+    DEs = [DE] * njobs
+    out = {"workload": "%d-point proton-position scan of examples/xchf, DIIS" % njobs}
+    neoxc.xchf_scf_batch(systems[:2], DEs[:2], nworkers=2, diis=True, mixed=True)
+    for mixed in (False, True):
+        for nw in (1, 8):
+            t0 = time.perf_counter()
+            res = neoxc.xchf_scf_batch(systems, DEs, nworkers=nw, diis=True, mixed=mixed)
+            dt = time.perf_counter() - t0
+            key = "%s_workers%d" % ("mixed" if mixed else "fp64", nw)
+            out[key] = {"solves_per_s": njobs / dt, "seconds": dt,
+                        "converged": sum(r["converged"] for r in res)}
     return out
 
 

@@ -312,6 +312,34 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    double* E_final, double* history, int64_t* niter,
                    int64_t* converged);
 
+/* ---- batched XCHF solves (no reference counterpart) ----------------------------
+ * One job = the arguments of neoxc_xchf_scf for one system; the outputs are
+ * written into the job.  neoxc_xchf_scf_batch runs the jobs on nworkers
+ * host threads, each with its own CUDA stream: a worker takes the next job
+ * as soon as it is free, and a job starts only when its device footprint
+ * fits in 80 % of the memory free at entry (one at a time if a single job is
+ * larger).  Each job's result equals a separate neoxc_xchf_scf call.
+ * Returns NEOXC_OK, or the first failing job's code (every job's own code is
+ * in its status field). */
+typedef struct neoxc_xchf_job {
+  int64_t nelec, nucst, nebf, npebf, npbf, nat, ngtg1;
+  double pmass;
+  const double *cat, *zan, *bcoef1, *gamma1;
+  const int64_t *KPESTR, *KPEEND, *AMPEB2C;
+  const double *AGEBFCC, *AGNBFCC, *ELCEX, *NUCEX;
+  const int64_t *ELCAM, *NUCAM;
+  const double *ELCBFC, *NUCBFC;
+  double *DE, *DP;           /* in: start densities; out: converged */
+  double *E_init, *E_final;  /* [16] each, slots as neoxc_xchf_scf */
+  double *history;           /* [4*maxit] or NULL */
+  int64_t niter, converged;  /* out */
+  int32_t status;            /* out: NEOXC_OK or an error code */
+  int32_t reserved;
+} neoxc_xchf_job;
+int64_t neoxc_xchf_job_size(void);   /* sizeof(neoxc_xchf_job), for bindings */
+int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
+                         int64_t options, int64_t maxit);
+
 /* ---- diagnostics (no reference counterpart) --------------------------- */
 /* Sustained FP64 FMA throughput of the current device in TFLOP/s (2 FLOP
  * per FMA), the denominator of the FP64 rooflines. */

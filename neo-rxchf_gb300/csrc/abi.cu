@@ -9,6 +9,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
+#include <thread>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -980,7 +982,7 @@ static double nuc_rep(int64_t nat, const double* zan, const double* cat) {
   return E;
 }
 
-int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
+static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
                    const double* cat, const double* zan, const double* bcoef1,
                    const double* gamma1, const int64_t* KPESTR,
@@ -1009,8 +1011,6 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
     return set_err(NEOXC_ERR_UNSUPPORTED, "XCHF SCF with gam_3: nebf <= 20");
   if (nelec > 2 && elem4 && nebf > kGam4MaxNE)
     return set_err(NEOXC_ERR_UNSUPPORTED, "element-wise gam_4: nebf <= %d", kGam4MaxNE);
-  cudaStream_t s;
-  RC(get_stream(&s));
   SysUpload u;
   RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
                   gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
@@ -1171,6 +1171,118 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
   CU(cudaMemcpyAsync(DE, dDE.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(DP, dDP.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
   return finish(s);
+}
+
+
+int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
+                   int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
+                   const double* cat, const double* zan, const double* bcoef1,
+                   const double* gamma1, const int64_t* KPESTR,
+                   const int64_t* KPEEND, const int64_t* AMPEB2C,
+                   const double* AGEBFCC, const double* AGNBFCC,
+                   const double* ELCEX, const double* NUCEX,
+                   const int64_t* ELCAM, const int64_t* NUCAM,
+                   const double* ELCBFC, const double* NUCBFC, int64_t options,
+                   int64_t maxit, double* DE, double* DP, double* E_init,
+                   double* E_final, double* history, int64_t* niter,
+                   int64_t* converged) {
+  cudaStream_t s;
+  RC(get_stream(&s));
+  return xchf_scf_on(s, nelec, nucst, nebf, npebf, npbf, nat, ngtg1, pmass, cat,
+                     zan, bcoef1, gamma1, KPESTR, KPEEND, AMPEB2C, AGEBFCC,
+                     AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC,
+                     options, maxit, DE, DP, E_init, E_final, history, niter,
+                     converged);
+}
+
+int64_t neoxc_xchf_job_size(void) { return (int64_t)sizeof(neoxc_xchf_job); }
+
+// Device bytes one solve holds at its peak (integral tensors, SCF state and
+// contraction scratch), for admission against the memory budget.
+static size_t xchf_job_bytes(const neoxc_xchf_job& j, int64_t options) {
+  const size_t ne = (size_t)j.nebf, np = (size_t)j.npbf;
+  const size_t e2 = ne * ne, p2 = np * np;
+  size_t d = 4 * e2 + 4 * p2 + 3 * e2 * p2 + e2 * e2 + 32 * (e2 + p2);
+  if (j.nelec > 1) d += 2 * e2 * e2 * p2 + eg2_partial_doubles((int)ne, (int)np);
+  if (j.nelec > 2) {
+    d += e2 * e2 * e2 * p2 + gam3_aux_doubles((int)ne, (int)np) +
+         eg3_partial_doubles((int)ne, (int)np);
+    d += (options & NEOXC_SCF_GAM4_ELEMENT) ? gam4_partial_doubles((int)ne, (int)np)
+                                            : gam4f_scratch_doubles((int)ne, (int)np);
+  }
+  return sizeof(double) * d + (1u << 20);
+}
+
+// Independent XCHF solves (geometry or proton-position scans, many small
+// molecules) on nworkers host threads, each with its own CUDA stream.  Jobs
+// are taken in order as workers free up, and a job starts only when its
+// device footprint fits in 80 % of the memory free at entry (one job at a
+// time if a single job exceeds that).  Every job gives the same result as a
+// separate neoxc_xchf_scf call (same kernels, same order on its stream).
+int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
+                         int64_t options, int64_t maxit) {
+  RC(need(jobs != nullptr && njobs >= 0 && nworkers >= 1, "jobs, njobs, nworkers"));
+  if (njobs == 0) return NEOXC_OK;
+  cudaStream_t s0;
+  RC(get_stream(&s0));   // checks the device and fixes it for the workers
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  size_t free_b = 0, total_b = 0;
+  CU(cudaMemGetInfo(&free_b, &total_b));
+  const size_t budget = (size_t)(0.8 * (double)free_b);
+  std::mutex mu;
+  std::condition_variable cv;
+  size_t in_use = 0;
+  int running = 0;
+  std::atomic<int64_t> next(0);
+  const int nw = (int)std::min<int64_t>(nworkers, njobs);
+  std::vector<std::thread> pool;
+  for (int w = 0; w < nw; w++) {
+    pool.emplace_back([&, w]() {
+      (void)w;
+      cudaSetDevice(dev);
+      cudaStream_t st = nullptr;
+      if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) st = nullptr;
+      for (;;) {
+        const int64_t k = next.fetch_add(1);
+        if (k >= njobs) break;
+        neoxc_xchf_job& j = jobs[k];
+        if (!st) {
+          j.status = NEOXC_ERR_CUDA;
+          continue;
+        }
+        const size_t need_b = xchf_job_bytes(j, options);
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return running == 0 || in_use + need_b <= budget; });
+          in_use += need_b;
+          running++;
+        }
+        j.status = xchf_scf_on(st, j.nelec, j.nucst, j.nebf, j.npebf, j.npbf, j.nat,
+                               j.ngtg1, j.pmass, j.cat, j.zan, j.bcoef1, j.gamma1,
+                               j.KPESTR, j.KPEEND, j.AMPEB2C, j.AGEBFCC, j.AGNBFCC,
+                               j.ELCEX, j.NUCEX, j.ELCAM, j.NUCAM, j.ELCBFC,
+                               j.NUCBFC, options, maxit, j.DE, j.DP, j.E_init,
+                               j.E_final, j.history, &j.niter, &j.converged);
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          in_use -= need_b;
+          running--;
+        }
+        cv.notify_all();
+      }
+      if (st) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+      }
+    });
+  }
+  for (auto& t : pool) t.join();
+  for (int64_t k = 0; k < njobs; k++)
+    if (jobs[k].status != NEOXC_OK)
+      return set_err(jobs[k].status, "XCHF batch: job %lld failed (code %d)",
+                     (long long)k, jobs[k].status);
+  return NEOXC_OK;
 }
 
 }  // extern "C"

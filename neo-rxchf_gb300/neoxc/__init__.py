@@ -22,7 +22,7 @@ from .basis import NeoSystem  # noqa: F401  (re-export)
 __all__ = [
     "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
     "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam4_fock_factored",
-    "gam3_dscf", "gam2_dscf", "xchf_scf", "SCF_SLOTS",
+    "gam3_dscf", "gam2_dscf", "xchf_scf", "xchf_scf_batch", "SCF_SLOTS",
     "eg4icr", "eg3ic1", "eg2ic1",
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
@@ -62,6 +62,8 @@ def _declare(L):
         "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
         "neoxc_gam4_fock_factored": (I, [i64] * 4 + [vp] * 7),
         "neoxc_xchf_scf": (I, [i64] * 7 + [d] + [vp] * 15 + [i64, i64] + [vp] * 7),
+        "neoxc_xchf_job_size": (i64, []),
+        "neoxc_xchf_scf_batch": (I, [vp, i64, i64, i64, i64]),
         "neoxc_dev_gam4_fock_factored": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg3ic1": (I, [i64] * 4 + [vp] * 6),
@@ -264,6 +266,63 @@ def xchf_scf(s: NeoSystem, DE, DP=None, nucst=None, maxit: int = 100,
             "final": dict(zip(SCF_SLOTS, Ef.tolist())),
             "history": hist[:4 * n].reshape(n, 4), "niter": n, "converged": bool(conv[0]),
             "DE": de.reshape(ne, ne, order="F"), "DP": dp.reshape(np_, np_, order="F")}
+
+
+class XchfJob(C.Structure):
+    """ctypes mirror of neoxc_xchf_job (include/neoxc.h)."""
+    _fields_ = ([(n, C.c_int64) for n in ("nelec", "nucst", "nebf", "npebf", "npbf", "nat",
+                                          "ngtg1")]
+                + [("pmass", C.c_double)]
+                + [(n, C.c_void_p) for n in ("cat", "zan", "bcoef1", "gamma1", "KPESTR",
+                                             "KPEEND", "AMPEB2C", "AGEBFCC", "AGNBFCC",
+                                             "ELCEX", "NUCEX", "ELCAM", "NUCAM", "ELCBFC",
+                                             "NUCBFC", "DE", "DP", "E_init", "E_final",
+                                             "history")]
+                + [("niter", C.c_int64), ("converged", C.c_int64),
+                   ("status", C.c_int32), ("reserved", C.c_int32)])
+
+
+def xchf_scf_batch(systems, DEs, DPs=None, nworkers: int = 8, maxit: int = 100,
+                   diis: bool = False, mixed=False, gam4_element: bool = False):
+    """Independent XCHF solves through neoxc_xchf_scf_batch (worker threads
+    with their own CUDA streams, memory-budget admission).  DPs: None for
+    the core-Hamiltonian proton guess of every job.  Returns one result dict
+    per system, as xchf_scf."""
+    if C.sizeof(XchfJob) != lib().neoxc_xchf_job_size():
+        raise NeoxcError("neoxc_xchf_job layout mismatch")
+    opts = ((1 if DPs is None else 0) | (2 if diis else 0) | (4 if gam4_element else 0)
+            | (8 if mixed else 0) | (16 if mixed is True else 0))
+    n = len(systems)
+    jobs = (XchfJob * n)()
+    keep = []
+    outs = []
+    for k, s in enumerate(systems):
+        ne, np_ = s.nebf, s.npbf
+        arrs, ptrs = _sysargs(s)
+        de = _fmat(DEs[k]).copy()
+        dp = np.zeros(np_ * np_) if DPs is None else _fmat(DPs[k]).copy()
+        Ei, Ef, hist = np.zeros(16), np.zeros(16), np.zeros(4 * maxit)
+        keep.append((arrs, de, dp, Ei, Ef, hist))
+        j = jobs[k]
+        j.nelec, j.nucst, j.nebf, j.npebf, j.npbf = s.nelec, s.nucst, ne, s.npebf, np_
+        j.nat, j.ngtg1, j.pmass = s.nat, s.ngtg, s.pmass
+        names = ("cat", "zan", "bcoef1", "gamma1", "KPESTR", "KPEEND", "AMPEB2C", "AGEBFCC",
+                 "AGNBFCC", "ELCEX", "NUCEX", "ELCAM", "NUCAM", "ELCBFC", "NUCBFC")
+        for name, a in zip(names, arrs):
+            setattr(j, name, a.ctypes.data)
+        j.DE, j.DP, j.E_init, j.E_final = de.ctypes.data, dp.ctypes.data, Ei.ctypes.data, Ef.ctypes.data
+        j.history = hist.ctypes.data
+        outs.append((ne, np_, de, dp, Ei, Ef, hist))
+    _check(lib().neoxc_xchf_scf_batch(C.cast(jobs, C.c_void_p), n, nworkers, opts, maxit))
+    res = []
+    for k, (ne, np_, de, dp, Ei, Ef, hist) in enumerate(outs):
+        nit = int(jobs[k].niter)
+        res.append({"initial": dict(zip(SCF_SLOTS, Ei.tolist())),
+                    "final": dict(zip(SCF_SLOTS, Ef.tolist())),
+                    "history": hist[:4 * nit].reshape(nit, 4), "niter": nit,
+                    "converged": bool(jobs[k].converged),
+                    "DE": de.reshape(ne, ne, order="F"), "DP": dp.reshape(np_, np_, order="F")})
+    return res
 
 
 def gam4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:

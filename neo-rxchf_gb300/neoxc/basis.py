@@ -346,3 +346,17 @@ def random_density(n: int, nocc: int, seed: int, prefac: float = 2.0) -> np.ndar
     q, _ = np.linalg.qr(rng.standard_normal((n, n)))
     c = q[:, :nocc] * 0.5
     return prefac * c @ c.T
+
+
+def proton_scan(s: NeoSystem, n: int, amplitude: float = 0.5, seed: int = 0):
+    """n copies of s with the quantum-proton basis centres displaced by a
+    common seeded offset, uniform in [-amplitude, amplitude]^3 bohr (a
+    proton-position scan; the classical nuclei and the electronic basis stay
+    where they are)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(n):
+        d = rng.uniform(-amplitude, amplitude, 3)
+        out.append(dataclasses.replace(s, NUCBFC=np.asarray(s.NUCBFC, float) + d[None, :],
+                                       name=s.name + "+scan"))
+    return out

@@ -229,6 +229,23 @@ def test_ctypes_signatures_match_header():
     assert checked >= 30
 
 
+def test_batch_job_struct_layout():
+    """The Python mirror of neoxc_xchf_job has the C struct's size."""
+    import ctypes
+    import neoxc
+    assert ctypes.sizeof(neoxc.XchfJob) == neoxc.lib(build_if_missing=True).neoxc_xchf_job_size()
+
+
+def test_proton_scan_moves_only_the_proton_basis():
+    from neoxc import basis
+    s = basis.synthetic(seed=4, nat=2, nebf=3, nprim=1, npbf=2)
+    scan = basis.proton_scan(s, 3, 0.5, seed=1)
+    for t in scan:
+        d = t.NUCBFC - s.NUCBFC
+        assert np.all(np.abs(d) <= 0.5) and np.allclose(d, d[0])
+        assert np.array_equal(t.ELCBFC, s.ELCBFC) and np.array_equal(t.cat, s.cat)
+
+
 def test_argument_checks_need_no_gpu():
     """Size validation happens on the host before any device work, and a
     shape outside the supported range is an error, never a CPU fallback."""

@@ -120,3 +120,22 @@ def test_mixed_precision_all_geminal_energy_error(nx, xchf, xchf_gpu_scf):
     err = r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]
     print("mixed-precision (gam_1 + gam_2 + gam_3) E error (Eh):", err)
     assert abs(err) <= 1e-6
+
+
+def test_batch_matches_separate_solves(nx, xchf):
+    """A proton-position scan of examples/xchf run as one batch on three
+    worker streams gives, job by job, exactly the result of a separate
+    neoxc_xchf_scf call (same kernels, same order on each stream)."""
+    from neoxc import basis
+    systems = basis.proton_scan(xchf["sys"], 5, 0.3, seed=7)
+    DEs = [xchf["DE0"]] * len(systems)
+    batch = nx.xchf_scf_batch(systems, DEs, nworkers=3, diis=True, mixed=True)
+    for s, b in zip(systems, batch):
+        a = nx.xchf_scf(s, xchf["DE0"], diis=True, mixed=True)
+        assert b["converged"] and a["converged"]
+        assert b["niter"] == a["niter"]
+        assert b["final"]["E_total"] == a["final"]["E_total"]
+        assert np.array_equal(b["DE"], a["DE"])
+    # displacing the proton changes the energy
+    Es = [b["final"]["E_total"] for b in batch]
+    assert max(Es) - min(Es) > 1e-4
