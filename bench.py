@@ -385,8 +385,42 @@ def scf_section(neoxc, with_cpu: bool):
         else:
             E_fp64 = r["final"]["E_total"]
     out["batch"] = scf_batch_section(neoxc, s, DE)
+    out["serving"] = scf_serving_section(neoxc, s, DE)
     if with_cpu:
         out["cpu_baseline"] = scf_cpu_baseline(s, DE, out["roothan"]["iterations"])
+    return out
+
+
+def scf_serving_section(neoxc, s, DE):
+    """Poisson arrivals of proton-scan requests (seeded) into the
+    continuous-batching server (8 worker streams, DIIS): p50/p99 time from
+    submission to converged energy, and completed solves/s, per rate."""
+    from neoxc import basis
+    out = {"workload": "examples/xchf proton-scan requests, Poisson arrivals, 8 workers, DIIS"}
+    for mixed, rates, n in ((True, (5.0, 10.0, 20.0, 40.0), 40), (False, (2.0,), 16)):
+        for lam in rates:
+            rng = np.random.Generator(np.random.PCG64(int(lam * 100) + (1 if mixed else 0)))
+            gaps = rng.exponential(1.0 / lam, n)
+            systems = basis.proton_scan(s, n, 0.5, seed=int(lam))
+            srv = neoxc.XchfServer(nworkers=8, diis=True, mixed=mixed)
+            try:
+                t0 = time.perf_counter()
+                tickets = []
+                for k in range(n):
+                    target = t0 + gaps[:k + 1].sum()
+                    dt = target - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    tickets.append(srv.submit(systems[k], DE))
+                res = [srv.wait(t) for t in tickets]
+            finally:
+                srv.stop()
+            lat = np.array([r["t_end"] - r["t_submit"] for r in res])
+            span = max(r["t_end"] for r in res) - min(r["t_submit"] for r in res)
+            out["%s_rate%g" % ("mixed" if mixed else "fp64", lam)] = {
+                "requests": n, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                "solves_per_s": n / span, "converged": sum(r["converged"] for r in res)}
     return out
 
 

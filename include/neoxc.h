@@ -335,10 +335,29 @@ typedef struct neoxc_xchf_job {
   int64_t niter, converged;  /* out */
   int32_t status;            /* out: NEOXC_OK or an error code */
   int32_t reserved;
+  double t_submit, t_start, t_end;  /* out (server): seconds since start */
 } neoxc_xchf_job;
 int64_t neoxc_xchf_job_size(void);   /* sizeof(neoxc_xchf_job), for bindings */
 int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
                          int64_t options, int64_t maxit);
+
+/* ---- serving loop for XCHF solves (no reference counterpart) -------------------
+ * Continuous batching: requests are queued with submit (non-blocking) and
+ * taken by nworkers threads, each with its own CUDA stream, as soon as a
+ * worker is free and the request's device footprint fits in the memory
+ * budget (80 % of the memory free at start); a request may arrive while
+ * others run and its work overlaps theirs on the GPU.  The job struct and
+ * its arrays must stay valid until wait() reports it done; the job's
+ * t_submit / t_start / t_end record the request's life.  wait() returns the
+ * job's status, or NEOXC_ERR_CUDA with "timeout" after timeout_s seconds
+ * (the job keeps running).  stop() drains the queue and joins the workers. */
+typedef struct neoxc_xchf_server neoxc_xchf_server;
+neoxc_xchf_server* neoxc_xchf_server_start(int64_t nworkers, int64_t options,
+                                           int64_t maxit);
+int neoxc_xchf_server_submit(neoxc_xchf_server* srv, neoxc_xchf_job* job);
+int neoxc_xchf_server_wait(neoxc_xchf_server* srv, neoxc_xchf_job* job,
+                           double timeout_s);
+int neoxc_xchf_server_stop(neoxc_xchf_server* srv);
 
 /* ---- diagnostics (no reference counterpart) --------------------------- */
 /* Sustained FP64 FMA throughput of the current device in TFLOP/s (2 FLOP

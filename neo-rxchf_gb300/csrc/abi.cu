@@ -9,7 +9,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
+#include <deque>
 #include <thread>
 #include <cmath>
 #include <cstdarg>
@@ -1282,6 +1284,130 @@ int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
     if (jobs[k].status != NEOXC_OK)
       return set_err(jobs[k].status, "XCHF batch: job %lld failed (code %d)",
                      (long long)k, jobs[k].status);
+  return NEOXC_OK;
+}
+
+
+// ---- serving loop --------------------------------------------------------------
+}  // extern "C"
+
+struct neoxc_xchf_server {
+  int dev = 0;
+  int64_t options = 0, maxit = 100;
+  size_t budget = 0, in_use = 0;
+  int running = 0;
+  bool stopping = false;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done, cv_mem;
+  std::deque<neoxc_xchf_job*> queue;
+  std::vector<std::thread> workers;
+  std::chrono::steady_clock::time_point t0;
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+// job completion marker: reserved = 1 once the worker has written the result
+static void server_worker(neoxc_xchf_server* S) {
+  cudaSetDevice(S->dev);
+  cudaStream_t st = nullptr;
+  const bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+  for (;;) {
+    neoxc_xchf_job* j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait(lk, [&] { return S->stopping || !S->queue.empty(); });
+      if (S->queue.empty()) break;   // stopping and drained
+      j = S->queue.front();
+      S->queue.pop_front();
+    }
+    const size_t need_b = xchf_job_bytes(*j, S->options);
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_mem.wait(lk, [&] { return S->running == 0 || S->in_use + need_b <= S->budget; });
+      S->in_use += need_b;
+      S->running++;
+    }
+    j->t_start = S->now();
+    j->status = ok ? xchf_scf_on(st, j->nelec, j->nucst, j->nebf, j->npebf, j->npbf,
+                                 j->nat, j->ngtg1, j->pmass, j->cat, j->zan, j->bcoef1,
+                                 j->gamma1, j->KPESTR, j->KPEEND, j->AMPEB2C,
+                                 j->AGEBFCC, j->AGNBFCC, j->ELCEX, j->NUCEX, j->ELCAM,
+                                 j->NUCAM, j->ELCBFC, j->NUCBFC, S->options, S->maxit,
+                                 j->DE, j->DP, j->E_init, j->E_final, j->history,
+                                 &j->niter, &j->converged)
+                   : NEOXC_ERR_CUDA;
+    j->t_end = S->now();
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->in_use -= need_b;
+      S->running--;
+      j->reserved = 1;
+    }
+    S->cv_mem.notify_all();
+    S->cv_done.notify_all();
+  }
+  if (ok) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+}
+
+extern "C" {
+
+neoxc_xchf_server* neoxc_xchf_server_start(int64_t nworkers, int64_t options,
+                                           int64_t maxit) {
+  if (nworkers < 1 || maxit < 1) {
+    set_err(NEOXC_ERR_ARG, "server: nworkers >= 1, maxit >= 1");
+    return nullptr;
+  }
+  cudaStream_t s0;
+  if (get_stream(&s0) != NEOXC_OK) return nullptr;
+  auto* S = new neoxc_xchf_server();
+  cudaGetDevice(&S->dev);
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  S->budget = (size_t)(0.8 * (double)free_b);
+  S->options = options;
+  S->maxit = maxit;
+  S->t0 = std::chrono::steady_clock::now();
+  for (int64_t w = 0; w < nworkers; w++) S->workers.emplace_back(server_worker, S);
+  return S;
+}
+
+int neoxc_xchf_server_submit(neoxc_xchf_server* S, neoxc_xchf_job* job) {
+  RC(need(S != nullptr && job != nullptr, "server, job"));
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stopping) return set_err(NEOXC_ERR_ARG, "server is stopping");
+    job->reserved = 0;
+    job->status = NEOXC_OK;
+    job->t_submit = S->now();
+    S->queue.push_back(job);
+  }
+  S->cv_work.notify_one();
+  return NEOXC_OK;
+}
+
+int neoxc_xchf_server_wait(neoxc_xchf_server* S, neoxc_xchf_job* job,
+                           double timeout_s) {
+  RC(need(S != nullptr && job != nullptr, "server, job"));
+  std::unique_lock<std::mutex> lk(S->mu);
+  const bool done = S->cv_done.wait_for(
+      lk, std::chrono::duration<double>(timeout_s), [&] { return job->reserved == 1; });
+  if (!done) return set_err(NEOXC_ERR_CUDA, "server wait: timeout");
+  return job->status;
+}
+
+int neoxc_xchf_server_stop(neoxc_xchf_server* S) {
+  RC(need(S != nullptr, "server"));
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stopping = true;
+  }
+  S->cv_work.notify_all();
+  for (auto& t : S->workers) t.join();
+  delete S;
   return NEOXC_OK;
 }
 

@@ -22,7 +22,7 @@ from .basis import NeoSystem  # noqa: F401  (re-export)
 __all__ = [
     "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
     "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam4_fock_factored",
-    "gam3_dscf", "gam2_dscf", "xchf_scf", "xchf_scf_batch", "SCF_SLOTS",
+    "gam3_dscf", "gam2_dscf", "xchf_scf", "xchf_scf_batch", "XchfServer", "SCF_SLOTS",
     "eg4icr", "eg3ic1", "eg2ic1",
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
@@ -64,6 +64,10 @@ def _declare(L):
         "neoxc_xchf_scf": (I, [i64] * 7 + [d] + [vp] * 15 + [i64, i64] + [vp] * 7),
         "neoxc_xchf_job_size": (i64, []),
         "neoxc_xchf_scf_batch": (I, [vp, i64, i64, i64, i64]),
+        "neoxc_xchf_server_start": (vp, [i64, i64, i64]),
+        "neoxc_xchf_server_submit": (I, [vp, vp]),
+        "neoxc_xchf_server_wait": (I, [vp, vp, d]),
+        "neoxc_xchf_server_stop": (I, [vp]),
         "neoxc_dev_gam4_fock_factored": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg3ic1": (I, [i64] * 4 + [vp] * 6),
@@ -279,7 +283,9 @@ class XchfJob(C.Structure):
                                              "NUCBFC", "DE", "DP", "E_init", "E_final",
                                              "history")]
                 + [("niter", C.c_int64), ("converged", C.c_int64),
-                   ("status", C.c_int32), ("reserved", C.c_int32)])
+                   ("status", C.c_int32), ("reserved", C.c_int32),
+                   ("t_submit", C.c_double), ("t_start", C.c_double),
+                   ("t_end", C.c_double)])
 
 
 def xchf_scf_batch(systems, DEs, DPs=None, nworkers: int = 8, maxit: int = 100,
@@ -290,39 +296,80 @@ def xchf_scf_batch(systems, DEs, DPs=None, nworkers: int = 8, maxit: int = 100,
     per system, as xchf_scf."""
     if C.sizeof(XchfJob) != lib().neoxc_xchf_job_size():
         raise NeoxcError("neoxc_xchf_job layout mismatch")
-    opts = ((1 if DPs is None else 0) | (2 if diis else 0) | (4 if gam4_element else 0)
-            | (8 if mixed else 0) | (16 if mixed is True else 0))
+    opts = _scf_options(DPs is None, diis, mixed, gam4_element)
     n = len(systems)
     jobs = (XchfJob * n)()
-    keep = []
-    outs = []
-    for k, s in enumerate(systems):
-        ne, np_ = s.nebf, s.npbf
-        arrs, ptrs = _sysargs(s)
-        de = _fmat(DEs[k]).copy()
-        dp = np.zeros(np_ * np_) if DPs is None else _fmat(DPs[k]).copy()
-        Ei, Ef, hist = np.zeros(16), np.zeros(16), np.zeros(4 * maxit)
-        keep.append((arrs, de, dp, Ei, Ef, hist))
-        j = jobs[k]
-        j.nelec, j.nucst, j.nebf, j.npebf, j.npbf = s.nelec, s.nucst, ne, s.npebf, np_
-        j.nat, j.ngtg1, j.pmass = s.nat, s.ngtg, s.pmass
-        names = ("cat", "zan", "bcoef1", "gamma1", "KPESTR", "KPEEND", "AMPEB2C", "AGEBFCC",
-                 "AGNBFCC", "ELCEX", "NUCEX", "ELCAM", "NUCAM", "ELCBFC", "NUCBFC")
-        for name, a in zip(names, arrs):
-            setattr(j, name, a.ctypes.data)
-        j.DE, j.DP, j.E_init, j.E_final = de.ctypes.data, dp.ctypes.data, Ei.ctypes.data, Ef.ctypes.data
-        j.history = hist.ctypes.data
-        outs.append((ne, np_, de, dp, Ei, Ef, hist))
+    bufs = [_fill_job(jobs[k], s, DEs[k], None if DPs is None else DPs[k], maxit)
+            for k, s in enumerate(systems)]
     _check(lib().neoxc_xchf_scf_batch(C.cast(jobs, C.c_void_p), n, nworkers, opts, maxit))
-    res = []
-    for k, (ne, np_, de, dp, Ei, Ef, hist) in enumerate(outs):
-        nit = int(jobs[k].niter)
-        res.append({"initial": dict(zip(SCF_SLOTS, Ei.tolist())),
-                    "final": dict(zip(SCF_SLOTS, Ef.tolist())),
-                    "history": hist[:4 * nit].reshape(nit, 4), "niter": nit,
-                    "converged": bool(jobs[k].converged),
-                    "DE": de.reshape(ne, ne, order="F"), "DP": dp.reshape(np_, np_, order="F")})
-    return res
+    return [_job_result(jobs[k], b) for k, b in enumerate(bufs)]
+
+
+def _scf_options(guess_prot, diis, mixed, gam4_element):
+    return ((1 if guess_prot else 0) | (2 if diis else 0) | (4 if gam4_element else 0)
+            | (8 if mixed else 0) | (16 if mixed is True else 0))
+
+
+def _fill_job(j, s, DE, DP, maxit):
+    """Point one neoxc_xchf_job at numpy buffers; returns the buffers (they
+    must outlive the job)."""
+    ne, np_ = s.nebf, s.npbf
+    arrs, _ = _sysargs(s)
+    de = _fmat(DE).copy()
+    dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
+    Ei, Ef, hist = np.zeros(16), np.zeros(16), np.zeros(4 * maxit)
+    j.nelec, j.nucst, j.nebf, j.npebf, j.npbf = s.nelec, s.nucst, ne, s.npebf, np_
+    j.nat, j.ngtg1, j.pmass = s.nat, s.ngtg, s.pmass
+    names = ("cat", "zan", "bcoef1", "gamma1", "KPESTR", "KPEEND", "AMPEB2C", "AGEBFCC",
+             "AGNBFCC", "ELCEX", "NUCEX", "ELCAM", "NUCAM", "ELCBFC", "NUCBFC")
+    for name, a in zip(names, arrs):
+        setattr(j, name, a.ctypes.data)
+    j.DE, j.DP, j.E_init, j.E_final = de.ctypes.data, dp.ctypes.data, Ei.ctypes.data, Ef.ctypes.data
+    j.history = hist.ctypes.data
+    return {"arrs": arrs, "ne": ne, "np": np_, "de": de, "dp": dp, "Ei": Ei, "Ef": Ef,
+            "hist": hist}
+
+
+def _job_result(j, b):
+    nit = int(j.niter)
+    return {"initial": dict(zip(SCF_SLOTS, b["Ei"].tolist())),
+            "final": dict(zip(SCF_SLOTS, b["Ef"].tolist())),
+            "history": b["hist"][:4 * nit].reshape(nit, 4), "niter": nit,
+            "converged": bool(j.converged),
+            "DE": b["de"].reshape(b["ne"], b["ne"], order="F"),
+            "DP": b["dp"].reshape(b["np"], b["np"], order="F"),
+            "t_submit": j.t_submit, "t_start": j.t_start, "t_end": j.t_end}
+
+
+class XchfServer:
+    """Continuous-batching XCHF solves (neoxc_xchf_server_*): submit()
+    queues a request and returns immediately; worker streams take requests
+    as they free up; wait() returns the result dict (with the request's
+    t_submit / t_start / t_end)."""
+
+    def __init__(self, nworkers: int = 8, maxit: int = 100, diis: bool = True, mixed=True,
+                 guess_prot: bool = True, gam4_element: bool = False):
+        self.maxit, self.guess_prot = maxit, guess_prot
+        self._h = lib().neoxc_xchf_server_start(
+            nworkers, _scf_options(guess_prot, diis, mixed, gam4_element), maxit)
+        if not self._h:
+            raise NeoxcError(lib().neoxc_last_error().decode())
+
+    def submit(self, s: NeoSystem, DE, DP=None):
+        job = XchfJob()
+        bufs = _fill_job(job, s, DE, None if self.guess_prot else DP, self.maxit)
+        _check(lib().neoxc_xchf_server_submit(self._h, C.byref(job)))
+        return (job, bufs)
+
+    def wait(self, ticket, timeout: float = 600.0):
+        job, bufs = ticket
+        _check(lib().neoxc_xchf_server_wait(self._h, C.byref(job), timeout))
+        return _job_result(job, bufs)
+
+    def stop(self):
+        if self._h:
+            _check(lib().neoxc_xchf_server_stop(self._h))
+            self._h = None
 
 
 def gam4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:

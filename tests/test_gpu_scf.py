@@ -139,3 +139,25 @@ def test_batch_matches_separate_solves(nx, xchf):
     # displacing the proton changes the energy
     Es = [b["final"]["E_total"] for b in batch]
     assert max(Es) - min(Es) > 1e-4
+
+
+def test_server_requests_match_separate_solves(nx, xchf):
+    """Continuous batching: requests submitted while others run (3 worker
+    streams) finish with exactly the separate-solve results, and each
+    request's timestamps are ordered."""
+    import time
+    from neoxc import basis
+    systems = basis.proton_scan(xchf["sys"], 6, 0.3, seed=9)
+    srv = nx.XchfServer(nworkers=3, diis=True, mixed=True)
+    try:
+        tickets = []
+        for s in systems:
+            tickets.append(srv.submit(s, xchf["DE0"]))
+            time.sleep(0.01)
+        results = [srv.wait(t) for t in tickets]
+    finally:
+        srv.stop()
+    for s, r in zip(systems, results):
+        a = nx.xchf_scf(s, xchf["DE0"], diis=True, mixed=True)
+        assert r["converged"] and r["final"]["E_total"] == a["final"]["E_total"]
+        assert r["t_submit"] <= r["t_start"] <= r["t_end"]
