@@ -267,7 +267,7 @@ gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
 
 // ---- gam_2 raw tensors: warp per contracted tuple --------------------------
 template <int RX, bool F32>
-__global__ void __launch_bounds__(64)
+__global__ void __launch_bounds__(64, F32 ? 16 : 8)
 gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
                 double* __restrict__ x2, long long t0, long long ntup) {
   const int ne = S.nebf, np = S.npbf;
@@ -451,7 +451,7 @@ __global__ void gam3_hcore_kernel(DevSystem S, double* __restrict__ Hc) {
 
 // ---- gam_3 raw tensor: warp per contracted tuple ----------------------------
 template <bool F32>
-__global__ void __launch_bounds__(64)
+__global__ void __launch_bounds__(64, F32 ? 16 : 8)
 gam3_raw_kernel(DevSystem S, const double* __restrict__ aux,
                 double* __restrict__ x3, long long t0, long long ntup) {
   const int ne = S.nebf, np = S.npbf;
