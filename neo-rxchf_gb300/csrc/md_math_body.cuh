@@ -137,6 +137,21 @@ struct Prim {
 // F[0..M] (common.f:317-348 XGAMMAF; T>20 upward, else series at M and
 // downward recursion)
 NX_BIG void boys(int M, real Tr, real* F) {
+  if (M == 0 && (double)Tr <= 20.0) {
+    // F0(T) = sqrt(pi/T) erf(sqrt(T)) / 2 (the T <= 20 series sums to this
+    // to its 1e-12 cutoff); the T > 20 branch below keeps XGAMMAF's
+    // asymptotic form.
+    if (sizeof(real) == sizeof(double)) {
+      const double T = (double)Tr;
+      F[0] = (real)(T < 1.0e-12 ? 1.0 - T / 3.0
+                                : 0.5 * sqrt(3.14159265358979323846 / T) * erf(sqrt(T)));
+    } else {
+      const float T = (float)Tr;
+      F[0] = (real)(T < 1.0e-6f ? 1.0f - T / 3.0f
+                                : 0.5f * sqrtf(3.14159265f / T) * erff(sqrtf(T)));
+    }
+    return;
+  }
   if (sizeof(real) == sizeof(double)) {
     // FP64: XGAMMAF's branches and cutoff; the series divisors 1/(m+1/2)
     // and the downward-recursion divisors 1/(2L+1) = (1/2)/(L+1/2) come from
@@ -642,6 +657,26 @@ NX_HD void g4_pairs(G4& s, const Prim* A, const Prim* B) {
 NX_BIG real g4_coulomb(const G4& s, const GK4& gk, const real* cof,
                         real pref, real T, real alpha,
                         const real* Rv) {
+  bool all_s = true;
+  for (int i = 0; i < 4; i++)
+    for (int d = 0; d < 3; d++) all_s = all_s && (s.A[i].l[d] + s.B[i].l[d] == 0);
+  if (all_s) {
+    // s shells: every Hermite expansion is E_0 = K, the derivative table is
+    // its base value and the Coulomb factor is R_000 = F_0(T)
+    real w = R_(1.0);
+    for (int d = 0; d < 3; d++) {
+      real base = R_(1.0);
+      for (int k = 0; k < gk.nk; k++) {
+        const real u = gk.c[k][0] * s.pr[0].P[d] + gk.c[k][1] * s.pr[1].P[d] +
+                       gk.c[k][2] * s.pr[2].P[d] + gk.c[k][3] * s.pr[3].P[d];
+        base *= exp(-gk.xi[k] * u * u);
+      }
+      w *= s.pr[0].K[d] * s.pr[1].K[d] * s.pr[2].K[d] * s.pr[3].K[d] * base;
+    }
+    real F[1];
+    boys(0, T, F);
+    return pref * (w * F[0]);
+  }
   real W[3][LTOT + 1];
   int nmax[3];
   real D[T4D * T4D * T4D * T4D];

@@ -146,9 +146,17 @@ def test_md_math_matches_oracle(orc, hostcheck):
         # relative on significant values, absolute floor for cancelled ones
         assert abs(a - b) <= 1e-10 * abs(b) + 1e-14, (what, a, b)
 
-    for trial in range(25):
-        A = O.prims([rp() for _ in range(4)])
-        B = O.prims([rp() for _ in range(4)])
+    def sp():   # an s primitive (the s-shell fast paths)
+        return O.prim(0, 0, 0, float(np.exp(rng.uniform(np.log(0.1), np.log(20)))),
+                      *rng.uniform(-1.5, 1.5, 3))
+
+    for trial in range(35):
+        if trial < 25:
+            A = O.prims([rp() for _ in range(4)])
+            B = O.prims([rp() for _ in range(4)])
+        else:
+            A = O.prims([sp() for _ in range(4)])
+            B = O.prims([sp() for _ in range(4)])
         g = np.zeros(6)
         for k in rng.choice(6, size=2, replace=False):
             g[k] = float(np.exp(rng.uniform(np.log(0.5), np.log(20))))
@@ -162,7 +170,7 @@ def test_md_math_matches_oracle(orc, hostcheck):
               L.orc_g3_xgvxcg(A3, B3, O.ptr(g), O.ptr(Cm)), "vxc")
         check(H.hc_g3(3, A3, B3, O.ptr(g), O.ptr(Cm), 1.0), L.orc_g3_xgveeg(A3, B3, O.ptr(g)), "vee")
         g1, g2 = g[g > 0][0], g[g > 0][1]
-        if trial < 10:
+        if trial < 10 or trial >= 25:
             check(H.hc_g4(0, A, B, g1, g2), L.orc_g4_xgveeg(A, B, g1, g2), "g4vee")
             check(H.hc_g4(1, A, B, g1, g2), L.orc_g4_xgvepg(A, B, g1, g2), "g4vep")
         r = [C.byref(A[0]), C.byref(A[1]), C.byref(B[0]), C.byref(B[1])]
