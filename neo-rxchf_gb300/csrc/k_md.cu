@@ -79,6 +79,12 @@ __device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
   perm3(B, 0, 2, 1, B132);
   perm3(A, 2, 0, 1, A312);
   perm3(B, 2, 0, 1, B312);
+  // Gaussian products of the three particle pairs, shared by every setup
+  using PairT = typename std::remove_all_extents<decltype(G3T::pr)>::type;
+  PairT pr[3], pr132[3], pr312[3];
+  for (int i = 0; i < 3; i++) gauss_pair(A[i], B[i], pr[i]);
+  perm3(pr, 0, 2, 1, pr132);
+  perm3(pr, 2, 0, 1, pr312);
   R g[6];
   const R zero = R(0.0), one = R(1.0);
   // centre of classical nucleus ia in the working precision
@@ -89,13 +95,13 @@ __device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
   double gTE = 0, gVEC = 0, gVEE = 0, gVEP = 0;
   for (int ik = 0; ik < ng; ik++) {
     gam6(g, A23, (R)gm[ik], -1, zero);
-    g3_setup(st, A, B, g, 2);
+    g3_setup_pairs(st, A, B, pr, g, 2);
     double xgTE = (double)g3_ke(st, zero, one);
     double xgVEC = 0.0;
     for (int ia = 0; ia < nat; ia++)
       xgVEC = xgVEC - S.zan[ia] * vxc(ia);
     double xgVEE = md::underflow((double)g3_vee(st));
-    g3_setup(st, A132, B132, g, 0);
+    g3_setup_pairs(st, A132, B132, pr132, g, 0);
     double xgVEP = -md::underflow((double)g3_vee(st));
     gTE = gTE + b[ik] * xgTE;
     gVEC = gVEC + b[ik] * xgVEC;
@@ -110,14 +116,14 @@ __device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
       const double bb = b[ik] * b[il];
       // order (p, e1, e2): gA12 = g(p,e1), gB13 = g(p,e2)
       gam6(g, A12, gk, B13, gl);
-      g3_setup(st, A312, B312, g, 2);
+      g3_setup_pairs(st, A312, B312, pr312, g, 2);
       double xgTPg = (double)g3_ke(st, gl, (R)S.pmass);
       double xgVPCg = 0.0;
       for (int ia = 0; ia < nat; ia++)
         xgVPCg = xgVPCg + S.zan[ia] * vxc(ia);
       // order (e1, e2, p): A13, B23
       gam6(g, A13, gk, B23, gl);
-      g3_setup(st, A, B, g, 2);
+      g3_setup_pairs(st, A, B, pr, g, 2);
       double xgTEg1 = (double)g3_ke(st, zero, one);
       double xgVECg1 = 0.0;
       for (int ia = 0; ia < nat; ia++)
@@ -126,25 +132,25 @@ __device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
       double xgsg = (double)g3_overlap(st);
       // A23, B13
       gam6(g, A23, gk, B13, gl);
-      g3_setup(st, A, B, g, 2);
+      g3_setup_pairs(st, A, B, pr, g, 2);
       double xgTEg2 = (double)g3_ke(st, gl, one);
       // A23, B23
       gam6(g, A23, gk, B23, gl);
-      g3_setup(st, A, B, g, 2);
+      g3_setup_pairs(st, A, B, pr, g, 2);
       double xgTEg3 = (double)g3_ke(st, zero, one);
       double xgVECg2 = 0.0;
       for (int ia = 0; ia < nat; ia++)
         xgVECg2 = xgVECg2 - S.zan[ia] * vxc(ia);
       // A13, B13
       gam6(g, A13, gk, B13, gl);
-      g3_setup(st, A, B, g, 0);
+      g3_setup_pairs(st, A, B, pr, g, 0);
       double xgVEEg1 = md::underflow((double)g3_vee(st));
       // order (e1, p, e2): A12 B23 and A23 B23
       gam6(g, A12, gk, B23, gl);
-      g3_setup(st, A132, B132, g, 0);
+      g3_setup_pairs(st, A132, B132, pr132, g, 0);
       double xgVEPg1 = -md::underflow((double)g3_vee(st));
       gam6(g, A23, gk, B23, gl);
-      g3_setup(st, A132, B132, g, 0);
+      g3_setup_pairs(st, A132, B132, pr132, g, 0);
       double xgVEPg2 = -md::underflow((double)g3_vee(st));
       gTPg = gTPg + bb * xgTPg;
       gTEg1 = gTEg1 + bb * xgTEg1;
@@ -175,17 +181,20 @@ __device__ void xcalc_gam2_rx(const Prim* A, const Prim* B,
   Prim A321[3], B321[3];
   perm3(A, 2, 1, 0, A321);
   perm3(B, 2, 1, 0, B321);
+  md::Pair pr[3], pr321[3];
+  for (int i = 0; i < 3; i++) md::gauss_pair(A[i], B[i], pr[i]);
+  perm3(pr, 2, 1, 0, pr321);
   double g[6], gVEPg2 = 0, gVEEg1 = 0, gVEEg2 = 0;
   for (int ik = 0; ik < ng; ik++)
     for (int il = 0; il < ng; il++) {
       const double gk = gm[ik], gl = gm[il], bb = b[ik] * b[il];
       gam6(g, A13, gk, B13, gl);
-      md::g3_setup(st, A321, B321, g, 0);
+      md::g3_setup_pairs(st, A321, B321, pr321, g, 0);
       double xgVEPg2 = -md::underflow(md::g3_vee(st));
-      md::g3_setup(st, A, B, g, 0);
+      md::g3_setup_pairs(st, A, B, pr, g, 0);
       double xgVEEg1 = md::underflow(md::g3_vee(st));
       gam6(g, A13, gk, B23, gl);
-      md::g3_setup(st, A, B, g, 0);
+      md::g3_setup_pairs(st, A, B, pr, g, 0);
       double xgVEEg2 = md::underflow(md::g3_vee(st));
       gVEPg2 = gVEPg2 + bb * xgVEPg2;
       gVEEg1 = gVEEg1 + bb * xgVEEg1;
@@ -415,11 +424,13 @@ gam3_w3_kernel(DevSystem S, double* __restrict__ W3) {
                        to_prim(S.pprim[ip])};
     const Prim B[3] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
                        to_prim(S.pprim[jp])};
+    md::Pair pr[3];
+    for (int i = 0; i < 3; i++) md::gauss_pair(A[i], B[i], pr[i]);
     double v = 0.0;
     for (int k = 0; k < S.ngtg; k++)
       for (int l = 0; l < S.ngtg; l++) {
         gam6(g, A13, S.ggem[k], B23, S.ggem[l]);
-        md::g3_setup(st, A, B, g, 0);
+        md::g3_setup_pairs(st, A, B, pr, g, 0);
         v = v + S.bgem[k] * S.bgem[l] * md::underflow(md::g3_overlap(st));
       }
     double cc = S.pprim[ip].coef * S.pprim[jp].coef;

@@ -268,15 +268,16 @@ struct GK3 {
 NX_BIG void dgauss3(const GK3& g, const real* X, int N1, int N2, int N3,
                    real* D /* [TD][TD][TD] */) {
   real grad[3] = {0, 0, 0}, H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  real base = R_(1.0);
+  real expo = R_(0.0);   // prod_k exp(-xi_k u_k^2) as one exponential
   for (int k = 0; k < g.nk; k++) {
     real u = g.c[k][0] * X[0] + g.c[k][1] * X[1] + g.c[k][2] * X[2];
-    base *= exp(-g.xi[k] * u * u);
+    expo -= g.xi[k] * u * u;
     for (int i = 0; i < 3; i++) {
       grad[i] += R_(2.0) * g.xi[k] * u * g.c[k][i];
       for (int j = 0; j < 3; j++) H[i][j] += R_(2.0) * g.xi[k] * g.c[k][i] * g.c[k][j];
     }
   }
+  const real base = exp(expo);
 #define D3(a, b, c) D[((a) * TD + (b)) * TD + (c)]
   for (int n1 = 0; n1 <= N1; n1++)
     for (int n2 = 0; n2 <= N2; n2++)
@@ -307,16 +308,17 @@ NX_BIG void dgauss4(const GK4& g, const real* X, const int* N, real* D) {
   real grad[4] = {0, 0, 0, 0}, H[4][4];
   for (int i = 0; i < 4; i++)
     for (int j = 0; j < 4; j++) H[i][j] = R_(0.0);
-  real base = R_(1.0);
+  real expo = R_(0.0);   // prod_k exp(-xi_k u_k^2) as one exponential
   for (int k = 0; k < g.nk; k++) {
     real u = g.c[k][0] * X[0] + g.c[k][1] * X[1] + g.c[k][2] * X[2] +
                g.c[k][3] * X[3];
-    base *= exp(-g.xi[k] * u * u);
+    expo -= g.xi[k] * u * u;
     for (int i = 0; i < 4; i++) {
       grad[i] += R_(2.0) * g.xi[k] * u * g.c[k][i];
       for (int j = 0; j < 4; j++) H[i][j] += R_(2.0) * g.xi[k] * g.c[k][i] * g.c[k][j];
     }
   }
+  const real base = exp(expo);
 #define D4(a, b, c, e) D[(((a) * T4D + (b)) * T4D + (c)) * T4D + (e)]
   for (int n1 = 0; n1 <= N[0]; n1++)
     for (int n2 = 0; n2 <= N[1]; n2++)
@@ -396,12 +398,15 @@ struct G3 {
   real D[3][TD * TD * TD];   // per dimension
 };
 
-NX_BIG void g3_setup(G3& s, const Prim* A, const Prim* B, const real* gam,
-                    int ke_shift) {
+// pairs: the Gaussian products of (A[i], B[i]), which do not depend on the
+// geminal exponents; callers that set up many geminal terms for the same
+// primitives compute them once (g3_setup below computes them itself).
+NX_BIG void g3_setup_pairs(G3& s, const Prim* A, const Prim* B,
+                          const Pair* pairs, const real* gam, int ke_shift) {
   for (int i = 0; i < 3; i++) {
     s.A[i] = A[i];
     s.B[i] = B[i];
-    gauss_pair(A[i], B[i], s.pr[i]);
+    s.pr[i] = pairs[i];
   }
   s.gam13 = gam[1] + gam[4];
   s.gam23 = gam[2] + gam[5];
@@ -434,6 +439,13 @@ NX_BIG void g3_setup(G3& s, const Prim* A, const Prim* B, const real* gam,
     const real X[3] = {s.pr[0].P[d], s.pr[1].P[d], s.pr[2].P[d]};
     dgauss3(s.gk, X, s.T[0][d], s.T[1][d], s.T[2][d], s.D[d]);
   }
+}
+
+NX_BIG void g3_setup(G3& s, const Prim* A, const Prim* B, const real* gam,
+                    int ke_shift) {
+  Pair pr[3];
+  for (int i = 0; i < 3; i++) gauss_pair(A[i], B[i], pr[i]);
+  g3_setup_pairs(s, A, B, pr, gam, ke_shift);
 }
 
 // 1-D overlap factor with ket momenta (L1, L3) of particles 1 and 3
@@ -663,16 +675,16 @@ NX_BIG real g4_coulomb(const G4& s, const GK4& gk, const real* cof,
   if (all_s) {
     // s shells: every Hermite expansion is E_0 = K, the derivative table is
     // its base value and the Coulomb factor is R_000 = F_0(T)
-    real w = R_(1.0);
+    real w = R_(1.0), expo = R_(0.0);
     for (int d = 0; d < 3; d++) {
-      real base = R_(1.0);
       for (int k = 0; k < gk.nk; k++) {
         const real u = gk.c[k][0] * s.pr[0].P[d] + gk.c[k][1] * s.pr[1].P[d] +
                        gk.c[k][2] * s.pr[2].P[d] + gk.c[k][3] * s.pr[3].P[d];
-        base *= exp(-gk.xi[k] * u * u);
+        expo -= gk.xi[k] * u * u;
       }
-      w *= s.pr[0].K[d] * s.pr[1].K[d] * s.pr[2].K[d] * s.pr[3].K[d] * base;
+      w *= s.pr[0].K[d] * s.pr[1].K[d] * s.pr[2].K[d] * s.pr[3].K[d];
     }
+    w *= exp(expo);
     real F[1];
     boys(0, T, F);
     return pref * (w * F[0]);
