@@ -332,12 +332,19 @@ typedef struct neoxc_xchf_job {
   double *DE, *DP;           /* in: start densities; out: converged */
   double *E_init, *E_final;  /* [16] each, slots as neoxc_xchf_scf */
   double *history;           /* [4*maxit] or NULL */
+  double *CE, *CP;           /* out, or NULL: final MO coefficients
+                                (column-major, ROOTHAN's VECE / VECP,
+                                orbitals by ascending energy) */
+  double *EE, *EP;           /* out, or NULL: orbital energies */
   int64_t niter, converged;  /* out */
   int32_t status;            /* out: NEOXC_OK or an error code */
   int32_t reserved;
   double t_submit, t_start, t_end;  /* out (server): seconds since start */
 } neoxc_xchf_job;
 int64_t neoxc_xchf_job_size(void);   /* sizeof(neoxc_xchf_job), for bindings */
+/* One job on the library stream (neoxc_xchf_scf with the job's arrays, plus
+ * the optional MO outputs); returns the job's status. */
+int neoxc_xchf_scf_job(neoxc_xchf_job* job, int64_t options, int64_t maxit);
 int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
                          int64_t options, int64_t maxit);
 
@@ -358,6 +365,33 @@ int neoxc_xchf_server_submit(neoxc_xchf_server* srv, neoxc_xchf_job* job);
 int neoxc_xchf_server_wait(neoxc_xchf_server* srv, neoxc_xchf_job* job,
                            double timeout_s);
 int neoxc_xchf_server_stop(neoxc_xchf_server* srv);
+
+/* ---- on-disk formats: xchf1_independent/GAM_IO.f (host only, no GPU) --- */
+/* Direct-access integral files (*.ufm, GAM_IO.f:1-245): record ia (1-based)
+ * holds the FP64 at packed index ia, records `recl` bytes long with the value
+ * first (RECL=8 counted in bytes = 8; ifort's default 4-byte units = 32).
+ * recl <= 0 takes NEOXC_UFM_RECL from the environment, default 8.
+ * Replaces the read loops of read_GAM_ee/ep/ecore/pcore and the writes in
+ * gam_ee.f:143-155, gam_ep.f:141, gam_4_OMP.f:263. */
+int neoxc_ufm_read(const char* path, int64_t n, int64_t recl, double* out);
+int neoxc_ufm_write(const char* path, const double* v, int64_t n, int64_t recl);
+/* GAM_IO.f:471-518 PUSQLF: nmo MOs of nbf coefficients (V column-major,
+ * V[:,j] = MO j) as FORMAT(I2,I3,1P,5E15.8) rows labelled MOD(j,100),
+ * MOD(row,1000) -- the FinalC*.dat files. */
+int neoxc_mo_write(const char* path, int64_t nbf, int64_t nmo, const double* V);
+/* GAM_IO.f:275-303 (read_elec_density's VEC group, FORMAT(I2,I3,5E15.8)):
+ * the guessC*.inp / FinalC*.dat layout back into V; a label that does not
+ * match returns NEOXC_ERR_IO (the reference prints 9060 and STOPs). */
+int neoxc_mo_read(const char* path, int64_t nbf, int64_t nmo, double* V);
+/* GAM_IO.f:306-339: D = prefac * sum_{k=kstart..klast} C(:,k) C(:,k)^T
+ * (1-based MO indices; read_elec_density: 1..nelec/2, prefac 2;
+ * read_nuc_density: NUCST..NUCST, prefac 1). */
+int neoxc_mo_density(int64_t nbf, int64_t kstart, int64_t klast, double prefac,
+                     const double* C, double* D);
+/* ENUCRP.dat (class_nuc_rep.f:39-41 write, xcscf.f:248-250 read): one
+ * list-directed real, the classical nuclear repulsion energy. */
+int neoxc_enuc_write(const char* path, double E_nuc);
+int neoxc_enuc_read(const char* path, double* E_nuc);
 
 /* ---- diagnostics (no reference counterpart) --------------------------- */
 /* Sustained FP64 FMA throughput of the current device in TFLOP/s (2 FLOP
@@ -468,6 +502,22 @@ void calc_gam_ee_(const int64_t* nebf, const int64_t* npebf,
                   const int64_t* ngee, const int64_t* AMPEB2C,
                   const double* AGEBFCC, const double* ELCEX,
                   const int64_t* ELCAM, const double* ELCBFC);
+/* GAM_IO.f readers and writer, same names, arguments and files as the
+ * reference (GAM_ee.ufm, GAM_ep.ufm, GAM_ecr.ufm, GAM_pcr.ufm, novlap.ufm,
+ * eovlap.ufm, guessCE.inp, guessCP.inp; write_MOs units 852/853/860/861/
+ * 870/871 -> FinalCE/FinalCP/FinalCAE/FinalCBE/FinalCAalpE/FinalCAbetE.dat).
+ * A failed read prints a message and leaves the output partly filled. */
+void read_gam_ee_(const int64_t* ne, const int64_t* ngee, double* GAM_ee);
+void read_gam_ep_(const int64_t* ne, const int64_t* np, const int64_t* ng1,
+                  double* GAM_ep);
+void read_gam_ecore_(const int64_t* ne, const int64_t* ne2, double* GAM_ecore);
+void read_gam_pcore_(const int64_t* np, const int64_t* np2, double* GAM_pcore);
+void read_nuc_ovlap_(const int64_t* np, double* GS);
+void read_elec_ovlap_(const int64_t* ne, double* GS);
+void read_elec_density_(const int64_t* nebf, const int64_t* n_particle, double* DE);
+void read_nuc_density_(const int64_t* npbf, const int64_t* n_particle,
+                       const int64_t* NUCST, double* DP);
+void write_mos_(const int64_t* IFIL, const int64_t* nbf, const double* VEC);
 
 #ifdef __cplusplus
 }

@@ -995,7 +995,9 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
                    const double* ELCBFC, const double* NUCBFC, int64_t options,
                    int64_t maxit, double* DE, double* DP, double* E_init,
                    double* E_final, double* history, int64_t* niter,
-                   int64_t* converged) {
+                   int64_t* converged, double* CE = nullptr,
+                   double* CP = nullptr, double* EE = nullptr,
+                   double* EP = nullptr) {
   (void)AMPEB2C;
   RC(need(nelec >= 1 && maxit >= 1, "nelec >= 1, maxit >= 1"));
   RC(need(nucst >= 1 && nucst <= npbf, "1 <= nucst <= npbf"));
@@ -1099,6 +1101,15 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
     CU(cudaMemcpyAsync(dDP.p, DP, sizeof(double) * p2, cudaMemcpyHostToDevice, s));
   }
   double* d_en = en.as<double>();
+  // final MOs and orbital energies (ROOTHAN's VECE/EE, VECP/EP) when asked
+  const bool want_mo = CE || CP || EE || EP;
+  DBuf dCE, dCP, dEE, dEP;
+  if (want_mo) {
+    RC(dalloc(dCE, sizeof(double) * e2, s));
+    RC(dalloc(dCP, sizeof(double) * p2, s));
+    RC(dalloc(dEE, sizeof(double) * ne, s));
+    RC(dalloc(dEP, sizeof(double) * np, s));
+  }
   auto fock_build = [&]() -> int {
     CU(launch_scf_fock1(ne, np, (int)nelec, Hce.as<double>(), Hcp.as<double>(),
                         Gep.as<double>(), G1.as<double>(), G1s.as<double>(),
@@ -1140,13 +1151,15 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
                          cudaMemcpyDeviceToHost, s));
     }
     CU(launch_roothan(np, fp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
-                      dDP.as<double>(), nullptr, nullptr, sts + 1, s));
+                      dDP.as<double>(), want_mo ? dEP.as<double>() : nullptr,
+                      want_mo ? dCP.as<double>() : nullptr, sts + 1, s));
     RC(fock_build());
     if (diis)
       CU(launch_diis(ne, fe.as<double>(), dDE.as<double>(), Se.as<double>(),
                      dwork.as<double>(), sts + 4, nullptr, s));
     CU(launch_roothan(ne, fe.as<double>(), Xe.as<double>(), 0, noccE, prefE,
-                      dDE.as<double>(), nullptr, nullptr, sts + 0, s));
+                      dDE.as<double>(), want_mo ? dEE.as<double>() : nullptr,
+                      want_mo ? dCE.as<double>() : nullptr, sts + 0, s));
     CU(launch_dendif(ne, np, dDE.as<double>(), DE0.as<double>(), dDP.as<double>(),
                      DP0.as<double>(), d_en, s));
     double h[kScfSlots];
@@ -1172,6 +1185,10 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
   *converged = done ? 1 : 0;
   CU(cudaMemcpyAsync(DE, dDE.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(DP, dDP.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  if (CE) CU(cudaMemcpyAsync(CE, dCE.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  if (CP) CU(cudaMemcpyAsync(CP, dCP.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  if (EE) CU(cudaMemcpyAsync(EE, dEE.p, sizeof(double) * ne, cudaMemcpyDeviceToHost, s));
+  if (EP) CU(cudaMemcpyAsync(EP, dEP.p, sizeof(double) * np, cudaMemcpyDeviceToHost, s));
   return finish(s);
 }
 
@@ -1198,6 +1215,20 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
 }
 
 int64_t neoxc_xchf_job_size(void) { return (int64_t)sizeof(neoxc_xchf_job); }
+
+int neoxc_xchf_scf_job(neoxc_xchf_job* j, int64_t options, int64_t maxit) {
+  RC(need(j != nullptr, "job"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  j->status = xchf_scf_on(s, j->nelec, j->nucst, j->nebf, j->npebf, j->npbf, j->nat,
+                          j->ngtg1, j->pmass, j->cat, j->zan, j->bcoef1, j->gamma1,
+                          j->KPESTR, j->KPEEND, j->AMPEB2C, j->AGEBFCC, j->AGNBFCC,
+                          j->ELCEX, j->NUCEX, j->ELCAM, j->NUCAM, j->ELCBFC,
+                          j->NUCBFC, options, maxit, j->DE, j->DP, j->E_init,
+                          j->E_final, j->history, &j->niter, &j->converged, j->CE,
+                          j->CP, j->EE, j->EP);
+  return j->status;
+}
 
 // Device bytes one solve holds at its peak (integral tensors, SCF state and
 // contraction scratch), for admission against the memory budget.
@@ -1265,7 +1296,8 @@ int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
                                j.KPESTR, j.KPEEND, j.AMPEB2C, j.AGEBFCC, j.AGNBFCC,
                                j.ELCEX, j.NUCEX, j.ELCAM, j.NUCAM, j.ELCBFC,
                                j.NUCBFC, options, maxit, j.DE, j.DP, j.E_init,
-                               j.E_final, j.history, &j.niter, &j.converged);
+                               j.E_final, j.history, &j.niter, &j.converged, j.CE,
+                               j.CP, j.EE, j.EP);
         {
           std::lock_guard<std::mutex> lk(mu);
           in_use -= need_b;
@@ -1335,7 +1367,8 @@ static void server_worker(neoxc_xchf_server* S) {
                                  j->AGEBFCC, j->AGNBFCC, j->ELCEX, j->NUCEX, j->ELCAM,
                                  j->NUCAM, j->ELCBFC, j->NUCBFC, S->options, S->maxit,
                                  j->DE, j->DP, j->E_init, j->E_final, j->history,
-                                 &j->niter, &j->converged)
+                                 &j->niter, &j->converged, j->CE, j->CP, j->EE,
+                                 j->EP)
                    : NEOXC_ERR_CUDA;
     j->t_end = S->now();
     {

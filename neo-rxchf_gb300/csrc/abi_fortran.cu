@@ -22,43 +22,57 @@ void report(const char* who, int rc) {
                  neoxc_last_error());
 }
 
-// Record length, in bytes, of the reference's direct-access integral files
-// (GAM_IO.f: OPEN(...,ACCESS='direct',RECL=8)).  gfortran counts RECL in
-// bytes; ifort without -assume byterecl counts 4-byte units (32 bytes).
-long ufm_recl() {
-  const char* e = std::getenv("NEOXC_UFM_RECL");
-  long v = e ? std::atol(e) : 8;
-  return v >= 8 ? v : 8;
-}
-
-// Read records 1..n (one FP64 each, at the start of every record).
+// Direct-access integral files (GAM_IO.f: OPEN(...,ACCESS='direct',
+// RECL=8)): record length from NEOXC_UFM_RECL (bytes, default 8).
 bool read_ufm(const char* name, long long n, std::vector<double>& out) {
   out.assign((size_t)n, 0.0);
-  std::FILE* f = std::fopen(name, "rb");
-  if (!f) return false;
-  const long recl = ufm_recl();
-  std::vector<unsigned char> buf((size_t)recl);
-  bool ok = true;
-  for (long long i = 0; i < n && ok; i++) {
-    if (std::fread(buf.data(), 1, (size_t)recl, f) != (size_t)recl) ok = false;
-    else std::memcpy(&out[(size_t)i], buf.data(), sizeof(double));
-  }
-  std::fclose(f);
-  return ok;
+  return neoxc_ufm_read(name, n, 0, out.data()) == NEOXC_OK;
 }
 
 bool write_ufm(const char* name, const double* v, long long n) {
-  std::FILE* f = std::fopen(name, "wb");
-  if (!f) return false;
-  const long recl = ufm_recl();
-  std::vector<unsigned char> buf((size_t)recl, 0);
-  bool ok = true;
-  for (long long i = 0; i < n && ok; i++) {
-    std::memcpy(buf.data(), &v[i], sizeof(double));
-    ok = std::fwrite(buf.data(), 1, (size_t)recl, f) == (size_t)recl;
+  return neoxc_ufm_write(name, v, n, 0) == NEOXC_OK;
+}
+
+// File names of the reference's MO units (GAM_IO.f:450-500); other units
+// get ifort's default name fort.<unit>.
+std::string mo_unit_file(int64_t unit) {
+  switch (unit) {
+    case 850: return "guessCE.inp";
+    case 851: return "guessCP.inp";
+    case 852: return "FinalCE.dat";
+    case 853: return "FinalCP.dat";
+    case 860: return "FinalCAE.dat";
+    case 861: return "FinalCBE.dat";
+    case 870: return "FinalCAalpE.dat";
+    case 871: return "FinalCAbetE.dat";
+    default: return "fort." + std::to_string((long long)unit);
   }
-  std::fclose(f);
-  return ok;
+}
+
+// read_elec_density / read_nuc_density: MOs from a guess file, then
+// D = prefac * sum_{k=kstart..klast} C(:,k) C(:,k)^T.
+void read_density(const char* who, const char* file, int64_t nbf, int64_t kstart,
+                  int64_t klast, double prefac, double* D) {
+  std::vector<double> C((size_t)(nbf * nbf));
+  int rc = neoxc_mo_read(file, nbf, nbf, C.data());
+  if (rc == NEOXC_OK) rc = neoxc_mo_density(nbf, kstart, klast, prefac, C.data(), D);
+  report(who, rc);
+}
+
+// read_GAM_ecore-style readers: records 1..n in packed order.
+void read_packed(const char* who, const char* file, int64_t n, double* out) {
+  report(who, neoxc_ufm_read(file, n, 0, out));
+}
+
+// read_nuc_ovlap / read_elec_ovlap: GS(i,j) = record pack_2D(n,j,i), the
+// transpose of the file's column-major order.
+void read_ovlap(const char* who, const char* file, int64_t n, double* GS) {
+  std::vector<double> r((size_t)(n * n));
+  const int rc = neoxc_ufm_read(file, n * n, 0, r.data());
+  report(who, rc);
+  if (rc != NEOXC_OK) return;
+  for (int64_t i = 0; i < n; i++)
+    for (int64_t j = 0; j < n; j++) GS[i + n * j] = r[(size_t)(j + n * i)];
 }
 
 }  // namespace
@@ -268,6 +282,55 @@ void calc_gam_ee_(const int64_t* nebf, const int64_t* npebf,
   report("calc_gam_ee", rc);
   if (rc == NEOXC_OK && !write_ufm("GAM_ee.ufm", gee.data(), *ngee))
     std::fprintf(stderr, "neoxc: calc_gam_ee: cannot write GAM_ee.ufm\n");
+}
+
+// ---- GAM_IO.f: integral files and MO files -------------------------------
+
+// GAM_IO.f:28-67 read_GAM_ee (GAM_ee.ufm, pack_4D order = record order)
+void read_gam_ee_(const int64_t* ne, const int64_t* ngee, double* GAM_ee) {
+  (void)ne;
+  read_packed("read_GAM_ee", "GAM_ee.ufm", *ngee, GAM_ee);
+}
+// GAM_IO.f:69-108 read_GAM_ep (GAM_ep.ufm)
+void read_gam_ep_(const int64_t* ne, const int64_t* np, const int64_t* ng1,
+                  double* GAM_ep) {
+  (void)ne; (void)np;
+  read_packed("read_GAM_ep", "GAM_ep.ufm", *ng1, GAM_ep);
+}
+// GAM_IO.f:110-142 read_GAM_ecore (GAM_ecr.ufm)
+void read_gam_ecore_(const int64_t* ne, const int64_t* ne2, double* GAM_ecore) {
+  (void)ne;
+  read_packed("read_GAM_ecore", "GAM_ecr.ufm", *ne2, GAM_ecore);
+}
+// GAM_IO.f:144-176 read_GAM_pcore (GAM_pcr.ufm)
+void read_gam_pcore_(const int64_t* np, const int64_t* np2, double* GAM_pcore) {
+  (void)np;
+  read_packed("read_GAM_pcore", "GAM_pcr.ufm", *np2, GAM_pcore);
+}
+// GAM_IO.f:178-211 read_nuc_ovlap (novlap.ufm)
+void read_nuc_ovlap_(const int64_t* np, double* GS) {
+  read_ovlap("read_nuc_ovlap", "novlap.ufm", *np, GS);
+}
+// GAM_IO.f:213-245 read_elec_ovlap (eovlap.ufm)
+void read_elec_ovlap_(const int64_t* ne, double* GS) {
+  read_ovlap("read_elec_ovlap", "eovlap.ufm", *ne, GS);
+}
+// GAM_IO.f:247-347 read_elec_density: guessCE.inp; nocc = n/2 doubly
+// occupied orbitals (prefac 2), or orbital 1 (prefac 1) for one particle.
+void read_elec_density_(const int64_t* nebf, const int64_t* n_particle, double* DE) {
+  const bool many = *n_particle > 1;
+  read_density("read_elec_density", "guessCE.inp", *nebf, 1,
+               many ? *n_particle / 2 : 1, many ? 2.0 : 1.0, DE);
+}
+// GAM_IO.f:349-448 read_nuc_density: guessCP.inp; orbital NUCST, prefac 1.
+void read_nuc_density_(const int64_t* npbf, const int64_t* n_particle,
+                       const int64_t* NUCST, double* DP) {
+  (void)n_particle;
+  read_density("read_nuc_density", "guessCP.inp", *npbf, *NUCST, *NUCST, 1.0, DP);
+}
+// GAM_IO.f:450-468 write_MOs -> PUSQLF :471-518 (unit -> file name map)
+void write_mos_(const int64_t* IFIL, const int64_t* nbf, const double* VEC) {
+  report("write_MOs", neoxc_mo_write(mo_unit_file(*IFIL).c_str(), *nbf, *nbf, VEC));
 }
 
 }  // extern "C"

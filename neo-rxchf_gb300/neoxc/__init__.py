@@ -22,7 +22,8 @@ from .basis import NeoSystem  # noqa: F401  (re-export)
 __all__ = [
     "NeoxcError", "lib", "device_ok", "calc_gam_ee", "gam2_ic1", "gam3_ic1",
     "rxchfne_gam2_ic1", "gam4_icr", "gam4_dscf", "gam4_fock_factored",
-    "gam3_dscf", "gam2_dscf", "xchf_scf", "xchf_scf_batch", "XchfServer", "SCF_SLOTS",
+    "gam3_dscf", "gam2_dscf", "xchf_scf", "xchf_scf_job", "xchf_scf_batch", "XchfServer",
+    "SCF_SLOTS",
     "eg4icr", "eg3ic1", "eg2ic1",
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
@@ -63,6 +64,14 @@ def _declare(L):
         "neoxc_gam4_fock_factored": (I, [i64] * 4 + [vp] * 7),
         "neoxc_xchf_scf": (I, [i64] * 7 + [d] + [vp] * 15 + [i64, i64] + [vp] * 7),
         "neoxc_xchf_job_size": (i64, []),
+        "neoxc_xchf_scf_job": (I, [vp, i64, i64]),
+        "neoxc_ufm_read": (I, [C.c_char_p, i64, i64, vp]),
+        "neoxc_ufm_write": (I, [C.c_char_p, vp, i64, i64]),
+        "neoxc_mo_write": (I, [C.c_char_p, i64, i64, vp]),
+        "neoxc_mo_read": (I, [C.c_char_p, i64, i64, vp]),
+        "neoxc_mo_density": (I, [i64, i64, i64, d, vp, vp]),
+        "neoxc_enuc_write": (I, [C.c_char_p, d]),
+        "neoxc_enuc_read": (I, [C.c_char_p, vp]),
         "neoxc_xchf_scf_batch": (I, [vp, i64, i64, i64, i64]),
         "neoxc_xchf_server_start": (vp, [i64, i64, i64]),
         "neoxc_xchf_server_submit": (I, [vp, vp]),
@@ -281,7 +290,7 @@ class XchfJob(C.Structure):
                                              "KPEEND", "AMPEB2C", "AGEBFCC", "AGNBFCC",
                                              "ELCEX", "NUCEX", "ELCAM", "NUCAM", "ELCBFC",
                                              "NUCBFC", "DE", "DP", "E_init", "E_final",
-                                             "history")]
+                                             "history", "CE", "CP", "EE", "EP")]
                 + [("niter", C.c_int64), ("converged", C.c_int64),
                    ("status", C.c_int32), ("reserved", C.c_int32),
                    ("t_submit", C.c_double), ("t_start", C.c_double),
@@ -318,6 +327,7 @@ def _fill_job(j, s, DE, DP, maxit):
     de = _fmat(DE).copy()
     dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
     Ei, Ef, hist = np.zeros(16), np.zeros(16), np.zeros(4 * maxit)
+    CE, CP, EE, EP = np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(ne), np.zeros(np_)
     j.nelec, j.nucst, j.nebf, j.npebf, j.npbf = s.nelec, s.nucst, ne, s.npebf, np_
     j.nat, j.ngtg1, j.pmass = s.nat, s.ngtg, s.pmass
     names = ("cat", "zan", "bcoef1", "gamma1", "KPESTR", "KPEEND", "AMPEB2C", "AGEBFCC",
@@ -326,8 +336,9 @@ def _fill_job(j, s, DE, DP, maxit):
         setattr(j, name, a.ctypes.data)
     j.DE, j.DP, j.E_init, j.E_final = de.ctypes.data, dp.ctypes.data, Ei.ctypes.data, Ef.ctypes.data
     j.history = hist.ctypes.data
+    j.CE, j.CP, j.EE, j.EP = CE.ctypes.data, CP.ctypes.data, EE.ctypes.data, EP.ctypes.data
     return {"arrs": arrs, "ne": ne, "np": np_, "de": de, "dp": dp, "Ei": Ei, "Ef": Ef,
-            "hist": hist}
+            "hist": hist, "CE": CE, "CP": CP, "EE": EE, "EP": EP}
 
 
 def _job_result(j, b):
@@ -338,7 +349,23 @@ def _job_result(j, b):
             "converged": bool(j.converged),
             "DE": b["de"].reshape(b["ne"], b["ne"], order="F"),
             "DP": b["dp"].reshape(b["np"], b["np"], order="F"),
+            "CE": b["CE"].reshape(b["ne"], b["ne"], order="F"),
+            "CP": b["CP"].reshape(b["np"], b["np"], order="F"),
+            "EE": b["EE"].copy(), "EP": b["EP"].copy(),
             "t_submit": j.t_submit, "t_start": j.t_start, "t_end": j.t_end}
+
+
+def xchf_scf_job(s: NeoSystem, DE, DP=None, maxit: int = 100, diis: bool = False,
+                 mixed=False, gam4_element: bool = False):
+    """One XCHF solve through neoxc_xchf_scf_job: as xchf_scf, plus the
+    final MO coefficients CE, CP (columns by ascending orbital energy) and
+    the orbital energies EE, EP."""
+    job = XchfJob()
+    bufs = _fill_job(job, s, DE, DP, maxit)
+    _check(lib().neoxc_xchf_scf_job(C.byref(job),
+                                    _scf_options(DP is None, diis, mixed, gam4_element),
+                                    maxit))
+    return _job_result(job, bufs)
 
 
 class XchfServer:

@@ -147,8 +147,10 @@ def roothan(F, S, nocc, prefac, first=0):
 
 
 def xchf_scf(ints: XchfIntegrals, DE, DP=None, nucst=1, maxit=100, tole=1.0e-6,
-             tolp=1.0e-4):
-    """xcscf.f:2-658 (plain Roothaan): returns (history, last Fock result, DE, DP)."""
+             tolp=1.0e-4, orbitals=None):
+    """xcscf.f:2-658 (plain Roothaan): returns (history, last Fock result, DE, DP).
+    With a list as `orbitals`, each iteration appends (it, EE, EP, CE, CP):
+    ROOTHAN's eigenvalues and MO coefficients of that iteration."""
     s = ints.s
     noccE, prefE = (s.nelec // 2, 2.0) if s.nelec > 1 else (1, 1.0)
     if DP is None:   # guess_prot: diagonalise the nuclear core Hamiltonian
@@ -161,9 +163,11 @@ def xchf_scf(ints: XchfIntegrals, DE, DP=None, nucst=1, maxit=100, tole=1.0e-6,
         r = xchf1_fock(ints, DE, DP)
         if it == 1:
             hist.append(("initial", dict(r)))
-        DP, _, _ = roothan(r["fockp"], ints.S_p(), 1, 1.0, nucst - 1)
+        DP, CP, eP = roothan(r["fockp"], ints.S_p(), 1, 1.0, nucst - 1)
         r = xchf1_fock(ints, DE, DP)
-        DE, _, _ = roothan(r["focke"], ints.S_e(), noccE, prefE, 0)
+        DE, CE, eE = roothan(r["focke"], ints.S_e(), noccE, prefE, 0)
+        if orbitals is not None:
+            orbitals.append((it, eE, eP, CE, CP))
         diffE = float(np.abs(DE0 - DE).max())
         diffP = float(np.abs(DP0 - DP).max())
         DE0, DP0 = DE.copy(), DP.copy()

@@ -8,7 +8,8 @@ Writes, next to this script:
   xchf_example.json   examples/xchf: input deck, initial MO guess
                       (guessCE.inp), converged MOs (answer/FinalC*.dat) and
                       the energy components printed in answer/XCHF.log for
-                      the initial guess and at convergence;
+                      the initial guess and at convergence, and the
+                      orbital energies printed there;
   spot_check.json     CS_Integrals/Spot_Check/TEST_G{2,3,4}: the single-
                       primitive inputs (first record block, as SCI.f:114-152
                       reads them) and the MD values printed in each ``out``.
@@ -35,6 +36,19 @@ def _components(log: str, header: str) -> dict:
     return out
 
 
+def _eigenvalues(log: str, header: str, end: str) -> list:
+    """Orbital energies of PREVNU's table (4 decimals): the rows between the
+    column-number rows and the coefficient rows (those carry LABEL)."""
+    i = log.index(header)
+    block = log[i + len(header):log.index(end, i)]
+    vals = []
+    for line in block.splitlines():
+        toks = line.split()
+        if toks and "LABEL" not in line and all("." in t for t in toks):
+            vals += [float(t) for t in toks]
+    return vals
+
+
 def xchf_example(ref: str) -> dict:
     d = os.path.join(ref, "examples", "xchf")
     log = open(os.path.join(d, "answer", "XCHF.log")).read()
@@ -46,7 +60,13 @@ def xchf_example(ref: str) -> dict:
         "finalCP": open(os.path.join(d, "answer", "FinalCP.dat")).read(),
         "initial": _components(log, "INITIAL GUESS ENERGETICS"),
         "final": _components(log, "FINAL NEOXCHF ENERGY"),
-        "log_lines": {"initial": "XCHF.log:306-321", "final": "XCHF.log:335-350"},
+        "orbital_energies": {
+            "electronic": _eigenvalues(log, "ELECTRONIC ORBITALS AND EIGENVALUES:",
+                                       "NUCLEAR ORBITALS AND EIGENVALUES:"),
+            "nuclear": _eigenvalues(log, "NUCLEAR ORBITALS AND EIGENVALUES:",
+                                    "TIMING SUMMARY")},
+        "log_lines": {"initial": "XCHF.log:306-321", "final": "XCHF.log:335-350",
+                      "orbital_energies": "XCHF.log:353-384"},
     }
 
 

@@ -161,3 +161,37 @@ def test_server_requests_match_separate_solves(nx, xchf):
         a = nx.xchf_scf(s, xchf["DE0"], diis=True, mixed=True)
         assert r["converged"] and r["final"]["E_total"] == a["final"]["E_total"]
         assert r["t_submit"] <= r["t_start"] <= r["t_end"]
+
+
+def test_xchf_scf_job_returns_final_mos(nx, xchf, xchf_gpu_scf, tmp_path):
+    """neoxc_xchf_scf_job: the same solve as neoxc_xchf_scf plus the final
+    MOs and orbital energies.  C^T S C = 1; the occupied MOs rebuild the
+    returned density; the orbital energies are the oracle's converged ones
+    (its last ROOTHAN) to 1e-7; the occupied space matches the reference's
+    answer/FinalC{E,P}.dat to the density tolerance; FinalCE.dat written from
+    the MOs reads back to its 8 printed digits."""
+    import xchf_scf as X
+    from neoxc import formats as F
+    s = xchf["sys"]
+    r = nx.xchf_scf_job(s, xchf["DE0"])
+    assert r["converged"] and r["niter"] == xchf_gpu_scf["niter"]
+    assert abs(r["final"]["E_total"] - xchf_gpu_scf["final"]["E_total"]) <= 1e-12
+    ints = X.XchfIntegrals(s)
+    orb = []
+    X.xchf_scf(ints, xchf["DE0"], orbitals=orb)
+    CE, CP = r["CE"], r["CP"]
+    assert np.abs(CE.T @ ints.S_e() @ CE - np.eye(s.nebf)).max() <= 1e-10
+    assert np.abs(CP.T @ ints.S_p() @ CP - np.eye(s.npbf)).max() <= 1e-10
+    assert np.all(np.diff(r["EE"]) >= 0)
+    assert np.abs(r["EE"] - orb[-1][1]).max() <= 1e-7, (r["EE"], orb[-1][1])
+    assert np.abs(r["EP"] - orb[-1][2]).max() <= 1e-7
+    nocc = s.nelec // 2
+    DE = F.mo_density(CE, 1, nocc, 2.0)
+    assert np.abs(DE - r["DE"]).max() <= 1e-12
+    assert np.abs(F.mo_density(CP, s.nucst, s.nucst, 1.0) - r["DP"]).max() <= 1e-12
+    dmax = np.abs(DE - xchf["DEf"]).max()
+    assert dmax <= 1e-5, dmax
+    assert np.abs(r["DP"] - xchf["DPf"]).max() <= 1e-7
+    out = tmp_path / "FinalCE.dat"
+    F.write_mos(out, CE)
+    assert np.abs(F.read_mos(out, s.nebf) - CE).max() <= 5e-9 * max(1.0, np.abs(CE).max())

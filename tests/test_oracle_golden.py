@@ -159,11 +159,16 @@ def test_xchf_scf_oracle_pinned(xchf, golden_xchf):
     gam_4) reproduces examples/xchf: every initial-guess component of
     XCHF.log:306-321 to the printed 10 decimals, and the converged total
     energy of XCHF.log:335 (the reference converged with SOSCF; the plain
-    Roothaan sequence reaches the same stationary point)."""
+    Roothaan sequence reaches the same stationary point).  The orbital
+    energies printed at XCHF.log:353-384: the electronic ones are those of
+    the first ROOTHAN diagonalisation (from the second iteration on, SOSCF
+    rotates the orbitals without diagonalising, xcscf.f:463-484, so EE is
+    never refreshed), the nuclear one is the last iteration's."""
     import xchf_scf as X
     s = xchf["sys"]
     ints = X.XchfIntegrals(s)
-    hist, r, DE, DP, ok = X.xchf_scf(ints, xchf["DE0"])
+    orb = []
+    hist, r, DE, DP, ok = X.xchf_scf(ints, xchf["DE0"], orbitals=orb)
     init = hist[0][1]
     ref = golden_xchf["initial"]
     for k in ("E_NUC", "E_ECORE", "E_PCORE", "E_EP", "E_EE", "E_GAM1", "E_GAM2", "E_GAM3",
@@ -180,3 +185,6 @@ def test_xchf_scf_oracle_pinned(xchf, golden_xchf):
     for k, mine in (("E_ECORE", "E_ecore"), ("E_EP", "E_ep"), ("E_GAM1", "E_gam1"),
                     ("E_GAM2", "E_gam2"), ("S_TOTAL", "S_total")):
         assert abs(r[mine] - fin[k]) <= 1e-5 * max(1.0, abs(fin[k])), k
+    eig = golden_xchf["orbital_energies"]
+    assert np.abs(orb[0][1] - eig["electronic"]).max() <= 5.001e-5
+    assert np.abs(orb[-1][2] - eig["nuclear"]).max() <= 5.001e-5
