@@ -366,6 +366,74 @@ int neoxc_xchf_server_wait(neoxc_xchf_server* srv, neoxc_xchf_job* job,
                            double timeout_s);
 int neoxc_xchf_server_stop(neoxc_xchf_server* srv);
 
+/* ---- open-shell XCUHF contractions: xcuhf/xcuhf_omg{1..4}.f ------------ */
+/* Same arguments, packed layouts and semantics as the reference: the Fock
+ * matrix (FAE or FP) accumulates (add2fock), the SAE / SP matrices and the energies are
+ * overwritten.  FAE_* computes the Fock matrix of the spin whose density
+ * and count come first; the reference's beta call swaps (NAE,DAE) with
+ * (NBE,DBE).  The spin-term flags (LAA, LAB, ..., L4A, L3A1B, ...) are
+ * derived from NAE/NBE exactly as in the reference.  Limits: nebf <= 256
+ * (OMG1/OMG2), 28 (OMG3), 12 (OMG4); beyond them NEOXC_ERR_UNSUPPORTED. */
+/* xcuhf_omg1.f:2-81 FAE_OMG1; GAM_1 / GAM_1s (pack_4D(je,ie,jp,ip)) are
+ * arguments here (the reference reads GAM_1.ufm / GAM_1s.ufm). */
+int neoxc_fae_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DAE,
+                   const double* DP, const double* GAM_1, const double* GAM_1s,
+                   double* FAE, double* SAE1, double* E_AE_OMG1, double* S_AE_OMG1);
+/* xcuhf_omg1.f:83-163 UFP_OMG1 */
+int neoxc_ufp_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DETOT,
+                   const double* DP, const double* GAM_1, const double* GAM_1s,
+                   double* FP, double* SP1, double* E_P_OMG1, double* S_P_OMG1);
+/* xcuhf_omg2.f:2-300 FAE_OMG2 (DETOT is unused, as in the reference) */
+int neoxc_fae_omg2(int64_t Nchunks, int64_t NAE, int64_t NBE, int64_t nebf,
+                   int64_t npbf, int64_t ng2, const double* DAE, const double* DBE,
+                   const double* DETOT, const double* DP, const double* GM2ICR,
+                   const double* GM2SICR, double* FAE, double* SAE2,
+                   double* E_AE_OMG2, double* S_AE_OMG2);
+/* xcuhf_omg2.f:302-612 UFP_OMG2 */
+int neoxc_ufp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DETOT, const double* DP, const double* GM2ICR,
+                   const double* GM2SICR, double* FP, double* SP2, double* E_P_OMG2,
+                   double* S_P_OMG2);
+/* xcuhf_omg3.f:2-282 FAE_OMG3 */
+int neoxc_fae_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM3ICR, double* FAE,
+                   double* E_AE_OMG3);
+/* xcuhf_omg3.f:284-588 UFP_OMG3 */
+int neoxc_ufp_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM3ICR, double* FP,
+                   double* E_P_OMG3);
+/* xcuhf_omg4.f:2-510 FAE_OMG4 (GM4ICR from OMG4_ICR) */
+int neoxc_fae_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM4ICR, double* FAE,
+                   double* E_AE_OMG4);
+/* xcuhf_omg4.f:512-1078 UFP_OMG4 */
+int neoxc_ufp_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM4ICR, double* FP,
+                   double* E_P_OMG4);
+/* xcuhf_omg4.f:1080-1315 OMG4_ICR: the raw 5-particle tensor
+ * (calc_GAM_4_integral, no permutational symmetrisation) at index_GAM_4PK2;
+ * GAM_ee is an argument (the reference reads GAM_ee.ufm). */
+int neoxc_omg4_icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ngee, int64_t ng2,
+                   int64_t ng4, const double* GAM_2s, const double* GAM_ee,
+                   double* GAM_4);
+/* Device pointers, on `stream`: FAE_OMGk, FAE_OMGk for beta (spins
+ * exchanged) and UFP_OMGk of one rank K (2: G = GM2ICR, Gs = GM2SICR;
+ * 3: GM3ICR; 4: OMG4_ICR, Gs = NULL) from one pass over the tensor.  Any
+ * output may be NULL.  Fock matrices accumulate, S* are overwritten,
+ * d_E[6] = {E_AE, E_BE, E_P, S_AE, S_BE, S_P} is overwritten. */
+int neoxc_dev_xcuhf_omg(void* stream, int64_t K, int64_t ne, int64_t np, int64_t NAE,
+                        int64_t NBE, const double* d_G, const double* d_Gs,
+                        const double* d_DAE, const double* d_DBE, const double* d_DP,
+                        double* d_FAE, double* d_FBE, double* d_FP, double* d_SAE,
+                        double* d_SBE, double* d_SP, double* d_E);
+int neoxc_dev_omg4_icr(void* stream, int64_t ne, int64_t np, const double* d_gee,
+                       const double* d_g2s, double* d_g4);
+
 /* ---- on-disk formats: xchf1_independent/GAM_IO.f (host only, no GPU) --- */
 /* Direct-access integral files (*.ufm, GAM_IO.f:1-245): record ia (1-based)
  * holds the FP64 at packed index ia, records `recl` bytes long with the value
@@ -518,6 +586,44 @@ void read_elec_density_(const int64_t* nebf, const int64_t* n_particle, double* 
 void read_nuc_density_(const int64_t* npbf, const int64_t* n_particle,
                        const int64_t* NUCST, double* DP);
 void write_mos_(const int64_t* IFIL, const int64_t* nbf, const double* VEC);
+/* xcuhf_omg{1..4}.f with the reference's argument lists; fae_omg1_ /
+ * ufp_omg1_ read GAM_1.ufm and GAM_1s.ufm, omg4_icr_ reads GAM_ee.ufm, from
+ * the working directory like the reference. */
+void fae_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+               const double* DAE, const double* DP, double* FAE, double* SAE1,
+               double* E_AE_OMG1, double* S_AE_OMG1);
+void ufp_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+               const double* DETOT, const double* DP, double* FP, double* SP1,
+               double* E_P_OMG1, double* S_P_OMG1);
+void fae_omg2_(const int64_t* Nchunks, const int64_t* NAE, const int64_t* NBE,
+               const int64_t* nebf, const int64_t* npbf, const int64_t* ng2,
+               const double* DAE, const double* DBE, const double* DETOT,
+               const double* DP, const double* GM2ICR, const double* GM2SICR,
+               double* FAE, double* SAE2, double* E_AE_OMG2, double* S_AE_OMG2);
+void ufp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng2, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DETOT,
+               const double* DP, const double* GM2ICR, const double* GM2SICR,
+               double* FP, double* SP2, double* E_P_OMG2, double* S_P_OMG2);
+void fae_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng3, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM3ICR, double* FAE, double* E_AE_OMG3);
+void ufp_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng3, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM3ICR, double* FP, double* E_P_OMG3);
+void fae_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng4, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM4ICR, double* FAE, double* E_AE_OMG4);
+void ufp_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng4, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM4ICR, double* FP, double* E_P_OMG4);
+void omg4_icr_(const int64_t* Nchunks, const int64_t* ne, const int64_t* np,
+               const int64_t* ngee, const int64_t* ng2, const int64_t* ng4,
+               const double* GAM_2s, double* GAM_4);
 
 #ifdef __cplusplus
 }

@@ -1445,3 +1445,277 @@ int neoxc_xchf_server_stop(neoxc_xchf_server* S) {
 }
 
 }  // extern "C"
+
+// ---- open-shell XCUHF contractions (xcuhf/xcuhf_omg{1..4}.f) --------------
+namespace {
+
+// FAE_OMG2 (LAA, LAB), FAE_OMG3 (LAA, LAB, LBB), FAE_OMG4 (LAAA, LAAB,
+// LBBA, LBBB) for the spin with na electrons (nb of the other spin).
+unsigned fae_flags(int K, int64_t na, int64_t nb) {
+  if (K == 2) return (na >= 2 ? 1u : 0u) | (na >= 1 && nb >= 1 ? 2u : 0u);
+  if (K == 3)
+    return (na >= 3 ? 1u : 0u) | (nb >= 1 && na >= 2 ? 2u : 0u) | (nb >= 2 ? 4u : 0u);
+  return (na >= 4 ? 1u : 0u) | (na >= 3 && nb >= 1 ? 2u : 0u) |
+         (nb >= 2 && na >= 2 ? 4u : 0u) | (nb >= 3 ? 8u : 0u);
+}
+
+// UFP_OMG2 (LAA, LAB), UFP_OMG3 (LAAA, LAAB, LBBA), UFP_OMG4 (L4A, L3A1B,
+// L2A2B, L1A3B): the terms whose first electron has the spin with na.
+unsigned ufp_flags(int K, int64_t na, int64_t nb) {
+  if (K == 2) return (na >= 2 ? 1u : 0u) | (na >= 1 && nb >= 1 ? 2u : 0u);
+  if (K == 3)
+    return (na >= 3 ? 1u : 0u) | (na >= 2 && nb >= 1 ? 2u : 0u) |
+           (nb >= 2 && na >= 1 ? 4u : 0u);
+  return (na >= 4 ? 1u : 0u) | (na >= 3 && nb >= 1 ? 2u : 0u) |
+         (na >= 2 && nb >= 2 ? 4u : 0u) | (na >= 1 && nb >= 3 ? 8u : 0u);
+}
+
+// One pass (two when the proton flags differ) over the rank-K tensor gives
+// FAE_OMGk (alpha), FAE_OMGk with the spins exchanged (beta) and UFP_OMGk.
+// Null outputs are skipped.  E[6] = {E_AE, E_BE, E_P, S_AE, S_BE, S_P}.
+// Size limits of the rank-K contraction, checked before any array is read.
+int spin_limits(int K, int64_t ne, int64_t np) {
+  RC(need(ne >= 1 && ne <= 256 && np >= 1, "1 <= nebf <= 256, npbf >= 1"));
+  RC(need(K >= 2 && K <= 4, "rank 2..4"));
+  if (K > 2 && !spin_smem_fits(K, (int)ne))
+    return set_err(NEOXC_ERR_UNSUPPORTED,
+                   "rank-%d open-shell contraction: nebf <= %d (one bra's kets "
+                   "are staged in shared memory)", K, K == 3 ? 28 : 12);
+  return NEOXC_OK;
+}
+
+int xcuhf_dev(cudaStream_t s, int K, int64_t ne, int64_t np, int64_t NAE,
+              int64_t NBE, const double* G, const double* Gs, const double* DAE,
+              const double* DBE, const double* DP, double* FAE, double* FBE,
+              double* FP, double* SAE, double* SBE, double* SP, double* E) {
+  RC(spin_limits(K, ne, np));
+  RC(need(K == 2 || !Gs, "overlap tensor only for rank 2"));
+  RC(need(NAE >= 0 && NBE >= 0, "NAE, NBE >= 0"));
+  RC(need(G && DAE && DBE && DP && E, "pointers"));
+  const int64_t n2 = ne * ne, p2 = np * np;
+  const bool want_a = FAE || SAE, want_b = FBE || SBE, want_p = FP || SP;
+  const unsigned fa = want_a ? fae_flags(K, NAE, NBE) : 0u;
+  const unsigned fb = want_b ? fae_flags(K, NBE, NAE) : 0u;
+  const unsigned pa = ufp_flags(K, NAE, NBE), pb = ufp_flags(K, NBE, NAE);
+  DBuf scr, fe, fp;
+  RC(dalloc(scr, sizeof(double) * spin_scratch_doubles(K, (int)ne, (int)np), s));
+  RC(dalloc(fe, sizeof(double) * 4 * n2, s));
+  RC(dalloc(fp, sizeof(double) * 2 * p2, s));
+  CU(cudaMemsetAsync(E, 0, sizeof(double) * 6, s));
+  const double scale = (double)K;   // EFAC = 2, 3, 4
+  double* x = fe.as<double>();
+  if (want_a || want_b) {
+    CU(launch_spin_omg(K, (int)ne, (int)np, G, Gs, DAE, DBE, DP, fa, fb,
+                       scr.as<double>(), x, fp.as<double>(), s));
+    if (want_a)
+      CU(launch_spin_finish((int)ne, x, Gs ? x + 2 * n2 : nullptr, DAE, scale, FAE,
+                            SAE, E + 0, E + 3, s));
+    if (want_b)
+      CU(launch_spin_finish((int)ne, x + n2, Gs ? x + 3 * n2 : nullptr, DBE, scale,
+                            FBE, SBE, E + 1, E + 4, s));
+  }
+  if (want_p) {
+    if (!(want_a && want_b && fa == pa && fb == pb))
+      CU(launch_spin_omg(K, (int)ne, (int)np, G, Gs, DAE, DBE, DP, pa, pb,
+                         scr.as<double>(), x, fp.as<double>(), s));
+    CU(launch_spin_finish((int)np, fp.as<double>(), Gs ? fp.as<double>() + p2 : nullptr,
+                          DP, 1.0, FP, SP, E + 2, E + 5, s));
+  }
+  return NEOXC_OK;
+}
+
+// Host wrapper of one reference routine: `proton` selects UFP_OMGk, else
+// FAE_OMGk for the spin of DAE.  Fock accumulates; S, E, Es overwritten.
+int xcuhf_host(int K, int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+               int64_t ng, const double* G, const double* Gs, const double* DAE,
+               const double* DBE, const double* DP, bool proton, double* F,
+               double* S, double* E, double* Es) {
+  RC(spin_limits(K, ne, np));
+  RC(need(DAE && DBE && DP && G && F && E, "pointers"));
+  RC(need(K == 2 ? (Gs && S && Es) : true, "GM2SICR, SAE2/SP2, S_*_OMG2"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  const int64_t n2 = ne * ne, p2 = np * np, nf = proton ? p2 : n2;
+  DBuf dg, dgs, da, db, dp, dF, dS, dE;
+  RC(upload(dg, G, sizeof(double) * ng, s));
+  if (Gs) RC(upload(dgs, Gs, sizeof(double) * ng, s));
+  RC(upload(da, DAE, sizeof(double) * n2, s));
+  RC(upload(db, DBE, sizeof(double) * n2, s));
+  RC(upload(dp, DP, sizeof(double) * p2, s));
+  RC(dalloc(dF, sizeof(double) * nf, s));
+  RC(dalloc(dS, sizeof(double) * nf, s));
+  RC(dalloc(dE, sizeof(double) * 6, s));
+  CU(cudaMemsetAsync(dF.p, 0, sizeof(double) * nf, s));
+  double* f = dF.as<double>();
+  double* sv = Gs ? dS.as<double>() : nullptr;
+  RC(xcuhf_dev(s, K, ne, np, NAE, NBE, dg.as<double>(), Gs ? dgs.as<double>() : nullptr,
+               da.as<double>(), db.as<double>(), dp.as<double>(), proton ? nullptr : f,
+               nullptr, proton ? f : nullptr, proton ? nullptr : sv, nullptr,
+               proton ? sv : nullptr, dE.as<double>()));
+  double e6[6];
+  CU(cudaMemcpyAsync(e6, dE.p, sizeof e6, cudaMemcpyDeviceToHost, s));
+  if (Gs) CU(cudaMemcpyAsync(S, dS.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
+  RC(accumulate_back(F, f, nf, s));   // synchronises the stream
+  *E = proton ? e6[2] : e6[0];
+  if (Es) *Es = proton ? e6[5] : e6[3];
+  return finish(s);
+}
+
+// FAE_OMG1 / UFP_OMG1: W = DAE (alpha Fock) or DETOT (proton Fock).
+int omg1_host(int64_t ne, int64_t np, int64_t ng1, const double* W, const double* DP,
+              const double* G1, const double* G1s, bool proton, double* F,
+              double* S, double* E, double* Es) {
+  RC(need(ng1 == ne * ne * np * np, "ng1 == nebf**2 npbf**2"));
+  RC(need(W && DP && G1 && G1s && F && S && E && Es, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  const int64_t n2 = ne * ne, p2 = np * np, nf = proton ? p2 : n2;
+  DBuf dg, dgs, dw, dp, fe, fpo, dF, dS, dE;
+  RC(upload(dg, G1, sizeof(double) * ng1, s));
+  RC(upload(dgs, G1s, sizeof(double) * ng1, s));
+  RC(upload(dw, W, sizeof(double) * n2, s));
+  RC(upload(dp, DP, sizeof(double) * p2, s));
+  RC(dalloc(fe, sizeof(double) * 2 * n2, s));
+  RC(dalloc(fpo, sizeof(double) * 2 * p2, s));
+  RC(dalloc(dF, sizeof(double) * nf, s));
+  RC(dalloc(dS, sizeof(double) * nf, s));
+  RC(dalloc(dE, sizeof(double) * 2, s));
+  CU(cudaMemsetAsync(dF.p, 0, sizeof(double) * nf, s));
+  CU(launch_omg1((int)ne, (int)np, dg.as<double>(), dgs.as<double>(), dw.as<double>(),
+                 dp.as<double>(), fe.as<double>(), fpo.as<double>(), s));
+  if (proton)
+    CU(launch_spin_finish((int)np, fpo.as<double>(), fpo.as<double>() + p2,
+                          dp.as<double>(), 1.0, dF.as<double>(), dS.as<double>(),
+                          dE.as<double>(), dE.as<double>() + 1, s));
+  else
+    CU(launch_spin_finish((int)ne, fe.as<double>(), fe.as<double>() + n2,
+                          dw.as<double>(), 1.0, dF.as<double>(), dS.as<double>(),
+                          dE.as<double>(), dE.as<double>() + 1, s));
+  double e2[2];
+  CU(cudaMemcpyAsync(e2, dE.p, sizeof e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(S, dS.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
+  RC(accumulate_back(F, dF.as<double>(), nf, s));
+  *E = e2[0];
+  *Es = e2[1];
+  return finish(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int neoxc_fae_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DAE,
+                   const double* DP, const double* GAM_1, const double* GAM_1s,
+                   double* FAE, double* SAE1, double* E_AE_OMG1, double* S_AE_OMG1) {
+  return omg1_host(nebf, npbf, ng1, DAE, DP, GAM_1, GAM_1s, false, FAE, SAE1,
+                   E_AE_OMG1, S_AE_OMG1);
+}
+
+int neoxc_ufp_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DETOT,
+                   const double* DP, const double* GAM_1, const double* GAM_1s,
+                   double* FP, double* SP1, double* E_P_OMG1, double* S_P_OMG1) {
+  return omg1_host(nebf, npbf, ng1, DETOT, DP, GAM_1, GAM_1s, true, FP, SP1,
+                   E_P_OMG1, S_P_OMG1);
+}
+
+int neoxc_fae_omg2(int64_t Nchunks, int64_t NAE, int64_t NBE, int64_t nebf,
+                   int64_t npbf, int64_t ng2, const double* DAE, const double* DBE,
+                   const double* DETOT, const double* DP, const double* GM2ICR,
+                   const double* GM2SICR, double* FAE, double* SAE2,
+                   double* E_AE_OMG2, double* S_AE_OMG2) {
+  (void)DETOT;
+  RC(need(Nchunks >= 1 && ng2 == nebf * nebf * nebf * nebf * npbf * npbf,
+          "Nchunks >= 1, ng2 == nebf**4 npbf**2"));
+  return xcuhf_host(2, nebf, npbf, NAE, NBE, ng2, GM2ICR, GM2SICR, DAE, DBE, DP,
+                    false, FAE, SAE2, E_AE_OMG2, S_AE_OMG2);
+}
+
+int neoxc_ufp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DETOT, const double* DP, const double* GM2ICR,
+                   const double* GM2SICR, double* FP, double* SP2, double* E_P_OMG2,
+                   double* S_P_OMG2) {
+  (void)DETOT;
+  RC(need(Nchunks >= 1 && ng2 == nebf * nebf * nebf * nebf * npbf * npbf,
+          "Nchunks >= 1, ng2 == nebf**4 npbf**2"));
+  return xcuhf_host(2, nebf, npbf, NAE, NBE, ng2, GM2ICR, GM2SICR, DAE, DBE, DP,
+                    true, FP, SP2, E_P_OMG2, S_P_OMG2);
+}
+
+int neoxc_fae_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM3ICR, double* FAE,
+                   double* E_AE_OMG3) {
+  const int64_t n3 = nebf * nebf * nebf;
+  RC(need(Nchunks >= 1 && ng3 == n3 * n3 * npbf * npbf, "Nchunks >= 1, ng3 == nebf**6 npbf**2"));
+  return xcuhf_host(3, nebf, npbf, NAE, NBE, ng3, GM3ICR, nullptr, DAE, DBE, DP, false,
+                    FAE, nullptr, E_AE_OMG3, nullptr);
+}
+
+int neoxc_ufp_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM3ICR, double* FP,
+                   double* E_P_OMG3) {
+  const int64_t n3 = nebf * nebf * nebf;
+  RC(need(Nchunks >= 1 && ng3 == n3 * n3 * npbf * npbf, "Nchunks >= 1, ng3 == nebf**6 npbf**2"));
+  return xcuhf_host(3, nebf, npbf, NAE, NBE, ng3, GM3ICR, nullptr, DAE, DBE, DP, true,
+                    FP, nullptr, E_P_OMG3, nullptr);
+}
+
+int neoxc_fae_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM4ICR, double* FAE,
+                   double* E_AE_OMG4) {
+  const int64_t n4 = nebf * nebf * nebf * nebf;
+  RC(need(Nchunks >= 1 && ng4 == n4 * n4 * npbf * npbf, "Nchunks >= 1, ng4 == nebf**8 npbf**2"));
+  return xcuhf_host(4, nebf, npbf, NAE, NBE, ng4, GM4ICR, nullptr, DAE, DBE, DP, false,
+                    FAE, nullptr, E_AE_OMG4, nullptr);
+}
+
+int neoxc_ufp_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                   int64_t NAE, int64_t NBE, const double* DAE, const double* DBE,
+                   const double* DP, const double* GM4ICR, double* FP,
+                   double* E_P_OMG4) {
+  const int64_t n4 = nebf * nebf * nebf * nebf;
+  RC(need(Nchunks >= 1 && ng4 == n4 * n4 * npbf * npbf, "Nchunks >= 1, ng4 == nebf**8 npbf**2"));
+  return xcuhf_host(4, nebf, npbf, NAE, NBE, ng4, GM4ICR, nullptr, DAE, DBE, DP, true,
+                    FP, nullptr, E_P_OMG4, nullptr);
+}
+
+int neoxc_dev_xcuhf_omg(void* stream, int64_t K, int64_t ne, int64_t np, int64_t NAE,
+                        int64_t NBE, const double* d_G, const double* d_Gs,
+                        const double* d_DAE, const double* d_DBE, const double* d_DP,
+                        double* d_FAE, double* d_FBE, double* d_FP, double* d_SAE,
+                        double* d_SBE, double* d_SP, double* d_E) {
+  return xcuhf_dev((cudaStream_t)stream, (int)K, ne, np, NAE, NBE, d_G, d_Gs, d_DAE,
+                   d_DBE, d_DP, d_FAE, d_FBE, d_FP, d_SAE, d_SBE, d_SP, d_E);
+}
+
+int neoxc_dev_omg4_icr(void* stream, int64_t ne, int64_t np, const double* d_gee,
+                       const double* d_g2s, double* d_g4) {
+  RC(need(ne >= 1 && np >= 1 && d_gee && d_g2s && d_g4, "sizes, pointers"));
+  CU(launch_omg4_icr((int)ne, (int)np, d_gee, d_g2s, d_g4, (cudaStream_t)stream));
+  return NEOXC_OK;
+}
+
+int neoxc_omg4_icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ngee, int64_t ng2,
+                   int64_t ng4, const double* GAM_2s, const double* GAM_ee,
+                   double* GAM_4) {
+  RC(need(Nchunks >= 1, "Nchunks >= 1"));
+  RC(need(ngee == ne * ne * ne * ne, "ngee == ne**4"));
+  RC(need(ng2 == ngee * np * np, "ng2 == ne**4 np**2"));
+  RC(need(ng4 == ngee * ngee * np * np, "ng4 == ne**8 np**2"));
+  RC(need(GAM_2s && GAM_ee && GAM_4, "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  DBuf dg2, dee, d4;
+  RC(upload(dg2, GAM_2s, sizeof(double) * ng2, s));
+  RC(upload(dee, GAM_ee, sizeof(double) * ngee, s));
+  RC(dalloc(d4, sizeof(double) * ng4, s));
+  CU(launch_omg4_icr((int)ne, (int)np, dee.as<double>(), dg2.as<double>(),
+                     d4.as<double>(), s));
+  CU(cudaMemcpyAsync(GAM_4, d4.p, sizeof(double) * ng4, cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+}  // extern "C"

@@ -333,4 +333,95 @@ void write_mos_(const int64_t* IFIL, const int64_t* nbf, const double* VEC) {
   report("write_MOs", neoxc_mo_write(mo_unit_file(*IFIL).c_str(), *nbf, *nbf, VEC));
 }
 
+// ---- xcuhf/xcuhf_omg{1..4}.f ---------------------------------------------
+
+// xcuhf_omg1.f:2-81 FAE_OMG1 (GAM_1.ufm, GAM_1s.ufm read as in :20-23)
+void fae_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+               const double* DAE, const double* DP, double* FAE, double* SAE1,
+               double* E_AE_OMG1, double* S_AE_OMG1) {
+  std::vector<double> g1, g1s;
+  if (!read_ufm("GAM_1.ufm", *ng1, g1) || !read_ufm("GAM_1s.ufm", *ng1, g1s)) {
+    std::fprintf(stderr, "neoxc: fae_omg1: cannot read GAM_1.ufm/GAM_1s.ufm\n");
+    return;
+  }
+  report("fae_omg1", neoxc_fae_omg1(*nebf, *npbf, *ng1, DAE, DP, g1.data(), g1s.data(),
+                                    FAE, SAE1, E_AE_OMG1, S_AE_OMG1));
+}
+// xcuhf_omg1.f:83-163 UFP_OMG1
+void ufp_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+               const double* DETOT, const double* DP, double* FP, double* SP1,
+               double* E_P_OMG1, double* S_P_OMG1) {
+  std::vector<double> g1, g1s;
+  if (!read_ufm("GAM_1.ufm", *ng1, g1) || !read_ufm("GAM_1s.ufm", *ng1, g1s)) {
+    std::fprintf(stderr, "neoxc: ufp_omg1: cannot read GAM_1.ufm/GAM_1s.ufm\n");
+    return;
+  }
+  report("ufp_omg1", neoxc_ufp_omg1(*nebf, *npbf, *ng1, DETOT, DP, g1.data(), g1s.data(),
+                                    FP, SP1, E_P_OMG1, S_P_OMG1));
+}
+// xcuhf_omg2.f:2-4 FAE_OMG2
+void fae_omg2_(const int64_t* Nchunks, const int64_t* NAE, const int64_t* NBE,
+               const int64_t* nebf, const int64_t* npbf, const int64_t* ng2,
+               const double* DAE, const double* DBE, const double* DETOT,
+               const double* DP, const double* GM2ICR, const double* GM2SICR,
+               double* FAE, double* SAE2, double* E_AE_OMG2, double* S_AE_OMG2) {
+  report("fae_omg2", neoxc_fae_omg2(*Nchunks, *NAE, *NBE, *nebf, *npbf, *ng2, DAE, DBE,
+                                    DETOT, DP, GM2ICR, GM2SICR, FAE, SAE2, E_AE_OMG2,
+                                    S_AE_OMG2));
+}
+// xcuhf_omg2.f:302-304 UFP_OMG2
+void ufp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng2, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DETOT,
+               const double* DP, const double* GM2ICR, const double* GM2SICR,
+               double* FP, double* SP2, double* E_P_OMG2, double* S_P_OMG2) {
+  report("ufp_omg2", neoxc_ufp_omg2(*Nchunks, *nebf, *npbf, *ng2, *NAE, *NBE, DAE, DBE,
+                                    DETOT, DP, GM2ICR, GM2SICR, FP, SP2, E_P_OMG2,
+                                    S_P_OMG2));
+}
+// xcuhf_omg3.f:2-3 FAE_OMG3
+void fae_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng3, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM3ICR, double* FAE, double* E_AE_OMG3) {
+  report("fae_omg3", neoxc_fae_omg3(*Nchunks, *nebf, *npbf, *ng3, *NAE, *NBE, DAE, DBE,
+                                    DP, GM3ICR, FAE, E_AE_OMG3));
+}
+// xcuhf_omg3.f:284-285 UFP_OMG3
+void ufp_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng3, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM3ICR, double* FP, double* E_P_OMG3) {
+  report("ufp_omg3", neoxc_ufp_omg3(*Nchunks, *nebf, *npbf, *ng3, *NAE, *NBE, DAE, DBE,
+                                    DP, GM3ICR, FP, E_P_OMG3));
+}
+// xcuhf_omg4.f:2-3 FAE_OMG4
+void fae_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng4, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM4ICR, double* FAE, double* E_AE_OMG4) {
+  report("fae_omg4", neoxc_fae_omg4(*Nchunks, *nebf, *npbf, *ng4, *NAE, *NBE, DAE, DBE,
+                                    DP, GM4ICR, FAE, E_AE_OMG4));
+}
+// xcuhf_omg4.f:512-513 UFP_OMG4
+void ufp_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+               const int64_t* ng4, const int64_t* NAE, const int64_t* NBE,
+               const double* DAE, const double* DBE, const double* DP,
+               const double* GM4ICR, double* FP, double* E_P_OMG4) {
+  report("ufp_omg4", neoxc_ufp_omg4(*Nchunks, *nebf, *npbf, *ng4, *NAE, *NBE, DAE, DBE,
+                                    DP, GM4ICR, FP, E_P_OMG4));
+}
+// xcuhf_omg4.f:1080-1081 OMG4_ICR (GAM_ee.ufm read as in read_GAM_ee)
+void omg4_icr_(const int64_t* Nchunks, const int64_t* ne, const int64_t* np,
+               const int64_t* ngee, const int64_t* ng2, const int64_t* ng4,
+               const double* GAM_2s, double* GAM_4) {
+  std::vector<double> gee;
+  if (!read_ufm("GAM_ee.ufm", *ngee, gee)) {
+    std::fprintf(stderr, "neoxc: omg4_icr: cannot read GAM_ee.ufm\n");
+    return;
+  }
+  report("omg4_icr", neoxc_omg4_icr(*Nchunks, *ne, *np, *ngee, *ng2, *ng4, GAM_2s,
+                                    gee.data(), GAM_4));
+}
+
 }  // extern "C"

@@ -50,6 +50,35 @@ cudaError_t launch_fock_reduce(int ne, int np, int nsub, const double* part,
                                double* fp, double* fp_tmp, double* E,
                                cudaStream_t s);
 
+// ---- open-shell XCUHF contractions (k_spin.cu, xcuhf/xcuhf_omg*.f) ------
+// Rank K = 2 (GM2ICR, optional GM2sICR as Gs), 3 (GM3ICR) or 4 (OMG4_ICR).
+// Flag bits per class (A = alpha-led, B = beta-led), in the order of the
+// reference's flag sets (FAE_OMG2: LAA, LAB; FAE_OMG3: LAA, LAB, LBB;
+// FAE_OMG4: LAAA, LAAB, LBBA, LBBB; UFP_*: the class-A subset of L4A,
+// L3A1B, L2A2B, L1A3B ...).  Outputs, device, overwritten:
+//   fe_out[a][i + ne*j] = sum_{ipjp} DP * (sum over the other electrons of
+//                         class/tensor a = 2*tensor + class),
+//   fp_out[t][ip + np*jp] = sum_{i1,j1} (DA part_A + DB part_B) of tensor t.
+size_t spin_scratch_doubles(int K, int ne, int np);
+// Ranks 3 and 4 stage a bra's ne^K kets in shared memory (up to nebf = 28
+// and 12); rank 2 falls back to global-memory gathers beyond that.
+bool spin_smem_fits(int K, int ne);
+cudaError_t launch_spin_omg(int K, int ne, int np, const double* G, const double* Gs,
+                            const double* DA, const double* DB, const double* DP,
+                            unsigned fa, unsigned fb, double* scratch,
+                            double* fe_out, double* fp_out, cudaStream_t s);
+// GAM_1 / GAM_1s: fe_out[t] = sum_ipjp DP G_t, fp_out[t] = sum W G_t.
+cudaError_t launch_omg1(int ne, int np, const double* G1, const double* G1s,
+                        const double* W, const double* DP, double* fe_out,
+                        double* fp_out, cudaStream_t s);
+// F (+)= scale x (if F), S = scale xs (if S and xs), E = <W,x>, Es = <W,xs>.
+cudaError_t launch_spin_finish(int n, const double* x, const double* xs,
+                               const double* W, double scale, double* F, double* S,
+                               double* E, double* Es, cudaStream_t s);
+// OMG4_ICR: raw calc_GAM_4_integral tensor (ne^8 np^2, index_GAM_4PK2).
+cudaError_t launch_omg4_icr(int ne, int np, const double* gee, const double* g2s,
+                            double* g4, cudaStream_t s);
+
 // ---- gam_4 (gam_4_OMP.f, gam4_DSCF_OMP.f, gam4_ICR_OMP.f) --------------
 constexpr int kGam4MaxNE = 24;   // shared-memory tables: 25*ne^2 doubles
 size_t gam4_partial_doubles(int ne, int np);   // scratch the DSCF path uses

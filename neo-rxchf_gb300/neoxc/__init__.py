@@ -28,6 +28,8 @@ __all__ = [
     "rxchfne_fae_omg2", "rxchfne_fp_omg2", "rxchfne_fbe_omg2",
     "rxchfne_omg2_fused", "xcfock_correction", "index_map",
     "index_gam_2pk", "index_gam_3pk", "index_gam_4pk2", "pack_4d",
+    "fae_omg1", "ufp_omg1", "fae_omg2", "ufp_omg2", "fae_omg3", "ufp_omg3", "fae_omg4",
+    "ufp_omg4", "omg4_icr", "dev_xcuhf_omg", "dev_omg4_icr",
 ]
 
 LIB_PATH = _build.LIB
@@ -60,6 +62,17 @@ def _declare(L):
         "neoxc_gam3_dscf": (I, [i64] * 8 + [d] + [vp] * 20),
         "neoxc_gam2_dscf": (I, [i64] * 8 + [d] + [vp] * 23),
         "neoxc_gam4_icr": (I, [i64] * 6 + [vp] * 3),
+        "neoxc_fae_omg1": (I, [i64] * 3 + [vp] * 8),
+        "neoxc_ufp_omg1": (I, [i64] * 3 + [vp] * 8),
+        "neoxc_fae_omg2": (I, [i64] * 6 + [vp] * 10),
+        "neoxc_ufp_omg2": (I, [i64] * 6 + [vp] * 10),
+        "neoxc_fae_omg3": (I, [i64] * 6 + [vp] * 6),
+        "neoxc_ufp_omg3": (I, [i64] * 6 + [vp] * 6),
+        "neoxc_fae_omg4": (I, [i64] * 6 + [vp] * 6),
+        "neoxc_ufp_omg4": (I, [i64] * 6 + [vp] * 6),
+        "neoxc_omg4_icr": (I, [i64] * 6 + [vp] * 3),
+        "neoxc_dev_xcuhf_omg": (I, [vp] + [i64] * 5 + [vp] * 12),
+        "neoxc_dev_omg4_icr": (I, [vp, i64, i64, vp, vp, vp]),
         "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
         "neoxc_gam4_fock_factored": (I, [i64] * 4 + [vp] * 7),
         "neoxc_xchf_scf": (I, [i64] * 7 + [d] + [vp] * 15 + [i64, i64] + [vp] * 7),
@@ -508,6 +521,107 @@ def rxchfne_omg2_fused(ne, np_, DAE, DBE, DP, gm2):
             fb.reshape(ne, ne, order="F"), float(E[0]))
 
 
+# ---- open-shell XCUHF contractions (xcuhf/xcuhf_omg{1..4}.f) ---------------------
+def fae_omg1(ne, np_, DAE, DP, gam1, gam1s, FAE=None):
+    """xcuhf_omg1.f FAE_OMG1 -> (FAE + dF, SAE1, E_AE_OMG1, S_AE_OMG1)."""
+    g, gs, da, dp = _f64(gam1), _f64(gam1s), _fmat(DAE), _fmat(DP)
+    f = np.zeros(ne * ne) if FAE is None else _fmat(FAE).copy()
+    sm, E, S = np.zeros(ne * ne), np.zeros(1), np.zeros(1)
+    _check(lib().neoxc_fae_omg1(ne, np_, len(g), _p(da), _p(dp), _p(g), _p(gs), _p(f),
+                                _p(sm), _p(E), _p(S)))
+    return f.reshape(ne, ne, order="F"), sm.reshape(ne, ne, order="F"), float(E[0]), float(S[0])
+
+
+def ufp_omg1(ne, np_, DETOT, DP, gam1, gam1s, FP=None):
+    """xcuhf_omg1.f UFP_OMG1 -> (FP + dF, SP1, E_P_OMG1, S_P_OMG1)."""
+    g, gs, dt, dp = _f64(gam1), _f64(gam1s), _fmat(DETOT), _fmat(DP)
+    f = np.zeros(np_ * np_) if FP is None else _fmat(FP).copy()
+    sm, E, S = np.zeros(np_ * np_), np.zeros(1), np.zeros(1)
+    _check(lib().neoxc_ufp_omg1(ne, np_, len(g), _p(dt), _p(dp), _p(g), _p(gs), _p(f),
+                                _p(sm), _p(E), _p(S)))
+    return (f.reshape(np_, np_, order="F"), sm.reshape(np_, np_, order="F"), float(E[0]),
+            float(S[0]))
+
+
+def fae_omg2(ne, np_, NAE, NBE, DAE, DBE, DP, gm2, gm2s, FAE=None, nchunks=1):
+    """xcuhf_omg2.f FAE_OMG2 -> (FAE + dF, SAE2, E_AE_OMG2, S_AE_OMG2)."""
+    g, gs, da, db, dp = _f64(gm2), _f64(gm2s), _fmat(DAE), _fmat(DBE), _fmat(DP)
+    dt = da + db
+    f = np.zeros(ne * ne) if FAE is None else _fmat(FAE).copy()
+    sm, E, S = np.zeros(ne * ne), np.zeros(1), np.zeros(1)
+    _check(lib().neoxc_fae_omg2(nchunks, NAE, NBE, ne, np_, len(g), _p(da), _p(db), _p(dt),
+                                _p(dp), _p(g), _p(gs), _p(f), _p(sm), _p(E), _p(S)))
+    return f.reshape(ne, ne, order="F"), sm.reshape(ne, ne, order="F"), float(E[0]), float(S[0])
+
+
+def ufp_omg2(ne, np_, NAE, NBE, DAE, DBE, DP, gm2, gm2s, FP=None, nchunks=1):
+    """xcuhf_omg2.f UFP_OMG2 -> (FP + dF, SP2, E_P_OMG2, S_P_OMG2)."""
+    g, gs, da, db, dp = _f64(gm2), _f64(gm2s), _fmat(DAE), _fmat(DBE), _fmat(DP)
+    dt = da + db
+    f = np.zeros(np_ * np_) if FP is None else _fmat(FP).copy()
+    sm, E, S = np.zeros(np_ * np_), np.zeros(1), np.zeros(1)
+    _check(lib().neoxc_ufp_omg2(nchunks, ne, np_, len(g), NAE, NBE, _p(da), _p(db), _p(dt),
+                                _p(dp), _p(g), _p(gs), _p(f), _p(sm), _p(E), _p(S)))
+    return (f.reshape(np_, np_, order="F"), sm.reshape(np_, np_, order="F"), float(E[0]),
+            float(S[0]))
+
+
+def _spin34(fn, n_out, ne, np_, NAE, NBE, DAE, DBE, DP, gm, F, nchunks):
+    g, da, db, dp = _f64(gm), _fmat(DAE), _fmat(DBE), _fmat(DP)
+    f = np.zeros(n_out * n_out) if F is None else _fmat(F).copy()
+    E = np.zeros(1)
+    _check(fn(nchunks, ne, np_, len(g), NAE, NBE, _p(da), _p(db), _p(dp), _p(g), _p(f),
+              _p(E)))
+    return f.reshape(n_out, n_out, order="F"), float(E[0])
+
+
+def fae_omg3(ne, np_, NAE, NBE, DAE, DBE, DP, gm3, FAE=None, nchunks=1):
+    """xcuhf_omg3.f FAE_OMG3 -> (FAE + dF, E_AE_OMG3)."""
+    return _spin34(lib().neoxc_fae_omg3, ne, ne, np_, NAE, NBE, DAE, DBE, DP, gm3, FAE, nchunks)
+
+
+def ufp_omg3(ne, np_, NAE, NBE, DAE, DBE, DP, gm3, FP=None, nchunks=1):
+    """xcuhf_omg3.f UFP_OMG3 -> (FP + dF, E_P_OMG3)."""
+    return _spin34(lib().neoxc_ufp_omg3, np_, ne, np_, NAE, NBE, DAE, DBE, DP, gm3, FP, nchunks)
+
+
+def fae_omg4(ne, np_, NAE, NBE, DAE, DBE, DP, gm4, FAE=None, nchunks=1):
+    """xcuhf_omg4.f FAE_OMG4 (gm4 from omg4_icr) -> (FAE + dF, E_AE_OMG4)."""
+    return _spin34(lib().neoxc_fae_omg4, ne, ne, np_, NAE, NBE, DAE, DBE, DP, gm4, FAE, nchunks)
+
+
+def ufp_omg4(ne, np_, NAE, NBE, DAE, DBE, DP, gm4, FP=None, nchunks=1):
+    """xcuhf_omg4.f UFP_OMG4 -> (FP + dF, E_P_OMG4)."""
+    return _spin34(lib().neoxc_ufp_omg4, np_, ne, np_, NAE, NBE, DAE, DBE, DP, gm4, FP, nchunks)
+
+
+def omg4_icr(ne: int, np_: int, gam_2s, gam_ee, nchunks: int = 1) -> np.ndarray:
+    """xcuhf_omg4.f OMG4_ICR -> the raw 5-particle tensor (index_GAM_4PK2)."""
+    g2, ge = _f64(gam_2s), _f64(gam_ee)
+    ng4 = ne ** 8 * np_ ** 2
+    out = np.empty(ng4)
+    _check(lib().neoxc_omg4_icr(nchunks, ne, np_, ne ** 4, ne ** 4 * np_ ** 2, ng4,
+                                _p(g2), _p(ge), _p(out)))
+    return out
+
+
+def dev_xcuhf_omg(stream, K, ne, np_, NAE, NBE, d_G, d_Gs, d_DAE, d_DBE, d_DP,
+                  d_FAE=None, d_FBE=None, d_FP=None, d_SAE=None, d_SBE=None, d_SP=None,
+                  d_E=None):
+    """FAE_OMGk (alpha and beta) and UFP_OMGk of rank K from one pass, on
+    ``stream`` (torch float64 CUDA tensors; None skips an output)."""
+    _check(lib().neoxc_dev_xcuhf_omg(C.c_void_p(stream), K, ne, np_, NAE, NBE,
+                                     _tptr(d_G), _tptr(d_Gs), _tptr(d_DAE), _tptr(d_DBE),
+                                     _tptr(d_DP), _tptr(d_FAE), _tptr(d_FBE), _tptr(d_FP),
+                                     _tptr(d_SAE), _tptr(d_SBE), _tptr(d_SP), _tptr(d_E)))
+
+
+def dev_omg4_icr(stream, ne, np_, d_gee, d_g2s, d_g4):
+    """OMG4_ICR into the device tensor d_g4 (ne**8 np**2 float64) on ``stream``."""
+    _check(lib().neoxc_dev_omg4_icr(C.c_void_p(stream), ne, np_, _tptr(d_gee), _tptr(d_g2s),
+                                    _tptr(d_g4)))
+
+
 def xcfock_correction(ne, np_, E_total, S_total, H_expect, se1, sp1, se2, sp2,
                       focke, fockp):
     """xchf1_fock.f XCfock_correction -> corrected (focke, fockp)."""
@@ -520,7 +634,7 @@ def xcfock_correction(ne, np_, E_total, S_total, H_expect, se1, sp1, se2, sp2,
 
 # ---- device-resident variants (torch CUDA tensors) --------------------------------
 def _tptr(t):
-    return C.c_void_p(t.data_ptr())
+    return C.c_void_p(None if t is None else t.data_ptr())
 
 
 def dev_gam4_dscf(stream, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_focke, d_fockp, d_E):

@@ -562,6 +562,13 @@ static double gam4_x(int64_t ne, int64_t np, const double *G2s,
   return (x1 + x2 + x3 + x4 + x5 + x6) / six;
 }
 
+/* calc_GAM_4_integral for callers outside this file (OMG4_ICR) */
+double orc_gam4_raw(int64_t ne, int64_t np, const double *G2s, const double *Gee,
+                    int64_t ip, int64_t jp, int64_t ie1, int64_t je1, int64_t ie2,
+                    int64_t je2, int64_t ie3, int64_t je3, int64_t ie4, int64_t je4) {
+  return gam4_x(ne, np, G2s, Gee, ip, jp, ie1, je1, ie2, je2, ie3, je3, ie4, je4);
+}
+
 /* gam_4_OMP.f:921-960 i10: argument order (ie1..ie4, je1..je4) */
 static double i10(int64_t ne, int64_t np, const double *G2s, const double *Gee,
                   int64_t ip, int64_t jp, int64_t ie1, int64_t ie2,

@@ -136,6 +136,49 @@ void orc_rxchfne_gam2_ic1(const orc_system *s, double *GM2ICR,
 
 void orc_calc_gam_ee(const orc_system *s, double *GAM_ee);
 
+/* gam_4_OMP.f:964-1192 calc_GAM_4_integral (one raw product element) */
+double orc_gam4_raw(int64_t ne, int64_t np, const double *G2s, const double *Gee,
+                    int64_t ip, int64_t jp, int64_t ie1, int64_t je1, int64_t ie2,
+                    int64_t je2, int64_t ie3, int64_t je3, int64_t ie4, int64_t je4);
+
+/* ---- open-shell XCUHF contractions (spin.c, xcuhf/xcuhf_omg{1..4}.f) ---- */
+void orc_fae_omg1(int64_t ne, int64_t np, const double *DAE, const double *DP,
+                  const double *G1, const double *G1s, double *FAE,
+                  double *SAE1, double *E, double *S);
+void orc_ufp_omg1(int64_t ne, int64_t np, const double *DETOT,
+                  const double *DP, const double *G1, const double *G1s,
+                  double *FP, double *SP1, double *E, double *S);
+void orc_fae_omg2(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                  const double *DAE, const double *DBE, const double *DP,
+                  const double *G2, const double *G2s, double *FAE,
+                  double *SAE2, double *E, double *S);
+void orc_ufp_omg2(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                  const double *DAE, const double *DBE, const double *DP,
+                  const double *G2, const double *G2s, double *FP,
+                  double *SP2, double *E, double *S);
+void orc_fae_omg3(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                  const double *DAE, const double *DBE, const double *DP,
+                  const double *G3, double *FAE, double *E);
+void orc_ufp_omg3(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                  const double *DAE, const double *DBE, const double *DP,
+                  const double *G3, double *FP, double *E);
+void orc_fae_omg4(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                  const double *DAE, const double *DBE, const double *DP,
+                  const double *G4, double *FAE, double *E);
+void orc_ufp_omg4(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                  const double *DAE, const double *DBE, const double *DP,
+                  const double *G4, double *FP, double *E);
+void orc_fae_omg4_direct(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                         const double *DAE, const double *DBE, const double *DP,
+                         const double *G2s, const double *Gee, double *FAE,
+                         double *E);
+void orc_ufp_omg4_direct(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
+                         const double *DAE, const double *DBE, const double *DP,
+                         const double *G2s, const double *Gee, double *FP,
+                         double *E);
+void orc_omg4_icr(int64_t ne, int64_t np, const double *G2s, const double *Gee,
+                  double *G4);
+
 /* gam_4 element assembly (gam_4_OMP.f symm_gam4 / calc_GAM_4_integral),
  * returned already divided by 16 as stored by GAM4_ICR. */
 double orc_gam4_element(int64_t ne, int64_t np, const double *GAM_2s,

@@ -1,7 +1,7 @@
 """ctypes binding for the CPU oracle (test infrastructure only).
 
 The oracle restates the NEO-RXCHF integral and contraction arithmetic on
-the CPU (``prim.c``, ``builders.c``, ``scf.c``).  Only the tests, the smoke check and
+the CPU (``prim.c``, ``builders.c``, ``scf.c``, ``spin.c``).  Only the tests, the smoke check and
 the CPU-baseline leg of ``bench.py`` load it; the product never does.
 """
 from __future__ import annotations
@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libneoxc_oracle.so")
-SOURCES = ["prim.c", "builders.c", "scf.c"]
+SOURCES = ["prim.c", "builders.c", "scf.c", "spin.c"]
 _lock = threading.Lock()
 _lib = None
 
@@ -133,6 +133,18 @@ def lib():
                 "orc_gam1": (None, [vp] * 3),
                 "orc_nuc_rep": (C.c_double, [vp]),
                 "orc_num_threads": (C.c_int, []),
+                "orc_gam4_raw": (d, [i64, i64, vp, vp] + [i64] * 10),
+                "orc_fae_omg1": (None, [i64, i64] + [vp] * 8),
+                "orc_ufp_omg1": (None, [i64, i64] + [vp] * 8),
+                "orc_fae_omg2": (None, [i64] * 4 + [vp] * 9),
+                "orc_ufp_omg2": (None, [i64] * 4 + [vp] * 9),
+                "orc_fae_omg3": (None, [i64] * 4 + [vp] * 6),
+                "orc_ufp_omg3": (None, [i64] * 4 + [vp] * 6),
+                "orc_fae_omg4": (None, [i64] * 4 + [vp] * 6),
+                "orc_ufp_omg4": (None, [i64] * 4 + [vp] * 6),
+                "orc_fae_omg4_direct": (None, [i64] * 4 + [vp] * 7),
+                "orc_ufp_omg4_direct": (None, [i64] * 4 + [vp] * 7),
+                "orc_omg4_icr": (None, [i64, i64, vp, vp, vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)

@@ -43,6 +43,12 @@ def golden_xchf():
 
 
 @pytest.fixture(scope="session")
+def golden_xcuhf():
+    with open(os.path.join(GOLDEN, "xcuhf_example.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
 def golden_spot():
     with open(os.path.join(GOLDEN, "spot_check.json")) as f:
         return json.load(f)

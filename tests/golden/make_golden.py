@@ -10,6 +10,10 @@ Writes, next to this script:
                       the energy components printed in answer/XCHF.log for
                       the initial guess and at convergence, and the
                       orbital energies printed there;
+  xcuhf_example.json  examples/xcuhf: input deck (core-Hamiltonian guess),
+                      converged MOs (answer/FinalC{AE,BE,P}.dat) and the
+                      energy components of answer/XCUHF.log for the initial
+                      guess and at convergence;
   spot_check.json     CS_Integrals/Spot_Check/TEST_G{2,3,4}: the single-
                       primitive inputs (first record block, as SCI.f:114-152
                       reads them) and the MD values printed in each ``out``.
@@ -25,12 +29,17 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def _components(log: str, header: str) -> dict:
+XCHF_KEYS = ("E_NUC", "E_ECORE", "E_PCORE", "E_EP", "E_EE", "E_GAM1", "E_GAM2",
+             "E_GAM3", "E_GAM4", "S_TOTAL", "E_TOTAL")
+XCUHF_KEYS = ("E_NUC", "E_ECORE", "E_PCORE", "E_EP", "E_EE", "E_OMG1", "E_OMG2",
+              "E_OMG3", "E_OMG4", "S_TOTAL", "E_TOTAL")
+
+
+def _components(log: str, header: str, keys=XCHF_KEYS) -> dict:
     i = log.index(header)
     block = log[i:i + 2500]
     out = {}
-    for key in ("E_NUC", "E_ECORE", "E_PCORE", "E_EP", "E_EE", "E_GAM1", "E_GAM2",
-                "E_GAM3", "E_GAM4", "S_TOTAL", "E_TOTAL"):
+    for key in keys:
         m = re.search(r"\b" + key + r"=\s*(-?[0-9.]+)", block)
         out[key] = float(m.group(1))
     return out
@@ -67,6 +76,22 @@ def xchf_example(ref: str) -> dict:
                                     "TIMING SUMMARY")},
         "log_lines": {"initial": "XCHF.log:306-321", "final": "XCHF.log:335-350",
                       "orbital_energies": "XCHF.log:353-384"},
+    }
+
+
+def xcuhf_example(ref: str) -> dict:
+    d = os.path.join(ref, "examples", "xcuhf")
+    log = open(os.path.join(d, "answer", "XCUHF.log")).read()
+    ans = os.path.join(d, "answer")
+    return {
+        "source": "examples/xcuhf (exam_xcuhf.inp, answer/)",
+        "inp": open(os.path.join(d, "exam_xcuhf.inp")).read(),
+        "finalCAE": open(os.path.join(ans, "FinalCAE.dat")).read(),
+        "finalCBE": open(os.path.join(ans, "FinalCBE.dat")).read(),
+        "finalCP": open(os.path.join(ans, "FinalCP.dat")).read(),
+        "initial": _components(log, "INITIAL GUESS ENERGETICS", XCUHF_KEYS),
+        "final": _components(log, "FINAL NEOXCHF ENERGY", XCUHF_KEYS),
+        "log_lines": {"initial": "XCUHF.log:337-352", "final": "XCUHF.log:366-381"},
     }
 
 
@@ -108,6 +133,8 @@ def spot_check(ref: str) -> dict:
 def main(ref: str):
     with open(os.path.join(HERE, "xchf_example.json"), "w") as f:
         json.dump(xchf_example(ref), f, indent=1)
+    with open(os.path.join(HERE, "xcuhf_example.json"), "w") as f:
+        json.dump(xcuhf_example(ref), f, indent=1)
     with open(os.path.join(HERE, "spot_check.json"), "w") as f:
         json.dump(spot_check(ref), f, indent=1)
 
