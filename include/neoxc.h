@@ -434,6 +434,116 @@ int neoxc_dev_xcuhf_omg(void* stream, int64_t K, int64_t ne, int64_t np, int64_t
 int neoxc_dev_omg4_icr(void* stream, int64_t ne, int64_t np, const double* d_gee,
                        const double* d_g2s, double* d_g4);
 
+/* ---- RXCHF-fe / RXCUHF-fe / RXCUHF-ae contractions: rxchf/, rxchfne/ --- */
+/* Same argument lists, packed layouts and semantics as the reference: every
+ * output matrix (Fock and overlap-Fock alike) accumulates (add2fock), the
+ * energies are overwritten.  The in-core tensors are arguments (GM2_1ICR,
+ * GM2_2ICR, GM2sICR from RXCHF_GAM2_IC1; GM3_1ICR, GM3_2ICR from
+ * RXCHF_GAM3_IC1; GM4ICR; GM2ICR, GM2exICR from RXCHFne_GAM2_IC1). */
+/* rxchfne/rxcuhfne_omg2.f:2-130 RXCUHFne_FE_OMG2 (DAbetE unused, as there) */
+int neoxc_rxcuhfne_fe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                           const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                           const double* DBE, const double* DP, const double* GM2ICR,
+                           const double* GM2exICR, double* FAalpE, double* FAbetE,
+                           double* E_AE_OMG2);
+/* rxcuhfne_omg2.f:239-345 RXCUHFne_FP_OMG2 */
+int neoxc_rxcuhfne_fp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                           int64_t NAalpE, int64_t NBE, const double* DAalpE,
+                           const double* DAtotE, const double* DBE, const double* DP,
+                           const double* GM2ICR, const double* GM2exICR, double* FP,
+                           double* E_P_OMG2);
+/* rxcuhfne_omg2.f:445-551 RXCUHFne_FBE_OMG2 */
+int neoxc_rxcuhfne_fbe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                            int64_t NAalpE, int64_t NBE, const double* DAalpE,
+                            const double* DAtotE, const double* DBE, const double* DP,
+                            const double* GM2ICR, const double* GM2exICR, double* FBE,
+                            double* E_BE_OMG2);
+/* rxchf/rxchf_omg2.f:2-114 RXCHF_FAE_OMG2 (F = FAE, S = SAE), :231-334
+ * RXCHF_FP_OMG2 (FP, SP), :449-552 RXCHF_FBE_OMG2 (FBE, SBE) */
+int neoxc_rxchf_fae_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                         const double* DAE, const double* DBE, const double* DP,
+                         const double* GM2_1ICR, const double* GM2_2ICR,
+                         const double* GM2sICR, double* FAE, double* SAE,
+                         double* E_AE_OMG2, double* S_AE_OMG2);
+int neoxc_rxchf_fp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                        const double* DAE, const double* DBE, const double* DP,
+                        const double* GM2_1ICR, const double* GM2_2ICR,
+                        const double* GM2sICR, double* FP, double* SP, double* E_P_OMG2,
+                        double* S_P_OMG2);
+int neoxc_rxchf_fbe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                         const double* DAE, const double* DBE, const double* DP,
+                         const double* GM2_1ICR, const double* GM2_2ICR,
+                         const double* GM2sICR, double* FBE, double* SBE,
+                         double* E_BE_OMG2, double* S_BE_OMG2);
+/* rxchf/rxchf_omg3.f:2-105 RXCHF_FAE_OMG3, :263-366 RXCHF_FP_OMG3,
+ * :486-589 RXCHF_FBE_OMG3 */
+int neoxc_rxchf_fae_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                         const double* DAE, const double* DBE, const double* DP,
+                         const double* GM3_1ICR, const double* GM3_2ICR, double* FAE,
+                         double* E_AE_OMG3);
+int neoxc_rxchf_fp_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                        const double* DAE, const double* DBE, const double* DP,
+                        const double* GM3_1ICR, const double* GM3_2ICR, double* FP,
+                        double* E_P_OMG3);
+int neoxc_rxchf_fbe_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                         const double* DAE, const double* DBE, const double* DP,
+                         const double* GM3_1ICR, const double* GM3_2ICR, double* FBE,
+                         double* E_BE_OMG3);
+/* rxchf/rxchf_omg4.f:2-105 RXCHF_FAE_OMG4, :223-326 RXCHF_FP_OMG4,
+ * :444-547 RXCHF_FBE_OMG4 */
+int neoxc_rxchf_fae_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                         const double* DAE, const double* DBE, const double* DP,
+                         const double* GM4ICR, double* FAE, double* E_AE_OMG4);
+int neoxc_rxchf_fp_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                        const double* DAE, const double* DBE, const double* DP,
+                        const double* GM4ICR, double* FP, double* E_P_OMG4);
+int neoxc_rxchf_fbe_omg4(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4,
+                         const double* DAE, const double* DBE, const double* DP,
+                         const double* GM4ICR, double* FBE, double* E_BE_OMG4);
+/* rxchf/rxcuhf_omg2.f:2-126 RXCUHF_FE_OMG2 (DAbetE unused, as there) */
+int neoxc_rxcuhf_fe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                         const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                         const double* DBE, const double* DP, const double* GM2_1ICR,
+                         const double* GM2_2ICR, const double* GM2sICR, double* FAalpE,
+                         double* FAbetE, double* SAalpE, double* E_AE_OMG2,
+                         double* S_AE_OMG2);
+/* rxcuhf_omg2.f:253-352 RXCUHF_FP_OMG2, :469-576 RXCUHF_FBE_OMG2 */
+int neoxc_rxcuhf_fp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                         int64_t NAalpE, int64_t NBE, const double* DAalpE,
+                         const double* DAtotE, const double* DBE, const double* DP,
+                         const double* GM2_1ICR, const double* GM2_2ICR,
+                         const double* GM2sICR, double* FP, double* SP, double* E_P_OMG2,
+                         double* S_P_OMG2);
+int neoxc_rxcuhf_fbe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                          int64_t NAalpE, int64_t NBE, const double* DAalpE,
+                          const double* DAtotE, const double* DBE, const double* DP,
+                          const double* GM2_1ICR, const double* GM2_2ICR,
+                          const double* GM2sICR, double* FBE, double* SBE,
+                          double* E_BE_OMG2, double* S_BE_OMG2);
+/* rxchf/rxcuhf_omg3.f:2-107 RXCUHF_FE_OMG3, :270-371 RXCUHF_FP_OMG3,
+ * :499-600 RXCUHF_FBE_OMG3 */
+int neoxc_rxcuhf_fe_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                         const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                         const double* DBE, const double* DP, const double* GM3_1ICR,
+                         const double* GM3_2ICR, double* FAalpE, double* FAbetE,
+                         double* E_AE_OMG3);
+int neoxc_rxcuhf_fp_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                         const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                         const double* DBE, const double* DP, const double* GM3_1ICR,
+                         const double* GM3_2ICR, double* FP, double* E_P_OMG3);
+int neoxc_rxcuhf_fbe_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                          const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                          const double* DBE, const double* DP, const double* GM3_1ICR,
+                          const double* GM3_2ICR, double* FBE, double* E_BE_OMG3);
+/* rxchf/rxchf_omg1.f:2-82 RXCHF_FP_OMG1 and :84-165 RXCHF_FBE_OMG1 (GAM_1 /
+ * GAM_1s as arguments; the special electron's density DBE) */
+int neoxc_rxchf_fp_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DBE,
+                        const double* DP, const double* GAM_1, const double* GAM_1s,
+                        double* FP, double* SP, double* E_P_OMG1, double* S_P_OMG1);
+int neoxc_rxchf_fbe_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DBE,
+                         const double* DP, const double* GAM_1, const double* GAM_1s,
+                         double* FBE, double* SBE, double* E_BE_OMG1, double* S_BE_OMG1);
+
 /* ---- on-disk formats: xchf1_independent/GAM_IO.f (host only, no GPU) --- */
 /* Direct-access integral files (*.ufm, GAM_IO.f:1-245): record ia (1-based)
  * holds the FP64 at packed index ia, records `recl` bytes long with the value
@@ -624,7 +734,102 @@ void ufp_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
 void omg4_icr_(const int64_t* Nchunks, const int64_t* ne, const int64_t* np,
                const int64_t* ngee, const int64_t* ng2, const int64_t* ng4,
                const double* GAM_2s, double* GAM_4);
-
+/* rxchf/rxchf_omg{1..4}.f, rxcuhf_omg{2,3}.f and rxchfne/rxcuhfne_omg2.f with
+ * the reference's argument lists; rxchf_fp_omg1_ / rxchf_fbe_omg1_ read
+ * GAM_1.ufm and GAM_1s.ufm from the working directory. */
+void rxcuhfne_fe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                       const int64_t* ng2, const double* DAalpE, const double* DAbetE,
+                       const double* DAtotE, const double* DBE, const double* DP,
+                       const double* GM2ICR, const double* GM2exICR, double* FAalpE,
+                       double* FAbetE, double* E_AE_OMG2);
+void rxcuhfne_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                       const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE,
+                       const double* DAalpE, const double* DAtotE, const double* DBE,
+                       const double* DP, const double* GM2ICR, const double* GM2exICR,
+                       double* FP, double* E_P_OMG2);
+void rxcuhfne_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf,
+                        const int64_t* npbf, const int64_t* ng2, const int64_t* NAalpE,
+                        const int64_t* NBE, const double* DAalpE, const double* DAtotE,
+                        const double* DBE, const double* DP, const double* GM2ICR,
+                        const double* GM2exICR, double* FBE, double* E_BE_OMG2);
+void rxchf_fae_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng2, const double* DAE, const double* DBE,
+                     const double* DP, const double* GM2_1ICR, const double* GM2_2ICR,
+                     const double* GM2sICR, double* FAE, double* SAE, double* E_AE_OMG2,
+                     double* S_AE_OMG2);
+void rxchf_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                    const int64_t* ng2, const double* DAE, const double* DBE,
+                    const double* DP, const double* GM2_1ICR, const double* GM2_2ICR,
+                    const double* GM2sICR, double* FP, double* SP, double* E_P_OMG2,
+                    double* S_P_OMG2);
+void rxchf_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng2, const double* DAE, const double* DBE,
+                     const double* DP, const double* GM2_1ICR, const double* GM2_2ICR,
+                     const double* GM2sICR, double* FBE, double* SBE, double* E_BE_OMG2,
+                     double* S_BE_OMG2);
+void rxchf_fae_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng3, const double* DAE, const double* DBE,
+                     const double* DP, const double* GM3_1ICR, const double* GM3_2ICR,
+                     double* FAE, double* E_AE_OMG3);
+void rxchf_fp_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                    const int64_t* ng3, const double* DAE, const double* DBE,
+                    const double* DP, const double* GM3_1ICR, const double* GM3_2ICR,
+                    double* FP, double* E_P_OMG3);
+void rxchf_fbe_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng3, const double* DAE, const double* DBE,
+                     const double* DP, const double* GM3_1ICR, const double* GM3_2ICR,
+                     double* FBE, double* E_BE_OMG3);
+void rxchf_fae_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng4, const double* DAE, const double* DBE,
+                     const double* DP, const double* GM4ICR, double* FAE,
+                     double* E_AE_OMG4);
+void rxchf_fp_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                    const int64_t* ng4, const double* DAE, const double* DBE,
+                    const double* DP, const double* GM4ICR, double* FP,
+                    double* E_P_OMG4);
+void rxchf_fbe_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng4, const double* DAE, const double* DBE,
+                     const double* DP, const double* GM4ICR, double* FBE,
+                     double* E_BE_OMG4);
+void rxcuhf_fe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng2, const double* DAalpE, const double* DAbetE,
+                     const double* DAtotE, const double* DBE, const double* DP,
+                     const double* GM2_1ICR, const double* GM2_2ICR,
+                     const double* GM2sICR, double* FAalpE, double* FAbetE,
+                     double* SAalpE, double* E_AE_OMG2, double* S_AE_OMG2);
+void rxcuhf_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE,
+                     const double* DAalpE, const double* DAtotE, const double* DBE,
+                     const double* DP, const double* GM2_1ICR, const double* GM2_2ICR,
+                     const double* GM2sICR, double* FP, double* SP, double* E_P_OMG2,
+                     double* S_P_OMG2);
+void rxcuhf_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                      const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE,
+                      const double* DAalpE, const double* DAtotE, const double* DBE,
+                      const double* DP, const double* GM2_1ICR, const double* GM2_2ICR,
+                      const double* GM2sICR, double* FBE, double* SBE,
+                      double* E_BE_OMG2, double* S_BE_OMG2);
+void rxcuhf_fe_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng3, const double* DAalpE, const double* DAbetE,
+                     const double* DAtotE, const double* DBE, const double* DP,
+                     const double* GM3_1ICR, const double* GM3_2ICR, double* FAalpE,
+                     double* FAbetE, double* E_AE_OMG3);
+void rxcuhf_fp_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                     const int64_t* ng3, const double* DAalpE, const double* DAbetE,
+                     const double* DAtotE, const double* DBE, const double* DP,
+                     const double* GM3_1ICR, const double* GM3_2ICR, double* FP,
+                     double* E_P_OMG3);
+void rxcuhf_fbe_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf,
+                      const int64_t* ng3, const double* DAalpE, const double* DAbetE,
+                      const double* DAtotE, const double* DBE, const double* DP,
+                      const double* GM3_1ICR, const double* GM3_2ICR, double* FBE,
+                      double* E_BE_OMG3);
+void rxchf_fp_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+                    const double* DBE, const double* DP, double* FP, double* SP,
+                    double* E_P_OMG1, double* S_P_OMG1);
+void rxchf_fbe_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+                     const double* DBE, const double* DP, double* FBE, double* SBE,
+                     double* E_BE_OMG1, double* S_BE_OMG1);
 #ifdef __cplusplus
 }
 #endif

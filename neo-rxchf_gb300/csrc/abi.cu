@@ -1719,3 +1719,211 @@ int neoxc_omg4_icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ngee, int64_
 }
 
 }  // extern "C"
+
+// ---- RXCHF-fe / RXCUHF-fe / RXCUHF-ae contractions (rxchf/, rxchfne/) -------
+namespace {
+
+// One reference routine on host arrays: tensors of ng elements, densities of
+// ne x ne (P: np x np), outputs F0..F2 (ne x ne, or np x np for the proton
+// routines) accumulated, energies E0 / E1 overwritten.
+int rx_host(RxRoutine r, int K, bool proton, int nf, int nen, int64_t ne, int64_t np,
+            int64_t ng, const double* T1, const double* T2, const double* Ts,
+            const double* A, const double* Abet, const double* Atot, const double* B,
+            const double* P, double* F0, double* F1, double* F2, double* E0,
+            double* E1) {
+  RC(need(ne >= 1 && np >= 1, "nebf, npbf >= 1"));
+  int64_t want = np * np;
+  for (int m = 0; m < 2 * K; m++) want *= ne;
+  RC(need(ng == want, "tensor size == nebf**(2k) npbf**2"));
+  RC(need(T1 && B && P && F0 && E0 && (nf < 2 || F1) && (nf < 3 || F2) && (nen < 2 || E1),
+          "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  const int64_t n2 = ne * ne, p2 = np * np, nout = proton ? p2 : n2;
+  DBuf d1, d2, ds, da, dab, dat, db, dp, scr, f0, f1, f2, dE;
+  RC(upload(d1, T1, sizeof(double) * ng, s));
+  if (T2) RC(upload(d2, T2, sizeof(double) * ng, s));
+  if (Ts) RC(upload(ds, Ts, sizeof(double) * ng, s));
+  if (A) RC(upload(da, A, sizeof(double) * n2, s));
+  if (Abet) RC(upload(dab, Abet, sizeof(double) * n2, s));
+  if (Atot) RC(upload(dat, Atot, sizeof(double) * n2, s));
+  RC(upload(db, B, sizeof(double) * n2, s));
+  RC(upload(dp, P, sizeof(double) * p2, s));
+  RC(dalloc(scr, sizeof(double) * rx_scratch_doubles((int)ne, (int)np), s));
+  RC(dalloc(f0, sizeof(double) * 3 * nout, s));
+  RC(dalloc(dE, sizeof(double) * 2, s));
+  CU(cudaMemsetAsync(f0.p, 0, sizeof(double) * 3 * nout, s));
+  double* f = f0.as<double>();
+  CU(launch_rx(r, (int)ne, (int)np, d1.as<double>(), T2 ? d2.as<double>() : nullptr,
+               Ts ? ds.as<double>() : nullptr, A ? da.as<double>() : nullptr,
+               Abet ? dab.as<double>() : nullptr, Atot ? dat.as<double>() : nullptr,
+               db.as<double>(), dp.as<double>(), scr.as<double>(), f, f + nout,
+               f + 2 * nout, dE.as<double>(), s));
+  double e2[2];
+  CU(cudaMemcpyAsync(e2, dE.p, sizeof e2, cudaMemcpyDeviceToHost, s));
+  RC(accumulate_back(F0, f, nout, s));
+  if (nf > 1) RC(accumulate_back(F1, f + nout, nout, s));
+  if (nf > 2) RC(accumulate_back(F2, f + 2 * nout, nout, s));
+  *E0 = e2[0];
+  if (nen > 1) *E1 = e2[1];
+  return finish(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+// rxchfne/rxcuhfne_omg2.f:2-130 RXCUHFne_FE_OMG2
+int neoxc_rxcuhfne_fe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                           const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                           const double* DBE, const double* DP, const double* GM2ICR,
+                           const double* GM2exICR, double* FAalpE, double* FAbetE,
+                           double* E_AE_OMG2) {
+  (void)DAbetE;
+  RC(need(Nchunks >= 1 && GM2exICR && DAalpE && DAtotE, "Nchunks, pointers"));
+  return rx_host(RxRoutine::CuhfneFE2, 2, false, 2, 1, nebf, npbf, ng2, GM2ICR, GM2exICR,
+                 nullptr, DAalpE, nullptr, DAtotE, DBE, DP, FAalpE, FAbetE, nullptr,
+                 E_AE_OMG2, nullptr);
+}
+// rxcuhfne_omg2.f:239-345 RXCUHFne_FP_OMG2
+int neoxc_rxcuhfne_fp_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                           int64_t NAalpE, int64_t NBE, const double* DAalpE,
+                           const double* DAtotE, const double* DBE, const double* DP,
+                           const double* GM2ICR, const double* GM2exICR, double* FP,
+                           double* E_P_OMG2) {
+  (void)NAalpE; (void)NBE;
+  RC(need(Nchunks >= 1 && GM2exICR && DAalpE && DAtotE, "Nchunks, pointers"));
+  return rx_host(RxRoutine::CuhfneFP2, 2, true, 1, 1, nebf, npbf, ng2, GM2ICR, GM2exICR,
+                 nullptr, DAalpE, nullptr, DAtotE, DBE, DP, FP, nullptr, nullptr, E_P_OMG2,
+                 nullptr);
+}
+// rxcuhfne_omg2.f:445-551 RXCUHFne_FBE_OMG2
+int neoxc_rxcuhfne_fbe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                            int64_t NAalpE, int64_t NBE, const double* DAalpE,
+                            const double* DAtotE, const double* DBE, const double* DP,
+                            const double* GM2ICR, const double* GM2exICR, double* FBE,
+                            double* E_BE_OMG2) {
+  (void)NAalpE; (void)NBE;
+  RC(need(Nchunks >= 1 && GM2exICR && DAalpE && DAtotE, "Nchunks, pointers"));
+  return rx_host(RxRoutine::CuhfneFBE2, 2, false, 1, 1, nebf, npbf, ng2, GM2ICR, GM2exICR,
+                 nullptr, DAalpE, nullptr, DAtotE, DBE, DP, FBE, nullptr, nullptr,
+                 E_BE_OMG2, nullptr);
+}
+
+// rxchf/rxchf_omg2.f:2-114 RXCHF_FAE_OMG2, :231-334 RXCHF_FP_OMG2,
+// :449-552 RXCHF_FBE_OMG2
+#define RXCHF_OMG2(name, routine, proton)                                              \
+  int name(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2, const double* DAE, \
+           const double* DBE, const double* DP, const double* GM2_1ICR,                \
+           const double* GM2_2ICR, const double* GM2sICR, double* F, double* S,        \
+           double* E, double* Es) {                                                    \
+    RC(need(Nchunks >= 1 && DAE && GM2_2ICR && GM2sICR, "Nchunks, pointers"));         \
+    return rx_host(routine, 2, proton, 2, 2, nebf, npbf, ng2, GM2_1ICR, GM2_2ICR,      \
+                   GM2sICR, DAE, nullptr, nullptr, DBE, DP, F, S, nullptr, E, Es);     \
+  }
+RXCHF_OMG2(neoxc_rxchf_fae_omg2, RxRoutine::FAE2, false)
+RXCHF_OMG2(neoxc_rxchf_fp_omg2, RxRoutine::FP2, true)
+RXCHF_OMG2(neoxc_rxchf_fbe_omg2, RxRoutine::FBE2, false)
+#undef RXCHF_OMG2
+
+// rxchf_omg3.f:2-105 RXCHF_FAE_OMG3, :263-366 RXCHF_FP_OMG3, :486-589 FBE
+#define RXCHF_OMG3(name, routine, proton)                                              \
+  int name(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3, const double* DAE, \
+           const double* DBE, const double* DP, const double* GM3_1ICR,                \
+           const double* GM3_2ICR, double* F, double* E) {                             \
+    RC(need(Nchunks >= 1 && DAE && GM3_2ICR, "Nchunks, pointers"));                    \
+    return rx_host(routine, 3, proton, 1, 1, nebf, npbf, ng3, GM3_1ICR, GM3_2ICR,      \
+                   nullptr, DAE, nullptr, nullptr, DBE, DP, F, nullptr, nullptr, E,    \
+                   nullptr);                                                           \
+  }
+RXCHF_OMG3(neoxc_rxchf_fae_omg3, RxRoutine::FAE3, false)
+RXCHF_OMG3(neoxc_rxchf_fp_omg3, RxRoutine::FP3, true)
+RXCHF_OMG3(neoxc_rxchf_fbe_omg3, RxRoutine::FBE3, false)
+#undef RXCHF_OMG3
+
+// rxchf_omg4.f:2-105 RXCHF_FAE_OMG4, :223-326 RXCHF_FP_OMG4, :444-547 FBE
+#define RXCHF_OMG4(name, routine, proton)                                              \
+  int name(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng4, const double* DAE, \
+           const double* DBE, const double* DP, const double* GM4ICR, double* F,       \
+           double* E) {                                                                \
+    RC(need(Nchunks >= 1 && DAE, "Nchunks, pointers"));                                \
+    return rx_host(routine, 4, proton, 1, 1, nebf, npbf, ng4, GM4ICR, nullptr, nullptr, \
+                   DAE, nullptr, nullptr, DBE, DP, F, nullptr, nullptr, E, nullptr);   \
+  }
+RXCHF_OMG4(neoxc_rxchf_fae_omg4, RxRoutine::FAE4, false)
+RXCHF_OMG4(neoxc_rxchf_fp_omg4, RxRoutine::FP4, true)
+RXCHF_OMG4(neoxc_rxchf_fbe_omg4, RxRoutine::FBE4, false)
+#undef RXCHF_OMG4
+
+// rxchf/rxcuhf_omg2.f:2-126 RXCUHF_FE_OMG2
+int neoxc_rxcuhf_fe_omg2(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2,
+                         const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                         const double* DBE, const double* DP, const double* GM2_1ICR,
+                         const double* GM2_2ICR, const double* GM2sICR, double* FAalpE,
+                         double* FAbetE, double* SAalpE, double* E_AE_OMG2,
+                         double* S_AE_OMG2) {
+  (void)DAbetE;
+  RC(need(Nchunks >= 1 && DAalpE && DAtotE && GM2_2ICR && GM2sICR, "Nchunks, pointers"));
+  return rx_host(RxRoutine::CuFE2, 2, false, 3, 2, nebf, npbf, ng2, GM2_1ICR, GM2_2ICR,
+                 GM2sICR, DAalpE, nullptr, DAtotE, DBE, DP, FAalpE, FAbetE, SAalpE,
+                 E_AE_OMG2, S_AE_OMG2);
+}
+// rxcuhf_omg2.f:253-352 RXCUHF_FP_OMG2 and :469-576 RXCUHF_FBE_OMG2
+#define RXCUHF_OMG2(name, routine, proton)                                             \
+  int name(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng2, int64_t NAalpE,   \
+           int64_t NBE, const double* DAalpE, const double* DAtotE, const double* DBE, \
+           const double* DP, const double* GM2_1ICR, const double* GM2_2ICR,           \
+           const double* GM2sICR, double* F, double* S, double* E, double* Es) {       \
+    (void)NAalpE; (void)NBE;                                                           \
+    RC(need(Nchunks >= 1 && DAalpE && DAtotE && GM2_2ICR && GM2sICR,                   \
+            "Nchunks, pointers"));                                                     \
+    return rx_host(routine, 2, proton, 2, 2, nebf, npbf, ng2, GM2_1ICR, GM2_2ICR,      \
+                   GM2sICR, DAalpE, nullptr, DAtotE, DBE, DP, F, S, nullptr, E, Es);   \
+  }
+RXCUHF_OMG2(neoxc_rxcuhf_fp_omg2, RxRoutine::CuFP2, true)
+RXCUHF_OMG2(neoxc_rxcuhf_fbe_omg2, RxRoutine::CuFBE2, false)
+#undef RXCUHF_OMG2
+
+// rxchf/rxcuhf_omg3.f:2-107 RXCUHF_FE_OMG3
+int neoxc_rxcuhf_fe_omg3(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,
+                         const double* DAalpE, const double* DAbetE, const double* DAtotE,
+                         const double* DBE, const double* DP, const double* GM3_1ICR,
+                         const double* GM3_2ICR, double* FAalpE, double* FAbetE,
+                         double* E_AE_OMG3) {
+  RC(need(Nchunks >= 1 && DAalpE && DAbetE && DAtotE && GM3_2ICR, "Nchunks, pointers"));
+  return rx_host(RxRoutine::CuFE3, 3, false, 2, 1, nebf, npbf, ng3, GM3_1ICR, GM3_2ICR,
+                 nullptr, DAalpE, DAbetE, DAtotE, DBE, DP, FAalpE, FAbetE, nullptr,
+                 E_AE_OMG3, nullptr);
+}
+// rxcuhf_omg3.f:270-371 RXCUHF_FP_OMG3 and :499-600 RXCUHF_FBE_OMG3
+#define RXCUHF_OMG3(name, routine, proton)                                             \
+  int name(int64_t Nchunks, int64_t nebf, int64_t npbf, int64_t ng3,                   \
+           const double* DAalpE, const double* DAbetE, const double* DAtotE,           \
+           const double* DBE, const double* DP, const double* GM3_1ICR,                \
+           const double* GM3_2ICR, double* F, double* E) {                             \
+    RC(need(Nchunks >= 1 && DAalpE && DAbetE && DAtotE && GM3_2ICR,                    \
+            "Nchunks, pointers"));                                                     \
+    return rx_host(routine, 3, proton, 1, 1, nebf, npbf, ng3, GM3_1ICR, GM3_2ICR,      \
+                   nullptr, DAalpE, DAbetE, DAtotE, DBE, DP, F, nullptr, nullptr, E,   \
+                   nullptr);                                                           \
+  }
+RXCUHF_OMG3(neoxc_rxcuhf_fp_omg3, RxRoutine::CuFP3, true)
+RXCUHF_OMG3(neoxc_rxcuhf_fbe_omg3, RxRoutine::CuFBE3, false)
+#undef RXCUHF_OMG3
+
+// rxchf/rxchf_omg1.f:2-82 RXCHF_FP_OMG1 (UFP_OMG1 with the special electron's
+// density) and :84-165 RXCHF_FBE_OMG1 (FAE_OMG1 with DBE)
+int neoxc_rxchf_fp_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DBE,
+                        const double* DP, const double* GAM_1, const double* GAM_1s,
+                        double* FP, double* SP, double* E_P_OMG1, double* S_P_OMG1) {
+  return omg1_host(nebf, npbf, ng1, DBE, DP, GAM_1, GAM_1s, true, FP, SP, E_P_OMG1,
+                   S_P_OMG1);
+}
+int neoxc_rxchf_fbe_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* DBE,
+                         const double* DP, const double* GAM_1, const double* GAM_1s,
+                         double* FBE, double* SBE, double* E_BE_OMG1, double* S_BE_OMG1) {
+  return omg1_host(nebf, npbf, ng1, DBE, DP, GAM_1, GAM_1s, false, FBE, SBE, E_BE_OMG1,
+                   S_BE_OMG1);
+}
+
+}  // extern "C"

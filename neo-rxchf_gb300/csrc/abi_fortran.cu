@@ -424,4 +424,85 @@ void omg4_icr_(const int64_t* Nchunks, const int64_t* ne, const int64_t* np,
                                     gee.data(), GAM_4));
 }
 
+// ---- rxchf/rxchf_omg{1..4}.f, rxcuhf_omg{2,3}.f, rxchfne/rxcuhfne_omg2.f -----
+// Same names and argument lists as the reference subroutines.
+void rxcuhfne_fe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const double* DAalpE, const double* DAbetE, const double* DAtotE, const double* DBE, const double* DP, const double* GM2ICR, const double* GM2exICR, double* FAalpE, double* FAbetE, double* E_AE_OMG2) {
+  report("rxcuhfne_fe_omg2", neoxc_rxcuhfne_fe_omg2(*Nchunks, *nebf, *npbf, *ng2, DAalpE, DAbetE, DAtotE, DBE, DP, GM2ICR, GM2exICR, FAalpE, FAbetE, E_AE_OMG2));
+}
+void rxcuhfne_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE, const double* DAalpE, const double* DAtotE, const double* DBE, const double* DP, const double* GM2ICR, const double* GM2exICR, double* FP, double* E_P_OMG2) {
+  report("rxcuhfne_fp_omg2", neoxc_rxcuhfne_fp_omg2(*Nchunks, *nebf, *npbf, *ng2, *NAalpE, *NBE, DAalpE, DAtotE, DBE, DP, GM2ICR, GM2exICR, FP, E_P_OMG2));
+}
+void rxcuhfne_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE, const double* DAalpE, const double* DAtotE, const double* DBE, const double* DP, const double* GM2ICR, const double* GM2exICR, double* FBE, double* E_BE_OMG2) {
+  report("rxcuhfne_fbe_omg2", neoxc_rxcuhfne_fbe_omg2(*Nchunks, *nebf, *npbf, *ng2, *NAalpE, *NBE, DAalpE, DAtotE, DBE, DP, GM2ICR, GM2exICR, FBE, E_BE_OMG2));
+}
+void rxchf_fae_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const double* DAE, const double* DBE, const double* DP, const double* GM2_1ICR, const double* GM2_2ICR, const double* GM2sICR, double* FAE, double* SAE, double* E_AE_OMG2, double* S_AE_OMG2) {
+  report("rxchf_fae_omg2", neoxc_rxchf_fae_omg2(*Nchunks, *nebf, *npbf, *ng2, DAE, DBE, DP, GM2_1ICR, GM2_2ICR, GM2sICR, FAE, SAE, E_AE_OMG2, S_AE_OMG2));
+}
+void rxchf_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const double* DAE, const double* DBE, const double* DP, const double* GM2_1ICR, const double* GM2_2ICR, const double* GM2sICR, double* FP, double* SP, double* E_P_OMG2, double* S_P_OMG2) {
+  report("rxchf_fp_omg2", neoxc_rxchf_fp_omg2(*Nchunks, *nebf, *npbf, *ng2, DAE, DBE, DP, GM2_1ICR, GM2_2ICR, GM2sICR, FP, SP, E_P_OMG2, S_P_OMG2));
+}
+void rxchf_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const double* DAE, const double* DBE, const double* DP, const double* GM2_1ICR, const double* GM2_2ICR, const double* GM2sICR, double* FBE, double* SBE, double* E_BE_OMG2, double* S_BE_OMG2) {
+  report("rxchf_fbe_omg2", neoxc_rxchf_fbe_omg2(*Nchunks, *nebf, *npbf, *ng2, DAE, DBE, DP, GM2_1ICR, GM2_2ICR, GM2sICR, FBE, SBE, E_BE_OMG2, S_BE_OMG2));
+}
+void rxchf_fae_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng3, const double* DAE, const double* DBE, const double* DP, const double* GM3_1ICR, const double* GM3_2ICR, double* FAE, double* E_AE_OMG3) {
+  report("rxchf_fae_omg3", neoxc_rxchf_fae_omg3(*Nchunks, *nebf, *npbf, *ng3, DAE, DBE, DP, GM3_1ICR, GM3_2ICR, FAE, E_AE_OMG3));
+}
+void rxchf_fp_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng3, const double* DAE, const double* DBE, const double* DP, const double* GM3_1ICR, const double* GM3_2ICR, double* FP, double* E_P_OMG3) {
+  report("rxchf_fp_omg3", neoxc_rxchf_fp_omg3(*Nchunks, *nebf, *npbf, *ng3, DAE, DBE, DP, GM3_1ICR, GM3_2ICR, FP, E_P_OMG3));
+}
+void rxchf_fbe_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng3, const double* DAE, const double* DBE, const double* DP, const double* GM3_1ICR, const double* GM3_2ICR, double* FBE, double* E_BE_OMG3) {
+  report("rxchf_fbe_omg3", neoxc_rxchf_fbe_omg3(*Nchunks, *nebf, *npbf, *ng3, DAE, DBE, DP, GM3_1ICR, GM3_2ICR, FBE, E_BE_OMG3));
+}
+void rxchf_fae_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng4, const double* DAE, const double* DBE, const double* DP, const double* GM4ICR, double* FAE, double* E_AE_OMG4) {
+  report("rxchf_fae_omg4", neoxc_rxchf_fae_omg4(*Nchunks, *nebf, *npbf, *ng4, DAE, DBE, DP, GM4ICR, FAE, E_AE_OMG4));
+}
+void rxchf_fp_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng4, const double* DAE, const double* DBE, const double* DP, const double* GM4ICR, double* FP, double* E_P_OMG4) {
+  report("rxchf_fp_omg4", neoxc_rxchf_fp_omg4(*Nchunks, *nebf, *npbf, *ng4, DAE, DBE, DP, GM4ICR, FP, E_P_OMG4));
+}
+void rxchf_fbe_omg4_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng4, const double* DAE, const double* DBE, const double* DP, const double* GM4ICR, double* FBE, double* E_BE_OMG4) {
+  report("rxchf_fbe_omg4", neoxc_rxchf_fbe_omg4(*Nchunks, *nebf, *npbf, *ng4, DAE, DBE, DP, GM4ICR, FBE, E_BE_OMG4));
+}
+void rxcuhf_fe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const double* DAalpE, const double* DAbetE, const double* DAtotE, const double* DBE, const double* DP, const double* GM2_1ICR, const double* GM2_2ICR, const double* GM2sICR, double* FAalpE, double* FAbetE, double* SAalpE, double* E_AE_OMG2, double* S_AE_OMG2) {
+  report("rxcuhf_fe_omg2", neoxc_rxcuhf_fe_omg2(*Nchunks, *nebf, *npbf, *ng2, DAalpE, DAbetE, DAtotE, DBE, DP, GM2_1ICR, GM2_2ICR, GM2sICR, FAalpE, FAbetE, SAalpE, E_AE_OMG2, S_AE_OMG2));
+}
+void rxcuhf_fp_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE, const double* DAalpE, const double* DAtotE, const double* DBE, const double* DP, const double* GM2_1ICR, const double* GM2_2ICR, const double* GM2sICR, double* FP, double* SP, double* E_P_OMG2, double* S_P_OMG2) {
+  report("rxcuhf_fp_omg2", neoxc_rxcuhf_fp_omg2(*Nchunks, *nebf, *npbf, *ng2, *NAalpE, *NBE, DAalpE, DAtotE, DBE, DP, GM2_1ICR, GM2_2ICR, GM2sICR, FP, SP, E_P_OMG2, S_P_OMG2));
+}
+void rxcuhf_fbe_omg2_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng2, const int64_t* NAalpE, const int64_t* NBE, const double* DAalpE, const double* DAtotE, const double* DBE, const double* DP, const double* GM2_1ICR, const double* GM2_2ICR, const double* GM2sICR, double* FBE, double* SBE, double* E_BE_OMG2, double* S_BE_OMG2) {
+  report("rxcuhf_fbe_omg2", neoxc_rxcuhf_fbe_omg2(*Nchunks, *nebf, *npbf, *ng2, *NAalpE, *NBE, DAalpE, DAtotE, DBE, DP, GM2_1ICR, GM2_2ICR, GM2sICR, FBE, SBE, E_BE_OMG2, S_BE_OMG2));
+}
+void rxcuhf_fe_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng3, const double* DAalpE, const double* DAbetE, const double* DAtotE, const double* DBE, const double* DP, const double* GM3_1ICR, const double* GM3_2ICR, double* FAalpE, double* FAbetE, double* E_AE_OMG3) {
+  report("rxcuhf_fe_omg3", neoxc_rxcuhf_fe_omg3(*Nchunks, *nebf, *npbf, *ng3, DAalpE, DAbetE, DAtotE, DBE, DP, GM3_1ICR, GM3_2ICR, FAalpE, FAbetE, E_AE_OMG3));
+}
+void rxcuhf_fp_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng3, const double* DAalpE, const double* DAbetE, const double* DAtotE, const double* DBE, const double* DP, const double* GM3_1ICR, const double* GM3_2ICR, double* FP, double* E_P_OMG3) {
+  report("rxcuhf_fp_omg3", neoxc_rxcuhf_fp_omg3(*Nchunks, *nebf, *npbf, *ng3, DAalpE, DAbetE, DAtotE, DBE, DP, GM3_1ICR, GM3_2ICR, FP, E_P_OMG3));
+}
+void rxcuhf_fbe_omg3_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npbf, const int64_t* ng3, const double* DAalpE, const double* DAbetE, const double* DAtotE, const double* DBE, const double* DP, const double* GM3_1ICR, const double* GM3_2ICR, double* FBE, double* E_BE_OMG3) {
+  report("rxcuhf_fbe_omg3", neoxc_rxcuhf_fbe_omg3(*Nchunks, *nebf, *npbf, *ng3, DAalpE, DAbetE, DAtotE, DBE, DP, GM3_1ICR, GM3_2ICR, FBE, E_BE_OMG3));
+}
+// rxchf/rxchf_omg1.f:2-82 RXCHF_FP_OMG1, :84-165 RXCHF_FBE_OMG1 (GAM_1.ufm,
+// GAM_1s.ufm read as in :20-23)
+void rxchf_fp_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+                    const double* DBE, const double* DP, double* FP, double* SP,
+                    double* E_P_OMG1, double* S_P_OMG1) {
+  std::vector<double> g1, g1s;
+  if (!read_ufm("GAM_1.ufm", *ng1, g1) || !read_ufm("GAM_1s.ufm", *ng1, g1s)) {
+    std::fprintf(stderr, "neoxc: rxchf_fp_omg1: cannot read GAM_1.ufm/GAM_1s.ufm\n");
+    return;
+  }
+  report("rxchf_fp_omg1", neoxc_rxchf_fp_omg1(*nebf, *npbf, *ng1, DBE, DP, g1.data(),
+                                              g1s.data(), FP, SP, E_P_OMG1, S_P_OMG1));
+}
+void rxchf_fbe_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
+                     const double* DBE, const double* DP, double* FBE, double* SBE,
+                     double* E_BE_OMG1, double* S_BE_OMG1) {
+  std::vector<double> g1, g1s;
+  if (!read_ufm("GAM_1.ufm", *ng1, g1) || !read_ufm("GAM_1s.ufm", *ng1, g1s)) {
+    std::fprintf(stderr, "neoxc: rxchf_fbe_omg1: cannot read GAM_1.ufm/GAM_1s.ufm\n");
+    return;
+  }
+  report("rxchf_fbe_omg1", neoxc_rxchf_fbe_omg1(*nebf, *npbf, *ng1, DBE, DP, g1.data(),
+                                                g1s.data(), FBE, SBE, E_BE_OMG1, S_BE_OMG1));
+}
+
 }  // extern "C"

@@ -79,6 +79,24 @@ cudaError_t launch_spin_finish(int n, const double* x, const double* xs,
 cudaError_t launch_omg4_icr(int ne, int np, const double* gee, const double* g2s,
                             double* g4, cudaStream_t s);
 
+// ---- RXCHF / RXCUHF special-electron contractions (k_rx.cu) -------------
+// One routine of rxchf_omg{2,3,4}.f, rxcuhf_omg{2,3}.f or rxcuhfne_omg2.f.
+// Tensors T1/T2/Ts and densities A (alpha / DAE), Abet, Atot, B (DBE), P as
+// the routine needs them; F0..F2 (device, accumulate) are the routine's
+// output matrices in the reference's argument order, E[0..1] its energies
+// (overwritten).
+enum class RxRoutine {
+  CuhfneFE2, CuhfneFP2, CuhfneFBE2,          // RXCUHFne_FE/FP/FBE_OMG2
+  FAE2, FP2, FBE2, FAE3, FP3, FBE3, FAE4, FP4, FBE4,   // RXCHF_FAE/FP/FBE_OMGk
+  CuFE2, CuFP2, CuFBE2, CuFE3, CuFP3, CuFBE3  // RXCUHF_FE/FP/FBE_OMGk
+};
+size_t rx_scratch_doubles(int ne, int np);
+cudaError_t launch_rx(RxRoutine r, int ne, int np, const double* T1, const double* T2,
+                      const double* Ts, const double* A, const double* Abet,
+                      const double* Atot, const double* B, const double* P,
+                      double* scratch, double* F0, double* F1, double* F2, double* E,
+                      cudaStream_t s);
+
 // ---- gam_4 (gam_4_OMP.f, gam4_DSCF_OMP.f, gam4_ICR_OMP.f) --------------
 constexpr int kGam4MaxNE = 24;   // shared-memory tables: 25*ne^2 doubles
 size_t gam4_partial_doubles(int ne, int np);   // scratch the DSCF path uses

@@ -30,6 +30,7 @@ __all__ = [
     "index_gam_2pk", "index_gam_3pk", "index_gam_4pk2", "pack_4d",
     "fae_omg1", "ufp_omg1", "fae_omg2", "ufp_omg2", "fae_omg3", "ufp_omg3", "fae_omg4",
     "ufp_omg4", "omg4_icr", "dev_xcuhf_omg", "dev_omg4_icr",
+    "rxcuhfne_omg2", "rxchf_omg", "rxcuhf_omg", "rxchf_omg1",
 ]
 
 LIB_PATH = _build.LIB
@@ -71,6 +72,26 @@ def _declare(L):
         "neoxc_fae_omg4": (I, [i64] * 6 + [vp] * 6),
         "neoxc_ufp_omg4": (I, [i64] * 6 + [vp] * 6),
         "neoxc_omg4_icr": (I, [i64] * 6 + [vp] * 3),
+        "neoxc_rxcuhfne_fe_omg2": (I, [i64] * 4 + [vp] * 10),
+        "neoxc_rxcuhfne_fp_omg2": (I, [i64] * 6 + [vp] * 8),
+        "neoxc_rxcuhfne_fbe_omg2": (I, [i64] * 6 + [vp] * 8),
+        "neoxc_rxchf_fae_omg2": (I, [i64] * 4 + [vp] * 10),
+        "neoxc_rxchf_fp_omg2": (I, [i64] * 4 + [vp] * 10),
+        "neoxc_rxchf_fbe_omg2": (I, [i64] * 4 + [vp] * 10),
+        "neoxc_rxchf_fae_omg3": (I, [i64] * 4 + [vp] * 7),
+        "neoxc_rxchf_fp_omg3": (I, [i64] * 4 + [vp] * 7),
+        "neoxc_rxchf_fbe_omg3": (I, [i64] * 4 + [vp] * 7),
+        "neoxc_rxchf_fae_omg4": (I, [i64] * 4 + [vp] * 6),
+        "neoxc_rxchf_fp_omg4": (I, [i64] * 4 + [vp] * 6),
+        "neoxc_rxchf_fbe_omg4": (I, [i64] * 4 + [vp] * 6),
+        "neoxc_rxcuhf_fe_omg2": (I, [i64] * 4 + [vp] * 13),
+        "neoxc_rxcuhf_fp_omg2": (I, [i64] * 6 + [vp] * 11),
+        "neoxc_rxcuhf_fbe_omg2": (I, [i64] * 6 + [vp] * 11),
+        "neoxc_rxcuhf_fe_omg3": (I, [i64] * 4 + [vp] * 10),
+        "neoxc_rxcuhf_fp_omg3": (I, [i64] * 4 + [vp] * 9),
+        "neoxc_rxcuhf_fbe_omg3": (I, [i64] * 4 + [vp] * 9),
+        "neoxc_rxchf_fp_omg1": (I, [i64] * 3 + [vp] * 8),
+        "neoxc_rxchf_fbe_omg1": (I, [i64] * 3 + [vp] * 8),
         "neoxc_dev_xcuhf_omg": (I, [vp] + [i64] * 5 + [vp] * 12),
         "neoxc_dev_omg4_icr": (I, [vp, i64, i64, vp, vp, vp]),
         "neoxc_gam4_dscf": (I, [i64] * 6 + [vp] * 7),
@@ -614,6 +635,80 @@ def dev_xcuhf_omg(stream, K, ne, np_, NAE, NBE, d_G, d_Gs, d_DAE, d_DBE, d_DP,
                                      _tptr(d_G), _tptr(d_Gs), _tptr(d_DAE), _tptr(d_DBE),
                                      _tptr(d_DP), _tptr(d_FAE), _tptr(d_FBE), _tptr(d_FP),
                                      _tptr(d_SAE), _tptr(d_SBE), _tptr(d_SP), _tptr(d_E)))
+
+
+# ---- special-electron contractions (rxchf/, rxchfne/) -----------------------------
+def _rx_call(fn, lead, ne, np_, dens, tensors, outs, nen):
+    """Call one RXCHF / RXCUHF routine: lead = the integer arguments before the
+    arrays, outs = list of (n, initial matrix or None); returns
+    (*matrices, *energies)."""
+    arrs = [_fmat(d) for d in dens] + [_f64(t) for t in tensors]
+    mats = [np.zeros(n * n) if F is None else _fmat(F).copy() for n, F in outs]
+    ens = [np.zeros(1) for _ in range(nen)]
+    _check(fn(*lead, *[_p(a) for a in arrs], *[_p(m) for m in mats], *[_p(e) for e in ens]))
+    res = [m.reshape(n, n, order="F") for (n, _), m in zip(outs, mats)]
+    return (*res, *[float(e[0]) for e in ens])
+
+
+def rxcuhfne_omg2(which, ne, np_, DAalpE, DAbetE, DAtotE, DBE, DP, gm2, gm2ex, F=None,
+                  F2=None, nchunks=1):
+    """rxcuhfne_omg2.f RXCUHFne_FE_OMG2 ('fe': FAalpE, FAbetE, E), _FP_OMG2
+    ('fp': FP, E) or _FBE_OMG2 ('fbe': FBE, E); F, F2 are added to."""
+    ng = len(np.ravel(gm2))
+    L = lib()
+    if which == "fe":
+        return _rx_call(L.neoxc_rxcuhfne_fe_omg2, (nchunks, ne, np_, ng), ne, np_,
+                        (DAalpE, DAbetE, DAtotE, DBE, DP), (gm2, gm2ex),
+                        [(ne, F), (ne, F2)], 1)
+    fn = L.neoxc_rxcuhfne_fp_omg2 if which == "fp" else L.neoxc_rxcuhfne_fbe_omg2
+    n = np_ if which == "fp" else ne
+    return _rx_call(fn, (nchunks, ne, np_, ng, 0, 0), ne, np_, (DAalpE, DAtotE, DBE, DP),
+                    (gm2, gm2ex), [(n, F)], 1)
+
+
+def rxchf_omg(which, k, ne, np_, DAE, DBE, DP, tensors, F=None, S=None, nchunks=1):
+    """rxchf_omg{2,3,4}.f RXCHF_{FAE,FP,FBE}_OMGk (which = 'fae', 'fp', 'fbe');
+    tensors = (GM2_1ICR, GM2_2ICR, GM2sICR) | (GM3_1ICR, GM3_2ICR) | (GM4ICR,).
+    Returns (F, S, E, S_E) for k = 2, else (F, E)."""
+    ng = len(np.ravel(tensors[0]))
+    fn = getattr(lib(), "neoxc_rxchf_%s_omg%d" % (which, k))
+    n = np_ if which == "fp" else ne
+    outs = [(n, F), (n, S)] if k == 2 else [(n, F)]
+    return _rx_call(fn, (nchunks, ne, np_, ng), ne, np_, (DAE, DBE, DP), tensors, outs,
+                    2 if k == 2 else 1)
+
+
+def rxcuhf_omg(which, k, ne, np_, DAalpE, DAbetE, DAtotE, DBE, DP, tensors, F=None,
+               F2=None, F3=None, nchunks=1):
+    """rxcuhf_omg{2,3}.f RXCUHF_{FE,FP,FBE}_OMGk.  k = 2: 'fe' -> (FAalpE,
+    FAbetE, SAalpE, E, S), 'fp' / 'fbe' -> (F, S, E, S_E); k = 3: 'fe' ->
+    (FAalpE, FAbetE, E), 'fp' / 'fbe' -> (F, E)."""
+    ng = len(np.ravel(tensors[0]))
+    L = lib()
+    fn = getattr(L, "neoxc_rxcuhf_%s_omg%d" % (which, k))
+    n = np_ if which == "fp" else ne
+    if k == 2:
+        if which == "fe":
+            return _rx_call(fn, (nchunks, ne, np_, ng), ne, np_,
+                            (DAalpE, DAbetE, DAtotE, DBE, DP), tensors,
+                            [(ne, F), (ne, F2), (ne, F3)], 2)
+        return _rx_call(fn, (nchunks, ne, np_, ng, 0, 0), ne, np_, (DAalpE, DAtotE, DBE, DP),
+                        tensors, [(n, F), (n, F2)], 2)
+    outs = [(ne, F), (ne, F2)] if which == "fe" else [(n, F)]
+    return _rx_call(fn, (nchunks, ne, np_, ng), ne, np_, (DAalpE, DAbetE, DAtotE, DBE, DP),
+                    tensors, outs, 1)
+
+
+def rxchf_omg1(which, ne, np_, DBE, DP, gam1, gam1s, F=None):
+    """rxchf_omg1.f RXCHF_FP_OMG1 ('fp') / RXCHF_FBE_OMG1 ('fbe') ->
+    (F + dF, S, E, S_E)."""
+    g, gs, db, dp = _f64(gam1), _f64(gam1s), _fmat(DBE), _fmat(DP)
+    n = np_ if which == "fp" else ne
+    f = np.zeros(n * n) if F is None else _fmat(F).copy()
+    sm, E, S = np.zeros(n * n), np.zeros(1), np.zeros(1)
+    fn = lib().neoxc_rxchf_fp_omg1 if which == "fp" else lib().neoxc_rxchf_fbe_omg1
+    _check(fn(ne, np_, len(g), _p(db), _p(dp), _p(g), _p(gs), _p(f), _p(sm), _p(E), _p(S)))
+    return f.reshape(n, n, order="F"), sm.reshape(n, n, order="F"), float(E[0]), float(S[0])
 
 
 def dev_omg4_icr(stream, ne, np_, d_gee, d_g2s, d_g4):

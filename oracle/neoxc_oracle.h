@@ -179,6 +179,67 @@ void orc_ufp_omg4_direct(int64_t ne, int64_t np, int64_t NAE, int64_t NBE,
 void orc_omg4_icr(int64_t ne, int64_t np, const double *G2s, const double *Gee,
                   double *G4);
 
+/* ---- special-electron contractions (rx.c: rxchf/, rxchfne/) ------------ */
+void orc_rxcuhfne_fe_omg2(int64_t ne, int64_t np, const double *DAalpE,
+                          const double *DAtotE, const double *DBE, const double *DP,
+                          const double *G, const double *Gx, double *FAalpE,
+                          double *FAbetE, double *E);
+void orc_rxcuhfne_fp_omg2(int64_t ne, int64_t np, const double *DAalpE,
+                          const double *DAtotE, const double *DBE, const double *DP,
+                          const double *G, const double *Gx, double *FP, double *E);
+void orc_rxcuhfne_fbe_omg2(int64_t ne, int64_t np, const double *DAalpE,
+                           const double *DAtotE, const double *DBE, const double *DP,
+                           const double *G, const double *Gx, double *FBE, double *E);
+void orc_rxchf_fae_omg2(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                        const double *DP, const double *G1, const double *G2,
+                        const double *Gs, double *FAE, double *SAE, double *E, double *S);
+void orc_rxchf_fp_omg2(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                       const double *DP, const double *G1, const double *G2,
+                       const double *Gs, double *FP, double *SP, double *E, double *S);
+void orc_rxchf_fbe_omg2(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                        const double *DP, const double *G1, const double *G2,
+                        const double *Gs, double *FBE, double *SBE, double *E, double *S);
+void orc_rxchf_fae_omg3(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                        const double *DP, const double *G1, const double *G2,
+                        double *FAE, double *E);
+void orc_rxchf_fp_omg3(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                       const double *DP, const double *G1, const double *G2, double *FP,
+                       double *E);
+void orc_rxchf_fbe_omg3(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                        const double *DP, const double *G1, const double *G2, double *FBE,
+                        double *E);
+void orc_rxchf_fae_omg4(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                        const double *DP, const double *G, double *FAE, double *E);
+void orc_rxchf_fp_omg4(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                       const double *DP, const double *G, double *FP, double *E);
+void orc_rxchf_fbe_omg4(int64_t ne, int64_t np, const double *DAE, const double *DBE,
+                        const double *DP, const double *G, double *FBE, double *E);
+void orc_rxcuhf_fe_omg2(int64_t ne, int64_t np, const double *DAalpE,
+                        const double *DAtotE, const double *DBE, const double *DP,
+                        const double *G1, const double *G2, const double *Gs,
+                        double *FAalpE, double *FAbetE, double *SAalpE, double *E,
+                        double *S);
+void orc_rxcuhf_fp_omg2(int64_t ne, int64_t np, const double *DAalpE,
+                        const double *DAtotE, const double *DBE, const double *DP,
+                        const double *G1, const double *G2, const double *Gs,
+                        double *FP, double *SP, double *E, double *S);
+void orc_rxcuhf_fbe_omg2(int64_t ne, int64_t np, const double *DAalpE,
+                         const double *DAtotE, const double *DBE, const double *DP,
+                         const double *G1, const double *G2, const double *Gs,
+                         double *FBE, double *SBE, double *E, double *S);
+void orc_rxcuhf_fe_omg3(int64_t ne, int64_t np, const double *DAalpE,
+                        const double *DAbetE, const double *DAtotE, const double *DBE,
+                        const double *DP, const double *G1, const double *G2,
+                        double *FAalpE, double *FAbetE, double *E);
+void orc_rxcuhf_fp_omg3(int64_t ne, int64_t np, const double *DAalpE,
+                        const double *DAbetE, const double *DAtotE, const double *DBE,
+                        const double *DP, const double *G1, const double *G2, double *FP,
+                        double *E);
+void orc_rxcuhf_fbe_omg3(int64_t ne, int64_t np, const double *DAalpE,
+                         const double *DAbetE, const double *DAtotE, const double *DBE,
+                         const double *DP, const double *G1, const double *G2,
+                         double *FBE, double *E);
+
 /* gam_4 element assembly (gam_4_OMP.f symm_gam4 / calc_GAM_4_integral),
  * returned already divided by 16 as stored by GAM4_ICR. */
 double orc_gam4_element(int64_t ne, int64_t np, const double *GAM_2s,

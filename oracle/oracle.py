@@ -1,7 +1,7 @@
 """ctypes binding for the CPU oracle (test infrastructure only).
 
 The oracle restates the NEO-RXCHF integral and contraction arithmetic on
-the CPU (``prim.c``, ``builders.c``, ``scf.c``, ``spin.c``).  Only the tests, the smoke check and
+the CPU (``prim.c``, ``builders.c``, ``scf.c``, ``spin.c``, ``rx.c``).  Only the tests, the smoke check and
 the CPU-baseline leg of ``bench.py`` load it; the product never does.
 """
 from __future__ import annotations
@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libneoxc_oracle.so")
-SOURCES = ["prim.c", "builders.c", "scf.c", "spin.c"]
+SOURCES = ["prim.c", "builders.c", "scf.c", "spin.c", "rx.c"]
 _lock = threading.Lock()
 _lib = None
 
@@ -145,6 +145,24 @@ def lib():
                 "orc_fae_omg4_direct": (None, [i64] * 4 + [vp] * 7),
                 "orc_ufp_omg4_direct": (None, [i64] * 4 + [vp] * 7),
                 "orc_omg4_icr": (None, [i64, i64, vp, vp, vp]),
+                "orc_rxcuhfne_fe_omg2": (None, [i64, i64] + [vp] * 9),
+                "orc_rxcuhfne_fp_omg2": (None, [i64, i64] + [vp] * 8),
+                "orc_rxcuhfne_fbe_omg2": (None, [i64, i64] + [vp] * 8),
+                "orc_rxchf_fae_omg2": (None, [i64, i64] + [vp] * 10),
+                "orc_rxchf_fp_omg2": (None, [i64, i64] + [vp] * 10),
+                "orc_rxchf_fbe_omg2": (None, [i64, i64] + [vp] * 10),
+                "orc_rxchf_fae_omg3": (None, [i64, i64] + [vp] * 7),
+                "orc_rxchf_fp_omg3": (None, [i64, i64] + [vp] * 7),
+                "orc_rxchf_fbe_omg3": (None, [i64, i64] + [vp] * 7),
+                "orc_rxchf_fae_omg4": (None, [i64, i64] + [vp] * 6),
+                "orc_rxchf_fp_omg4": (None, [i64, i64] + [vp] * 6),
+                "orc_rxchf_fbe_omg4": (None, [i64, i64] + [vp] * 6),
+                "orc_rxcuhf_fe_omg2": (None, [i64, i64] + [vp] * 12),
+                "orc_rxcuhf_fp_omg2": (None, [i64, i64] + [vp] * 11),
+                "orc_rxcuhf_fbe_omg2": (None, [i64, i64] + [vp] * 11),
+                "orc_rxcuhf_fe_omg3": (None, [i64, i64] + [vp] * 10),
+                "orc_rxcuhf_fp_omg3": (None, [i64, i64] + [vp] * 9),
+                "orc_rxcuhf_fbe_omg3": (None, [i64, i64] + [vp] * 9),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
