@@ -341,6 +341,100 @@ def factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
     return out
 
 
+def open_shell_section(neoxc, torch, dev, stream):
+    """XCUHF in-core contractions (k_spin.cu): one neoxc_dev_xcuhf_omg call
+    gives FAE_OMGk, FAE_OMGk for beta and UFP_OMGk (three reference routines)
+    from one pass over the stored tensor.  Tensors larger than L2, seeded on
+    the device; NAE = NBE = 2.  Roofline: HBM, algorithmic bytes = one read
+    of the tensor(s) per call."""
+    f64 = torch.float64
+    peak = read_hbm_peak()
+    out = {"api": "neoxc_dev_xcuhf_omg (device)", "peak_gbs": peak}
+    sp = stream.cuda_stream
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    for k, ne, np_ in ((2, 40, 4), (3, 12, 4), (4, 10, 2)):
+        n = ne ** (2 * k) * np_ ** 2
+        ntens = 2 if k == 2 else 1
+        free, _ = torch.cuda.mem_get_info(dev)
+        if free < 1.5 * 8 * n * ntens:
+            out["omg%d" % k] = {"skipped": "needs %.1f GB free" % (8e-9 * n * ntens)}
+            continue
+        G = torch.rand(n, generator=gen, dtype=f64, device=dev)
+        Gs = torch.rand(n, generator=gen, dtype=f64, device=dev) if k == 2 else None
+        A = torch.rand((ne, ne), generator=gen, dtype=f64, device=dev)
+        DA = (A @ A.T).contiguous().view(-1) / ne
+        B = torch.rand((ne, ne), generator=gen, dtype=f64, device=dev)
+        DB = (B @ B.T).contiguous().view(-1) / ne
+        DP = torch.eye(np_, dtype=f64, device=dev).view(-1)
+        FA = torch.zeros(ne * ne, dtype=f64, device=dev)
+        FB, FP = torch.zeros_like(FA), torch.zeros(np_ * np_, dtype=f64, device=dev)
+        S = [torch.zeros_like(FA), torch.zeros_like(FA), torch.zeros_like(FP)] if k == 2 \
+            else [None, None, None]
+        E = torch.zeros(6, dtype=f64, device=dev)
+
+        def call():
+            neoxc.dev_xcuhf_omg(sp, k, ne, np_, 2, 2, G, Gs, DA, DB, DP, FA, FB, FP,
+                                S[0], S[1], S[2], E)
+        for _ in range(2):
+            call()
+        torch.cuda.synchronize(dev)
+        steps = 5
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            call()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = a.elapsed_time(b) / steps
+        nbytes = 8 * n * ntens
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out["omg%d" % k] = {"nebf": ne, "npbf": np_, "tensor_GB": nbytes / 1e9,
+                            "ms_per_call": ms, "elements_per_s": n / (ms * 1e-3),
+                            "roofline": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
+                                         "peak": peak, "frac": gbs / peak if peak else None,
+                                         "algorithmic_bytes": nbytes},
+                            "launches_per_call": 5}
+        del G, Gs
+        torch.cuda.empty_cache()
+    return out
+
+
+def xcuhf_scf_section(neoxc):
+    """XCUHF (open-shell) SCF on the reference's examples/xcuhf system
+    (fixture tests/golden/xcuhf_example.json): core-Hamiltonian guesses for
+    both spins and the proton, every integral including the raw OMG4_ICR
+    tensor built on the GPU, UHF_FOCK / UROOTHAN with DIIS there.  The
+    converged energy is compared with XCUHF.log's."""
+    import re
+    from neoxc import basis
+    with open(os.path.join(ROOT, "tests", "golden", "xcuhf_example.json")) as f:
+        g = json.load(f)
+    s = basis.parse_inp(g["inp"], name="examples/xcuhf")
+    m = re.search(r"&XCUHF\s*nae=(\d+),\s*nbe=(\d+)", g["inp"], re.I)
+    nae, nbe = int(m.group(1)), int(m.group(2))
+    E_log = g["final"]["E_TOTAL"]
+    out = {"workload": "examples/xcuhf XCUHF (nebf=%d, npebf=%d, npbf=%d, NG=%d, NAE=%d, "
+                       "NBE=%d), core-Hamiltonian guesses" % (s.nebf, s.npebf, s.npbf, s.ngtg,
+                                                              nae, nbe),
+           "api": "neoxc_xcuhf_scf (host arrays; integrals and SCF on the GPU)"}
+    neoxc.xcuhf_scf(s, nae, nbe, maxit=2)   # warm-up
+    for name, mixed in (("diis", False), ("diis_mixed", True)):
+        t0 = time.perf_counter()
+        r = neoxc.xcuhf_scf(s, nae, nbe, diis=True, mixed=mixed)
+        dt = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        neoxc.xcuhf_scf(s, nae, nbe, maxit=1, mixed=mixed)
+        dt1 = time.perf_counter() - t1
+        out[name] = {"solves_per_s": 1.0 / dt, "ms_per_solve": 1e3 * dt,
+                     "iterations": r["niter"], "converged": r["converged"],
+                     "ms_integrals_plus_first_iteration": 1e3 * dt1,
+                     "ms_per_iteration": 1e3 * (dt - dt1) / max(1, r["niter"] - 1),
+                     "E_total": r["final"]["E_total"],
+                     "E_err_vs_log": r["final"]["E_total"] - E_log}
+    return out
+
+
 def scf_section(neoxc, with_cpu: bool):
     """XCHF RHF SCF solves/s on the reference's examples/xchf system (inputs
     from the committed fixture tests/golden/xchf_example.json: exam_xchf.inp
@@ -384,6 +478,7 @@ def scf_section(neoxc, with_cpu: bool):
                                       % ("gam_3" if mixed == "gam3" else "gam_1, gam_2, gam_3"))
         else:
             E_fp64 = r["final"]["E_total"]
+    out["xcuhf"] = xcuhf_scf_section(neoxc)
     out["batch"] = scf_batch_section(neoxc, s, DE)
     out["serving"] = scf_serving_section(neoxc, s, DE)
     if with_cpu:
@@ -573,6 +668,7 @@ def main():
     }
     line["factored"] = factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
                                         d_gee, d_g2s, d_DE, d_DP, mean_ms, float(d_E.item()))
+    line["open_shell"] = open_shell_section(neoxc, torch, dev, stream)
     line["scf"] = scf_section(neoxc, not args.no_cpu_baseline and ws == 1)
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(ne, np_, gee, g2s, DE, DP)

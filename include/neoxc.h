@@ -299,6 +299,8 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
 #define NEOXC_SCF_GAM4_ELEMENT 4   /* element-wise GAM4_DSCF for gam_4     */
 #define NEOXC_SCF_MIXED 8          /* gam_3 MD integrals in FP32 (new)     */
 #define NEOXC_SCF_MIXED_GAM2 16    /* gam_1, gam_2 MD integrals in FP32 (new) */
+#define NEOXC_SCF_GUESS_ELEC 32    /* XCUHF: DAE, DBE from the electronic core
+                                      Hamiltonian (guess_A_elec) */
 int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
                    const double* cat, const double* zan, const double* bcoef1,
@@ -365,6 +367,36 @@ int neoxc_xchf_server_submit(neoxc_xchf_server* srv, neoxc_xchf_job* job);
 int neoxc_xchf_server_wait(neoxc_xchf_server* srv, neoxc_xchf_job* job,
                            double timeout_s);
 int neoxc_xchf_server_stop(neoxc_xchf_server* srv);
+
+/* xcuhf/xcuhf_scf.f:2-582 (Roothaan branch; SOSCF not ported) with
+ * UHF_FOCK (xcuhf_fock.f:2-427) on the device: builds every integral
+ * (overlaps, core Hamiltonians, GAM_ep, GAM_1/GAM_1s, GAM_ee, GM2ICR /
+ * GM2sICR, GM3ICR, OMG4_ICR) and iterates UHF_FOCK / UROOTHAN (proton,
+ * alpha, beta from one Fock build) / DENDIF until the alpha and beta
+ * densities move less than 1e-6 (and the proton's less than 1e-4 when
+ * npbf > 1).  NAE + NBE = nelec.  DAE, DBE in: start densities unless
+ * NEOXC_SCF_GUESS_ELEC; DP as in neoxc_xchf_scf; all three out.
+ * E_init / E_final [16]: 0 E_total, 1 E_nuc, 2 E_ecore, 3 E_pcore, 4 E_ep,
+ * 5 E_ee, 6 E_OMG1, 7 E_OMG2, 8 E_OMG3, 9 E_OMG4 (2..9 divided by S_total,
+ * as the log prints them), 10 S_total, 11 S_OMG1, 12 S_OMG2 (raw),
+ * 13 / 14 / 15 last alpha / beta / proton density change.  history
+ * [4*maxit]: E_total, its change, max(alpha, beta) density change, proton
+ * density change.  Options: NEOXC_SCF_GUESS_ELEC, NEOXC_SCF_GUESS_PROT,
+ * NEOXC_SCF_DIIS (alpha and beta Fock matrices, separately, once both
+ * densities move less than 0.1 per iteration),
+ * NEOXC_SCF_MIXED, NEOXC_SCF_MIXED_GAM2.  Limits: nebf, npbf <= 64,
+ * nebf <= 20 with gam_3, nebf <= 12 with OMG4. */
+int neoxc_xcuhf_scf(int64_t nelec, int64_t NAE, int64_t NBE, int64_t nucst,
+                    int64_t nebf, int64_t npebf, int64_t npbf, int64_t nat,
+                    int64_t ngtg1, double pmass, const double* cat, const double* zan,
+                    const double* bcoef1, const double* gamma1, const int64_t* KPESTR,
+                    const int64_t* KPEEND, const int64_t* AMPEB2C,
+                    const double* AGEBFCC, const double* AGNBFCC, const double* ELCEX,
+                    const double* NUCEX, const int64_t* ELCAM, const int64_t* NUCAM,
+                    const double* ELCBFC, const double* NUCBFC, int64_t options,
+                    int64_t maxit, double* DAE, double* DBE, double* DP, double* E_init,
+                    double* E_final, double* history, int64_t* niter,
+                    int64_t* converged);
 
 /* ---- open-shell XCUHF contractions: xcuhf/xcuhf_omg{1..4}.f ------------ */
 /* Same arguments, packed layouts and semantics as the reference: the Fock

@@ -1927,3 +1927,225 @@ int neoxc_rxchf_fbe_omg1(int64_t nebf, int64_t npbf, int64_t ng1, const double* 
 }
 
 }  // extern "C"
+
+// ---- XCUHF SCF on the device (xcuhf/xcuhf_scf.f, Roothaan branch) ----------
+namespace {
+
+int xcuhf_scf_on(cudaStream_t s, int64_t nelec, int64_t NAE, int64_t NBE, int64_t nucst,
+                 int64_t nebf, int64_t npebf, int64_t npbf, int64_t nat, int64_t ngtg1,
+                 double pmass, const double* cat, const double* zan, const double* bcoef1,
+                 const double* gamma1, const int64_t* KPESTR, const int64_t* KPEEND,
+                 const double* AGEBFCC, const double* AGNBFCC, const double* ELCEX,
+                 const double* NUCEX, const int64_t* ELCAM, const int64_t* NUCAM,
+                 const double* ELCBFC, const double* NUCBFC, int64_t options,
+                 int64_t maxit, double* DAE, double* DBE, double* DP, double* E_init,
+                 double* E_final, double* history, int64_t* niter, int64_t* converged) {
+  RC(need(nelec >= 1 && NAE >= 0 && NBE >= 0 && NAE + NBE == nelec,
+          "nelec >= 1, NAE + NBE == nelec"));
+  RC(need(maxit >= 1 && nucst >= 1 && nucst <= npbf, "maxit >= 1, 1 <= nucst <= npbf"));
+  RC(need(NAE <= nebf && NBE <= nebf, "NAE, NBE <= nebf"));
+  RC(need(DAE && DBE && DP && E_init && E_final && niter && converged, "pointers"));
+  RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_GUESS_ELEC |
+                                NEOXC_SCF_DIIS | NEOXC_SCF_MIXED |
+                                NEOXC_SCF_MIXED_GAM2)) == 0,
+          "options"));
+  if (nebf > kScfMaxN || npbf > kScfMaxN)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "XCUHF SCF: nebf, npbf <= %d", kScfMaxN);
+  if (nelec > 2 && nebf > 20)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "XCUHF SCF with gam_3: nebf <= 20");
+  if (nelec > 3 && !spin_smem_fits(4, (int)nebf))
+    return set_err(NEOXC_ERR_UNSUPPORTED, "XCUHF SCF with OMG4: nebf <= 12");
+  const int mixed = (options & NEOXC_SCF_MIXED) ? 1 : 0;
+  const int mixed_gam2 = (options & NEOXC_SCF_MIXED_GAM2) ? 1 : 0;
+  const bool diis = (options & NEOXC_SCF_DIIS) != 0;
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1, gamma1,
+                  KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC,
+                  NUCBFC));
+  const int ne = (int)nebf, np = (int)npbf;
+  const size_t e2 = (size_t)ne * ne, p2 = (size_t)np * np;
+  const size_t ng1 = e2 * p2, ng2 = e2 * e2 * p2;
+  const size_t ng3 = nelec > 2 ? e2 * e2 * e2 * p2 : 0;
+  const size_t ng4 = nelec > 3 ? e2 * e2 * e2 * e2 * p2 : 0;
+  // integrals: as the XCHF SCF, plus the raw OMG4_ICR tensor
+  DBuf Se, Sp, Hce, Hcp, Gep, G1, G1s, Gee, G2, G2s, G3, G4;
+  RC(dalloc(Se, sizeof(double) * e2, s));
+  RC(dalloc(Sp, sizeof(double) * p2, s));
+  RC(dalloc(Hce, sizeof(double) * e2, s));
+  RC(dalloc(Hcp, sizeof(double) * p2, s));
+  RC(dalloc(Gep, sizeof(double) * ng1, s));
+  RC(dalloc(G1, sizeof(double) * ng1, s));
+  RC(dalloc(G1s, sizeof(double) * ng1, s));
+  RC(dalloc(Gee, sizeof(double) * e2 * e2, s));
+  RC(dalloc(G2, sizeof(double) * (nelec > 1 ? ng2 : 1), s));
+  RC(dalloc(G2s, sizeof(double) * (nelec > 1 ? ng2 : 1), s));
+  RC(dalloc(G3, sizeof(double) * (ng3 ? ng3 : 1), s));
+  RC(dalloc(G4, sizeof(double) * (ng4 ? ng4 : 1), s));
+  CU(launch_scf_onebody(u.d, Se.as<double>(), Sp.as<double>(), Hce.as<double>(),
+                        Hcp.as<double>(), s));
+  CU(launch_gam_ep(u.d, Gep.as<double>(), s));
+  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, mixed_gam2));
+  CU(launch_gam_ee(u.d, Gee.as<double>(), s));
+  if (nelec > 1) {
+    CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s, mixed_gam2));
+    CU(launch_gam2_symmetrize(ne, np, 0, G2.as<double>(), G2s.as<double>(), s));
+  }
+  if (nelec > 2) {
+    DBuf aux;
+    RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
+    CU(launch_gam3_aux(u.d, aux.as<double>(), s, Gee.as<double>(), Hce.as<double>()));
+    CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed));
+    CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
+  }
+  if (nelec > 3)
+    CU(launch_omg4_icr(ne, np, Gee.as<double>(), G2s.as<double>(), G4.as<double>(), s));
+  // SCF state
+  DBuf dA, dB, dP, A0, B0, P0, fa, fb, fp, sa1, sb1, sp1, sa2, sb2, sp2, Xe, Xp, en, part,
+      e6, st, wa, wb;
+  RC(upload(dA, DAE, sizeof(double) * e2, s));
+  RC(upload(dB, DBE, sizeof(double) * e2, s));
+  RC(dalloc(dP, sizeof(double) * p2, s));
+  for (DBuf* b : {&A0, &B0, &fa, &fb, &sa1, &sb1, &sa2, &sb2, &Xe})
+    RC(dalloc(*b, sizeof(double) * e2, s));
+  for (DBuf* b : {&P0, &fp, &sp1, &sp2, &Xp}) RC(dalloc(*b, sizeof(double) * p2, s));
+  RC(dalloc(en, sizeof(double) * kScfSlots, s));
+  RC(dalloc(part, sizeof(double) * scf_fock1_part_doubles(ne, np), s));
+  RC(dalloc(e6, sizeof(double) * 18, s));
+  // status words: 0..7 eigensolver sweeps, 8..9 / 10..11 alpha / beta DIIS
+  RC(dalloc(st, sizeof(int) * 16, s));
+  RC(dalloc(wa, sizeof(double) * (diis ? diis_doubles(ne) : 1), s));
+  RC(dalloc(wb, sizeof(double) * (diis ? diis_doubles(ne) : 1), s));
+  if (diis) {
+    CU(cudaMemsetAsync(wa.p, 0, sizeof(double) * diis_doubles(ne), s));
+    CU(cudaMemsetAsync(wb.p, 0, sizeof(double) * diis_doubles(ne), s));
+  }
+  for (DBuf* b : {&A0, &B0, &sa2, &sb2}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * e2, s));
+  for (DBuf* b : {&P0, &sp2}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * p2, s));
+  CU(cudaMemsetAsync(st.p, 0, sizeof(int) * 16, s));
+  CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kScfSlots, s));
+  const double Enuc = nuc_rep(nat, zan, cat);
+  CU(cudaMemcpyAsync(en.as<double>() + 1, &Enuc, sizeof(double), cudaMemcpyHostToDevice, s));
+  int* sts = st.as<int>();
+  CU(launch_inv_sqrt(ne, Se.as<double>(), Xe.as<double>(), sts + 0, s));
+  CU(launch_inv_sqrt(np, Sp.as<double>(), Xp.as<double>(), sts + 1, s));
+  if (options & NEOXC_SCF_GUESS_ELEC) {
+    // guess_A_elec (xcuhf_scf.f:585-609): lowest NAE / NBE core orbitals
+    CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), 0, (int)NAE, 1.0,
+                      dA.as<double>(), nullptr, nullptr, sts + 2, s));
+    CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), 0, (int)NBE, 1.0,
+                      dB.as<double>(), nullptr, nullptr, sts + 2, s));
+  }
+  if (options & NEOXC_SCF_GUESS_PROT) {
+    // guess_prot2 (xcuhf_scf.f:611-640)
+    CU(launch_roothan(np, Hcp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
+                      dP.as<double>(), nullptr, nullptr, sts + 3, s));
+  } else {
+    CU(cudaMemcpyAsync(dP.p, DP, sizeof(double) * p2, cudaMemcpyHostToDevice, s));
+  }
+  double* d_en = en.as<double>();
+  double* d_e6 = e6.as<double>();
+  auto fock_build = [&]() -> int {
+    CU(launch_uhf_fock1(ne, np, Hce.as<double>(), Hcp.as<double>(), Gep.as<double>(),
+                        G1.as<double>(), G1s.as<double>(), Gee.as<double>(),
+                        dA.as<double>(), dB.as<double>(), dP.as<double>(), fa.as<double>(),
+                        fb.as<double>(), fp.as<double>(), sa1.as<double>(),
+                        sb1.as<double>(), sp1.as<double>(), part.as<double>(), d_en, s));
+    for (int k = 2; k <= 4 && k <= nelec; k++) {
+      const double* G = k == 2 ? G2.as<double>() : (k == 3 ? G3.as<double>() : G4.as<double>());
+      double* E = d_e6 + 6 * (k - 2);
+      RC(xcuhf_dev(s, k, ne, np, NAE, NBE, G, k == 2 ? G2s.as<double>() : nullptr,
+                   dA.as<double>(), dB.as<double>(), dP.as<double>(), fa.as<double>(),
+                   fb.as<double>(), fp.as<double>(), k == 2 ? sa2.as<double>() : nullptr,
+                   k == 2 ? sb2.as<double>() : nullptr, k == 2 ? sp2.as<double>() : nullptr,
+                   E));
+      // UHF_FOCK keeps the proton-side energies: E_P_OMGk (and S_P_OMG2)
+      CU(cudaMemcpyAsync(d_en + 5 + k, E + 2, sizeof(double), cudaMemcpyDeviceToDevice, s));
+      if (k == 2)
+        CU(cudaMemcpyAsync(d_en + 12, E + 5, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    CU(launch_uhf_assemble(ne, np, d_en, sa1.as<double>(), sb1.as<double>(),
+                           sp1.as<double>(), sa2.as<double>(), sb2.as<double>(),
+                           sp2.as<double>(), fa.as<double>(), fb.as<double>(),
+                           fp.as<double>(), s));
+    return NEOXC_OK;
+  };
+  const double tolE = 1.0e-6, tolP = 1.0e-4;   // xcuhf_scf.f TOLE, TOLP
+  // DIIS joins once the spin densities move less than this per iteration:
+  // extrapolating from the core-Hamiltonian guess onward diverges here.
+  const double kDiisStart = 0.1;
+  bool diis_on = false;
+  double Eold = 0.0;
+  int64_t it = 0;
+  bool done = false;
+  for (it = 1; it <= maxit && !done; it++) {
+    RC(fock_build());
+    if (it == 1)
+      CU(cudaMemcpyAsync(E_init, d_en, sizeof(double) * kScfSlots, cudaMemcpyDeviceToHost,
+                         s));
+    // UROOTHAN for the proton, alpha and beta from the same Fock build
+    CU(launch_roothan(np, fp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
+                      dP.as<double>(), nullptr, nullptr, sts + 1, s));
+    if (diis_on) {
+      CU(launch_diis(ne, fa.as<double>(), dA.as<double>(), Se.as<double>(),
+                     wa.as<double>(), sts + 8, nullptr, s));
+      CU(launch_diis(ne, fb.as<double>(), dB.as<double>(), Se.as<double>(),
+                     wb.as<double>(), sts + 10, nullptr, s));
+    }
+    CU(launch_roothan(ne, fa.as<double>(), Xe.as<double>(), 0, (int)NAE, 1.0,
+                      dA.as<double>(), nullptr, nullptr, sts + 0, s));
+    CU(launch_roothan(ne, fb.as<double>(), Xe.as<double>(), 0, (int)NBE, 1.0,
+                      dB.as<double>(), nullptr, nullptr, sts + 6, s));
+    CU(launch_uhf_dendif(ne, np, dA.as<double>(), A0.as<double>(), dB.as<double>(),
+                         B0.as<double>(), dP.as<double>(), P0.as<double>(), d_en, s));
+    double h[kScfSlots];
+    int hs[8];
+    CU(cudaMemcpyAsync(h, d_en, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    RC(finish(s));
+    for (int k : {0, 1, 2, 3, 6})
+      if (hs[k] > 40)
+        return set_err(NEOXC_ERR_CUDA, "UROOTHAN: Jacobi eigensolver did not converge");
+    if (history) {
+      history[4 * (it - 1) + 0] = h[0];
+      history[4 * (it - 1) + 1] = h[0] - Eold;
+      history[4 * (it - 1) + 2] = std::max(h[13], h[14]);
+      history[4 * (it - 1) + 3] = h[15];
+    }
+    Eold = h[0];
+    for (int k = 0; k < kScfSlots; k++) E_final[k] = h[k];
+    if (diis && std::max(h[13], h[14]) < kDiisStart) diis_on = true;
+    const bool de = h[13] < tolE && h[14] < tolE;
+    done = npbf > 1 ? (de && h[15] < tolP) : de;
+    if (done) *niter = it;
+  }
+  if (!done) *niter = maxit;
+  *converged = done ? 1 : 0;
+  CU(cudaMemcpyAsync(DAE, dA.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(DBE, dB.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(DP, dP.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+}  // namespace
+
+extern "C" int neoxc_xcuhf_scf(int64_t nelec, int64_t NAE, int64_t NBE, int64_t nucst,
+                               int64_t nebf, int64_t npebf, int64_t npbf, int64_t nat,
+                               int64_t ngtg1, double pmass, const double* cat,
+                               const double* zan, const double* bcoef1,
+                               const double* gamma1, const int64_t* KPESTR,
+                               const int64_t* KPEEND, const int64_t* AMPEB2C,
+                               const double* AGEBFCC, const double* AGNBFCC,
+                               const double* ELCEX, const double* NUCEX,
+                               const int64_t* ELCAM, const int64_t* NUCAM,
+                               const double* ELCBFC, const double* NUCBFC,
+                               int64_t options, int64_t maxit, double* DAE, double* DBE,
+                               double* DP, double* E_init, double* E_final,
+                               double* history, int64_t* niter, int64_t* converged) {
+  (void)AMPEB2C;
+  cudaStream_t s;
+  RC(get_stream(&s));
+  return xcuhf_scf_on(s, nelec, NAE, NBE, nucst, nebf, npebf, npbf, nat, ngtg1, pmass, cat,
+                      zan, bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
+                      ELCAM, NUCAM, ELCBFC, NUCBFC, options, maxit, DAE, DBE, DP, E_init,
+                      E_final, history, niter, converged);
+}

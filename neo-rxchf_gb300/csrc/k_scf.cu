@@ -344,6 +344,151 @@ __global__ void assemble_kernel(int ne, int np, double* __restrict__ en,
     fockp[k] = (one / S) * fockp[k] - H * (sp1[k] + sp2[k]);
 }
 
+// ---- XCUHF (xcuhf/xcuhf_fock.f UHF_FOCK) ----------------------------------
+// One-body and HF terms of IC_construct_FAE / IC_construct_FP for both spins
+// (xcuhf_hfterms.f FAE_ecore, FAE_GAMep, FAE_GAMee; xcuhf_omg1.f FAE_OMG1;
+// FP_pcore, FP_GAMep, UFP_OMG1).  t < ne^2: electron (i,j) of both spins;
+// then proton (p,q).  Energy channels (as fock1_kernel, so
+// fock1_energy_kernel files them into en[2..6], en[11]):
+//   0 E_AE_ecore + E_BE_ecore, 1 E_P_pcore, 2 E_P_GAMep,
+//   3 E_AE_GAMee + E_BE_GAMee, 4 E_P_OMG1, 5 S_P_OMG1.
+__global__ void uhf_fock1_kernel(int ne, int np, const double* __restrict__ Hce,
+                                 const double* __restrict__ Hcp,
+                                 const double* __restrict__ Gep,
+                                 const double* __restrict__ G1,
+                                 const double* __restrict__ G1s,
+                                 const double* __restrict__ Gee,
+                                 const double* __restrict__ DAE,
+                                 const double* __restrict__ DBE,
+                                 const double* __restrict__ DP,
+                                 double* __restrict__ FAE, double* __restrict__ FBE,
+                                 double* __restrict__ FP, double* __restrict__ SAE1,
+                                 double* __restrict__ SBE1, double* __restrict__ SP1,
+                                 double* __restrict__ part) {
+  const int nt = ne * ne + np * np;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const int n2 = ne * ne;
+  double e[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (t < n2) {
+    const int i = t / ne, j = t - i * ne;
+    const double fc = Hce[i * ne + j];   // GAM_ecore(pack_2D(ne,je,ie))
+    double fep = 0.0, fg1 = 0.0, s1 = 0.0;
+    for (int p = 0; p < np; p++)
+      for (int q = 0; q < np; q++) {
+        const double dp = DP[p + np * q];
+        const long long o = ((long long)(p * np + q) * ne + i) * ne + j;
+        fep = fep + dp * Gep[o];
+        fg1 = fg1 + dp * G1[o];
+        s1 = s1 + dp * G1s[o];
+      }
+    // FAE_GAMee: DETOT (i j|k l) - D_spin (i l|k j)
+    double J = 0.0, KA = 0.0, KB = 0.0;
+    for (int k = 0; k < ne; k++)
+      for (int l = 0; l < ne; l++) {
+        const double v12 = Gee[(((long long)i * ne + j) * ne + k) * ne + l];
+        const double v21 = Gee[(((long long)i * ne + l) * ne + k) * ne + j];
+        const double da = DAE[k + ne * l], db = DBE[k + ne * l];
+        J = J + (da + db) * v12;
+        KA = KA + da * v21;
+        KB = KB + db * v21;
+      }
+    const int c = i + ne * j;
+    FAE[c] = fc + fep + (J - KA) + fg1;
+    FBE[c] = fc + fep + (J - KB) + fg1;
+    SAE1[c] = s1;
+    SBE1[c] = s1;
+    const double da = DAE[c], db = DBE[c];
+    e[0] = (da + db) * fc;
+    e[3] = 0.5 * (da * (J - KA) + db * (J - KB));
+  } else {
+    const int k = t - n2, p = k / np, q = k - p * np;
+    const double fc = Hcp[p * np + q];
+    double fep = 0.0, fg1 = 0.0, s1 = 0.0;
+    for (int i = 0; i < ne; i++)
+      for (int j = 0; j < ne; j++) {
+        const double dt = DAE[i + ne * j] + DBE[i + ne * j];
+        const long long o = ((long long)(p * np + q) * ne + i) * ne + j;
+        fep = fep + dt * Gep[o];
+        fg1 = fg1 + dt * G1[o];
+        s1 = s1 + dt * G1s[o];
+      }
+    const int c = p + np * q;
+    FP[c] = fc + fep + fg1;
+    SP1[c] = s1;
+    const double dp = DP[c];
+    e[1] = dp * fc;
+    e[2] = dp * fep;
+    e[4] = dp * fg1;
+    e[5] = dp * s1;
+  }
+  for (int c = 0; c < 6; c++) part[(long long)c * nt + t] = e[c];
+}
+
+// UHF_FOCK tail (xcuhf_fock.f:318-371) and UHF_Fock_correction (:742-780):
+// S_total = 1 + S_OMG1 + S_OMG2, Psi_H_Psi = the raw components, printed
+// components divided by S_total, F = XF / S_total - Psi_H_Psi / S_total^2
+// (XS1 + XS2) for FP, FAE, FBE.
+__global__ void uhf_assemble_kernel(int ne, int np, double* __restrict__ en,
+                                    const double* __restrict__ sae1,
+                                    const double* __restrict__ sbe1,
+                                    const double* __restrict__ sp1,
+                                    const double* __restrict__ sae2,
+                                    const double* __restrict__ sbe2,
+                                    const double* __restrict__ sp2,
+                                    double* __restrict__ FAE, double* __restrict__ FBE,
+                                    double* __restrict__ FP) {
+  __shared__ double sS, sPsi;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double S_total = 1.0 + en[11] + en[12];
+    const double psi = en[3] + en[2] + en[5] + en[4] + en[6] + en[7] + en[8] + en[9];
+    for (int k = 2; k <= 9; k++) en[k] = en[k] / S_total;
+    en[0] = (en[3] + en[2] + en[4] + en[5]) + en[6] + en[7] + en[8] + en[9] + en[1];
+    en[10] = S_total;
+    sS = S_total;
+    sPsi = psi;
+  }
+  __syncthreads();
+  const double c1 = 1.0 / sS, c2 = sPsi / (sS * sS);
+  for (int k = threadIdx.x; k < np * np; k += blockDim.x)
+    FP[k] = c1 * FP[k] - c2 * (sp1[k] + sp2[k]);
+  for (int k = threadIdx.x; k < ne * ne; k += blockDim.x) {
+    FAE[k] = c1 * FAE[k] - c2 * (sae1[k] + sae2[k]);
+    FBE[k] = c1 * FBE[k] - c2 * (sbe1[k] + sbe2[k]);
+  }
+}
+
+// DENDIF + COPYDEN for alpha, beta and the proton (xcuhf_scf.f:512-523):
+// en[13], en[14], en[15].
+__global__ void uhf_dendif_kernel(int ne, int np, const double* __restrict__ DA,
+                                  double* __restrict__ DA0, const double* __restrict__ DB,
+                                  double* __restrict__ DB0, const double* __restrict__ DP,
+                                  double* __restrict__ DP0, double* __restrict__ en) {
+  __shared__ double sw[32];
+  for (int which = 0; which < 3; which++) {
+    const int n = which == 2 ? np : ne;
+    const double* D = which == 0 ? DA : (which == 1 ? DB : DP);
+    double* D0 = which == 0 ? DA0 : (which == 1 ? DB0 : DP0);
+    double mx = 0.0;
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+      mx = fmax(mx, fabs(D0[k] - D[k]));
+      D0[k] = D[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sw[w] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double r = 0.0;
+      for (int k = 0; k < (int)(blockDim.x + 31) / 32; k++) r = fmax(r, sw[k]);
+      en[13 + which] = r;
+    }
+    __syncthreads();
+  }
+}
+
 // ---- symmetric eigensolver: cyclic Jacobi with round-robin pairing ------------
 // A (row-major n x n, symmetric) and V in shared memory; on return A is
 // diagonal to working precision and V holds the eigenvectors as columns.
@@ -787,6 +932,37 @@ cudaError_t launch_dendif(int ne, int np, const double* DE, double* DE0,
                           const double* DP, double* DP0, double* en,
                           cudaStream_t s) {
   dendif_kernel<<<1, 256, 0, s>>>(ne, np, DE, DE0, DP, DP0, en);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_uhf_fock1(int ne, int np, const double* Hce, const double* Hcp,
+                             const double* Gep, const double* G1, const double* G1s,
+                             const double* Gee, const double* DAE, const double* DBE,
+                             const double* DP, double* FAE, double* FBE, double* FP,
+                             double* SAE1, double* SBE1, double* SP1, double* part,
+                             double* en, cudaStream_t s) {
+  const int nt = ne * ne + np * np;
+  uhf_fock1_kernel<<<(nt + 127) / 128, 128, 0, s>>>(ne, np, Hce, Hcp, Gep, G1, G1s, Gee,
+                                                    DAE, DBE, DP, FAE, FBE, FP, SAE1,
+                                                    SBE1, SP1, part);
+  fock1_energy_kernel<<<1, 256, 0, s>>>(nt, part, en);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_uhf_assemble(int ne, int np, double* en, const double* sae1,
+                                const double* sbe1, const double* sp1,
+                                const double* sae2, const double* sbe2,
+                                const double* sp2, double* FAE, double* FBE, double* FP,
+                                cudaStream_t s) {
+  uhf_assemble_kernel<<<1, 256, 0, s>>>(ne, np, en, sae1, sbe1, sp1, sae2, sbe2, sp2,
+                                        FAE, FBE, FP);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_uhf_dendif(int ne, int np, const double* DA, double* DA0,
+                              const double* DB, double* DB0, const double* DP,
+                              double* DP0, double* en, cudaStream_t s) {
+  uhf_dendif_kernel<<<1, 256, 0, s>>>(ne, np, DA, DA0, DB, DB0, DP, DP0, en);
   return cudaGetLastError();
 }
 

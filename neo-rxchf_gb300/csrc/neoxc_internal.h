@@ -221,6 +221,24 @@ cudaError_t launch_inv_sqrt(int n, const double* S, double* X, int* status,
 cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
                            int nocc, double prefac, double* D, double* evals,
                            double* C, int* status, cudaStream_t s);
+// XCUHF (UHF_FOCK): one-body / HF terms of both spins and the proton
+// (energies into en[2..6], en[11]; en[7..9], en[12] zeroed), the
+// normalisation + UHF_Fock_correction, and DENDIF of alpha, beta, proton
+// into en[13..15].
+cudaError_t launch_uhf_fock1(int ne, int np, const double* Hce, const double* Hcp,
+                             const double* Gep, const double* G1, const double* G1s,
+                             const double* Gee, const double* DAE, const double* DBE,
+                             const double* DP, double* FAE, double* FBE, double* FP,
+                             double* SAE1, double* SBE1, double* SP1, double* part,
+                             double* en, cudaStream_t s);
+cudaError_t launch_uhf_assemble(int ne, int np, double* en, const double* sae1,
+                                const double* sbe1, const double* sp1,
+                                const double* sae2, const double* sbe2,
+                                const double* sp2, double* FAE, double* FBE, double* FP,
+                                cudaStream_t s);
+cudaError_t launch_uhf_dendif(int ne, int np, const double* DA, double* DA0,
+                              const double* DB, double* DB0, const double* DP,
+                              double* DP0, double* en, cudaStream_t s);
 cudaError_t launch_dendif(int ne, int np, const double* DE, double* DE0,
                           const double* DP, double* DP0, double* en,
                           cudaStream_t s);

@@ -30,7 +30,7 @@ __all__ = [
     "index_gam_2pk", "index_gam_3pk", "index_gam_4pk2", "pack_4d",
     "fae_omg1", "ufp_omg1", "fae_omg2", "ufp_omg2", "fae_omg3", "ufp_omg3", "fae_omg4",
     "ufp_omg4", "omg4_icr", "dev_xcuhf_omg", "dev_omg4_icr",
-    "rxcuhfne_omg2", "rxchf_omg", "rxcuhf_omg", "rxchf_omg1",
+    "rxcuhfne_omg2", "rxchf_omg", "rxcuhf_omg", "rxchf_omg1", "xcuhf_scf", "XCUHF_SLOTS",
 ]
 
 LIB_PATH = _build.LIB
@@ -98,6 +98,7 @@ def _declare(L):
         "neoxc_gam4_fock_factored": (I, [i64] * 4 + [vp] * 7),
         "neoxc_xchf_scf": (I, [i64] * 7 + [d] + [vp] * 15 + [i64, i64] + [vp] * 7),
         "neoxc_xchf_job_size": (i64, []),
+        "neoxc_xcuhf_scf": (I, [i64] * 9 + [d] + [vp] * 15 + [i64, i64] + [vp] * 8),
         "neoxc_xchf_scf_job": (I, [vp, i64, i64]),
         "neoxc_ufm_read": (I, [C.c_char_p, i64, i64, vp]),
         "neoxc_ufm_write": (I, [C.c_char_p, vp, i64, i64]),
@@ -313,6 +314,40 @@ def xchf_scf(s: NeoSystem, DE, DP=None, nucst=None, maxit: int = 100,
             "final": dict(zip(SCF_SLOTS, Ef.tolist())),
             "history": hist[:4 * n].reshape(n, 4), "niter": n, "converged": bool(conv[0]),
             "DE": de.reshape(ne, ne, order="F"), "DP": dp.reshape(np_, np_, order="F")}
+
+
+XCUHF_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_omg1",
+               "E_omg2", "E_omg3", "E_omg4", "S_total", "S_omg1", "S_omg2", "dDAE", "dDBE",
+               "dDP")
+
+
+def xcuhf_scf(s: NeoSystem, nae: int, nbe: int, DAE=None, DBE=None, DP=None, nucst=None,
+              maxit: int = 100, diis: bool = False, mixed=False):
+    """xcuhf_scf.f XCUHF SCF on the GPU (UROOTHAN for the proton, alpha and
+    beta from each UHF_FOCK build; optional DIIS).  DAE / DBE None: core
+    Hamiltonian guess for both spins (guess_A_elec); DP None: guess_prot2.
+    Energies are the log's components (XCUHF_SLOTS, 2..9 divided by
+    S_total).  Returns initial / final energetics, history, densities."""
+    ne, np_ = s.nebf, s.npbf
+    guess_e = DAE is None or DBE is None
+    opts = ((1 if DP is None else 0) | (32 if guess_e else 0) | (2 if diis else 0)
+            | (8 if mixed else 0) | (16 if mixed is True else 0))
+    da = np.zeros(ne * ne) if guess_e else _fmat(DAE).copy()
+    db = np.zeros(ne * ne) if guess_e else _fmat(DBE).copy()
+    dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
+    Ei, Ef, hist = np.zeros(16), np.zeros(16), np.zeros(4 * maxit)
+    nit, conv = np.zeros(1, np.int64), np.zeros(1, np.int64)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_xcuhf_scf(s.nelec, nae, nbe, s.nucst if nucst is None else nucst, ne,
+                                 s.npebf, np_, s.nat, s.ngtg, s.pmass, *ptrs, opts, maxit,
+                                 _p(da), _p(db), _p(dp), _p(Ei), _p(Ef), _p(hist), _p(nit),
+                                 _p(conv)))
+    n = int(nit[0])
+    return {"initial": dict(zip(XCUHF_SLOTS, Ei.tolist())),
+            "final": dict(zip(XCUHF_SLOTS, Ef.tolist())),
+            "history": hist[:4 * n].reshape(n, 4), "niter": n, "converged": bool(conv[0]),
+            "DAE": da.reshape(ne, ne, order="F"), "DBE": db.reshape(ne, ne, order="F"),
+            "DP": dp.reshape(np_, np_, order="F")}
 
 
 class XchfJob(C.Structure):

@@ -233,3 +233,31 @@ def test_xcuhf_example_gpu_energetics(nx, xcuhf_example, golden_xcuhf):
     assert abs(S_total - ref["S_TOTAL"]) <= 6e-11 * ref["S_TOTAL"]
     for key, val in (("E_OMG1", E1), ("E_OMG2", E2), ("E_OMG3", E3), ("E_OMG4", E4)):
         assert abs(val / S_total - ref[key]) <= 6e-11, (key, val / S_total, ref[key])
+
+
+def test_xcuhf_device_scf_example(nx, xcuhf_example, golden_xcuhf):
+    """neoxc_xcuhf_scf on examples/xcuhf from the core-Hamiltonian guesses:
+    the initial energetics reproduce XCUHF.log:337-352 and the SCF reaches
+    the log's converged energy (XCUHF.log:366, reached there with SOSCF;
+    plain Roothaan and DIIS find the same stationary point)."""
+    x = xcuhf_example
+    s = x["s"]
+    names = {"E_NUC": "E_nuc", "E_ECORE": "E_ecore", "E_PCORE": "E_pcore", "E_EP": "E_ep",
+             "E_EE": "E_ee", "E_OMG1": "E_omg1", "E_OMG2": "E_omg2", "E_OMG3": "E_omg3",
+             "E_OMG4": "E_omg4", "S_TOTAL": "S_total", "E_TOTAL": "E_total"}
+    iters = {}
+    for diis in (False, True):
+        r = nx.xcuhf_scf(s, x["nae"], x["nbe"], diis=diis, maxit=250)
+        for key, mine in names.items():
+            ref = golden_xcuhf["initial"][key]
+            assert abs(r["initial"][mine] - ref) <= 6e-11 * max(1.0, abs(ref)), (key, diis)
+        assert r["converged"], (diis, r["history"][-3:])
+        fin = golden_xcuhf["final"]
+        print("XCUHF device SCF diis=%s: %d iterations, E = %.10f (log %.10f)"
+              % (diis, r["niter"], r["final"]["E_total"], fin["E_TOTAL"]))
+        assert abs(r["final"]["E_total"] - fin["E_TOTAL"]) <= 1e-8, r["final"]["E_total"]
+        for key in ("E_ECORE", "E_EP", "E_EE", "E_OMG1", "E_OMG2", "E_OMG3", "E_OMG4",
+                    "S_TOTAL"):
+            assert abs(r["final"][names[key]] - fin[key]) <= 2e-5 * max(1.0, abs(fin[key])), key
+        iters[diis] = r["niter"]
+    assert iters[True] < iters[False]
