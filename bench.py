@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--nebf", type=int, default=NEBF)
     ap.add_argument("--npbf", type=int, default=NPBF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf"], default=None,
+                    help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
 
 
@@ -581,6 +583,12 @@ def main():
     neoxc.lib()
     if not neoxc.device_ok():
         raise SystemExit("no usable GB300: " + neoxc.lib().neoxc_last_error().decode())
+    if args.only == "open_shell":
+        print(json.dumps(open_shell_section(neoxc, torch, dev, torch.cuda.current_stream(dev))))
+        return
+    if args.only == "xcuhf_scf":
+        print(json.dumps(xcuhf_scf_section(neoxc)))
+        return
     ne, np_ = args.nebf, args.npbf
     ng4 = ne ** 8 * np_ ** 2
     gee, g2s, DE, DP = synthetic_inputs(ne, np_)

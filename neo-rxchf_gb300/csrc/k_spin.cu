@@ -17,6 +17,8 @@
 // as bit masks, so FAE with swapped arguments (the reference's beta call)
 // and UFP's class B are the same code.  Per-CTA partials are reduced by a
 // second deterministic kernel (no floating-point atomics).
+#include <type_traits>
+
 #include "neoxc_internal.h"
 
 namespace neoxc {
@@ -33,20 +35,41 @@ __host__ __device__ inline long long pw(int ne, int e) {
   return r;
 }
 
-template <int K>
+// Ket block of one bra: the shared-memory copy (int strides) or the global
+// tensor (64-bit strides).
+template <int K, typename I>
 struct Slab {
-  const double* p;     // shared-memory copy or the global tensor
-  long long st[K];     // stride of each ket slot
+  const double* p;
+  I st[K];             // stride of each ket slot
   __device__ double operator()(const int* j) const {
-    long long o = 0;
+    I o = 0;
 #pragma unroll
-    for (int m = 0; m < K; m++) o += j[m] * st[m];
+    for (int m = 0; m < K; m++) o += (I)j[m] * st[m];
     return p[o];
   }
 };
 
+// Shared-memory pitches of the ket block: slot K-1 contiguous, every other
+// slot's pitch rounded up to an odd number of doubles, so lanes that differ
+// in any one ket index hit different banks.  Returns the padded size.
+__host__ __device__ inline int ket_pitches(int K, int ne, int* pt) {
+  pt[K - 1] = 1;
+  for (int m = K - 2; m >= 0; m--) pt[m] = (pt[m + 1] * ne) | 1;
+  return pt[0] * ne;
+}
+
+// x / d for x < 65536 and 2 <= d <= 256 with one multiply-high:
+// m = ceil(2^32 / d) is exact in that range.
+struct DivNe {
+  unsigned d, m;
+  __device__ explicit DivNe(int ne)
+      : d((unsigned)ne), m((unsigned)(((1ull << 32) + (unsigned)ne - 1) / (unsigned)ne)) {}
+  __device__ unsigned operator()(unsigned x) const { return d == 1 ? x : __umulhi(x, m); }
+};
+
 // K = 2: G(j1,j2), G(j2,j1)
-__device__ inline void acc2(const Slab<2>& g, int j1, int j2, double a2, double b2,
+template <typename S>
+__device__ inline void acc2(const S& g, int j1, int j2, double a2, double b2,
                             unsigned fa, unsigned fb, double& A, double& B) {
   const int k12[2] = {j1, j2}, k21[2] = {j2, j1};
   const double o12 = g(k12), o21 = g(k21);
@@ -58,7 +81,8 @@ __device__ inline void acc2(const Slab<2>& g, int j1, int j2, double a2, double 
 }
 
 // K = 3: OMG6 (bit0), the two mixed pairs OMG12/OMG13 (bit1), OMG23 (bit2)
-__device__ inline void acc3(const Slab<3>& g, const int* j, double a2, double b2,
+template <typename S>
+__device__ inline void acc3(const S& g, const int* j, double a2, double b2,
                             double a3, double b3, unsigned fa, unsigned fb,
                             double& A, double& B) {
   const int j1 = j[0], j2 = j[1], j3 = j[2];
@@ -79,7 +103,8 @@ __device__ inline void acc3(const Slab<3>& g, const int* j, double a2, double b2
 
 // K = 4: the 24-term set (bit0), the three 6-term sets (bit1), the three
 // 4-term sets (bit2) and the last 6-term set (bit3) of calc_FAEOMG4.
-__device__ inline void acc4(const Slab<4>& g, const int* j, const double* a,
+template <typename S>
+__device__ inline void acc4(const S& g, const int* j, const double* a,
                             const double* b, unsigned fa, unsigned fb, double& A,
                             double& B) {
   const int j1 = j[0], j2 = j[1], j3 = j[2], j4 = j[3];
@@ -126,22 +151,26 @@ __device__ inline void acc4(const Slab<4>& g, const int* j, const double* a,
   if (fb & 8u) B = fma(a[0] * a[1] * a[2], bbb, B);
 }
 
-// CTA (ipjp, i1, i2); loops over the remaining bras (i3[, i4]).
-// part[((cta)*nacc + a)*ne + j1], a = 2*tensor + class.
+// CTA (ipjp, i1, i2) for rank 2, (ipjp, i1, i2, i3) for ranks 3 and 4 (rank
+// 4 loops over i4).  Outputs per CTA: part[(cta*nacc + a)*ne + j1]
+// (a = 2*tensor + class; the electron Fock rows) and ppart[cta*2 + t] =
+// sum_j1 (DA(i1,j1) A_t[j1] + DB(i1,j1) B_t[j1]) (the proton terms).
 template <int K, bool SMEM>
 __global__ void __launch_bounds__(kSpinThreads)
 spin_kernel(int ne, int np, const double* __restrict__ G,
             const double* __restrict__ Gs, const double* __restrict__ DA,
             const double* __restrict__ DB, unsigned fa, unsigned fb,
-            double* __restrict__ part) {
+            double* __restrict__ part, double* __restrict__ ppart) {
   extern __shared__ double sm[];
   const int n2 = ne * ne;
   const int nten = (K == 2 && Gs) ? 2 : 1;
   const long long slab = pw(ne, K);
+  int pt[K];
+  const int slabp = ket_pitches(K, ne, pt);      // padded shared-memory block
   double* sDA = sm;
   double* sDB = sm + n2;
-  double* sG = sm + 2 * n2;                      // SMEM: nten * ne^K
-  double* sred = sG + (SMEM ? nten * slab : 0);  // [blockDim]
+  double* sG = sm + 2 * n2;                      // SMEM: nten * slabp
+  double* sred = sG + (SMEM ? nten * slabp : 0); // [blockDim]
   for (int k = threadIdx.x; k < n2; k += blockDim.x) {
     sDA[k] = DA[k];
     sDB[k] = DB[k];
@@ -149,6 +178,7 @@ spin_kernel(int ne, int np, const double* __restrict__ G,
   __syncthreads();
   int cta = blockIdx.x;
   int ib[4] = {0, 0, 0, 0};
+  if (K >= 3) { ib[2] = cta % ne; cta /= ne; }
   ib[1] = cta % ne; cta /= ne;
   ib[0] = cta % ne; cta /= ne;
   const long long ipjp = cta;
@@ -156,48 +186,59 @@ spin_kernel(int ne, int np, const double* __restrict__ G,
   const int j1 = threadIdx.x % ne;
   const int q0 = threadIdx.x / ne;
   const bool active = q0 < lanes;
-  const long long nrest = slab / ne;
+  const int nrest = (int)(slab / ne);
+  const DivNe dv(ne);
+  using I = typename std::conditional<SMEM, int, long long>::type;
+  long long gst[K];    // global stride of ket slot m: ne^(2(K-1-m))
+  for (int m = 0; m < K; m++) gst[m] = pw(ne, 2 * (K - 1 - m));
   double accA[2] = {0.0, 0.0}, accB[2] = {0.0, 0.0};
-  const int ninner = K == 2 ? 1 : (K == 3 ? ne : n2);
+  const int ninner = K == 4 ? ne : 1;
   for (int in = 0; in < ninner; in++) {
-    if (K >= 3) ib[2] = K == 3 ? in : in / ne;
-    if (K == 4) ib[3] = in % ne;
+    if (K == 4) ib[3] = in;
     long long base = ipjp * pw(ne, 2 * K);
-    for (int m = 0; m < K; m++) base += ib[m] * pw(ne, 2 * (K - 1 - m) + 1);
-    Slab<K> g[2];
+    for (int m = 0; m < K; m++) base += ib[m] * (gst[m] * ne);
+    Slab<K, I> g[2];
     for (int t = 0; t < 2; t++) {
       const double* src = t == 0 ? G : Gs;
       if (SMEM) {
-        g[t].p = sG + t * slab;
-        for (int m = 0; m < K; m++) g[t].st[m] = pw(ne, K - 1 - m);
+        g[t].p = sG + t * slabp;
+        for (int m = 0; m < K; m++) g[t].st[m] = (I)pt[m];
       } else {
         g[t].p = src ? src + base : nullptr;
-        for (int m = 0; m < K; m++) g[t].st[m] = pw(ne, 2 * (K - 1 - m));
+        for (int m = 0; m < K; m++) g[t].st[m] = (I)gst[m];
       }
     }
     if (SMEM) {
       __syncthreads();
       for (int t = 0; t < nten; t++) {
         const double* src = (t == 0 ? G : Gs) + base;
-        for (long long k = threadIdx.x; k < slab; k += blockDim.x) {
-          long long r = k, o = 0;
+        for (int k = threadIdx.x; k < (int)slab; k += blockDim.x) {
+          unsigned r = (unsigned)k;
+          long long o = 0;
+          int so = 0;
+#pragma unroll
           for (int m = K - 1; m >= 0; m--) {
-            o += (r % ne) * pw(ne, 2 * (K - 1 - m));
-            r /= ne;
+            const unsigned q = dv(r);
+            const int x = (int)(r - q * (unsigned)ne);
+            o += (long long)x * gst[m];
+            so += x * pt[m];
+            r = q;
           }
-          sG[t * slab + k] = __ldg(src + o);
+          sG[t * slabp + so] = __ldg(src + o);
         }
       }
       __syncthreads();
     }
     if (active) {
       double a[3], b[3];
-      for (long long q = q0; q < nrest; q += lanes) {
+      for (int q = q0; q < nrest; q += lanes) {
         int j[4] = {j1, 0, 0, 0};
-        long long r = q;
+        unsigned r = (unsigned)q;
+#pragma unroll
         for (int m = K - 1; m >= 1; m--) {
-          j[m] = (int)(r % ne);
-          r /= ne;
+          const unsigned qq = dv(r);
+          j[m] = (int)(r - qq * (unsigned)ne);
+          r = qq;
         }
         for (int m = 1; m < K; m++) {
           a[m - 1] = sDA[ib[m] + ne * j[m]];
@@ -214,8 +255,9 @@ spin_kernel(int ne, int np, const double* __restrict__ G,
       }
     }
   }
-  // reduce over the lanes of each j1
+  // reduce over the lanes of each j1; thread j1 keeps its row sums
   const int nacc = 2 * nten;
+  double row[4] = {0.0, 0.0, 0.0, 0.0};
   for (int acc = 0; acc < nacc; acc++) {
     __syncthreads();
     const double v = (acc & 1) ? accB[acc >> 1] : accA[acc >> 1];
@@ -225,48 +267,69 @@ spin_kernel(int ne, int np, const double* __restrict__ G,
       double s = 0.0;
       for (int t = threadIdx.x; t < lanes * ne; t += ne) s += sred[t];
       part[((size_t)blockIdx.x * nacc + acc) * ne + threadIdx.x] = s;
+      row[acc] = s;
+    }
+  }
+  // proton terms of this CTA: sum over j1 in a fixed order
+  for (int t = 0; t < nten; t++) {
+    __syncthreads();
+    if ((int)threadIdx.x < ne) {
+      const int j = threadIdx.x;
+      sred[j] = sDA[ib[0] + ne * j] * row[2 * t] + sDB[ib[0] + ne * j] * row[2 * t + 1];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int j = 0; j < ne; j++) s += sred[j];
+      ppart[(size_t)blockIdx.x * 2 + t] = s;
     }
   }
 }
 
-// fe_out[a][i1 + ne*j1] = sum_ipjp DP(ipjp) sum_i2 part;
-// fp_out[t][ip + np*jp] = sum_{i1,j1} (DA part_{2t} + DB part_{2t+1}).
-__global__ void spin_reduce_kernel(int ne, int np, int nacc,
-                                   const double* __restrict__ part,
-                                   const double* __restrict__ DA,
-                                   const double* __restrict__ DB,
-                                   const double* __restrict__ DP,
-                                   double* __restrict__ fe_out,
-                                   double* __restrict__ fp_out) {
-  const int n2 = ne * ne, p2 = np * np, nten = nacc / 2;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nacc * n2) {
-    const int a = t / n2, r = t - a * n2, i1 = r / ne, j1 = r - i1 * ne;
-    double s = 0.0;
-    for (int ipjp = 0; ipjp < p2; ipjp++) {
-      const int ip = ipjp / np, jp = ipjp - ip * np;
-      double ss = 0.0;
-      for (int i2 = 0; i2 < ne; i2++)
-        ss += part[(((size_t)(ipjp * ne + i1) * ne + i2) * nacc + a) * ne + j1];
-      s = fma(DP[ip + np * jp], ss, s);
-    }
-    fe_out[(size_t)a * n2 + i1 + ne * j1] = s;
-  } else if (t < nacc * n2 + nten * p2) {
-    const int u = t - nacc * n2, tn = u / p2, ipjp = u - tn * p2;
+// fe_out[a][i1 + ne*j1] = sum_ipjp DP(ipjp) sum_sub part; thread per
+// output, the CTAs of one (ipjp, i1) are nsub consecutive ones.
+__global__ void spin_reduce_e_kernel(int ne, int np, int nacc, int nsub,
+                                     const double* __restrict__ part,
+                                     const double* __restrict__ DP,
+                                     double* __restrict__ fe_out) {
+  // one warp per output; lanes take the nsub sub-blocks strided, then a
+  // fixed-order shuffle tree (deterministic)
+  const int n2 = ne * ne, p2 = np * np;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= nacc * n2) return;
+  const int a = t / n2, r = t - a * n2, i1 = r / ne, j1 = r - i1 * ne;
+  double s = 0.0;
+  for (int ipjp = 0; ipjp < p2; ipjp++) {
     const int ip = ipjp / np, jp = ipjp - ip * np;
-    double s = 0.0;
-    for (int i1 = 0; i1 < ne; i1++)
-      for (int j1 = 0; j1 < ne; j1++) {
-        double sa = 0.0, sb = 0.0;
-        for (int i2 = 0; i2 < ne; i2++) {
-          const size_t c = ((size_t)(ipjp * ne + i1) * ne + i2) * nacc;
-          sa += part[(c + 2 * tn) * ne + j1];
-          sb += part[(c + 2 * tn + 1) * ne + j1];
-        }
-        s = fma(DA[i1 + ne * j1], sa, fma(DB[i1 + ne * j1], sb, s));
-      }
-    fp_out[(size_t)tn * p2 + ip + np * jp] = s;
+    const size_t c0 = (size_t)(ipjp * ne + i1) * nsub;
+    double ss = 0.0;
+    for (int sb = lane; sb < nsub; sb += 32) ss += part[((c0 + sb) * nacc + a) * ne + j1];
+    s = fma(DP[ip + np * jp], ss, s);
   }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) fe_out[(size_t)a * n2 + i1 + ne * j1] = s;
+}
+
+// fp_out[t][ip + np*jp] = sum over the ne*nsub CTAs of (ipjp) of ppart;
+// one block per (t, ipjp), fixed-order tree reduction.
+__global__ void spin_reduce_p_kernel(int ne, int np, int nsub,
+                                     const double* __restrict__ ppart,
+                                     double* __restrict__ fp_out) {
+  __shared__ double red[256];
+  const int p2 = np * np;
+  const int tn = blockIdx.x / p2, ipjp = blockIdx.x - tn * p2;
+  const int ip = ipjp / np, jp = ipjp - ip * np;
+  const size_t c0 = (size_t)ipjp * ne * nsub, nc = (size_t)ne * nsub;
+  double s = 0.0;
+  for (size_t c = threadIdx.x; c < nc; c += blockDim.x) s += ppart[(c0 + c) * 2 + tn];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) fp_out[(size_t)tn * p2 + ip + np * jp] = red[0];
 }
 
 // GAM_1 / GAM_1s contractions (FAE_OMG1, UFP_OMG1): GAM_1[ip][jp][ie][je].
@@ -378,7 +441,9 @@ omg4_icr_kernel(int ne, int np, long long ng4, const double* __restrict__ gee,
 }  // namespace
 
 bool spin_smem_fits(int K, int ne) {
-  const long long slab = pw(ne, K);
+  if (ne < 1 || ne > kSpinThreads || pw(ne, K) > 65536) return false;
+  int pt[4];
+  const long long slab = ket_pitches(K, ne, pt);
   const int nten = K == 2 ? 2 : 1;
   return sizeof(double) * (2 * (size_t)ne * ne + nten * slab + kSpinThreads) <=
          200 * 1024;
@@ -389,18 +454,19 @@ namespace {
 template <int K, bool SMEM>
 cudaError_t launch_spin_kernel(int ne, int np, const double* G, const double* Gs,
                                const double* DA, const double* DB, unsigned fa,
-                               unsigned fb, double* part, cudaStream_t s) {
+                               unsigned fb, double* part, double* ppart, cudaStream_t s) {
   const int nten = (K == 2 && Gs) ? 2 : 1;
   const int lanes = kSpinThreads / ne;
   const int bs = ne * lanes;
-  const size_t smem = sizeof(double) *
-      (2 * (size_t)ne * ne + (SMEM ? nten * (size_t)pw(ne, K) : 0) + bs);
+  int pt[4];
+  const size_t slabp = (size_t)ket_pitches(K, ne, pt);
+  const size_t smem = sizeof(double) * (2 * (size_t)ne * ne + (SMEM ? nten * slabp : 0) + bs);
   cudaError_t e = cudaFuncSetAttribute(spin_kernel<K, SMEM>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const long long grid = (long long)np * np * ne * ne;
+  const long long grid = (long long)np * np * ne * ne * (K >= 3 ? ne : 1);
   spin_kernel<K, SMEM><<<(unsigned)grid, bs, smem, s>>>(ne, np, G, Gs, DA, DB, fa,
-                                                         fb, part);
+                                                         fb, part, ppart);
   return cudaGetLastError();
 }
 
@@ -408,8 +474,8 @@ cudaError_t launch_spin_kernel(int ne, int np, const double* G, const double* Gs
 
 size_t spin_scratch_doubles(int K, int ne, int np) {
   const int nacc = K == 2 ? 4 : 2;
-  return (size_t)np * np * ne * ne * nacc * ne + (size_t)nacc * ne * ne +
-         (size_t)2 * np * np;
+  const size_t ncta = (size_t)np * np * ne * ne * (K >= 3 ? ne : 1);
+  return ncta * nacc * ne + ncta * 2;
 }
 
 cudaError_t launch_spin_omg(int K, int ne, int np, const double* G, const double* Gs,
@@ -418,22 +484,29 @@ cudaError_t launch_spin_omg(int K, int ne, int np, const double* G, const double
                             double* fe_out, double* fp_out, cudaStream_t s) {
   if (ne < 1 || ne > kSpinThreads || np < 1 || K < 2 || K > 4 || (K != 2 && Gs))
     return cudaErrorInvalidValue;
+  const int nacc = (K == 2 && Gs) ? 4 : 2;
+  const size_t ncta = (size_t)np * np * ne * ne * (K >= 3 ? ne : 1);
+  double* part = scratch;
+  double* ppart = scratch + ncta * (K == 2 ? 4 : 2) * ne;
   cudaError_t e;
   const bool fits = spin_smem_fits(K, ne);
   if (K == 2)
-    e = fits ? launch_spin_kernel<2, true>(ne, np, G, Gs, DA, DB, fa, fb, scratch, s)
-             : launch_spin_kernel<2, false>(ne, np, G, Gs, DA, DB, fa, fb, scratch, s);
+    e = fits ? launch_spin_kernel<2, true>(ne, np, G, Gs, DA, DB, fa, fb, part, ppart, s)
+             : launch_spin_kernel<2, false>(ne, np, G, Gs, DA, DB, fa, fb, part, ppart, s);
   else if (!fits)   // ranks 3 and 4 stage the whole ket block
     return cudaErrorInvalidValue;
   else if (K == 3)
-    e = launch_spin_kernel<3, true>(ne, np, G, nullptr, DA, DB, fa, fb, scratch, s);
+    e = launch_spin_kernel<3, true>(ne, np, G, nullptr, DA, DB, fa, fb, part, ppart, s);
   else
-    e = launch_spin_kernel<4, true>(ne, np, G, nullptr, DA, DB, fa, fb, scratch, s);
+    e = launch_spin_kernel<4, true>(ne, np, G, nullptr, DA, DB, fa, fb, part, ppart, s);
   if (e != cudaSuccess) return e;
-  const int nacc = (K == 2 && Gs) ? 4 : 2;
-  const int nout = nacc * ne * ne + (nacc / 2) * np * np;
-  spin_reduce_kernel<<<(nout + 127) / 128, 128, 0, s>>>(ne, np, nacc, scratch, DA, DB,
-                                                         DP, fe_out, fp_out);
+  const int nsub = K == 2 ? ne : ne * ne;
+  const int ne_out = nacc * ne * ne;
+  spin_reduce_e_kernel<<<(ne_out + 3) / 4, 128, 0, s>>>(ne, np, nacc, nsub, part, DP,
+                                                        fe_out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  spin_reduce_p_kernel<<<(nacc / 2) * np * np, 256, 0, s>>>(ne, np, nsub, ppart, fp_out);
   return cudaGetLastError();
 }
 
