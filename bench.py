@@ -347,8 +347,10 @@ def open_shell_section(neoxc, torch, dev, stream):
     """XCUHF in-core contractions (k_spin.cu): one neoxc_dev_xcuhf_omg call
     gives FAE_OMGk, FAE_OMGk for beta and UFP_OMGk (three reference routines)
     from one pass over the stored tensor.  Tensors larger than L2, seeded on
-    the device; NAE = NBE = 2.  Roofline: HBM, algorithmic bytes = one read
-    of the tensor(s) per call."""
+    the device; NAE = NBE = 2.  The tensor is read once (algorithmic bytes,
+    reported against HBM), but the bound is the FP64 pipe: ncu shows 90 %
+    FP64-pipe activity and 3.5 % DRAM for rank 3
+    (profiles/spin_kernel_rank3_open_shell.md)."""
     f64 = torch.float64
     peak = read_hbm_peak()
     out = {"api": "neoxc_dev_xcuhf_omg (device)", "peak_gbs": peak}
@@ -393,9 +395,10 @@ def open_shell_section(neoxc, torch, dev, stream):
         gbs = nbytes / (ms * 1e-3) / 1e9
         out["omg%d" % k] = {"nebf": ne, "npbf": np_, "tensor_GB": nbytes / 1e9,
                             "ms_per_call": ms, "elements_per_s": n / (ms * 1e-3),
-                            "roofline": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
-                                         "peak": peak, "frac": gbs / peak if peak else None,
-                                         "algorithmic_bytes": nbytes},
+                            "hbm": {"achieved": gbs, "unit": "GB/s", "peak": peak,
+                                    "frac": gbs / peak if peak else None,
+                                    "algorithmic_bytes": nbytes},
+                            "bound": "fp64",
                             "launches_per_call": 5}
         del G, Gs
         torch.cuda.empty_cache()

@@ -67,9 +67,15 @@ __device__ __forceinline__ void perm3(const P* X, int a, int b, int c, P* Y) {
 // (FP64 integrals) or md32::Prim (FP32 integrals of the mixed path); the
 // integral calls resolve to md:: / md32:: by argument-dependent lookup and
 // every sum over geminal terms is FP64 in both.
+//
+// The reference's result is a linear combination over geminal terms,
+//   ansE = sum_k b_k T1(k) + sum_kl b_k b_l T2(k,l),  ansS = sum_kl b_k b_l S2(k,l),
+// so one primitive tuple is split into ng + ng^2 independent work items
+// (gi < ng: single-geminal term k = gi; else the pair (k,l)) that the lanes
+// of a warp share.
 template <class P, class G3T>
-__device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
-                           G3T& st, double& ansE, double& ansS) {
+__device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
+                                G3T& st, int gi, double& ansE, double& ansS) {
   using R = typename std::remove_cv<decltype(P::a)>::type;
   const int ng = S.ngtg, nat = S.nat;
   const double* b = S.bgem;
@@ -92,8 +98,8 @@ __device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
     const R C3[3] = {(R)S.cat[3 * ia], (R)S.cat[3 * ia + 1], (R)S.cat[3 * ia + 2]};
     return md::underflow((double)g3_vxc(st, C3));
   };
-  double gTE = 0, gVEC = 0, gVEE = 0, gVEP = 0;
-  for (int ik = 0; ik < ng; ik++) {
+  if (gi < ng) {
+    const int ik = gi;
     gam6(g, A23, (R)gm[ik], -1, zero);
     g3_setup_pairs(st, A, B, pr, g, 2);
     double xgTE = (double)g3_ke(st, zero, one);
@@ -103,78 +109,65 @@ __device__ void xcalc_gam2(const P* A, const P* B, const DevSystem& S,
     double xgVEE = md::underflow((double)g3_vee(st));
     g3_setup_pairs(st, A132, B132, pr132, g, 0);
     double xgVEP = -md::underflow((double)g3_vee(st));
-    gTE = gTE + b[ik] * xgTE;
-    gVEC = gVEC + b[ik] * xgVEC;
-    gVEP = gVEP + b[ik] * xgVEP;
-    gVEE = gVEE + b[ik] * xgVEE;
+    // 2 (gTE + gVEC + gVEP) + 4 gVEE / 2
+    ansE = 2.0 * (b[ik] * xgTE + b[ik] * xgVEC + b[ik] * xgVEP) + 4.0 * (b[ik] * xgVEE) * 0.5;
+    ansS = 0.0;
+    return;
   }
-  double gTPg = 0, gTEg1 = 0, gTEg2 = 0, gTEg3 = 0, gVPCg = 0, gVECg1 = 0,
-         gVECg2 = 0, gVEPg1 = 0, gVEPg2 = 0, gVEEg1 = 0, gVEEg2 = 0, gsg = 0;
-  for (int ik = 0; ik < ng; ik++)
-    for (int il = 0; il < ng; il++) {
-      const R gk = (R)gm[ik], gl = (R)gm[il];
-      const double bb = b[ik] * b[il];
-      // order (p, e1, e2): gA12 = g(p,e1), gB13 = g(p,e2)
-      gam6(g, A12, gk, B13, gl);
-      g3_setup_pairs(st, A312, B312, pr312, g, 2);
-      double xgTPg = (double)g3_ke(st, gl, (R)S.pmass);
-      double xgVPCg = 0.0;
-      for (int ia = 0; ia < nat; ia++)
-        xgVPCg = xgVPCg + S.zan[ia] * vxc(ia);
-      // order (e1, e2, p): A13, B23
-      gam6(g, A13, gk, B23, gl);
-      g3_setup_pairs(st, A, B, pr, g, 2);
-      double xgTEg1 = (double)g3_ke(st, zero, one);
-      double xgVECg1 = 0.0;
-      for (int ia = 0; ia < nat; ia++)
-        xgVECg1 = xgVECg1 - S.zan[ia] * vxc(ia);
-      double xgVEEg2 = md::underflow((double)g3_vee(st));
-      double xgsg = (double)g3_overlap(st);
-      // A23, B13
-      gam6(g, A23, gk, B13, gl);
-      g3_setup_pairs(st, A, B, pr, g, 2);
-      double xgTEg2 = (double)g3_ke(st, gl, one);
-      // A23, B23
-      gam6(g, A23, gk, B23, gl);
-      g3_setup_pairs(st, A, B, pr, g, 2);
-      double xgTEg3 = (double)g3_ke(st, zero, one);
-      double xgVECg2 = 0.0;
-      for (int ia = 0; ia < nat; ia++)
-        xgVECg2 = xgVECg2 - S.zan[ia] * vxc(ia);
-      // A13, B13
-      gam6(g, A13, gk, B13, gl);
-      g3_setup_pairs(st, A, B, pr, g, 0);
-      double xgVEEg1 = md::underflow((double)g3_vee(st));
-      // order (e1, p, e2): A12 B23 and A23 B23
-      gam6(g, A12, gk, B23, gl);
-      g3_setup_pairs(st, A132, B132, pr132, g, 0);
-      double xgVEPg1 = -md::underflow((double)g3_vee(st));
-      gam6(g, A23, gk, B23, gl);
-      g3_setup_pairs(st, A132, B132, pr132, g, 0);
-      double xgVEPg2 = -md::underflow((double)g3_vee(st));
-      gTPg = gTPg + bb * xgTPg;
-      gTEg1 = gTEg1 + bb * xgTEg1;
-      gTEg2 = gTEg2 + bb * xgTEg2;
-      gTEg3 = gTEg3 + bb * xgTEg3;
-      gVPCg = gVPCg + bb * xgVPCg;
-      gVECg1 = gVECg1 + bb * xgVECg1;
-      gVECg2 = gVECg2 + bb * xgVECg2;
-      gVEPg1 = gVEPg1 + bb * xgVEPg1;
-      gVEPg2 = gVEPg2 + bb * xgVEPg2;
-      gVEEg1 = gVEEg1 + bb * xgVEEg1;
-      gVEEg2 = gVEEg2 + bb * xgVEEg2;
-      gsg = gsg + bb * xgsg;
-    }
-  ansE = 2.0 * (gTE + gVEC + gVEP) + 4.0 * gVEE * 0.5 + gTPg + gVPCg + gTEg1 +
-         gTEg3 + 2.0 * (gVEPg1 + gVECg1) + gTEg2 + gVEPg2 + gVECg2 +
-         2.0 * gVEEg1 * 0.5 + 2.0 * gVEEg2 * 0.5;
-  ansS = gsg;
+  const int ik = (gi - ng) / ng, il = (gi - ng) - ik * ng;
+  const R gk = (R)gm[ik], gl = (R)gm[il];
+  const double bb = b[ik] * b[il];
+  // order (p, e1, e2): gA12 = g(p,e1), gB13 = g(p,e2)
+  gam6(g, A12, gk, B13, gl);
+  g3_setup_pairs(st, A312, B312, pr312, g, 2);
+  double xgTPg = (double)g3_ke(st, gl, (R)S.pmass);
+  double xgVPCg = 0.0;
+  for (int ia = 0; ia < nat; ia++)
+    xgVPCg = xgVPCg + S.zan[ia] * vxc(ia);
+  // order (e1, e2, p): A13, B23
+  gam6(g, A13, gk, B23, gl);
+  g3_setup_pairs(st, A, B, pr, g, 2);
+  double xgTEg1 = (double)g3_ke(st, zero, one);
+  double xgVECg1 = 0.0;
+  for (int ia = 0; ia < nat; ia++)
+    xgVECg1 = xgVECg1 - S.zan[ia] * vxc(ia);
+  double xgVEEg2 = md::underflow((double)g3_vee(st));
+  double xgsg = (double)g3_overlap(st);
+  // A23, B13
+  gam6(g, A23, gk, B13, gl);
+  g3_setup_pairs(st, A, B, pr, g, 2);
+  double xgTEg2 = (double)g3_ke(st, gl, one);
+  // A23, B23
+  gam6(g, A23, gk, B23, gl);
+  g3_setup_pairs(st, A, B, pr, g, 2);
+  double xgTEg3 = (double)g3_ke(st, zero, one);
+  double xgVECg2 = 0.0;
+  for (int ia = 0; ia < nat; ia++)
+    xgVECg2 = xgVECg2 - S.zan[ia] * vxc(ia);
+  // A13, B13
+  gam6(g, A13, gk, B13, gl);
+  g3_setup_pairs(st, A, B, pr, g, 0);
+  double xgVEEg1 = md::underflow((double)g3_vee(st));
+  // order (e1, p, e2): A12 B23 and A23 B23
+  gam6(g, A12, gk, B23, gl);
+  g3_setup_pairs(st, A132, B132, pr132, g, 0);
+  double xgVEPg1 = -md::underflow((double)g3_vee(st));
+  gam6(g, A23, gk, B23, gl);
+  g3_setup_pairs(st, A132, B132, pr132, g, 0);
+  double xgVEPg2 = -md::underflow((double)g3_vee(st));
+  // gTPg + gVPCg + gTEg1 + gTEg3 + 2 (gVEPg1 + gVECg1) + gTEg2 + gVEPg2 +
+  // gVECg2 + 2 gVEEg1 / 2 + 2 gVEEg2 / 2
+  ansE = bb * xgTPg + bb * xgVPCg + bb * xgTEg1 + bb * xgTEg3 +
+         2.0 * (bb * xgVEPg1 + bb * xgVECg1) + bb * xgTEg2 + bb * xgVEPg2 +
+         bb * xgVECg2 + 2.0 * (bb * xgVEEg1) * 0.5 + 2.0 * (bb * xgVEEg2) * 0.5;
+  ansS = bb * xgsg;
 }
 
-// rxchfne/rxchfne_gam_2_OMP.f:2-530 (live terms :409-456)
-__device__ void xcalc_gam2_rx(const Prim* A, const Prim* B,
-                              const DevSystem& S, G3& st, double& ansE1,
-                              double& ansE2) {
+// rxchfne/rxchfne_gam_2_OMP.f:2-530 (live terms :409-456): one geminal pair
+// (ik, il) = (gi / ng, gi % ng) per work item:
+//   ansE1 = bb (xgVEPg2 + xgVEEg1), ansE2 = bb xgVEEg2.
+__device__ void xcalc_gam2_rx_item(const Prim* A, const Prim* B, const DevSystem& S,
+                                   G3& st, int gi, double& ansE1, double& ansE2) {
   const int ng = S.ngtg;
   const double* b = S.bgem;
   const double* gm = S.ggem;
@@ -184,24 +177,19 @@ __device__ void xcalc_gam2_rx(const Prim* A, const Prim* B,
   md::Pair pr[3], pr321[3];
   for (int i = 0; i < 3; i++) md::gauss_pair(A[i], B[i], pr[i]);
   perm3(pr, 2, 1, 0, pr321);
-  double g[6], gVEPg2 = 0, gVEEg1 = 0, gVEEg2 = 0;
-  for (int ik = 0; ik < ng; ik++)
-    for (int il = 0; il < ng; il++) {
-      const double gk = gm[ik], gl = gm[il], bb = b[ik] * b[il];
-      gam6(g, A13, gk, B13, gl);
-      md::g3_setup_pairs(st, A321, B321, pr321, g, 0);
-      double xgVEPg2 = -md::underflow(md::g3_vee(st));
-      md::g3_setup_pairs(st, A, B, pr, g, 0);
-      double xgVEEg1 = md::underflow(md::g3_vee(st));
-      gam6(g, A13, gk, B23, gl);
-      md::g3_setup_pairs(st, A, B, pr, g, 0);
-      double xgVEEg2 = md::underflow(md::g3_vee(st));
-      gVEPg2 = gVEPg2 + bb * xgVEPg2;
-      gVEEg1 = gVEEg1 + bb * xgVEEg1;
-      gVEEg2 = gVEEg2 + bb * xgVEEg2;
-    }
-  ansE1 = gVEPg2 + gVEEg1;
-  ansE2 = gVEEg2;
+  double g[6];
+  const int ik = gi / ng, il = gi - ik * ng;
+  const double gk = gm[ik], gl = gm[il], bb = b[ik] * b[il];
+  gam6(g, A13, gk, B13, gl);
+  md::g3_setup_pairs(st, A321, B321, pr321, g, 0);
+  double xgVEPg2 = -md::underflow(md::g3_vee(st));
+  md::g3_setup_pairs(st, A, B, pr, g, 0);
+  double xgVEEg1 = md::underflow(md::g3_vee(st));
+  gam6(g, A13, gk, B23, gl);
+  md::g3_setup_pairs(st, A, B, pr, g, 0);
+  double xgVEEg2 = md::underflow(md::g3_vee(st));
+  ansE1 = bb * xgVEPg2 + bb * xgVEEg1;
+  ansE2 = bb * xgVEEg2;
 }
 
 // gam_3_OMP.f:617-984 xcalc_GAM3_MD, particles (e1, e2, e3, p):
@@ -247,30 +235,41 @@ __device__ __forceinline__ md32::Prim to_prim32(const DevPrim& d) {
   return p;
 }
 
-// ---- GAM_ee: thread per contracted (iec1,jec1,iec2,jec2) ------------------
+// ---- GAM_ee: warp per contracted (iec1,jec1,iec2,jec2) ----------------------
+// lanes share the primitive quartets; warp-shuffle contraction.
 __global__ void __launch_bounds__(128)
 gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
   const int ne = S.nebf;
   const long long n4 = (long long)ne * ne * ne * ne;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n4;
-       t += (long long)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * blockDim.x / 32;
+  for (long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32; t < n4;
+       t += nw) {
     // pack_4D(jec2, iec2, jec1, iec1) - 1 == t
     long long r = t;
     const int jc2 = (int)(r % ne); r /= ne;
     const int ic2 = (int)(r % ne); r /= ne;
     const int jc1 = (int)(r % ne); r /= ne;
     const int ic1 = (int)r;
+    const int s1 = S.kpestr[ic1], n1 = S.kpeend[ic1] - s1 + 1;
+    const int t1 = S.kpestr[jc1], m1 = S.kpeend[jc1] - t1 + 1;
+    const int s2 = S.kpestr[ic2], n2 = S.kpeend[ic2] - s2 + 1;
+    const int t2 = S.kpestr[jc2], m2 = S.kpeend[jc2] - t2 + 1;
+    const int nq = n1 * m1 * n2 * m2;
     double acc = 0.0;
-    for (int i1 = S.kpestr[ic1]; i1 <= S.kpeend[ic1]; i1++)
-      for (int j1 = S.kpestr[jc1]; j1 <= S.kpeend[jc1]; j1++)
-        for (int i2 = S.kpestr[ic2]; i2 <= S.kpeend[ic2]; i2++)
-          for (int j2 = S.kpestr[jc2]; j2 <= S.kpeend[jc2]; j2++) {
-            const DevPrim &a1 = S.eprim[i1], &a2 = S.eprim[i2];
-            const DevPrim &b1 = S.eprim[j1], &b2 = S.eprim[j2];
-            double v = md::gfvee(to_prim(a1), to_prim(a2), to_prim(b1), to_prim(b2));
-            acc = acc + v * a1.coef * b1.coef * a2.coef * b2.coef;
-          }
-    gee[t] = acc;
+    for (int q = lane; q < nq; q += 32) {
+      int qq = q;
+      const int j2 = t2 + qq % m2; qq /= m2;
+      const int i2 = s2 + qq % n2; qq /= n2;
+      const int j1 = t1 + qq % m1; qq /= m1;
+      const int i1 = s1 + qq;
+      const DevPrim &a1 = S.eprim[i1], &a2 = S.eprim[i2];
+      const DevPrim &b1 = S.eprim[j1], &b2 = S.eprim[j2];
+      double v = md::gfvee(to_prim(a1), to_prim(a2), to_prim(b1), to_prim(b2));
+      acc = acc + v * a1.coef * b1.coef * a2.coef * b2.coef;
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) gee[t] = acc;
   }
 }
 
@@ -295,13 +294,18 @@ gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
   const int s_i2 = S.kpestr[ic2], n_i2 = S.kpeend[ic2] - s_i2 + 1;
   const int s_j2 = S.kpestr[jc2], n_j2 = S.kpeend[jc2] - s_j2 + 1;
   const int nq = n_i1 * n_j1 * n_i2 * n_j2;
+  const int ng = S.ngtg;
+  const int nitem = RX ? ng * ng : ng + ng * ng;   // geminal work items
   const DevPrim& pa = S.pprim[ip];
   const DevPrim& pb = S.pprim[jp];
   const double cp = pa.coef * pb.coef;
   typename std::conditional<F32, md32::G3, G3>::type st;
   double o1 = 0.0, o2 = 0.0;
-  for (int q = lane; q < nq; q += 32) {
-    int qq = q;
+  // lanes take (geminal item, primitive combination) pairs, the primitive
+  // combination fastest so that neighbouring lanes share the geminal item
+  for (int q2 = lane; q2 < nq * nitem; q2 += 32) {
+    const int gi = q2 / nq;
+    int qq = q2 - gi * nq;
     const int j2 = s_j2 + qq % n_j2; qq /= n_j2;
     const int i2 = s_i2 + qq % n_i2; qq /= n_i2;
     const int j1 = s_j1 + qq % n_j1; qq /= n_j1;
@@ -310,12 +314,12 @@ gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
     if constexpr (F32) {
       md32::Prim A[3] = {to_prim32(S.eprim[i1]), to_prim32(S.eprim[i2]), to_prim32(pa)};
       md32::Prim B[3] = {to_prim32(S.eprim[j1]), to_prim32(S.eprim[j2]), to_prim32(pb)};
-      xcalc_gam2(A, B, S, st, a1, a2);
+      xcalc_gam2_item(A, B, S, st, gi, a1, a2);
     } else {
       Prim A[3] = {to_prim(S.eprim[i1]), to_prim(S.eprim[i2]), to_prim(pa)};
       Prim B[3] = {to_prim(S.eprim[j1]), to_prim(S.eprim[j2]), to_prim(pb)};
-      if (RX) xcalc_gam2_rx(A, B, S, st, a1, a2);
-      else xcalc_gam2(A, B, S, st, a1, a2);
+      if (RX) xcalc_gam2_rx_item(A, B, S, st, gi, a1, a2);
+      else xcalc_gam2_item(A, B, S, st, gi, a1, a2);
     }
     const double c = cp * S.eprim[i1].coef * S.eprim[j1].coef *
                      S.eprim[i2].coef * S.eprim[j2].coef;
@@ -569,7 +573,7 @@ __global__ void gam3_sym_kernel(int ne, int np, double* __restrict__ g,
 
 cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s) {
   const long long n4 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf;
-  long long blocks = (n4 + 127) / 128;
+  long long blocks = (n4 * 32 + 127) / 128;   // a warp per contracted quartet
   if (blocks > 152 * 64) blocks = 152 * 64;
   gam_ee_kernel<<<(unsigned)blocks, 128, 0, s>>>(sys, gee);
   return cudaGetLastError();

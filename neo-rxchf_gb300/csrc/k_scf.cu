@@ -105,23 +105,23 @@ __global__ void gam_ep_kernel(DevSystem S, double* __restrict__ Gep) {
 }
 
 // ---- gam_1 (gam_1_OMP.f:398-836 xcalc_GAM1_MD) -----------------------------
-// A = (e, p), B = (e', p'); returns ansE, ansS.  P is md::Prim (FP64) or
-// md32::Prim (FP32 integrals, mixed path); the integral calls resolve by
-// argument-dependent lookup and every geminal/atom sum is FP64.
+// A = (e, p), B = (e', p'); one geminal work item of the reference's
+// result (gi < ng: the single-geminal terms of k = gi; else the pair
+// (k, l)): ansE = TE + TP - VCE + VCP - VMX and ansS = 2 OGX + OGG are
+// linear in these items, so the lanes of a warp share them.  P is md::Prim
+// (FP64) or md32::Prim (FP32 integrals, mixed path); the integral calls
+// resolve by argument-dependent lookup and every geminal/atom sum is FP64.
 template <class P>
-__device__ __noinline__ void xcalc_gam1(const P* A, const P* B,
-                                        const DevSystem& S, double* ansE,
-                                        double* ansS) {
+__device__ __noinline__ void xcalc_gam1_item(const P* A, const P* B, const DevSystem& S,
+                                             int gi, double* ansE, double* ansS) {
   using R = typename std::remove_cv<decltype(P::a)>::type;
   const R zero = R(0.0), one = R(1.0), pmass = (R)S.pmass;
-  double tegx = 0.0, tpgx = 0.0, texg = 0.0, tpxg = 0.0, tegg = 0.0,
-         tpgg = 0.0, VCEGX = 0.0, VCEGG = 0.0, VCPGX = 0.0, VCPGG = 0.0,
-         VMGX = 0.0, VMGG = 0.0;
-  for (int k = 0; k < S.ngtg; k++) {
-    const R GV = (R)S.ggem[k];
-    const double BV = S.bgem[k];
-    tegx = tegx + BV * (double)pgike1(A[0], A[1], B[0], B[1], GV, zero, one);
-    tpgx = tpgx + BV * (double)pgike1(A[1], A[0], B[1], B[0], GV, zero, pmass);
+  const int ng = S.ngtg;
+  if (gi < ng) {
+    const R GV = (R)S.ggem[gi];
+    const double BV = S.bgem[gi];
+    const double tegx = BV * (double)pgike1(A[0], A[1], B[0], B[1], GV, zero, one);
+    const double tpgx = BV * (double)pgike1(A[1], A[0], B[1], B[0], GV, zero, pmass);
     double ve = 0.0, vp = 0.0;
     for (int c = 0; c < S.nat; c++) {
       const R C[3] = {(R)S.cat[3 * c], (R)S.cat[3 * c + 1], (R)S.cat[3 * c + 2]};
@@ -129,42 +129,28 @@ __device__ __noinline__ void xcalc_gam1(const P* A, const P* B,
       vp = (double)g2_xggvec(A[1], A[0], B[1], B[0], GV, zero, C) * S.zan[c] + vp;
     }
     const double vm = (double)g2_xggvee(A[0], A[1], B[0], B[1], GV, zero);
-    VCEGX = VCEGX + BV * ve;
-    VCPGX = VCPGX + BV * vp;
-    VMGX = VMGX + BV * vm;
-    texg = texg + BV * (double)pgike1(A[0], A[1], B[0], B[1], zero, GV, one);
-    tpxg = tpxg + BV * (double)pgike1(A[1], A[0], B[1], B[0], zero, GV, pmass);
-    for (int l = 0; l < S.ngtg; l++) {
-      const R GW = (R)S.ggem[l];
-      const double BW = S.bgem[l];
-      tegg = tegg + BV * BW * (double)pgike1(A[0], A[1], B[0], B[1], GV, GW, one);
-      tpgg = tpgg + BV * BW * (double)pgike1(A[1], A[0], B[1], B[0], GV, GW, pmass);
-      double vee = 0.0, vpp = 0.0;
-      for (int c = 0; c < S.nat; c++) {
-        const R C[3] = {(R)S.cat[3 * c], (R)S.cat[3 * c + 1], (R)S.cat[3 * c + 2]};
-        vee = (double)g2_xggvec(A[0], A[1], B[0], B[1], GV, GW, C) * S.zan[c] + vee;
-        vpp = (double)g2_xggvec(A[1], A[0], B[1], B[0], GV, GW, C) * S.zan[c] + vpp;
-      }
-      const double vmm = (double)g2_xggvee(A[0], A[1], B[0], B[1], GV, GW);
-      VCEGG = VCEGG + BV * BW * vee;
-      VCPGG = VCPGG + BV * BW * vpp;
-      VMGG = VMGG + BV * BW * vmm;
-    }
+    const double texg = BV * (double)pgike1(A[0], A[1], B[0], B[1], zero, GV, one);
+    const double tpxg = BV * (double)pgike1(A[1], A[0], B[1], B[0], zero, GV, pmass);
+    // TE + TP - 2 VCEGX + 2 VCPGX - 2 VMGX (this k's share)
+    *ansE = (tegx + texg) + (tpgx + tpxg) - 2.0 * (BV * ve) + 2.0 * (BV * vp) -
+            2.0 * (BV * vm);
+    *ansS = 2.0 * (BV * (double)g2_xggs(A[0], A[1], B[0], B[1], GV, zero));
+    return;
   }
-  const double TE = tegx + texg + tegg, TP = tpgx + tpxg + tpgg;
-  const double VCE = 2.0 * VCEGX + VCEGG, VCP = 2.0 * VCPGX + VCPGG;
-  const double VMX = 2.0 * VMGX + VMGG;
-  *ansE = TE + TP - VCE + VCP - VMX;
-  double OGX = 0.0, OGG = 0.0;
-  for (int k = 0; k < S.ngtg; k++) {
-    const R GV = (R)S.ggem[k];
-    const double BV = S.bgem[k];
-    OGX = OGX + BV * (double)g2_xggs(A[0], A[1], B[0], B[1], GV, zero);
-    for (int l = 0; l < S.ngtg; l++)
-      OGG = OGG + BV * S.bgem[l] *
-                      (double)g2_xggs(A[0], A[1], B[0], B[1], GV, (R)S.ggem[l]);
+  const int k = (gi - ng) / ng, l = (gi - ng) - k * ng;
+  const R GV = (R)S.ggem[k], GW = (R)S.ggem[l];
+  const double BB = S.bgem[k] * S.bgem[l];
+  const double tegg = BB * (double)pgike1(A[0], A[1], B[0], B[1], GV, GW, one);
+  const double tpgg = BB * (double)pgike1(A[1], A[0], B[1], B[0], GV, GW, pmass);
+  double vee = 0.0, vpp = 0.0;
+  for (int c = 0; c < S.nat; c++) {
+    const R C[3] = {(R)S.cat[3 * c], (R)S.cat[3 * c + 1], (R)S.cat[3 * c + 2]};
+    vee = (double)g2_xggvec(A[0], A[1], B[0], B[1], GV, GW, C) * S.zan[c] + vee;
+    vpp = (double)g2_xggvec(A[1], A[0], B[1], B[0], GV, GW, C) * S.zan[c] + vpp;
   }
-  *ansS = 2.0 * OGX + OGG;
+  const double vmm = (double)g2_xggvee(A[0], A[1], B[0], B[1], GV, GW);
+  *ansE = tegg + tpgg - BB * vee + BB * vpp - BB * vmm;
+  *ansS = BB * (double)g2_xggs(A[0], A[1], B[0], B[1], GV, GW);
 }
 
 __device__ __forceinline__ md32::Prim to_prim32(const DevPrim& p) {
@@ -194,18 +180,21 @@ __global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
   const int ip = r;
   const int na = S.kpeend[ie] - S.kpestr[ie] + 1;
   const int nb = S.kpeend[je] - S.kpestr[je] + 1;
+  const int nq = na * nb, ng = S.ngtg;
   double e = 0.0, sv = 0.0;
-  for (int k = lane; k < na * nb; k += 32) {
+  // lanes take (geminal item, primitive pair), the pair fastest
+  for (int q2 = lane; q2 < nq * (ng + ng * ng); q2 += 32) {
+    const int gi = q2 / nq, k = q2 - gi * nq;
     const int a = S.kpestr[ie] + k / nb, b = S.kpestr[je] + k % nb;
     double aE, aS;
     if constexpr (F32) {
       md32::Prim A[2] = {to_prim32(S.eprim[a]), to_prim32(S.pprim[ip])};
       md32::Prim B[2] = {to_prim32(S.eprim[b]), to_prim32(S.pprim[jp])};
-      xcalc_gam1(A, B, S, &aE, &aS);
+      xcalc_gam1_item(A, B, S, gi, &aE, &aS);
     } else {
       Prim A[2] = {to_prim(S.eprim[a]), to_prim(S.pprim[ip])};
       Prim B[2] = {to_prim(S.eprim[b]), to_prim(S.pprim[jp])};
-      xcalc_gam1(A, B, S, &aE, &aS);
+      xcalc_gam1_item(A, B, S, gi, &aE, &aS);
     }
     const double cip = S.pprim[ip].coef, cjp = S.pprim[jp].coef;
     const double cie = S.eprim[a].coef, cje = S.eprim[b].coef;
@@ -225,6 +214,8 @@ __global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
 // ---- one-body part of xchf1_fock (E_from_GAM_ecore/pcore/ep/ee/1, S_from_GAM_1s)
 // t < ne^2 : electronic (i,j);  ne^2 <= t < ne^2+np^2 : nuclear (p,q).
 // part[c*nt + t]: c = 0 E_ecore, 1 E_pcore, 2 E_ep, 3 E_ee, 4 E_gam1, 5 S_gam1.
+// xfocke / xfockp (optional): the NEO-HF part without GAM_1 (xchf1_fock.f's
+// Xfocke / Xfockp, :218-219).
 __global__ void fock1_kernel(int ne, int np, int nelec,
                              const double* __restrict__ Hce,
                              const double* __restrict__ Hcp,
@@ -236,7 +227,9 @@ __global__ void fock1_kernel(int ne, int np, int nelec,
                              const double* __restrict__ DP,
                              double* __restrict__ focke, double* __restrict__ fockp,
                              double* __restrict__ se1, double* __restrict__ sp1,
-                             double* __restrict__ part) {
+                             double* __restrict__ part,
+                             double* __restrict__ xfocke,
+                             double* __restrict__ xfockp) {
   const int nt = ne * ne + np * np;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
@@ -264,6 +257,7 @@ __global__ void fock1_kernel(int ne, int np, int nelec,
         }
     }
     focke[i + ne * j] = fc + fep + fee + fg1;
+    if (xfocke) xfocke[i + ne * j] = fc + fep + fee;
     se1[i + ne * j] = s1;
     const double d = DE[i + ne * j];
     e[0] = d * fc;
@@ -284,6 +278,7 @@ __global__ void fock1_kernel(int ne, int np, int nelec,
         s1 = s1 + de * G1s[o];
       }
     fockp[p + np * q] = fc + fep + fg1;
+    if (xfockp) xfockp[p + np * q] = fc + fep;
     sp1[p + np * q] = s1;
     e[1] = DP[p + np * q] * fc;
   }
@@ -865,11 +860,11 @@ cudaError_t launch_scf_fock1(int ne, int np, int nelec, const double* Hce,
                              const double* Gee, const double* DE,
                              const double* DP, double* focke, double* fockp,
                              double* se1, double* sp1, double* part, double* en,
-                             cudaStream_t s) {
+                             cudaStream_t s, double* xfocke, double* xfockp) {
   const int nt = ne * ne + np * np;
   fock1_kernel<<<(nt + 127) / 128, 128, 0, s>>>(ne, np, nelec, Hce, Hcp, Gep, G1,
                                                 G1s, Gee, DE, DP, focke, fockp,
-                                                se1, sp1, part);
+                                                se1, sp1, part, xfocke, xfockp);
   fock1_energy_kernel<<<1, 256, 0, s>>>(nt, part, en);
   return cudaGetLastError();
 }

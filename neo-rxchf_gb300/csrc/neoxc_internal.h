@@ -211,7 +211,8 @@ cudaError_t launch_scf_fock1(int ne, int np, int nelec, const double* Hce,
                              const double* Gee, const double* DE,
                              const double* DP, double* focke, double* fockp,
                              double* se1, double* sp1, double* part, double* en,
-                             cudaStream_t s);
+                             cudaStream_t s, double* xfocke = nullptr,
+                             double* xfockp = nullptr);
 cudaError_t launch_scf_assemble(int ne, int np, double* en, const double* se1,
                                 const double* sp1, const double* se2,
                                 const double* sp2, double* focke,
