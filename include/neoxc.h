@@ -210,6 +210,90 @@ int neoxc_xcfock_correction(int64_t nebf, int64_t npbf, double E_total,
                             const double* se2, const double* sp2,
                             double* focke, double* fockp);
 
+/* ---- one-body tables and the whole XCHF Fock build ---------------------- */
+/* The integrals xcneo_driver computes before the geminal ones
+ * (xcneo_HYBRID.f:665-690,761): pure_ovlap.f:2-105 elec_ovlap -> Se,
+ * :107-203 nuc_ovlap -> Sp, gam_epcore.f:2-198 calc_GAM_epcore -> GAM_ecore,
+ * GAM_pcore, gam_ep.f:2-165 calc_GAM_ep -> GAM_ep, gam_1_OMP.f:2-396
+ * GAM1_OMP_MD -> GAM_1, GAM_1s.  Each output holds the records of the
+ * reference's file in order: Se, GAM_ecore pack_2D(nebf,je,ie) (eovlap.ufm,
+ * GAM_ecr.ufm); Sp, GAM_pcore pack_2D(npbf,jp,ip) (novlap.ufm, GAM_pcr.ufm);
+ * GAM_ep, GAM_1, GAM_1s pack_4D(je,ie,jp,ip) (GAM_ep.ufm, GAM_1.ufm,
+ * GAM_1s.ufm).  A NULL output is skipped, and the inputs only it needs may
+ * be NULL: the electronic basis (AMPEB2C, AGEBFCC, ELCEX, ELCAM, ELCBFC)
+ * serves all but Sp/GAM_pcore, the nuclear basis (AGNBFCC, NUCEX, NUCAM,
+ * NUCBFC) all but Se/GAM_ecore, the classical nuclei (nat, zan, cat) the
+ * core and GAM_1 tables, the geminal (ngtg1 >= 1, bcoef1, gamma1) GAM_1. */
+int neoxc_onebody_integrals(int64_t nebf, int64_t npebf, int64_t npbf,
+                            int64_t nat, int64_t ngtg1, double pmass,
+                            const double* cat, const double* zan,
+                            const double* bcoef1, const double* gamma1,
+                            const int64_t* AMPEB2C, const double* AGEBFCC,
+                            const double* AGNBFCC, const double* ELCEX,
+                            const double* NUCEX, const int64_t* ELCAM,
+                            const int64_t* NUCAM, const double* ELCBFC,
+                            const double* NUCBFC, double* Se, double* Sp,
+                            double* GAM_ecore, double* GAM_pcore,
+                            double* GAM_ep, double* GAM_1, double* GAM_1s);
+/* class_nuc_rep.f:2-45: E_nuc = sum_{i<j} Z_i Z_j / |R_i - R_j| (host
+ * arithmetic, O(nat^2)). */
+int neoxc_class_nuc_rep(int64_t nat, const double* zan, const double* cat,
+                        double* E_nuc);
+
+/* The LOGICAL switches of xchf1_fock as bits of `modes`.  A geminal term
+ * with neither its DSCF nor its IC bit is the reference's disk branch
+ * (S_from_GAM_2s / E_from_GAM_2 / E_from_GAM_3 / E_from_GAM_4): its tables
+ * come in the IC arguments (GM2ICR = GAM_2.ufm, GM2SICR = GAM_2s.ufm,
+ * GM3IC1 = GAM_3.ufm, GM4ICR = GAM_4.ufm / 16, the scale E_from_GAM_4
+ * applies; xchf1_fock_ reads the files). */
+#define NEOXC_FOCK_NEOHF    1   /* LNEOHF: NEO-HF terms only */
+#define NEOXC_FOCK_GAM4     2   /* LGAM4: include gam_4 */
+#define NEOXC_FOCK_G4DSCF   4   /* LG4DSCF: gam_4 from GAM_ee, GAM_2s */
+#define NEOXC_FOCK_G4IC     8   /* LG4IC: gam_4 from GM4ICR */
+#define NEOXC_FOCK_G3DSCF  16   /* LG3DSCF: gam_3 rebuilt from the basis */
+#define NEOXC_FOCK_G3IC1   32   /* LG3IC1: gam_3 from GM3IC1 */
+#define NEOXC_FOCK_G2DSCF  64   /* LG2DSCF: gam_2 rebuilt from the basis */
+#define NEOXC_FOCK_G2IC1  128   /* LG2IC1: gam_2 from GM2ICR, GM2SICR */
+#define NEOXC_FOCK_GAM4_FACTORED 256  /* direct gam_4 by the factorised build
+                                         (same result for pair-symmetric tables) */
+
+/* xchf1_independent/xchf1_fock.f:2-361 xchf1_fock, the XCHF Fock build the
+ * SCF runs twice per iteration (xcscf.f:364,428), in one device pass:
+ * E_from_GAM_ecore/pcore/ep/ee, S_from_GAM_1s/E_from_GAM_1 (GAM_1, GAM_1s
+ * are arguments; the reference reads GAM_1.ufm, GAM_1s.ufm), the gam_2,
+ * gam_3, gam_4 terms in the branch `modes` selects, S_total/E_total and
+ * XCfock_correction.  Same arguments as the reference, with E_nuc read
+ * (not written) and GAM_2s added for the direct gam_4 (GAM4_DSCF reads
+ * GAM_2s.ufm; NULL takes GM2SICR).  Outputs overwritten: focke, fockp,
+ * Xfocke, Xfockp (the NEO-HF part, :218-219) and the energies.  LCMF's
+ * printed checks are not reproduced.  Limits: nebf <= 24 for gam_4,
+ * nebf <= 20 for the direct gam_3. */
+int neoxc_xchf1_fock(int64_t modes, int64_t NG4CHK, int64_t NG3CHK,
+                     int64_t NG2CHK, int64_t npebf, int64_t nebf, int64_t npbf,
+                     int64_t nelec, int64_t ngee, int64_t ng1, int64_t ng2,
+                     int64_t ng3, int64_t ng4, const double* DE,
+                     const double* DP, const double* GAM_ecore,
+                     const double* GAM_pcore, const double* GAM_ep,
+                     const double* GAM_ee, const double* GAM_1,
+                     const double* GAM_1s, const double* GM4ICR,
+                     const double* GM3IC1, const double* GM2ICR,
+                     const double* GM2SICR, const double* GAM_2s,
+                     int64_t ng2prm, int64_t ngtg1, int64_t ng3prm,
+                     int64_t nat, double pmass, const double* cat,
+                     const double* zan, const double* bcoef1,
+                     const double* gamma1, const int64_t* KPESTR,
+                     const int64_t* KPEEND, const int64_t* AMPEB2C,
+                     const double* AGEBFCC, const double* AGNBFCC,
+                     const double* ELCEX, const double* NUCEX,
+                     const int64_t* ELCAM, const int64_t* NUCAM,
+                     const double* ELCBFC, const double* NUCBFC,
+                     double* focke, double* fockp, double* Xfocke,
+                     double* Xfockp, double* E_total, const double* E_nuc,
+                     double* E_ecore, double* E_pcore, double* E_ep,
+                     double* E_ee, double* E_gam1, double* E_gam2,
+                     double* E_gam3, double* E_gam4, double* S_total,
+                     double* S_gam1, double* S_gam2);
+
 /* ---- device-resident variants (no host copies; for SCF loops) --------- */
 int neoxc_dev_gam4_dscf(void* stream, int64_t ne, int64_t np,
                         const double* d_GAM_ee, const double* d_GAM_2s,
@@ -862,6 +946,99 @@ void rxchf_fp_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1
 void rxchf_fbe_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng1,
                      const double* DBE, const double* DP, double* FBE, double* SBE,
                      double* E_BE_OMG1, double* S_BE_OMG1);
+/* Integral phase of xcneo_driver with the reference's file outputs:
+ * class_nuc_rep_ -> ENUCRP.dat, elec_ovlap_ -> eovlap.ufm, nuc_ovlap_ ->
+ * novlap.ufm, calc_gam_epcore_ -> GAM_ecr.ufm + GAM_pcr.ufm, calc_gam_ep_ ->
+ * GAM_ep.ufm, gam1_omp_md_ -> GAM_1.ufm + GAM_1s.ufm, gam2_conv_
+ * (gam2_CONV_OMP.f GAM2_CONV) -> GAM_2.ufm + GAM_2s.ufm, gam3_conv_
+ * (gam3_CONV_OMP.f GAM3_CONV) -> GAM_3.ufm.  The CONV routines' unsymmetrised
+ * scratch files (GAM_2X.ufm, GAM_2sX.ufm, GAM_3X.ufm) are not written. */
+void class_nuc_rep_(const int64_t* nat, const double* zan, const double* cat);
+void elec_ovlap_(const int64_t* npebf, const int64_t* nebf, const int64_t* nebf2,
+                 const int64_t* AMPEB2C, const double* AGEBFCC,
+                 const double* ELCEX, const int64_t* ELCAM, const double* ELCBFC);
+void nuc_ovlap_(const int64_t* npbf, const int64_t* npbf2, const double* AGNBFCC,
+                const double* NUCEX, const int64_t* NUCAM, const double* NUCBFC);
+void calc_gam_epcore_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                      const int64_t* nebf2, const int64_t* npbf2, const int64_t* nat,
+                      const double* pmass, const double* zan, const double* cat,
+                      const int64_t* AMPEB2C, const double* AGEBFCC,
+                      const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                      const int64_t* ELCAM, const int64_t* NUCAM,
+                      const double* ELCBFC, const double* NUCBFC);
+void calc_gam_ep_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                  const int64_t* ng1, const int64_t* AMPEB2C, const double* AGEBFCC,
+                  const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                  const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                  const double* NUCBFC);
+void gam1_omp_md_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                  const int64_t* ng1, const int64_t* ng1prm, const int64_t* nat,
+                  const int64_t* ngtg1, const double* pmass, const double* cat,
+                  const double* zan, const double* bcoef1, const double* gamma1,
+                  const int64_t* AMPEB2C, const double* AGEBFCC,
+                  const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                  const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                  const double* NUCBFC);
+void gam2_conv_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npebf,
+                const int64_t* npbf, const int64_t* ng2, const int64_t* ng2prm,
+                const int64_t* nat, const int64_t* ngtg1, const double* pmass,
+                const double* cat, const double* zan, const double* bcoef1,
+                const double* gamma1, const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC, const double* AGNBFCC,
+                const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC);
+void gam3_conv_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npebf,
+                const int64_t* npbf, const int64_t* ng3, const int64_t* ng3prm,
+                const int64_t* nat, const int64_t* ngtg1, const double* pmass,
+                const double* cat, const double* zan, const double* bcoef1,
+                const double* gamma1, const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC, const double* AGNBFCC,
+                const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC);
+/* xchf1_fock.f disk contractions: E_from_GAM_2 (:1152-1281, GAM_2.ufm; focke,
+ * fockp accumulate, E_gam2 overwritten), S_from_GAM_2s (:1283-1388, GAM_2s.ufm; se2,
+ * sp2, S_gam2 overwritten), E_from_GAM_3 (:1390-1550, GAM_3.ufm),
+ * E_from_GAM_4 (:1552-1710, GAM_4.ufm, values / 16). */
+void e_from_gam_2_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng2,
+                   const double* DE, const double* DP, double* focke, double* fockp,
+                   double* E_gam2);
+void s_from_gam_2s_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng2,
+                    const double* DE, const double* DP, double* se2, double* sp2,
+                    double* S_gam2);
+void e_from_gam_3_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng3,
+                   const double* DE, const double* DP, double* focke, double* fockp,
+                   double* E_gam3);
+void e_from_gam_4_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng4,
+                   const double* DE, const double* DP, double* focke, double* fockp,
+                   double* E_gam4);
+/* xchf1_fock.f:2-361 with the reference's argument list; the LOGICAL*8
+ * switches are read by their low bit (ifort .TRUE. = -1, gfortran 1).  The
+ * disk branches read GAM_1.ufm, GAM_1s.ufm (always, as the reference does
+ * outside NEO-HF), GAM_2.ufm, GAM_2s.ufm, GAM_3.ufm, GAM_4.ufm, and the
+ * direct gam_4 reads GAM_2s.ufm. */
+void xchf1_fock_(const int64_t* LNEOHF, const int64_t* LGAM4, const int64_t* LG4DSCF,
+                 const int64_t* LG4IC, const int64_t* LG3DSCF, const int64_t* LG3IC1,
+                 const int64_t* LG2DSCF, const int64_t* LG2IC1, const int64_t* LCMF,
+                 const int64_t* NG4CHK, const int64_t* NG3CHK, const int64_t* NG2CHK,
+                 const int64_t* SZG4IC, const int64_t* SZG3IC1, const int64_t* SZG2ICR,
+                 const int64_t* npebf, const int64_t* nebf, const int64_t* nebf2,
+                 const int64_t* npbf, const int64_t* npbf2, const int64_t* nelec,
+                 const int64_t* ngee, const int64_t* ng1, const int64_t* ng2,
+                 const int64_t* ng3, const int64_t* ng4, const double* DE,
+                 const double* DP, const double* GAM_ecore, const double* GAM_pcore,
+                 const double* GAM_ep, const double* GAM_ee, const double* GM4ICR,
+                 const double* GM3IC1, const double* GM2ICR, const double* GM2SICR,
+                 const int64_t* ng2prm, const int64_t* ngtg1, const int64_t* ng3prm,
+                 const int64_t* nat, const double* pmass, const double* cat,
+                 const double* zan, const double* bcoef1, const double* gamma1,
+                 const int64_t* KPESTR, const int64_t* KPEEND, const int64_t* AMPEB2C,
+                 const double* AGEBFCC, const double* AGNBFCC, const double* ELCEX,
+                 const double* NUCEX, const int64_t* ELCAM, const int64_t* NUCAM,
+                 const double* ELCBFC, const double* NUCBFC, double* focke,
+                 double* fockp, double* Xfocke, double* Xfockp, double* E_total,
+                 const double* E_nuc, double* E_ecore, double* E_pcore, double* E_ep,
+                 double* E_ee, double* E_gam1, double* E_gam2, double* E_gam3,
+                 double* E_gam4, double* S_total, double* S_gam1, double* S_gam2);
 #ifdef __cplusplus
 }
 #endif

@@ -842,6 +842,31 @@ int neoxc_xcfock_correction(int64_t ne, int64_t np, double E_total,
 // and contracted into per-CTA partials; one reduction gives the Fock
 // matrices (accumulated) and E_gam3 (overwritten).  Nchunks (the reference's
 // NG3CHK) is accepted and validated; the slicing is by proton pair.
+// The direct gam_3 loop on device buffers: dfe, dfp accumulate (one add of
+// the finished contraction, like add2fock), dE overwritten.
+static int gam3_dscf_dev(const SysUpload& u, cudaStream_t s, const double* dde,
+                         const double* ddp, double* dfe, double* dfp,
+                         double* dE) {
+  const int ne = u.d.nebf, np = u.d.npbf;
+  const int64_t n6 = (int64_t)ne * ne * ne * ne * ne * ne;
+  DBuf slice, part, aux;
+  RC(dalloc(slice, sizeof(double) * n6, s));
+  RC(dalloc(part, sizeof(double) * eg3_partial_doubles(ne, np), s));
+  RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
+  CU(launch_gam3_aux(u.d, aux.as<double>(), s));
+  for (int64_t pp = 0; pp < (int64_t)np * np; pp++) {
+    CU(launch_gam3_raw_range(u.d, aux.as<double>(), pp * n6, n6,
+                             slice.as<double>(), s));
+    CU(launch_gam3_symmetrize(ne, 1, slice.as<double>(), s));
+    CU(launch_eg3_partials(ne, np, pp, 1, dde, slice.as<double>(),
+                           part.as<double>(), s));
+  }
+  const size_t nparts = (size_t)np * np * ne * ne * ne * ne;
+  CU(launch_fock_reduce(ne, np, ne * ne, part.as<double>(), dde, ddp, 3.0, 1,
+                        dfe, dfp, part.as<double>() + nparts, dE, s));
+  return NEOXC_OK;
+}
+
 int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
                     int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
                     double pmass, const double* cat, const double* zan,
@@ -867,12 +892,7 @@ int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
                   gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
                   NUCAM, ELCBFC, NUCBFC));
-  const int ne = (int)nebf, np = (int)npbf;
-  DBuf slice, part, dde, ddp, dfe, dfp, dE, aux;
-  RC(dalloc(slice, sizeof(double) * n6, s));
-  RC(dalloc(part, sizeof(double) * eg3_partial_doubles(ne, np), s));
-  RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
-  CU(launch_gam3_aux(u.d, aux.as<double>(), s));
+  DBuf dde, ddp, dfe, dfp, dE;
   RC(upload(dde, DE, sizeof(double) * nebf * nebf, s));
   RC(upload(ddp, DP, sizeof(double) * npbf * npbf, s));
   RC(dalloc(dfe, sizeof(double) * nebf * nebf, s));
@@ -880,26 +900,42 @@ int neoxc_gam3_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   RC(dalloc(dE, sizeof(double), s));
   CU(cudaMemsetAsync(dfe.p, 0, sizeof(double) * nebf * nebf, s));
   CU(cudaMemsetAsync(dfp.p, 0, sizeof(double) * npbf * npbf, s));
-  for (int64_t pp = 0; pp < npbf * npbf; pp++) {
-    CU(launch_gam3_raw_range(u.d, aux.as<double>(), pp * n6, n6,
-                             slice.as<double>(), s));
-    CU(launch_gam3_symmetrize(ne, 1, slice.as<double>(), s));
-    CU(launch_eg3_partials(ne, np, pp, 1, dde.as<double>(), slice.as<double>(),
-                           part.as<double>(), s));
-  }
-  const size_t nparts = (size_t)np * np * ne * ne * ne * ne;
-  CU(launch_fock_reduce(ne, np, ne * ne, part.as<double>(), dde.as<double>(),
-                        ddp.as<double>(), 3.0, 1, dfe.as<double>(),
-                        dfp.as<double>(), part.as<double>() + nparts,
-                        dE.as<double>(), s));
+  RC(gam3_dscf_dev(u, s, dde.as<double>(), ddp.as<double>(), dfe.as<double>(),
+                   dfp.as<double>(), dE.as<double>()));
   RC(accumulate_back(focke, dfe.as<double>(), nebf * nebf, s));
   RC(accumulate_back(fockp, dfp.as<double>(), npbf * npbf, s));
   CU(cudaMemcpyAsync(E_gam3, dE.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   return finish(s);
 }
 
-// gam2_DSCF_OMP.f:2-140 GAM2_DSCF: focke, fockp, se2, sp2 accumulate (the
-// reference's add2fock); E_gam2, S_gam2 overwritten.
+// gam2_DSCF_OMP.f:2-140 GAM2_DSCF on device buffers: dfe, dfp, dse, dsp
+// accumulate (the reference's add2fock); dE[0] = E_gam2, dE[1] = S_gam2.
+static int gam2_dscf_dev(const SysUpload& u, cudaStream_t s, const double* dde,
+                         const double* ddp, double* dfe, double* dfp,
+                         double* dse, double* dsp, double* dE, double* dS) {
+  const int ne = u.d.nebf, np = u.d.npbf;
+  const int64_t n4 = (int64_t)ne * ne * ne * ne;
+  const size_t npart = (size_t)np * np * ne * ne * ne;
+  DBuf s1, s2, part;
+  RC(dalloc(s1, sizeof(double) * n4, s));
+  RC(dalloc(s2, sizeof(double) * n4, s));
+  RC(dalloc(part, sizeof(double) * (2 * npart + 2 * np * np), s));
+  double* pv = part.as<double>();
+  double* ps = pv + npart;
+  double* ftmp = ps + npart;
+  for (int64_t pp = 0; pp < (int64_t)np * np; pp++) {
+    CU(launch_gam2_raw_range(u.d, 0, pp * n4, n4, s1.as<double>(),
+                             s2.as<double>(), s));
+    CU(launch_gam2_symmetrize(ne, 1, 0, s1.as<double>(), s2.as<double>(), s));
+    CU(launch_eg2_partials(ne, np, pp, 1, dde, s1.as<double>(),
+                           s2.as<double>(), pv, ps, s));
+  }
+  CU(launch_fock_reduce(ne, np, ne, pv, dde, ddp, 2.0, 1, dfe, dfp, ftmp, dE, s));
+  CU(launch_fock_reduce(ne, np, ne, ps, dde, ddp, 1.0, 1, dse, dsp,
+                        ftmp + np * np, dS, s));
+  return NEOXC_OK;
+}
+
 int neoxc_gam2_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
                     int64_t ng2, int64_t ng2prm, int64_t nat, int64_t ngtg1,
                     double pmass, const double* cat, const double* zan,
@@ -925,12 +961,7 @@ int neoxc_gam2_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
                   gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
                   NUCAM, ELCBFC, NUCBFC));
-  const int ne = (int)nebf, np = (int)npbf;
-  const size_t npart = (size_t)np * np * ne * ne * ne;
-  DBuf s1, s2, part, dde, ddp, dfe, dfp, dse, dsp, dE;
-  RC(dalloc(s1, sizeof(double) * n4, s));
-  RC(dalloc(s2, sizeof(double) * n4, s));
-  RC(dalloc(part, sizeof(double) * (2 * npart + 2 * np * np), s));
+  DBuf dde, ddp, dfe, dfp, dse, dsp, dE;
   RC(upload(dde, DE, sizeof(double) * nebf * nebf, s));
   RC(upload(ddp, DP, sizeof(double) * npbf * npbf, s));
   RC(dalloc(dfe, sizeof(double) * nebf * nebf, s));
@@ -940,22 +971,9 @@ int neoxc_gam2_dscf(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   RC(dalloc(dE, 2 * sizeof(double), s));
   for (DBuf* b : {&dfe, &dse}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * nebf * nebf, s));
   for (DBuf* b : {&dfp, &dsp}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * npbf * npbf, s));
-  double* pv = part.as<double>();
-  double* ps = pv + npart;
-  double* ftmp = ps + npart;
-  for (int64_t pp = 0; pp < npbf * npbf; pp++) {
-    CU(launch_gam2_raw_range(u.d, 0, pp * n4, n4, s1.as<double>(),
-                             s2.as<double>(), s));
-    CU(launch_gam2_symmetrize(ne, 1, 0, s1.as<double>(), s2.as<double>(), s));
-    CU(launch_eg2_partials(ne, np, pp, 1, dde.as<double>(), s1.as<double>(),
-                           s2.as<double>(), pv, ps, s));
-  }
-  CU(launch_fock_reduce(ne, np, ne, pv, dde.as<double>(), ddp.as<double>(), 2.0,
-                        1, dfe.as<double>(), dfp.as<double>(), ftmp,
-                        dE.as<double>(), s));
-  CU(launch_fock_reduce(ne, np, ne, ps, dde.as<double>(), ddp.as<double>(), 1.0,
-                        1, dse.as<double>(), dsp.as<double>(), ftmp + np * np,
-                        dE.as<double>() + 1, s));
+  RC(gam2_dscf_dev(u, s, dde.as<double>(), ddp.as<double>(), dfe.as<double>(),
+                   dfp.as<double>(), dse.as<double>(), dsp.as<double>(),
+                   dE.as<double>(), dE.as<double>() + 1));
   RC(accumulate_back(focke, dfe.as<double>(), nebf * nebf, s));
   RC(accumulate_back(fockp, dfp.as<double>(), npbf * npbf, s));
   RC(accumulate_back(se2, dse.as<double>(), nebf * nebf, s));
@@ -982,6 +1000,316 @@ static double nuc_rep(int64_t nat, const double* zan, const double* cat) {
       if (R2 != 0.0) E = E + zan[i] * zan[j] / sqrt(R2);
     }
   return E;
+}
+
+int neoxc_class_nuc_rep(int64_t nat, const double* zan, const double* cat,
+                        double* E_nuc) {
+  RC(need(nat >= 0 && E_nuc && (nat == 0 || (zan && cat)), "nat, zan, cat, E_nuc"));
+  *E_nuc = nuc_rep(nat, zan, cat);
+  return NEOXC_OK;
+}
+
+// ---- one-body tables: pure_ovlap.f, gam_epcore.f, gam_ep.f, gam_1_OMP.f ----
+// The same kernels the device SCF builds its tables with; outputs that are
+// not asked for are not computed, and the parts of the system only they
+// need are replaced by one s function at the origin.
+int neoxc_onebody_integrals(int64_t nebf, int64_t npebf, int64_t npbf,
+                            int64_t nat, int64_t ngtg1, double pmass,
+                            const double* cat, const double* zan,
+                            const double* bcoef1, const double* gamma1,
+                            const int64_t* AMPEB2C, const double* AGEBFCC,
+                            const double* AGNBFCC, const double* ELCEX,
+                            const double* NUCEX, const int64_t* ELCAM,
+                            const int64_t* NUCAM, const double* ELCBFC,
+                            const double* NUCBFC, double* Se, double* Sp,
+                            double* GAM_ecore, double* GAM_pcore,
+                            double* GAM_ep, double* GAM_1, double* GAM_1s) {
+  const bool want_g1 = GAM_1 || GAM_1s;
+  const bool want_core = GAM_ecore || GAM_pcore;
+  const bool want_e = Se || GAM_ecore || GAM_ep || want_g1;
+  const bool want_p = Sp || GAM_pcore || GAM_ep || want_g1;
+  if (!want_e && !want_p) return NEOXC_OK;
+  if (want_e)
+    RC(need(nebf >= 1 && npebf >= nebf && AMPEB2C && AGEBFCC && ELCEX && ELCAM &&
+                ELCBFC,
+            "electronic basis"));
+  if (want_p) RC(need(npbf >= 1 && AGNBFCC && NUCEX && NUCAM && NUCBFC, "nuclear basis"));
+  const bool nuclei = want_core || want_g1;
+  if (nuclei) {
+    RC(need(nat >= 0 && (nat == 0 || (zan && cat)), "nat, zan, cat"));
+    RC(need(pmass > 0.0, "pmass > 0"));
+  }
+  if (want_g1) RC(need(ngtg1 >= 1 && bcoef1 && gamma1, "ngtg1 >= 1, bcoef1, gamma1"));
+  const double one = 1.0, zero3[3] = {0.0, 0.0, 0.0}, b0 = 0.0;
+  const int64_t l0[3] = {0, 0, 0};
+  const int64_t ne = want_e ? nebf : 1, npe = want_e ? npebf : 1;
+  const int64_t np = want_p ? npbf : 1;
+  std::vector<int64_t> kps((size_t)ne, 1), kpe((size_t)ne, 1);
+  if (want_e) RC(neoxc_make_kpe(ne, npe, AMPEB2C, kps.data(), kpe.data()));
+  const int64_t na = nuclei ? nat : 0;
+  cudaStream_t s;
+  RC(get_stream(&s));
+  SysUpload u;
+  RC(stage_system(u, s, ne, npe, np, na, want_g1 ? ngtg1 : 1, nuclei ? pmass : 1.0,
+                  na ? cat : zero3, na ? zan : &one, want_g1 ? bcoef1 : &b0,
+                  want_g1 ? gamma1 : &one, kps.data(), kpe.data(),
+                  want_e ? AGEBFCC : &one, want_p ? AGNBFCC : &one,
+                  want_e ? ELCEX : &one, want_p ? NUCEX : &one, want_e ? ELCAM : l0,
+                  want_p ? NUCAM : l0, want_e ? ELCBFC : zero3,
+                  want_p ? NUCBFC : zero3));
+  const size_t e2 = (size_t)ne * ne, p2 = (size_t)np * np, n1 = e2 * p2;
+  DBuf a, b, c, d, g, g1, g1s;
+  auto back = [&](double* host, const DBuf& dev, size_t n) -> int {
+    if (host)
+      CU(cudaMemcpyAsync(host, dev.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    return NEOXC_OK;
+  };
+  if (Se || Sp || want_core) {
+    RC(dalloc(a, sizeof(double) * e2, s));
+    RC(dalloc(b, sizeof(double) * p2, s));
+    RC(dalloc(c, sizeof(double) * e2, s));
+    RC(dalloc(d, sizeof(double) * p2, s));
+    CU(launch_scf_onebody(u.d, a.as<double>(), b.as<double>(), c.as<double>(),
+                          d.as<double>(), s));
+    RC(back(Se, a, e2));
+    RC(back(Sp, b, p2));
+    RC(back(GAM_ecore, c, e2));
+    RC(back(GAM_pcore, d, p2));
+  }
+  if (GAM_ep) {
+    RC(dalloc(g, sizeof(double) * n1, s));
+    CU(launch_gam_ep(u.d, g.as<double>(), s));
+    RC(back(GAM_ep, g, n1));
+  }
+  if (want_g1) {
+    RC(dalloc(g1, sizeof(double) * n1, s));
+    RC(dalloc(g1s, sizeof(double) * n1, s));
+    CU(launch_gam1(u.d, g1.as<double>(), g1s.as<double>(), s, 0));
+    RC(back(GAM_1, g1, n1));
+    RC(back(GAM_1s, g1s, n1));
+  }
+  return finish(s);
+}
+
+// ---- xchf1_independent/xchf1_fock.f:2-361 xchf1_fock ------------------------
+// One stream, every term on the device in the reference's order: the one-body
+// and GAM_1 terms (fock1 kernel, which also keeps the NEO-HF part), gam_2,
+// gam_3, gam_4 in the branch `modes` selects (each adds its finished
+// contraction to the Fock matrices once, as add2fock does), then S_total,
+// E_total and XCfock_correction (assemble kernel).
+int neoxc_xchf1_fock(int64_t modes, int64_t NG4CHK, int64_t NG3CHK,
+                     int64_t NG2CHK, int64_t npebf, int64_t nebf, int64_t npbf,
+                     int64_t nelec, int64_t ngee, int64_t ng1, int64_t ng2,
+                     int64_t ng3, int64_t ng4, const double* DE,
+                     const double* DP, const double* GAM_ecore,
+                     const double* GAM_pcore, const double* GAM_ep,
+                     const double* GAM_ee, const double* GAM_1,
+                     const double* GAM_1s, const double* GM4ICR,
+                     const double* GM3IC1, const double* GM2ICR,
+                     const double* GM2SICR, const double* GAM_2s,
+                     int64_t ng2prm, int64_t ngtg1, int64_t ng3prm,
+                     int64_t nat, double pmass, const double* cat,
+                     const double* zan, const double* bcoef1,
+                     const double* gamma1, const int64_t* KPESTR,
+                     const int64_t* KPEEND, const int64_t* AMPEB2C,
+                     const double* AGEBFCC, const double* AGNBFCC,
+                     const double* ELCEX, const double* NUCEX,
+                     const int64_t* ELCAM, const int64_t* NUCAM,
+                     const double* ELCBFC, const double* NUCBFC,
+                     double* focke, double* fockp, double* Xfocke,
+                     double* Xfockp, double* E_total, const double* E_nuc,
+                     double* E_ecore, double* E_pcore, double* E_ep,
+                     double* E_ee, double* E_gam1, double* E_gam2,
+                     double* E_gam3, double* E_gam4, double* S_total,
+                     double* S_gam1, double* S_gam2) {
+  (void)AMPEB2C;
+  RC(need((modes & ~(int64_t)(255 | NEOXC_FOCK_GAM4_FACTORED)) == 0, "modes"));
+  RC(need(nebf >= 1 && npbf >= 1 && nelec >= 1, "nebf, npbf, nelec >= 1"));
+  RC(need(nebf <= 4096 && npbf <= 4096, "nebf, npbf <= 4096"));
+  const int64_t e2 = nebf * nebf, p2 = npbf * npbf, n4 = e2 * e2;
+  RC(need(ng1 == e2 * p2, "ng1 == nebf**2 npbf**2"));
+  RC(need(DE && DP && GAM_ecore && GAM_pcore && GAM_ep && E_nuc && focke &&
+              fockp && Xfocke && Xfockp && E_total && E_ecore && E_pcore &&
+              E_ep && E_ee && E_gam1 && E_gam2 && E_gam3 && E_gam4 &&
+              S_total && S_gam1 && S_gam2,
+          "pointers"));
+  const bool neohf = (modes & NEOXC_FOCK_NEOHF) != 0;
+  const bool t2 = !neohf && nelec > 1, t3 = !neohf && nelec > 2;
+  const bool t4 = t3 && (modes & NEOXC_FOCK_GAM4);
+  const bool d2 = t2 && (modes & NEOXC_FOCK_G2DSCF);
+  const bool d3 = t3 && (modes & NEOXC_FOCK_G3DSCF);
+  const bool d4 = t4 && (modes & NEOXC_FOCK_G4DSCF);
+  if (nelec > 1) RC(need(GAM_ee && ngee == n4, "GAM_ee, ngee == nebf**4"));
+  if (!neohf) RC(need(GAM_1 && GAM_1s, "GAM_1, GAM_1s"));
+  if (t2) {
+    RC(need(NG2CHK >= 1 && ng2 == n4 * p2, "NG2CHK >= 1, ng2 == nebf**4 npbf**2"));
+    if (d2)
+      RC(need(ng2prm == npebf * npebf * npebf * npebf * npbf * npbf, "ng2prm"));
+    else
+      RC(need(GM2ICR && GM2SICR, "GM2ICR, GM2SICR"));
+  }
+  if (t3) {
+    RC(need(NG3CHK >= 1 && ng3 == n4 * e2 * p2, "NG3CHK >= 1, ng3 == nebf**6 npbf**2"));
+    if (d3) {
+      RC(need(ng3prm == npebf * npebf * npebf * npebf * npebf * npebf * npbf * npbf,
+              "ng3prm"));
+      if (nebf > 20) return set_err(NEOXC_ERR_UNSUPPORTED, "GAM3_DSCF: nebf <= 20");
+    } else {
+      RC(need(GM3IC1 != nullptr, "GM3IC1"));
+    }
+  }
+  const bool fact4 = d4 && (modes & NEOXC_FOCK_GAM4_FACTORED);
+  const double* g2s_host = GAM_2s ? GAM_2s : GM2SICR;
+  if (t4) {
+    RC(need(NG4CHK >= 1 && ng4 == n4 * n4 * p2, "NG4CHK >= 1, ng4 == nebf**8 npbf**2"));
+    if (fact4) {
+      if (nebf > kGam4FactMaxNE || npbf > 255)
+        return set_err(NEOXC_ERR_UNSUPPORTED,
+                       "factorised gam_4: nebf <= %d, npbf <= 255", kGam4FactMaxNE);
+    } else if (nebf > kGam4MaxNE) {
+      return set_err(NEOXC_ERR_UNSUPPORTED, "gam_4: nebf <= %d", kGam4MaxNE);
+    }
+    if (d4)
+      RC(need(g2s_host && ng2 == n4 * p2, "GAM_2s (or GM2SICR), ng2 == nebf**4 npbf**2"));
+    else
+      RC(need(GM4ICR != nullptr, "GM4ICR"));
+  }
+  if (d2 || d3)
+    RC(need(KPESTR && KPEEND && AGEBFCC && AGNBFCC && ELCEX && NUCEX && ELCAM &&
+                NUCAM && ELCBFC && NUCBFC && bcoef1 && gamma1 &&
+                (nat == 0 || (cat && zan)),
+            "basis arrays"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  const int ne = (int)nebf, np = (int)npbf;
+  SysUpload u;
+  if (d2 || d3)
+    RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1,
+                    gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM,
+                    NUCAM, ELCBFC, NUCBFC));
+  DBuf dde, ddp, hce, hcp, gep, gee, g1, g1s, fe, fp, xfe, xfp, se1, sp1, se2, sp2,
+      en, part, scr, g2, g2s, g3, g4;
+  RC(upload(dde, DE, sizeof(double) * e2, s));
+  RC(upload(ddp, DP, sizeof(double) * p2, s));
+  RC(upload(hce, GAM_ecore, sizeof(double) * e2, s));
+  RC(upload(hcp, GAM_pcore, sizeof(double) * p2, s));
+  RC(upload(gep, GAM_ep, sizeof(double) * ng1, s));
+  if (nelec > 1) RC(upload(gee, GAM_ee, sizeof(double) * n4, s));
+  else RC(dalloc(gee, sizeof(double), s));
+  if (!neohf) {
+    RC(upload(g1, GAM_1, sizeof(double) * ng1, s));
+    RC(upload(g1s, GAM_1s, sizeof(double) * ng1, s));
+  } else {
+    // the NEO-HF branch returns before E_from_GAM_1 (:222-235)
+    RC(dalloc(g1, sizeof(double) * ng1, s));
+    RC(dalloc(g1s, sizeof(double) * ng1, s));
+    CU(cudaMemsetAsync(g1.p, 0, sizeof(double) * ng1, s));
+    CU(cudaMemsetAsync(g1s.p, 0, sizeof(double) * ng1, s));
+  }
+  for (DBuf* b : {&fe, &xfe, &se1, &se2}) RC(dalloc(*b, sizeof(double) * e2, s));
+  for (DBuf* b : {&fp, &xfp, &sp1, &sp2}) RC(dalloc(*b, sizeof(double) * p2, s));
+  CU(cudaMemsetAsync(se2.p, 0, sizeof(double) * e2, s));
+  CU(cudaMemsetAsync(sp2.p, 0, sizeof(double) * p2, s));
+  RC(dalloc(en, sizeof(double) * kScfSlots, s));
+  CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kScfSlots, s));
+  CU(cudaMemcpyAsync(en.as<double>() + 1, E_nuc, sizeof(double),
+                     cudaMemcpyHostToDevice, s));
+  RC(dalloc(part, sizeof(double) * scf_fock1_part_doubles(ne, np), s));
+  size_t nscr = 1;
+  if (t2 && !d2) nscr = std::max(nscr, eg2_partial_doubles(ne, np));
+  if (t3 && !d3) nscr = std::max(nscr, eg3_partial_doubles(ne, np));
+  if (t4)
+    nscr = std::max(nscr, fact4 ? gam4f_scratch_doubles(ne, np)
+                          : d4  ? gam4_partial_doubles(ne, np)
+                                : eg4_partial_doubles(ne, np));
+  RC(dalloc(scr, sizeof(double) * nscr, s));
+  double* d_en = en.as<double>();
+  CU(launch_scf_fock1(ne, np, (int)nelec, hce.as<double>(), hcp.as<double>(),
+                      gep.as<double>(), g1.as<double>(), g1s.as<double>(),
+                      gee.as<double>(), dde.as<double>(), ddp.as<double>(),
+                      fe.as<double>(), fp.as<double>(), se1.as<double>(),
+                      sp1.as<double>(), part.as<double>(), d_en, s,
+                      xfe.as<double>(), xfp.as<double>()));
+  if (t2) {
+    if (d2) {
+      RC(gam2_dscf_dev(u, s, dde.as<double>(), ddp.as<double>(), fe.as<double>(),
+                       fp.as<double>(), se2.as<double>(), sp2.as<double>(),
+                       d_en + 7, d_en + 12));
+    } else {
+      RC(upload(g2, GM2ICR, sizeof(double) * ng2, s));
+      RC(upload(g2s, GM2SICR, sizeof(double) * ng2, s));
+      CU(launch_eg2ic1(ne, np, dde.as<double>(), ddp.as<double>(), g2.as<double>(),
+                       g2s.as<double>(), scr.as<double>(), fe.as<double>(),
+                       se2.as<double>(), fp.as<double>(), sp2.as<double>(),
+                       d_en + 7, d_en + 12, s));
+    }
+  }
+  if (t3) {
+    if (d3) {
+      RC(gam3_dscf_dev(u, s, dde.as<double>(), ddp.as<double>(), fe.as<double>(),
+                       fp.as<double>(), d_en + 8));
+    } else {
+      RC(upload(g3, GM3IC1, sizeof(double) * ng3, s));
+      CU(launch_eg3ic1(ne, np, dde.as<double>(), ddp.as<double>(), g3.as<double>(),
+                       scr.as<double>(), fe.as<double>(), fp.as<double>(),
+                       d_en + 8, s));
+    }
+  }
+  if (t4) {
+    if (d4) {
+      const double* d_g2s = g2s.as<double>();
+      if (!(g2s.p && g2s_host == GM2SICR)) {
+        RC(upload(g4, g2s_host, sizeof(double) * ng2, s));
+        d_g2s = g4.as<double>();
+      }
+      if (fact4)
+        CU(launch_gam4_factored(ne, np, gee.as<double>(), d_g2s, dde.as<double>(),
+                                ddp.as<double>(), scr.as<double>(), fe.as<double>(),
+                                fp.as<double>(), d_en + 9, 1, s));
+      else
+        CU(launch_gam4_dscf(ne, np, gee.as<double>(), d_g2s, dde.as<double>(),
+                            ddp.as<double>(), scr.as<double>(), fe.as<double>(),
+                            fp.as<double>(), d_en + 9, s));
+    } else {
+      RC(upload(g4, GM4ICR, sizeof(double) * ng4, s));
+      CU(launch_eg4icr(ne, np, dde.as<double>(), ddp.as<double>(), g4.as<double>(),
+                       scr.as<double>(), fe.as<double>(), fp.as<double>(), d_en + 9, s));
+    }
+  }
+  if (!neohf)
+    CU(launch_scf_assemble(ne, np, d_en, se1.as<double>(), sp1.as<double>(),
+                           se2.as<double>(), sp2.as<double>(), fe.as<double>(),
+                           fp.as<double>(), s));
+  double h_en[kScfSlots];
+  CU(cudaMemcpyAsync(focke, neohf ? xfe.p : fe.p, sizeof(double) * e2,
+                     cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(fockp, neohf ? xfp.p : fp.p, sizeof(double) * p2,
+                     cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(Xfocke, xfe.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(Xfockp, xfp.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h_en, d_en, sizeof(h_en), cudaMemcpyDeviceToHost, s));
+  RC(finish(s));
+  *E_ecore = h_en[2];
+  *E_pcore = h_en[3];
+  *E_ep = h_en[4];
+  *E_ee = h_en[5];
+  if (neohf) {
+    // :222-235: E_total = E_NEOHF, S_total = 1, the XC terms stay zero
+    *E_total = h_en[2] + h_en[3] + h_en[4] + h_en[5] + *E_nuc;
+    *S_total = 1.0;
+    *E_gam1 = *E_gam2 = *E_gam3 = *E_gam4 = 0.0;
+    *S_gam1 = *S_gam2 = 0.0;
+    return NEOXC_OK;
+  }
+  *E_gam1 = h_en[6];
+  *E_gam2 = h_en[7];
+  *E_gam3 = h_en[8];
+  *E_gam4 = h_en[9];
+  *S_gam1 = h_en[11];
+  *S_gam2 = h_en[12];
+  *S_total = h_en[10];
+  *E_total = h_en[0];
+  return NEOXC_OK;
 }
 
 static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,

@@ -75,6 +75,14 @@ void read_ovlap(const char* who, const char* file, int64_t n, double* GS) {
     for (int64_t j = 0; j < n; j++) GS[i + n * j] = r[(size_t)(j + n * i)];
 }
 
+// GAM_4.ufm holds gam_4 (gam_4_OMP.f:263-293); E_from_GAM_4 (xchf1_fock.f:1552-1710)
+// divides each record by 16, which makes it the GM4ICR EG4ICR contracts.
+bool read_gam4_over16(int64_t ng4, std::vector<double>& g) {
+  if (!read_ufm("GAM_4.ufm", ng4, g)) return false;
+  for (double& v : g) v = v / 16.0;
+  return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -503,6 +511,284 @@ void rxchf_fbe_omg1_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng
   }
   report("rxchf_fbe_omg1", neoxc_rxchf_fbe_omg1(*nebf, *npbf, *ng1, DBE, DP, g1.data(),
                                                 g1s.data(), FBE, SBE, E_BE_OMG1, S_BE_OMG1));
+}
+
+// ---- integral phase of xcneo_driver (xcneo_HYBRID.f:661-690,761,874,964) ----
+// class_nuc_rep.f:2-45 -> ENUCRP.dat (:39-41)
+void class_nuc_rep_(const int64_t* nat, const double* zan, const double* cat) {
+  double E = 0.0;
+  int rc = neoxc_class_nuc_rep(*nat, zan, cat, &E);
+  if (rc == NEOXC_OK) rc = neoxc_enuc_write("ENUCRP.dat", E);
+  report("class_nuc_rep", rc);
+}
+
+// pure_ovlap.f:2-105 elec_ovlap -> eovlap.ufm (:86)
+void elec_ovlap_(const int64_t* npebf, const int64_t* nebf, const int64_t* nebf2,
+                 const int64_t* AMPEB2C, const double* AGEBFCC,
+                 const double* ELCEX, const int64_t* ELCAM, const double* ELCBFC) {
+  std::vector<double> S((size_t)*nebf2);
+  int rc = *nebf2 == *nebf * *nebf ? NEOXC_OK : NEOXC_ERR_ARG;
+  if (rc == NEOXC_OK)
+    rc = neoxc_onebody_integrals(*nebf, *npebf, 1, 0, 0, 1.0, nullptr, nullptr, nullptr,
+                                 nullptr, AMPEB2C, AGEBFCC, nullptr, ELCEX, nullptr,
+                                 ELCAM, nullptr, ELCBFC, nullptr, S.data(), nullptr,
+                                 nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (rc == NEOXC_OK && !write_ufm("eovlap.ufm", S.data(), *nebf2)) rc = NEOXC_ERR_IO;
+  report("elec_ovlap", rc);
+}
+
+// pure_ovlap.f:107-203 nuc_ovlap -> novlap.ufm (:184)
+void nuc_ovlap_(const int64_t* npbf, const int64_t* npbf2, const double* AGNBFCC,
+                const double* NUCEX, const int64_t* NUCAM, const double* NUCBFC) {
+  std::vector<double> S((size_t)*npbf2);
+  int rc = *npbf2 == *npbf * *npbf ? NEOXC_OK : NEOXC_ERR_ARG;
+  if (rc == NEOXC_OK)
+    rc = neoxc_onebody_integrals(1, 1, *npbf, 0, 0, 1.0, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr, nullptr, AGNBFCC, nullptr, NUCEX,
+                                 nullptr, NUCAM, nullptr, NUCBFC, nullptr, S.data(),
+                                 nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (rc == NEOXC_OK && !write_ufm("novlap.ufm", S.data(), *npbf2)) rc = NEOXC_ERR_IO;
+  report("nuc_ovlap", rc);
+}
+
+// gam_epcore.f:2-198 calc_GAM_epcore -> GAM_ecr.ufm (:161), GAM_pcr.ufm (:178)
+void calc_gam_epcore_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                      const int64_t* nebf2, const int64_t* npbf2, const int64_t* nat,
+                      const double* pmass, const double* zan, const double* cat,
+                      const int64_t* AMPEB2C, const double* AGEBFCC,
+                      const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                      const int64_t* ELCAM, const int64_t* NUCAM,
+                      const double* ELCBFC, const double* NUCBFC) {
+  std::vector<double> he((size_t)*nebf2), hp((size_t)*npbf2);
+  int rc = (*nebf2 == *nebf * *nebf && *npbf2 == *npbf * *npbf) ? NEOXC_OK : NEOXC_ERR_ARG;
+  if (rc == NEOXC_OK)
+    rc = neoxc_onebody_integrals(*nebf, *npebf, *npbf, *nat, 0, *pmass, cat, zan,
+                                 nullptr, nullptr, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX,
+                                 NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, nullptr, nullptr,
+                                 he.data(), hp.data(), nullptr, nullptr, nullptr);
+  if (rc == NEOXC_OK && !(write_ufm("GAM_ecr.ufm", he.data(), *nebf2) &&
+                          write_ufm("GAM_pcr.ufm", hp.data(), *npbf2)))
+    rc = NEOXC_ERR_IO;
+  report("calc_GAM_epcore", rc);
+}
+
+// gam_ep.f:2-165 calc_GAM_ep -> GAM_ep.ufm (:141)
+void calc_gam_ep_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                  const int64_t* ng1, const int64_t* AMPEB2C, const double* AGEBFCC,
+                  const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                  const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                  const double* NUCBFC) {
+  std::vector<double> g((size_t)*ng1);
+  int rc = *ng1 == *nebf * *nebf * *npbf * *npbf ? NEOXC_OK : NEOXC_ERR_ARG;
+  if (rc == NEOXC_OK)
+    rc = neoxc_onebody_integrals(*nebf, *npebf, *npbf, 0, 0, 1.0, nullptr, nullptr,
+                                 nullptr, nullptr, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX,
+                                 NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, nullptr, nullptr,
+                                 nullptr, nullptr, g.data(), nullptr, nullptr);
+  if (rc == NEOXC_OK && !write_ufm("GAM_ep.ufm", g.data(), *ng1)) rc = NEOXC_ERR_IO;
+  report("calc_GAM_ep", rc);
+}
+
+// gam_1_OMP.f:2-396 GAM1_OMP_MD -> GAM_1.ufm, GAM_1s.ufm (:358-361)
+void gam1_omp_md_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                  const int64_t* ng1, const int64_t* ng1prm, const int64_t* nat,
+                  const int64_t* ngtg1, const double* pmass, const double* cat,
+                  const double* zan, const double* bcoef1, const double* gamma1,
+                  const int64_t* AMPEB2C, const double* AGEBFCC,
+                  const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                  const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                  const double* NUCBFC) {
+  std::vector<double> g((size_t)*ng1), gs((size_t)*ng1);
+  int rc = (*ng1 == *nebf * *nebf * *npbf * *npbf &&
+            *ng1prm == *npebf * *npebf * *npbf * *npbf) ? NEOXC_OK : NEOXC_ERR_ARG;
+  if (rc == NEOXC_OK)
+    rc = neoxc_onebody_integrals(*nebf, *npebf, *npbf, *nat, *ngtg1, *pmass, cat, zan,
+                                 bcoef1, gamma1, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX,
+                                 NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, nullptr, nullptr,
+                                 nullptr, nullptr, nullptr, g.data(), gs.data());
+  if (rc == NEOXC_OK && !(write_ufm("GAM_1.ufm", g.data(), *ng1) &&
+                          write_ufm("GAM_1s.ufm", gs.data(), *ng1)))
+    rc = NEOXC_ERR_IO;
+  report("GAM1_OMP_MD", rc);
+}
+
+// gam2_CONV_OMP.f GAM2_CONV: the symmetrised gam_2 / gam_2s into GAM_2.ufm,
+// GAM_2s.ufm (the in-core GAM2_IC1 result, written by record)
+void gam2_conv_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npebf,
+                const int64_t* npbf, const int64_t* ng2, const int64_t* ng2prm,
+                const int64_t* nat, const int64_t* ngtg1, const double* pmass,
+                const double* cat, const double* zan, const double* bcoef1,
+                const double* gamma1, const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC, const double* AGNBFCC,
+                const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC) {
+  std::vector<double> g((size_t)*ng2), gs((size_t)*ng2);
+  int rc = neoxc_gam2_ic1(*Nchunks, *nebf, *npebf, *npbf, *ng2, *ng2prm, *nat, *ngtg1,
+                          *pmass, cat, zan, bcoef1, gamma1, KPESTR, KPEEND, AMPEB2C,
+                          AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC,
+                          g.data(), gs.data());
+  if (rc == NEOXC_OK && !(write_ufm("GAM_2.ufm", g.data(), *ng2) &&
+                          write_ufm("GAM_2s.ufm", gs.data(), *ng2)))
+    rc = NEOXC_ERR_IO;
+  report("GAM2_CONV", rc);
+}
+
+// gam3_CONV_OMP.f GAM3_CONV: the six-permutation symmetrised gam_3 into
+// GAM_3.ufm (:180-253)
+void gam3_conv_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npebf,
+                const int64_t* npbf, const int64_t* ng3, const int64_t* ng3prm,
+                const int64_t* nat, const int64_t* ngtg1, const double* pmass,
+                const double* cat, const double* zan, const double* bcoef1,
+                const double* gamma1, const int64_t* KPESTR, const int64_t* KPEEND,
+                const int64_t* AMPEB2C, const double* AGEBFCC, const double* AGNBFCC,
+                const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+                const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC) {
+  std::vector<double> g((size_t)*ng3);
+  int rc = neoxc_gam3_ic1(*Nchunks, *nebf, *npebf, *npbf, *ng3, *ng3prm, *nat, *ngtg1,
+                          *pmass, cat, zan, bcoef1, gamma1, KPESTR, KPEEND, AMPEB2C,
+                          AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC,
+                          g.data());
+  if (rc == NEOXC_OK && !write_ufm("GAM_3.ufm", g.data(), *ng3)) rc = NEOXC_ERR_IO;
+  report("GAM3_CONV", rc);
+}
+
+// ---- xchf1_fock.f disk contractions ---------------------------------------
+// E_from_GAM_2 (xchf1_fock.f:1152-1281): focke, fockp accumulate, E_gam2 overwritten.
+// The device contraction also forms the overlap terms; they are discarded.
+void e_from_gam_2_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng2,
+                   const double* DE, const double* DP, double* focke, double* fockp,
+                   double* E_gam2) {
+  std::vector<double> g;
+  if (!read_ufm("GAM_2.ufm", *ng2, g)) {
+    std::fprintf(stderr, "neoxc: E_from_GAM_2: cannot read GAM_2.ufm\n");
+    return;
+  }
+  std::vector<double> se((size_t)(*nebf * *nebf)), sp((size_t)(*npbf * *npbf));
+  double S = 0.0;
+  report("E_from_GAM_2", neoxc_eg2ic1(1, *nebf, *npbf, *ng2, DE, DP, g.data(), g.data(),
+                                      focke, se.data(), fockp, sp.data(), E_gam2, &S));
+}
+
+// S_from_GAM_2s (xchf1_fock.f:1283-1388): se2, sp2, S_gam2 overwritten.
+void s_from_gam_2s_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng2,
+                    const double* DE, const double* DP, double* se2, double* sp2,
+                    double* S_gam2) {
+  std::vector<double> g;
+  if (!read_ufm("GAM_2s.ufm", *ng2, g)) {
+    std::fprintf(stderr, "neoxc: S_from_GAM_2s: cannot read GAM_2s.ufm\n");
+    return;
+  }
+  std::vector<double> fe((size_t)(*nebf * *nebf), 0.0), fp((size_t)(*npbf * *npbf), 0.0);
+  double E = 0.0;
+  report("S_from_GAM_2s", neoxc_eg2ic1(1, *nebf, *npbf, *ng2, DE, DP, g.data(), g.data(),
+                                       fe.data(), se2, fp.data(), sp2, &E, S_gam2));
+}
+
+// E_from_GAM_3 (xchf1_fock.f:1390-1550)
+void e_from_gam_3_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng3,
+                   const double* DE, const double* DP, double* focke, double* fockp,
+                   double* E_gam3) {
+  std::vector<double> g;
+  if (!read_ufm("GAM_3.ufm", *ng3, g)) {
+    std::fprintf(stderr, "neoxc: E_from_GAM_3: cannot read GAM_3.ufm\n");
+    return;
+  }
+  report("E_from_GAM_3", neoxc_eg3ic1(1, *nebf, *npbf, *ng3, DE, DP, g.data(), focke,
+                                      fockp, E_gam3));
+}
+
+void e_from_gam_4_(const int64_t* nebf, const int64_t* npbf, const int64_t* ng4,
+                   const double* DE, const double* DP, double* focke, double* fockp,
+                   double* E_gam4) {
+  std::vector<double> g;
+  if (!read_gam4_over16(*ng4, g)) {
+    std::fprintf(stderr, "neoxc: E_from_GAM_4: cannot read GAM_4.ufm\n");
+    return;
+  }
+  report("E_from_GAM_4", neoxc_eg4icr(1, *nebf, *npbf, *ng4, DE, DP, g.data(), focke,
+                                      fockp, E_gam4));
+}
+
+// xchf1_fock.f:2-361.  LOGICAL*8 arguments are tested by their low bit.
+void xchf1_fock_(const int64_t* LNEOHF, const int64_t* LGAM4, const int64_t* LG4DSCF,
+                 const int64_t* LG4IC, const int64_t* LG3DSCF, const int64_t* LG3IC1,
+                 const int64_t* LG2DSCF, const int64_t* LG2IC1, const int64_t* LCMF,
+                 const int64_t* NG4CHK, const int64_t* NG3CHK, const int64_t* NG2CHK,
+                 const int64_t* SZG4IC, const int64_t* SZG3IC1, const int64_t* SZG2ICR,
+                 const int64_t* npebf, const int64_t* nebf, const int64_t* nebf2,
+                 const int64_t* npbf, const int64_t* npbf2, const int64_t* nelec,
+                 const int64_t* ngee, const int64_t* ng1, const int64_t* ng2,
+                 const int64_t* ng3, const int64_t* ng4, const double* DE,
+                 const double* DP, const double* GAM_ecore, const double* GAM_pcore,
+                 const double* GAM_ep, const double* GAM_ee, const double* GM4ICR,
+                 const double* GM3IC1, const double* GM2ICR, const double* GM2SICR,
+                 const int64_t* ng2prm, const int64_t* ngtg1, const int64_t* ng3prm,
+                 const int64_t* nat, const double* pmass, const double* cat,
+                 const double* zan, const double* bcoef1, const double* gamma1,
+                 const int64_t* KPESTR, const int64_t* KPEEND, const int64_t* AMPEB2C,
+                 const double* AGEBFCC, const double* AGNBFCC, const double* ELCEX,
+                 const double* NUCEX, const int64_t* ELCAM, const int64_t* NUCAM,
+                 const double* ELCBFC, const double* NUCBFC, double* focke,
+                 double* fockp, double* Xfocke, double* Xfockp, double* E_total,
+                 const double* E_nuc, double* E_ecore, double* E_pcore, double* E_ep,
+                 double* E_ee, double* E_gam1, double* E_gam2, double* E_gam3,
+                 double* E_gam4, double* S_total, double* S_gam1, double* S_gam2) {
+  (void)LCMF;
+  (void)nebf2;
+  (void)npbf2;
+  auto on = [](const int64_t* l) { return (*l & 1) != 0; };
+  int64_t modes = 0;
+  if (on(LNEOHF)) modes |= NEOXC_FOCK_NEOHF;
+  if (on(LGAM4)) modes |= NEOXC_FOCK_GAM4;
+  if (on(LG4DSCF)) modes |= NEOXC_FOCK_G4DSCF;
+  if (on(LG4IC)) modes |= NEOXC_FOCK_G4IC;
+  if (on(LG3DSCF)) modes |= NEOXC_FOCK_G3DSCF;
+  if (on(LG3IC1)) modes |= NEOXC_FOCK_G3IC1;
+  if (on(LG2DSCF)) modes |= NEOXC_FOCK_G2DSCF;
+  if (on(LG2IC1)) modes |= NEOXC_FOCK_G2IC1;
+  const char* fac = std::getenv("NEOXC_GAM4_FACTORED");
+  if (fac && std::strcmp(fac, "1") == 0) modes |= NEOXC_FOCK_GAM4_FACTORED;
+  const bool neohf = (modes & NEOXC_FOCK_NEOHF) != 0;
+  const bool t2 = !neohf && *nelec > 1, t3 = !neohf && *nelec > 2;
+  const bool t4 = t3 && (modes & NEOXC_FOCK_GAM4);
+  // the tables the reference reads from the working directory
+  std::vector<double> g1, g1s, g2, g2s, g3, g4, g2s4;
+  bool ok = true;
+  if (!neohf) ok = read_ufm("GAM_1.ufm", *ng1, g1) && read_ufm("GAM_1s.ufm", *ng1, g1s);
+  const double *p2 = GM2ICR, *p2s = GM2SICR, *p3 = GM3IC1, *p4 = GM4ICR, *p2s4 = nullptr;
+  if (ok && t2 && !(modes & (NEOXC_FOCK_G2DSCF | NEOXC_FOCK_G2IC1))) {
+    ok = read_ufm("GAM_2.ufm", *ng2, g2) && read_ufm("GAM_2s.ufm", *ng2, g2s);
+    p2 = g2.data();
+    p2s = g2s.data();
+  }
+  if (ok && t3 && !(modes & (NEOXC_FOCK_G3DSCF | NEOXC_FOCK_G3IC1))) {
+    ok = read_ufm("GAM_3.ufm", *ng3, g3);
+    p3 = g3.data();
+  }
+  if (ok && t4 && (modes & NEOXC_FOCK_G4DSCF)) {
+    ok = read_ufm("GAM_2s.ufm", *ng2, g2s4);   // gam4_DSCF_OMP.f:46-47
+    p2s4 = g2s4.data();
+  } else if (ok && t4 && !(modes & NEOXC_FOCK_G4IC)) {
+    ok = read_gam4_over16(*ng4, g4);
+    p4 = g4.data();
+  }
+  if (!ok) {
+    std::fprintf(stderr, "neoxc: xchf1_fock: cannot read an integral file\n");
+    return;
+  }
+  (void)SZG4IC;
+  (void)SZG3IC1;
+  (void)SZG2ICR;
+  report("xchf1_fock",
+         neoxc_xchf1_fock(modes, *NG4CHK, *NG3CHK, *NG2CHK, *npebf, *nebf, *npbf, *nelec,
+                          *ngee, *ng1, *ng2, *ng3, *ng4, DE, DP, GAM_ecore, GAM_pcore,
+                          GAM_ep, GAM_ee, g1.empty() ? nullptr : g1.data(),
+                          g1s.empty() ? nullptr : g1s.data(), p4, p3, p2, p2s, p2s4,
+                          *ng2prm, *ngtg1, *ng3prm, *nat, *pmass, cat, zan, bcoef1,
+                          gamma1, KPESTR, KPEEND, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX,
+                          NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, focke, fockp, Xfocke,
+                          Xfockp, E_total, E_nuc, E_ecore, E_pcore, E_ep, E_ee, E_gam1,
+                          E_gam2, E_gam3, E_gam4, S_total, S_gam1, S_gam2));
 }
 
 }  // extern "C"

@@ -31,6 +31,7 @@ __all__ = [
     "fae_omg1", "ufp_omg1", "fae_omg2", "ufp_omg2", "fae_omg3", "ufp_omg3", "fae_omg4",
     "ufp_omg4", "omg4_icr", "dev_xcuhf_omg", "dev_omg4_icr",
     "rxcuhfne_omg2", "rxchf_omg", "rxcuhf_omg", "rxchf_omg1", "xcuhf_scf", "XCUHF_SLOTS",
+    "onebody_integrals", "class_nuc_rep", "xchf1_fock", "FOCK",
 ]
 
 LIB_PATH = _build.LIB
@@ -121,6 +122,9 @@ def _declare(L):
         "neoxc_rxchfne_fbe_omg2": (I, [i64] * 6 + [vp] * 6),
         "neoxc_rxchfne_omg2_fused": (I, [i64] * 2 + [vp] * 8),
         "neoxc_xcfock_correction": (I, [i64, i64, d, d, d] + [vp] * 6),
+        "neoxc_onebody_integrals": (I, [i64] * 5 + [d] + [vp] * 20),
+        "neoxc_class_nuc_rep": (I, [i64, vp, vp, vp]),
+        "neoxc_xchf1_fock": (I, [i64] * 13 + [vp] * 13 + [i64] * 4 + [d] + [vp] * 32),
         "neoxc_probe_fp64": (I, [vp]),
         "neoxc_dev_gam4_dscf": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_dev_gam4_dscf_noalloc": (I, [vp, i64, i64] + [vp] * 7),
@@ -283,6 +287,74 @@ def gam2_dscf(s: NeoSystem, DE, DP, focke=None, fockp=None, se2=None, sp2=None,
                                  _p(fe), _p(fp), _p(se), _p(sp), _p(E), _p(S)))
     return (*_fock_out(fe, fp, ne, np_), *_fock_out(se, sp, ne, np_),
             float(E[0]), float(S[0]))
+
+
+# ---- one-body tables and the whole Fock build (xchf1_fock.f) --------------
+ONEBODY = ("Se", "Sp", "GAM_ecore", "GAM_pcore", "GAM_ep", "GAM_1", "GAM_1s")
+
+
+def onebody_integrals(s: NeoSystem, which=ONEBODY) -> dict:
+    """elec_ovlap / nuc_ovlap (pure_ovlap.f), calc_GAM_epcore, calc_GAM_ep,
+    GAM1_OMP_MD: each table in its file's record order (C-order [i][j] for
+    the 2-index ones, [ip][jp][ie][je] for GAM_ep / GAM_1 / GAM_1s)."""
+    ne, np_ = s.nebf, s.npbf
+    size = {"Se": ne * ne, "Sp": np_ * np_, "GAM_ecore": ne * ne, "GAM_pcore": np_ * np_,
+            "GAM_ep": s.ng1, "GAM_1": s.ng1, "GAM_1s": s.ng1}
+    out = {k: np.empty(size[k]) for k in which}
+    keep = [s.cat_f, s.zan_f, s.bgem_f, s.ggem_f, s.AMPEB2C_f, s.AGEBFCC_f, s.AGNBFCC_f,
+            s.ELCEX_f, s.NUCEX_f, s.ELCAM_f, s.NUCAM_f, s.ELCBFC_f, s.NUCBFC_f]
+    outs = [_p(out[k]) if k in out else None for k in ONEBODY]
+    _check(lib().neoxc_onebody_integrals(ne, s.npebf, np_, s.nat, s.ngtg, s.pmass,
+                                         *[_p(a) for a in keep], *outs))
+    return out
+
+
+def class_nuc_rep(s: NeoSystem) -> float:
+    """class_nuc_rep.f: classical nuclear repulsion."""
+    E = np.zeros(1)
+    _check(lib().neoxc_class_nuc_rep(s.nat, _p(s.zan_f), _p(s.cat_f), _p(E)))
+    return float(E[0])
+
+
+FOCK = {"neohf": 1, "gam4": 2, "g4dscf": 4, "g4ic": 8, "g3dscf": 16, "g3ic1": 32,
+        "g2dscf": 64, "g2ic1": 128, "gam4_factored": 256}
+FOCK_ENERGIES = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_gam1",
+                 "E_gam2", "E_gam3", "E_gam4", "S_total", "S_gam1", "S_gam2")
+
+
+def xchf1_fock(s: NeoSystem, DE, DP, tables: dict, E_nuc: float, modes=("gam4", "g4dscf",
+               "g3ic1", "g2ic1"), nchunks: int = 1) -> dict:
+    """xchf1_fock.f xchf1_fock on the device.  ``tables`` holds the arrays by
+    their reference names (GAM_ecore, GAM_pcore, GAM_ep, GAM_ee, GAM_1,
+    GAM_1s, GM2ICR, GM2SICR, GM3IC1, GM4ICR, GAM_2s; missing ones are passed
+    as NULL); ``modes`` names the LOGICAL switches that are true (FOCK)."""
+    ne, np_ = s.nebf, s.npbf
+    m = 0
+    for k in modes:
+        m |= FOCK[k]
+    de, dp = _fmat(DE), _fmat(DP)
+
+    def t(name):
+        v = tables.get(name)
+        return None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+
+    names = ("GAM_ecore", "GAM_pcore", "GAM_ep", "GAM_ee", "GAM_1", "GAM_1s", "GM4ICR",
+             "GM3IC1", "GM2ICR", "GM2SICR", "GAM_2s")
+    tab = [t(n) for n in names]
+    fe, fp, xfe, xfp = (np.zeros(ne * ne), np.zeros(np_ * np_), np.zeros(ne * ne),
+                        np.zeros(np_ * np_))
+    en = {k: np.zeros(1) for k in FOCK_ENERGIES}
+    en["E_nuc"][0] = E_nuc
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_xchf1_fock(
+        m, nchunks, nchunks, nchunks, s.npebf, ne, np_, s.nelec, s.ngee, s.ng1, s.ng2,
+        s.ng3, s.ng4, _p(de), _p(dp), *[None if a is None else _p(a) for a in tab],
+        s.ng2prm, s.ngtg, s.ng3prm, s.nat, s.pmass, *ptrs, _p(fe), _p(fp), _p(xfe),
+        _p(xfp), *[_p(en[k]) for k in FOCK_ENERGIES]))
+    out = {k: float(v[0]) for k, v in en.items()}
+    out["focke"], out["fockp"] = _fock_out(fe, fp, ne, np_)
+    out["Xfocke"], out["Xfockp"] = _fock_out(xfe, xfp, ne, np_)
+    return out
 
 
 SCF_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_gam1", "E_gam2",

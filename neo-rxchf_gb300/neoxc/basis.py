@@ -90,6 +90,8 @@ class NeoSystem:
 
     # ---- sizes (xcneo_HYBRID.f:463-473) ---------------------------------
     @property
+    def ng1(self): return self.nebf ** 2 * self.npbf ** 2
+    @property
     def ngee(self): return self.nebf ** 4
     @property
     def ng2(self): return self.nebf ** 4 * self.npbf ** 2
