@@ -310,6 +310,7 @@ void orc_gam_ep(const orc_system *s, double *Gep);
 void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
                     double *ansE, double *ansS);
 void orc_gam1(const orc_system *s, double *G1, double *G1s);
+void orc_rxchf_gam1(const orc_system *s, double *G1, double *G1s);
 double orc_nuc_rep(const orc_system *s);
 
 /* density from MO coefficients (GAM_IO.f read_elec_density) */

@@ -131,6 +131,7 @@ def lib():
                 "orc_gam_epcore": (None, [vp] * 3),
                 "orc_gam_ep": (None, [vp] * 2),
                 "orc_gam1": (None, [vp] * 3),
+                "orc_rxchf_gam1": (None, [vp] * 3),
                 "orc_nuc_rep": (C.c_double, [vp]),
                 "orc_num_threads": (C.c_int, []),
                 "orc_gam4_raw": (d, [i64, i64, vp, vp] + [i64] * 10),

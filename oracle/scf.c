@@ -117,9 +117,12 @@ void orc_gam_ep(const orc_system *s, double *Gep) {
         }
 }
 
-/* gam_1_OMP.f:398-836 xcalc_GAM1_MD: A = (e1, p), B = (e1', p') */
-void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
-                    double *ansE, double *ansS) {
+/* gam_1_OMP.f:398-836 xcalc_GAM1_MD: A = (e1, p), B = (e1', p').
+ * with_single = 0 is rxchf/rxchf_gam_1_OMP.f RXCHF_xcalc_GAM1_MD: the same
+ * sums without the single-geminal terms (tegx, texg, VCEGX, ..., OGX stay
+ * zero), only the geminal-pair loop. */
+static void xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
+                       int with_single, double *ansE, double *ansS) {
   const double zero = 0.0, one = 1.0;
   const int ng = (int)s->ngtg;
   const double pmass = s->pmass;
@@ -128,27 +131,29 @@ void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
          VMGX = zero, VMGG = zero, sval;
   for (int k = 0; k < ng; k++) {
     double GV = s->ggem[k], BCFV = s->bgem[k];
-    double tegxi = orc_pgike1(&A[0], &A[1], &B[0], &B[1], GV, zero, one, &sval);
-    double tpgxi = orc_pgike1(&A[1], &A[0], &B[1], &B[0], GV, zero, pmass, &sval);
-    tegx = tegx + BCFV * tegxi;
-    tpgx = tpgx + BCFV * tpgxi;
-    double VCEGXI = zero, VCPGXI = zero;
-    for (int64_t c = 0; c < s->nat; c++) {
-      const double C[3] = {s->cat[3 * c], s->cat[3 * c + 1], s->cat[3 * c + 2]};
-      double ZNUC = s->zan[c];
-      double a = orc_g2_xggvec(&A[0], &A[1], &B[0], &B[1], GV, zero, C);
-      VCEGXI = a * ZNUC + VCEGXI;
-      double b = orc_g2_xggvec(&A[1], &A[0], &B[1], &B[0], GV, zero, C);
-      VCPGXI = b * ZNUC + VCPGXI;
+    if (with_single) {
+      double tegxi = orc_pgike1(&A[0], &A[1], &B[0], &B[1], GV, zero, one, &sval);
+      double tpgxi = orc_pgike1(&A[1], &A[0], &B[1], &B[0], GV, zero, pmass, &sval);
+      tegx = tegx + BCFV * tegxi;
+      tpgx = tpgx + BCFV * tpgxi;
+      double VCEGXI = zero, VCPGXI = zero;
+      for (int64_t c = 0; c < s->nat; c++) {
+        const double C[3] = {s->cat[3 * c], s->cat[3 * c + 1], s->cat[3 * c + 2]};
+        double ZNUC = s->zan[c];
+        double a = orc_g2_xggvec(&A[0], &A[1], &B[0], &B[1], GV, zero, C);
+        VCEGXI = a * ZNUC + VCEGXI;
+        double b = orc_g2_xggvec(&A[1], &A[0], &B[1], &B[0], GV, zero, C);
+        VCPGXI = b * ZNUC + VCPGXI;
+      }
+      double VMGXI = orc_g2_xggvee(&A[0], &A[1], &B[0], &B[1], GV, zero);
+      VCEGX = VCEGX + BCFV * VCEGXI;
+      VCPGX = VCPGX + BCFV * VCPGXI;
+      VMGX = VMGX + BCFV * VMGXI;
+      double texgi = orc_pgike1(&A[0], &A[1], &B[0], &B[1], zero, GV, one, &sval);
+      double tpxgi = orc_pgike1(&A[1], &A[0], &B[1], &B[0], zero, GV, pmass, &sval);
+      texg = texg + BCFV * texgi;
+      tpxg = tpxg + BCFV * tpxgi;
     }
-    double VMGXI = orc_g2_xggvee(&A[0], &A[1], &B[0], &B[1], GV, zero);
-    VCEGX = VCEGX + BCFV * VCEGXI;
-    VCPGX = VCPGX + BCFV * VCPGXI;
-    VMGX = VMGX + BCFV * VMGXI;
-    double texgi = orc_pgike1(&A[0], &A[1], &B[0], &B[1], zero, GV, one, &sval);
-    double tpxgi = orc_pgike1(&A[1], &A[0], &B[1], &B[0], zero, GV, pmass, &sval);
-    texg = texg + BCFV * texgi;
-    tpxg = tpxg + BCFV * tpxgi;
     for (int l = 0; l < ng; l++) {
       double GW = s->ggem[l], BCFW = s->bgem[l];
       double teggi = orc_pgike1(&A[0], &A[1], &B[0], &B[1], GV, GW, one, &sval);
@@ -179,8 +184,10 @@ void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
   double OXX = zero, OGX = zero, OGG = zero;
   for (int k = 0; k < ng; k++) {
     double GV = s->ggem[k], BCFV = s->bgem[k];
-    double ogxix = orc_g2_xggs(&A[0], &A[1], &B[0], &B[1], GV, zero);
-    OGX = OGX + BCFV * ogxix;
+    if (with_single) {
+      double ogxix = orc_g2_xggs(&A[0], &A[1], &B[0], &B[1], GV, zero);
+      OGX = OGX + BCFV * ogxix;
+    }
     for (int l = 0; l < ng; l++) {
       double GW = s->ggem[l], BCFW = s->bgem[l];
       double oggix = orc_g2_xggs(&A[0], &A[1], &B[0], &B[1], GV, GW);
@@ -190,9 +197,15 @@ void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
   *ansS = OXX + 2.0 * OGX + OGG;
 }
 
+void orc_xcalc_gam1(const orc_prim *A, const orc_prim *B, const orc_system *s,
+                    double *ansE, double *ansS) {
+  xcalc_gam1(A, B, s, 1, ansE, ansS);
+}
+
 /* gam_1_OMP.f:2-395 GAM1_OMP_MD -> GAM_1, GAM_1s (ng1 = nebf^2 npbf^2),
  * packed by pack_4D(nebf,nebf,npbf, jec1,iec1,jp,ip) */
-void orc_gam1(const orc_system *s, double *G1, double *G1s) {
+static void gam1_tables(const orc_system *s, int with_single, double *G1,
+                        double *G1s) {
   const int64_t ne = s->nebf, npe = s->npebf, np = s->npbf;
   memset(G1, 0, sizeof(double) * (size_t)(ne * ne * np * np));
   memset(G1s, 0, sizeof(double) * (size_t)(ne * ne * np * np));
@@ -206,7 +219,7 @@ void orc_gam1(const orc_system *s, double *G1, double *G1s) {
           e_prim(s, je1, &B[0]);
           p_prim(s, jp, &B[1]);
           double ansE, ansS;
-          orc_xcalc_gam1(A, B, s, &ansE, &ansS);
+          xcalc_gam1(A, B, s, with_single, &ansE, &ansS);
           int64_t iec1 = s->AMPEB2C[ie1 - 1], jec1 = s->AMPEB2C[je1 - 1];
           double cip = s->AGNBFCC[ip - 1], cjp = s->AGNBFCC[jp - 1];
           double cie = s->AGEBFCC[ie1 - 1], cje = s->AGEBFCC[je1 - 1];
@@ -214,6 +227,16 @@ void orc_gam1(const orc_system *s, double *G1, double *G1s) {
           G1[ia - 1] = G1[ia - 1] + ansE * cip * cjp * cie * cje;
           G1s[ia - 1] = G1s[ia - 1] + ansS * cip * cjp * cie * cje;
         }
+}
+
+void orc_gam1(const orc_system *s, double *G1, double *G1s) {
+  gam1_tables(s, 1, G1, G1s);
+}
+
+/* rxchf/rxchf_gam_1_OMP.f:2-175 RXCHF_GAM1_OMP_MD (the special electron and
+ * the proton share every geminal factor) */
+void orc_rxchf_gam1(const orc_system *s, double *G1, double *G1s) {
+  gam1_tables(s, 0, G1, G1s);
 }
 
 /* class_nuc_rep.f:2-45 class_nuc_rep */

@@ -49,6 +49,12 @@ def golden_xcuhf():
 
 
 @pytest.fixture(scope="session")
+def golden_rx():
+    with open(os.path.join(GOLDEN, "rx_examples.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
 def golden_spot():
     with open(os.path.join(GOLDEN, "spot_check.json")) as f:
         return json.load(f)

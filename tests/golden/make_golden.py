@@ -14,6 +14,10 @@ Writes, next to this script:
                       converged MOs (answer/FinalC{AE,BE,P}.dat) and the
                       energy components of answer/XCUHF.log for the initial
                       guess and at convergence;
+  rx_examples.json    examples/rxchf/one_special_electron (RXCHF-ne) and
+                      examples/rxcuhf/rxchf-{ne,ae} (RXCUHF, EXCHLEV 0 / 1):
+                      input decks and the energy components of their logs
+                      for the initial guess and at convergence;
   spot_check.json     CS_Integrals/Spot_Check/TEST_G{2,3,4}: the single-
                       primitive inputs (first record block, as SCI.f:114-152
                       reads them) and the MD values printed in each ``out``.
@@ -95,6 +99,31 @@ def xcuhf_example(ref: str) -> dict:
     }
 
 
+RX_KEYS = ("E_NUC", "E_ECORE", "E_EE", "E_OMG1", "E_OMG2", "S_TOTAL", "E_TOTAL")
+RX_EXAMPLES = {   # name: (directory under examples/, input deck, log)
+    "rxchf_ne": ("rxchf/one_special_electron", "exam_rxchf.inp", "RXCHF.log"),
+    "rxcuhf_ne": ("rxcuhf/rxchf-ne", "exam_rxcuhfne.inp", "RXCHF-ne.log"),
+    "rxcuhf_ae": ("rxcuhf/rxchf-ae", "exam_rxcuhfae.inp", "RXCHF-ae.log"),
+}
+
+
+def rx_examples(ref: str) -> dict:
+    out = {}
+    for name, (sub, inp, logname) in RX_EXAMPLES.items():
+        d = os.path.join(ref, "examples", sub)
+        log = open(os.path.join(d, "answer", logname)).read()
+        m = re.search(r"FINAL NEORX\w* ENERGY IS\s+(-?[0-9.]+)\s+AFTER\s+(\d+)", log)
+        out[name] = {
+            "source": "examples/%s/%s, answer/%s" % (sub, inp, logname),
+            "inp": open(os.path.join(d, inp)).read(),
+            "initial": _components(log, "INITIAL GUESS ENERGETICS", RX_KEYS),
+            "final": _components(log, m.group(0), RX_KEYS),
+            "final_energy": float(m.group(1)),
+            "iterations": int(m.group(2)),
+        }
+    return out
+
+
 def _first_block(path: str):
     rows = [l.split() for l in open(path).read().splitlines()]
     k = 0
@@ -137,6 +166,8 @@ def main(ref: str):
         json.dump(xcuhf_example(ref), f, indent=1)
     with open(os.path.join(HERE, "spot_check.json"), "w") as f:
         json.dump(spot_check(ref), f, indent=1)
+    with open(os.path.join(HERE, "rx_examples.json"), "w") as f:
+        json.dump(rx_examples(ref), f, indent=1)
 
 
 if __name__ == "__main__":
