@@ -235,6 +235,17 @@ int neoxc_onebody_integrals(int64_t nebf, int64_t npebf, int64_t npbf,
                             const double* NUCBFC, double* Se, double* Sp,
                             double* GAM_ecore, double* GAM_pcore,
                             double* GAM_ep, double* GAM_1, double* GAM_1s);
+/* rxchf/rxchf_gam_1_OMP.f:2-175 RXCHF_GAM1_OMP_MD: GAM_1 / GAM_1s of the
+ * special electron and the proton, which share every geminal factor (the
+ * geminal-pair terms of GAM1_OMP_MD only); same layout as GAM_1 above. */
+int neoxc_rxchf_gam1(int64_t nebf, int64_t npebf, int64_t npbf, int64_t ng1,
+                     int64_t ng1prm, int64_t nat, int64_t ngtg1, double pmass,
+                     const double* cat, const double* zan, const double* bcoef1,
+                     const double* gamma1, const int64_t* AMPEB2C,
+                     const double* AGEBFCC, const double* AGNBFCC,
+                     const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+                     const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC,
+                     double* GAM_1, double* GAM_1s);
 /* class_nuc_rep.f:2-45: E_nuc = sum_{i<j} Z_i Z_j / |R_i - R_j| (host
  * arithmetic, O(nat^2)). */
 int neoxc_class_nuc_rep(int64_t nat, const double* zan, const double* cat,
@@ -481,6 +492,47 @@ int neoxc_xcuhf_scf(int64_t nelec, int64_t NAE, int64_t NBE, int64_t nucst,
                     int64_t maxit, double* DAE, double* DBE, double* DP, double* E_init,
                     double* E_final, double* history, int64_t* niter,
                     int64_t* converged);
+
+/* One-special-electron RXCHF SCF on the device (NBE = 1), `kind`:
+ *   NEOXC_RX_NE     rxchfne/rxchfne_scf.f xcrxchfne: RXCHF-ne, NAE
+ *                   closed-shell regular electrons (NAalpE, NAbetE unused);
+ *   NEOXC_RX_CU_NE  rxchfne/rxcuhfne_scf.f xcrxcuhfne, EXCHLEV 0: NAalpE
+ *                   alpha and NAbetE beta regular electrons (NAE unused);
+ *   NEOXC_RX_CU_AE  the same with EXCHLEV 1 (LADDEXCH: RXCUHFne_*_OMG2).
+ * Builds Se, Sp, GAM_ecore, GAM_pcore, GAM_ee, GAM_1 / GAM_1s of
+ * RXCHF_GAM1_OMP_MD (rxchf/rxchf_gam_1_OMP.f) and GM2ICR / GM2exICR of
+ * RXCHFne_GAM2_IC1; guesses as RXCHF_guess_elec / RXCUHF_guess_elec
+ * (rxchf/rxchf_scf.f:785-844, rxchf/rxcuhf_scf.f:863-934) and guess_prot2;
+ * then the LOCBSE2 iteration: per iteration a Fock build (RXCHFne_FOCK,
+ * rxchfne_fock.f:2-250, or RXCUHFne_FOCK) and the proton's UROOTHAN, then
+ * micro-iterations (at most 200) of regular-electron UROOTHAN and
+ * RXCHF_OCBSE2 / RXCUHF_OCBSE2 (rxchf/rxchf_scf.f:1124-1330) for the
+ * special electron, each followed by a Fock build, until the regular and
+ * special densities move less than 1e-6; converged when the proton density
+ * of an iteration moved less than 1e-4.  The second-order steps the
+ * reference takes for the regular electrons (LSOSCF) are not ported: they
+ * change the path, not the converged state.
+ * Out: DA (DAE, or DAalpE), DAbet (DAbetE, open shell only), DBE, DP;
+ * E_init / E_final [16]: 0 E_TOTAL (with E_nuc), 1 E_NUC, 2 E_ECORE, 3 E_EE,
+ * 4 E_OMG1, 5 E_OMG2, 6 S_TOTAL (the components the logs print), 7 E_P_OMG1,
+ * 8 E_P_OMG2, 9 S_P_OMG1, 10 E_BE_OMG1, 11 S_BE_OMG1, 12 / 13 / 14 last
+ * regular / special / proton density change, 15 micro-iterations of the
+ * last iteration; history [3*maxit]: E_TOTAL, micro-iterations, proton
+ * density change per iteration.  Limits: nebf, npbf <= 64. */
+#define NEOXC_RX_NE 0
+#define NEOXC_RX_CU_NE 1
+#define NEOXC_RX_CU_AE 2
+int neoxc_rx_scf(int64_t kind, int64_t NAE, int64_t NAalpE, int64_t NAbetE,
+                 int64_t nucst, int64_t nebf, int64_t npebf, int64_t npbf,
+                 int64_t nat, int64_t ngtg1, double pmass, const double* cat,
+                 const double* zan, const double* bcoef1, const double* gamma1,
+                 const int64_t* KPESTR, const int64_t* KPEEND,
+                 const int64_t* AMPEB2C, const double* AGEBFCC,
+                 const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                 const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                 const double* NUCBFC, int64_t maxit, double* DA, double* DAbet,
+                 double* DBE, double* DP, double* E_init, double* E_final,
+                 double* history, int64_t* niter, int64_t* converged);
 
 /* ---- open-shell XCUHF contractions: xcuhf/xcuhf_omg{1..4}.f ------------ */
 /* Same arguments, packed layouts and semantics as the reference: the Fock
@@ -979,6 +1031,14 @@ void gam1_omp_md_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf
                   const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
                   const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
                   const double* NUCBFC);
+void rxchf_gam1_omp_md_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                        const int64_t* ng1, const int64_t* ng1prm, const int64_t* nat,
+                        const int64_t* ngtg1, const double* pmass, const double* cat,
+                        const double* zan, const double* bcoef1, const double* gamma1,
+                        const int64_t* AMPEB2C, const double* AGEBFCC,
+                        const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                        const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                        const double* NUCBFC);
 void gam2_conv_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npebf,
                 const int64_t* npbf, const int64_t* ng2, const int64_t* ng2prm,
                 const int64_t* nat, const int64_t* ngtg1, const double* pmass,

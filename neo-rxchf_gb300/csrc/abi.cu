@@ -1013,17 +1013,15 @@ int neoxc_class_nuc_rep(int64_t nat, const double* zan, const double* cat,
 // The same kernels the device SCF builds its tables with; outputs that are
 // not asked for are not computed, and the parts of the system only they
 // need are replaced by one s function at the origin.
-int neoxc_onebody_integrals(int64_t nebf, int64_t npebf, int64_t npbf,
-                            int64_t nat, int64_t ngtg1, double pmass,
-                            const double* cat, const double* zan,
-                            const double* bcoef1, const double* gamma1,
-                            const int64_t* AMPEB2C, const double* AGEBFCC,
-                            const double* AGNBFCC, const double* ELCEX,
-                            const double* NUCEX, const int64_t* ELCAM,
-                            const int64_t* NUCAM, const double* ELCBFC,
-                            const double* NUCBFC, double* Se, double* Sp,
-                            double* GAM_ecore, double* GAM_pcore,
-                            double* GAM_ep, double* GAM_1, double* GAM_1s) {
+static int onebody_impl(int64_t nebf, int64_t npebf, int64_t npbf, int64_t nat,
+                        int64_t ngtg1, double pmass, const double* cat, const double* zan,
+                        const double* bcoef1, const double* gamma1,
+                        const int64_t* AMPEB2C, const double* AGEBFCC,
+                        const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                        const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                        const double* NUCBFC, double* Se, double* Sp, double* GAM_ecore,
+                        double* GAM_pcore, double* GAM_ep, double* GAM_1, double* GAM_1s,
+                        int gam1_pairs_only) {
   const bool want_g1 = GAM_1 || GAM_1s;
   const bool want_core = GAM_ecore || GAM_pcore;
   const bool want_e = Se || GAM_ecore || GAM_ep || want_g1;
@@ -1084,11 +1082,43 @@ int neoxc_onebody_integrals(int64_t nebf, int64_t npebf, int64_t npbf,
   if (want_g1) {
     RC(dalloc(g1, sizeof(double) * n1, s));
     RC(dalloc(g1s, sizeof(double) * n1, s));
-    CU(launch_gam1(u.d, g1.as<double>(), g1s.as<double>(), s, 0));
+    CU(launch_gam1(u.d, g1.as<double>(), g1s.as<double>(), s, 0, gam1_pairs_only));
     RC(back(GAM_1, g1, n1));
     RC(back(GAM_1s, g1s, n1));
   }
   return finish(s);
+}
+
+int neoxc_onebody_integrals(int64_t nebf, int64_t npebf, int64_t npbf,
+                            int64_t nat, int64_t ngtg1, double pmass,
+                            const double* cat, const double* zan,
+                            const double* bcoef1, const double* gamma1,
+                            const int64_t* AMPEB2C, const double* AGEBFCC,
+                            const double* AGNBFCC, const double* ELCEX,
+                            const double* NUCEX, const int64_t* ELCAM,
+                            const int64_t* NUCAM, const double* ELCBFC,
+                            const double* NUCBFC, double* Se, double* Sp,
+                            double* GAM_ecore, double* GAM_pcore,
+                            double* GAM_ep, double* GAM_1, double* GAM_1s) {
+  return onebody_impl(nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1, gamma1,
+                      AMPEB2C, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC,
+                      Se, Sp, GAM_ecore, GAM_pcore, GAM_ep, GAM_1, GAM_1s, 0);
+}
+
+// rxchf/rxchf_gam_1_OMP.f:2-175 RXCHF_GAM1_OMP_MD
+int neoxc_rxchf_gam1(int64_t nebf, int64_t npebf, int64_t npbf, int64_t ng1, int64_t ng1prm,
+                     int64_t nat, int64_t ngtg1, double pmass, const double* cat,
+                     const double* zan, const double* bcoef1, const double* gamma1,
+                     const int64_t* AMPEB2C, const double* AGEBFCC, const double* AGNBFCC,
+                     const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+                     const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC,
+                     double* GAM_1, double* GAM_1s) {
+  RC(need(ng1 == nebf * nebf * npbf * npbf && ng1prm == npebf * npebf * npbf * npbf,
+          "ng1 == nebf**2 npbf**2, ng1prm == npebf**2 npbf**2"));
+  RC(need(GAM_1 && GAM_1s, "GAM_1, GAM_1s"));
+  return onebody_impl(nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1, gamma1,
+                      AMPEB2C, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC,
+                      nullptr, nullptr, nullptr, nullptr, nullptr, GAM_1, GAM_1s, 1);
 }
 
 // ---- xchf1_independent/xchf1_fock.f:2-361 xchf1_fock ------------------------
@@ -2476,4 +2506,234 @@ extern "C" int neoxc_xcuhf_scf(int64_t nelec, int64_t NAE, int64_t NBE, int64_t 
                       zan, bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
                       ELCAM, NUCAM, ELCBFC, NUCBFC, options, maxit, DAE, DBE, DP, E_init,
                       E_final, history, niter, converged);
+}
+
+// ---- one-special-electron RXCHF SCF on the device ---------------------------
+// rxchfne/rxchfne_scf.f xcrxchfne (closed-shell regular electrons) and
+// rxchfne/rxcuhfne_scf.f xcrxcuhfne (open shell, EXCHLEV 0 or 1), LOCBSE2
+// branch with UROOTHAN for the regular electrons.
+namespace {
+
+int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t NAbetE,
+              int64_t nucst, int64_t nebf, int64_t npebf, int64_t npbf, int64_t nat,
+              int64_t ngtg1, double pmass, const double* cat, const double* zan,
+              const double* bcoef1, const double* gamma1, const int64_t* KPESTR,
+              const int64_t* KPEEND, const double* AGEBFCC, const double* AGNBFCC,
+              const double* ELCEX, const double* NUCEX, const int64_t* ELCAM,
+              const int64_t* NUCAM, const double* ELCBFC, const double* NUCBFC,
+              int64_t maxit, double* DA, double* DAbet, double* DBE, double* DP,
+              double* E_init, double* E_final, double* history, int64_t* niter,
+              int64_t* converged) {
+  RC(need(kind == NEOXC_RX_NE || kind == NEOXC_RX_CU_NE || kind == NEOXC_RX_CU_AE, "kind"));
+  const bool open = kind != NEOXC_RX_NE;
+  if (open)
+    RC(need(NAalpE >= 1 && NAbetE >= 0, "NAalpE >= 1, NAbetE >= 0"));
+  else
+    RC(need(NAE >= 1, "NAE >= 1"));
+  RC(need(maxit >= 1 && nucst >= 1 && nucst <= npbf, "maxit >= 1, 1 <= nucst <= npbf"));
+  RC(need(DA && DBE && DP && E_init && E_final && niter && converged && (!open || DAbet),
+          "pointers"));
+  if (nebf > kScfMaxN || npbf > kScfMaxN)
+    return set_err(NEOXC_ERR_UNSUPPORTED, "RXCHF SCF: nebf, npbf <= %d", kScfMaxN);
+  const int nocca = open ? (int)NAalpE : (NAE > 1 ? (int)(NAE / 2) : (int)NAE);
+  const double prefA = (!open && NAE > 1) ? 2.0 : 1.0;
+  const int nreg = open ? (int)(NAalpE + NAbetE) : (int)NAE;
+  RC(need(nocca < nebf && (!open || NAbetE < nebf), "regular orbitals < nebf"));
+  SysUpload u;
+  RC(stage_system(u, s, nebf, npebf, npbf, nat, ngtg1, pmass, cat, zan, bcoef1, gamma1,
+                  KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC,
+                  NUCBFC));
+  const int ne = (int)nebf, np = (int)npbf;
+  const size_t e2 = (size_t)ne * ne, p2 = (size_t)np * np, ng1 = e2 * p2, ng2 = e2 * e2 * p2;
+  // integrals: Se, Sp, GAM_ecore/pcore, RXCHF GAM_1, GAM_ee, RXCHFne gam_2
+  DBuf Se, Sp, Hce, Hcp, G1, G1s, Gee, G2, G2x, Xe, Xp;
+  for (DBuf* b : {&Se, &Hce, &Xe}) RC(dalloc(*b, sizeof(double) * e2, s));
+  for (DBuf* b : {&Sp, &Hcp, &Xp}) RC(dalloc(*b, sizeof(double) * p2, s));
+  RC(dalloc(G1, sizeof(double) * ng1, s));
+  RC(dalloc(G1s, sizeof(double) * ng1, s));
+  RC(dalloc(Gee, sizeof(double) * e2 * e2, s));
+  RC(dalloc(G2, sizeof(double) * ng2, s));
+  RC(dalloc(G2x, sizeof(double) * ng2, s));
+  CU(launch_scf_onebody(u.d, Se.as<double>(), Sp.as<double>(), Hce.as<double>(),
+                        Hcp.as<double>(), s));
+  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, 0, 1));
+  CU(launch_gam_ee(u.d, Gee.as<double>(), s));
+  CU(launch_gam2_raw(u.d, 1, G2.as<double>(), G2x.as<double>(), s));
+  CU(launch_gam2_symmetrize(ne, np, 1, G2.as<double>(), G2x.as<double>(), s));
+  // SCF state
+  DBuf dA, dB, dT, dBE, dP, A0, B0, BE0, P0, CA, CBE, Ctmp, FA, FB, FP, FBE, XFA1, XFB1,
+      XFA2, XFB2, XFP, XSP, XFBE, XSBE, feo, fpo, part, scr, ocb, en, info, st, dumE;
+  for (DBuf* b : {&dA, &dB, &dT, &dBE, &A0, &B0, &BE0, &CA, &CBE, &Ctmp, &FA, &FB, &FBE,
+                  &XFA1, &XFB1, &XFA2, &XFB2, &XFBE, &XSBE})
+    RC(dalloc(*b, sizeof(double) * e2, s));
+  for (DBuf* b : {&dP, &P0, &FP, &XFP, &XSP}) RC(dalloc(*b, sizeof(double) * p2, s));
+  RC(dalloc(feo, sizeof(double) * 2 * e2, s));
+  RC(dalloc(fpo, sizeof(double) * 2 * p2, s));
+  RC(dalloc(part, sizeof(double) * rx_fock1_part_doubles(ne), s));
+  RC(dalloc(scr, sizeof(double) * std::max(omg2_partial_doubles(ne, np),
+                                           rx_scratch_doubles(ne, np)), s));
+  RC(dalloc(ocb, sizeof(double) * ocbse_scratch_doubles(ne), s));
+  RC(dalloc(en, sizeof(double) * kRxSlots, s));
+  RC(dalloc(info, sizeof(double) * 4, s));
+  RC(dalloc(st, sizeof(int) * 16, s));
+  RC(dalloc(dumE, sizeof(double) * 4, s));
+  for (DBuf* b : {&A0, &B0, &BE0, &CBE, &dB, &dT})
+    CU(cudaMemsetAsync(b->p, 0, sizeof(double) * e2, s));
+  CU(cudaMemsetAsync(P0.p, 0, sizeof(double) * p2, s));
+  CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kRxSlots, s));
+  CU(cudaMemsetAsync(st.p, 0, sizeof(int) * 16, s));
+  const double Enuc = nuc_rep(nat, zan, cat);
+  CU(cudaMemcpyAsync(en.as<double>() + 1, &Enuc, sizeof(double), cudaMemcpyHostToDevice, s));
+  int* sts = st.as<int>();
+  double* d_en = en.as<double>();
+  CU(launch_inv_sqrt(ne, Se.as<double>(), Xe.as<double>(), sts + 0, s));
+  CU(launch_inv_sqrt(np, Sp.as<double>(), Xp.as<double>(), sts + 1, s));
+  // guesses: RXCHF_guess_elec / RXCUHF_guess_elec (one UROOTHAN of the
+  // electronic core Hamiltonian: regular orbitals first, the special
+  // electron in the next one), guess_prot2
+  CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), 0, nocca, prefA, dA.as<double>(),
+                    nullptr, CA.as<double>(), sts + 2, s));
+  if (open && NAbetE > 0)
+    CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), 0, (int)NAbetE, 1.0,
+                      dB.as<double>(), nullptr, nullptr, sts + 3, s));
+  CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), nocca, 1, 1.0, dBE.as<double>(),
+                    nullptr, Ctmp.as<double>(), sts + 4, s));
+  CU(cudaMemcpyAsync(CBE.p, Ctmp.as<double>() + (size_t)ne * nocca, sizeof(double) * ne,
+                     cudaMemcpyDeviceToDevice, s));
+  CU(launch_roothan(np, Hcp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
+                    dP.as<double>(), nullptr, nullptr, sts + 5, s));
+  const bool exch = kind == NEOXC_RX_CU_AE;
+  auto fock = [&]() -> int {
+    CU(launch_rx_fock1(ne, open ? 1 : 0, nreg > 1 ? 1 : 0, Hce.as<double>(), Gee.as<double>(),
+                       dA.as<double>(), open ? dB.as<double>() : nullptr, XFA1.as<double>(),
+                       open ? XFB1.as<double>() : nullptr, open ? dT.as<double>() : nullptr,
+                       part.as<double>(), d_en, s));
+    for (DBuf* b : {&XFA2, &XFB2, &XFBE}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * e2, s));
+    CU(cudaMemsetAsync(XFP.p, 0, sizeof(double) * p2, s));
+    // RXCHF_FP_OMG1 / RXCHF_FBE_OMG1 with the special electron's density
+    CU(launch_omg1(ne, np, G1.as<double>(), G1s.as<double>(), dBE.as<double>(),
+                   dP.as<double>(), feo.as<double>(), fpo.as<double>(), s));
+    CU(launch_spin_finish(np, fpo.as<double>(), fpo.as<double>() + p2, dP.as<double>(), 1.0,
+                          XFP.as<double>(), XSP.as<double>(), d_en + 7, d_en + 9, s));
+    CU(launch_spin_finish(ne, feo.as<double>(), feo.as<double>() + e2, dBE.as<double>(), 1.0,
+                          XFBE.as<double>(), XSBE.as<double>(), d_en + 10, d_en + 11, s));
+    if (exch) {   // RXCUHFne_FE/FP/FBE_OMG2 (LADDEXCH)
+      CU(launch_rx(RxRoutine::CuhfneFE2, ne, np, G2.as<double>(), G2x.as<double>(), nullptr,
+                   dA.as<double>(), nullptr, dT.as<double>(), dBE.as<double>(), dP.as<double>(),
+                   scr.as<double>(), XFA2.as<double>(), XFB2.as<double>(), nullptr,
+                   dumE.as<double>(), s));
+      CU(launch_rx(RxRoutine::CuhfneFP2, ne, np, G2.as<double>(), G2x.as<double>(), nullptr,
+                   dA.as<double>(), nullptr, dT.as<double>(), dBE.as<double>(), dP.as<double>(),
+                   scr.as<double>(), XFP.as<double>(), nullptr, nullptr, d_en + 8, s));
+      CU(launch_rx(RxRoutine::CuhfneFBE2, ne, np, G2.as<double>(), G2x.as<double>(), nullptr,
+                   dA.as<double>(), nullptr, dT.as<double>(), dBE.as<double>(), dP.as<double>(),
+                   scr.as<double>(), XFBE.as<double>(), nullptr, nullptr, dumE.as<double>(), s));
+    } else {
+      // RXCHFne_FAE/FP/FBE_OMG2 in one pass; the FAE part depends on DBE and
+      // DP only, so the open-shell alpha and beta matrices are the same one
+      CU(launch_rxchfne_omg2(ne, np, open ? dT.as<double>() : dA.as<double>(),
+                             dBE.as<double>(), dP.as<double>(), G2.as<double>(),
+                             scr.as<double>(), XFA2.as<double>(), XFP.as<double>(),
+                             XFBE.as<double>(), d_en + 8, s));
+    }
+    CU(launch_rx_assemble(ne, np, d_en, XFA1.as<double>(), XFA2.as<double>(),
+                          open ? XFB1.as<double>() : nullptr,
+                          open ? (exch ? XFB2.as<double>() : XFA2.as<double>()) : nullptr,
+                          XFP.as<double>(), XSP.as<double>(), XFBE.as<double>(),
+                          XSBE.as<double>(), FA.as<double>(), FB.as<double>(),
+                          FP.as<double>(), FBE.as<double>(), s));
+    return NEOXC_OK;
+  };
+  auto check_eig = [&](int n_status) -> int {
+    int hs[16];
+    CU(cudaMemcpyAsync(hs, st.p, sizeof(int) * n_status, cudaMemcpyDeviceToHost, s));
+    RC(finish(s));
+    for (int k = 0; k < n_status; k++)
+      if (hs[k] > 40)
+        return set_err(NEOXC_ERR_CUDA, "UROOTHAN: Jacobi eigensolver did not converge");
+    return NEOXC_OK;
+  };
+  const double tolE = 1.0e-6, tolP = 1.0e-4;   // rxchfne_scf.f TOLE, TOLP
+  const int maxmicro = 200;
+  bool done = false;
+  double h[kRxSlots];
+  double* dBdiff = info.as<double>() + 2;
+  for (int64_t it = 1; it <= maxit && !done; it++) {
+    RC(fock());
+    if (it == 1) {
+      CU(cudaMemcpyAsync(E_init, d_en, sizeof(double) * kRxSlots, cudaMemcpyDeviceToHost, s));
+      RC(finish(s));
+    }
+    CU(launch_roothan(np, FP.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
+                      dP.as<double>(), nullptr, nullptr, sts + 6, s));
+    CU(launch_rx_dendif(np, dP.as<double>(), P0.as<double>(), d_en + 14, s));
+    int micro = 0;
+    double dreg = 0.0;
+    for (micro = 1; micro <= maxmicro; micro++) {
+      if (micro == 1) RC(fock());
+      CU(launch_roothan(ne, FA.as<double>(), Xe.as<double>(), 0, nocca, prefA, dA.as<double>(),
+                        nullptr, CA.as<double>(), sts + 7, s));
+      CU(launch_rx_dendif(ne, dA.as<double>(), A0.as<double>(), d_en + 12, s));
+      if (open && NAbetE > 0) {
+        CU(launch_roothan(ne, FB.as<double>(), Xe.as<double>(), 0, (int)NAbetE, 1.0,
+                          dB.as<double>(), nullptr, nullptr, sts + 8, s));
+        CU(launch_rx_dendif(ne, dB.as<double>(), B0.as<double>(), dBdiff, s));
+      }
+      // RXCHF_OCBSE2 / RXCUHF_OCBSE2 with the Fock matrix of the densities
+      // before this micro-iteration's regular update
+      CU(launch_ocbse2(ne, nocca, CA.as<double>(), CBE.as<double>(), FBE.as<double>(),
+                       Se.as<double>(), ocb.as<double>(), CBE.as<double>(), dBE.as<double>(),
+                       info.as<double>(), sts + 9, s));
+      CU(launch_rx_dendif(ne, dBE.as<double>(), BE0.as<double>(), d_en + 13, s));
+      RC(fock());
+      double hi[4];
+      CU(cudaMemcpyAsync(h, d_en, sizeof(h), cudaMemcpyDeviceToHost, s));
+      CU(cudaMemcpyAsync(hi, info.p, sizeof(hi), cudaMemcpyDeviceToHost, s));
+      RC(check_eig(11));
+      if (!(hi[1] > 0.0))
+        return set_err(NEOXC_ERR_CUDA, "OCBSE2: the projected special orbital vanished");
+      dreg = (open && NAbetE > 0) ? std::max(h[12], hi[2]) : h[12];
+      if (dreg < tolE && h[13] < tolE) break;
+    }
+    if (micro > maxmicro) micro = maxmicro;
+    h[12] = dreg;
+    h[15] = (double)micro;
+    if (history) {
+      history[3 * (it - 1) + 0] = h[0];
+      history[3 * (it - 1) + 1] = (double)micro;
+      history[3 * (it - 1) + 2] = h[14];
+    }
+    for (int k = 0; k < kRxSlots; k++) E_final[k] = h[k];
+    *niter = it;
+    done = h[14] < tolP;
+  }
+  *converged = done ? 1 : 0;
+  CU(cudaMemcpyAsync(DA, dA.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  if (open) CU(cudaMemcpyAsync(DAbet, dB.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(DBE, dBE.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(DP, dP.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  return finish(s);
+}
+
+}  // namespace
+
+extern "C" int neoxc_rx_scf(int64_t kind, int64_t NAE, int64_t NAalpE, int64_t NAbetE,
+                            int64_t nucst, int64_t nebf, int64_t npebf, int64_t npbf,
+                            int64_t nat, int64_t ngtg1, double pmass, const double* cat,
+                            const double* zan, const double* bcoef1, const double* gamma1,
+                            const int64_t* KPESTR, const int64_t* KPEEND,
+                            const int64_t* AMPEB2C, const double* AGEBFCC,
+                            const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                            const int64_t* ELCAM, const int64_t* NUCAM,
+                            const double* ELCBFC, const double* NUCBFC, int64_t maxit,
+                            double* DA, double* DAbet, double* DBE, double* DP,
+                            double* E_init, double* E_final, double* history,
+                            int64_t* niter, int64_t* converged) {
+  (void)AMPEB2C;
+  cudaStream_t s;
+  RC(get_stream(&s));
+  return rx_scf_on(s, kind, NAE, NAalpE, NAbetE, nucst, nebf, npebf, npbf, nat, ngtg1, pmass,
+                   cat, zan, bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
+                   ELCAM, NUCAM, ELCBFC, NUCBFC, maxit, DA, DAbet, DBE, DP, E_init, E_final,
+                   history, niter, converged);
 }

@@ -612,6 +612,25 @@ void gam1_omp_md_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf
   report("GAM1_OMP_MD", rc);
 }
 
+// rxchf/rxchf_gam_1_OMP.f:2-175 RXCHF_GAM1_OMP_MD -> GAM_1.ufm, GAM_1s.ufm
+void rxchf_gam1_omp_md_(const int64_t* nebf, const int64_t* npebf, const int64_t* npbf,
+                        const int64_t* ng1, const int64_t* ng1prm, const int64_t* nat,
+                        const int64_t* ngtg1, const double* pmass, const double* cat,
+                        const double* zan, const double* bcoef1, const double* gamma1,
+                        const int64_t* AMPEB2C, const double* AGEBFCC,
+                        const double* AGNBFCC, const double* ELCEX, const double* NUCEX,
+                        const int64_t* ELCAM, const int64_t* NUCAM, const double* ELCBFC,
+                        const double* NUCBFC) {
+  std::vector<double> g((size_t)*ng1), gs((size_t)*ng1);
+  int rc = neoxc_rxchf_gam1(*nebf, *npebf, *npbf, *ng1, *ng1prm, *nat, *ngtg1, *pmass, cat,
+                            zan, bcoef1, gamma1, AMPEB2C, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
+                            ELCAM, NUCAM, ELCBFC, NUCBFC, g.data(), gs.data());
+  if (rc == NEOXC_OK && !(write_ufm("GAM_1.ufm", g.data(), *ng1) &&
+                          write_ufm("GAM_1s.ufm", gs.data(), *ng1)))
+    rc = NEOXC_ERR_IO;
+  report("RXCHF_GAM1_OMP_MD", rc);
+}
+
 // gam2_CONV_OMP.f GAM2_CONV: the symmetrised gam_2 / gam_2s into GAM_2.ufm,
 // GAM_2s.ufm (the in-core GAM2_IC1 result, written by record)
 void gam2_conv_(const int64_t* Nchunks, const int64_t* nebf, const int64_t* npebf,

@@ -167,7 +167,7 @@ __device__ __forceinline__ md32::Prim to_prim32(const DevPrim& p) {
 // the warp sums them in a fixed shuffle order (deterministic).
 template <bool F32>
 __global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
-                            double* __restrict__ G1s) {
+                            double* __restrict__ G1s, int pairs_only) {
   const int ne = S.nebf, np = S.npbf;
   const int total = np * np * ne * ne;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
@@ -181,10 +181,11 @@ __global__ void gam1_kernel(DevSystem S, double* __restrict__ G1,
   const int na = S.kpeend[ie] - S.kpestr[ie] + 1;
   const int nb = S.kpeend[je] - S.kpestr[je] + 1;
   const int nq = na * nb, ng = S.ngtg;
+  const int g0 = pairs_only ? ng : 0, nit = pairs_only ? ng * ng : ng + ng * ng;
   double e = 0.0, sv = 0.0;
   // lanes take (geminal item, primitive pair), the pair fastest
-  for (int q2 = lane; q2 < nq * (ng + ng * ng); q2 += 32) {
-    const int gi = q2 / nq, k = q2 - gi * nq;
+  for (int q2 = lane; q2 < nq * nit; q2 += 32) {
+    const int gq = q2 / nq, k = q2 - gq * nq, gi = g0 + gq;
     const int a = S.kpestr[ie] + k / nb, b = S.kpestr[je] + k % nb;
     double aE, aS;
     if constexpr (F32) {
@@ -842,11 +843,11 @@ cudaError_t launch_gam_ep(const DevSystem& S, double* Gep, cudaStream_t s) {
 }
 
 cudaError_t launch_gam1(const DevSystem& S, double* G1, double* G1s,
-                        cudaStream_t s, int fp32) {
+                        cudaStream_t s, int fp32, int pairs_only) {
   const long long warps = (long long)S.npbf * S.npbf * S.nebf * S.nebf;
   const long long blocks = (warps * 32 + 127) / 128;
-  if (fp32) gam1_kernel<true><<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s);
-  else gam1_kernel<false><<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s);
+  if (fp32) gam1_kernel<true><<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s, pairs_only);
+  else gam1_kernel<false><<<(unsigned)blocks, 128, 0, s>>>(S, G1, G1s, pairs_only);
   return cudaGetLastError();
 }
 

@@ -202,8 +202,10 @@ constexpr int kScfSlots = 16;
 cudaError_t launch_scf_onebody(const DevSystem& sys, double* Se, double* Sp,
                                double* Hce, double* Hcp, cudaStream_t s);
 cudaError_t launch_gam_ep(const DevSystem& sys, double* Gep, cudaStream_t s);
+// pairs_only = 1: RXCHF_GAM1_OMP_MD (rxchf/rxchf_gam_1_OMP.f), the
+// geminal-pair terms only.
 cudaError_t launch_gam1(const DevSystem& sys, double* G1, double* G1s,
-                        cudaStream_t s, int fp32 = 0);
+                        cudaStream_t s, int fp32 = 0, int pairs_only = 0);
 size_t scf_fock1_part_doubles(int ne, int np);
 cudaError_t launch_scf_fock1(int ne, int np, int nelec, const double* Hce,
                              const double* Hcp, const double* Gep,
@@ -248,6 +250,36 @@ cudaError_t launch_dendif(int ne, int np, const double* DE, double* DE0,
 size_t diis_doubles(int n);
 cudaError_t launch_diis(int n, double* F, const double* D, const double* S,
                         double* work, int* state, double* err, cudaStream_t s);
+
+// ---- one-special-electron RXCHF SCF pieces (k_rxscf.cu) ------------------
+// Device energy slots of the RX Fock build: 0 E_total (with E_nuc) 1 E_nuc
+// 2 E_ecore 3 E_ee 4 E_OMG1 5 E_OMG2 6 S_total 7 E_P_OMG1 8 E_P_OMG2
+// 9 S_P_OMG1 10 E_BE_OMG1 11 S_BE_OMG1 12-15 density changes.
+constexpr int kRxSlots = 16;
+size_t rx_fock1_part_doubles(int ne);
+// Regular electrons' FAE_ecore + GAMee terms: closed (open = 0: FA1 from DA)
+// or open shell (FA1 / FB1 per spin, DT = DA + DB); en[2], en[3].
+cudaError_t launch_rx_fock1(int ne, int open, int with_ee, const double* Hce,
+                            const double* Gee, const double* DA, const double* DB,
+                            double* FA1, double* FB1, double* DT, double* part,
+                            double* en, cudaStream_t s);
+cudaError_t launch_rx_assemble(int ne, int np, double* en, const double* XFA1,
+                               const double* XFA2, const double* XFB1,
+                               const double* XFB2, const double* XFP,
+                               const double* XSP, const double* XFBE,
+                               const double* XSBE, double* FA, double* FB, double* FP,
+                               double* FBE, cudaStream_t s);
+cudaError_t launch_rx_dendif(int n, const double* D, double* D0, double* out,
+                             cudaStream_t s);
+// RXCHF_OCBSE2: new special-electron orbitals CB (column-major n x n) and
+// DB from the regular orbitals CA (nocca occupied), the previous special
+// orbital cb0 and FBE.  info[2] = {discarded orbital, projected norm},
+// status[2] of the subspace eigensolver.
+size_t ocbse_scratch_doubles(int n);
+cudaError_t launch_ocbse2(int n, int nocca, const double* CA, const double* cb0,
+                          const double* F, const double* S, double* scratch,
+                          double* CB, double* DB, double* info, int* status,
+                          cudaStream_t s);
 
 // ---- index maps on the device (pack_GAM.f) -----------------------------
 cudaError_t launch_index_fill(int kind, int ne, int np, int64_t count,

@@ -31,7 +31,7 @@ __all__ = [
     "fae_omg1", "ufp_omg1", "fae_omg2", "ufp_omg2", "fae_omg3", "ufp_omg3", "fae_omg4",
     "ufp_omg4", "omg4_icr", "dev_xcuhf_omg", "dev_omg4_icr",
     "rxcuhfne_omg2", "rxchf_omg", "rxcuhf_omg", "rxchf_omg1", "xcuhf_scf", "XCUHF_SLOTS",
-    "onebody_integrals", "class_nuc_rep", "xchf1_fock", "FOCK",
+    "onebody_integrals", "class_nuc_rep", "xchf1_fock", "FOCK", "rx_scf", "RX_SLOTS", "rxchf_gam1",
 ]
 
 LIB_PATH = _build.LIB
@@ -124,7 +124,9 @@ def _declare(L):
         "neoxc_xcfock_correction": (I, [i64, i64, d, d, d] + [vp] * 6),
         "neoxc_onebody_integrals": (I, [i64] * 5 + [d] + [vp] * 20),
         "neoxc_class_nuc_rep": (I, [i64, vp, vp, vp]),
+        "neoxc_rxchf_gam1": (I, [i64] * 7 + [d] + [vp] * 15),
         "neoxc_xchf1_fock": (I, [i64] * 13 + [vp] * 13 + [i64] * 4 + [d] + [vp] * 32),
+        "neoxc_rx_scf": (I, [i64] * 10 + [d] + [vp] * 15 + [i64] + [vp] * 9),
         "neoxc_probe_fp64": (I, [vp]),
         "neoxc_dev_gam4_dscf": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_dev_gam4_dscf_noalloc": (I, [vp, i64, i64] + [vp] * 7),
@@ -309,6 +311,17 @@ def onebody_integrals(s: NeoSystem, which=ONEBODY) -> dict:
     return out
 
 
+def rxchf_gam1(s: NeoSystem):
+    """rxchf_gam_1_OMP.f RXCHF_GAM1_OMP_MD -> (GAM_1, GAM_1s)."""
+    g, gs = np.empty(s.ng1), np.empty(s.ng1)
+    keep = [s.cat_f, s.zan_f, s.bgem_f, s.ggem_f, s.AMPEB2C_f, s.AGEBFCC_f, s.AGNBFCC_f,
+            s.ELCEX_f, s.NUCEX_f, s.ELCAM_f, s.NUCAM_f, s.ELCBFC_f, s.NUCBFC_f]
+    _check(lib().neoxc_rxchf_gam1(s.nebf, s.npebf, s.npbf, s.ng1,
+                                  s.npebf ** 2 * s.npbf ** 2, s.nat, s.ngtg, s.pmass,
+                                  *[_p(a) for a in keep], _p(g), _p(gs)))
+    return g, gs
+
+
 def class_nuc_rep(s: NeoSystem) -> float:
     """class_nuc_rep.f: classical nuclear repulsion."""
     E = np.zeros(1)
@@ -355,6 +368,34 @@ def xchf1_fock(s: NeoSystem, DE, DP, tables: dict, E_nuc: float, modes=("gam4", 
     out["focke"], out["fockp"] = _fock_out(fe, fp, ne, np_)
     out["Xfocke"], out["Xfockp"] = _fock_out(xfe, xfp, ne, np_)
     return out
+
+
+RX_KINDS = {"rxchf_ne": 0, "rxcuhf_ne": 1, "rxcuhf_ae": 2}
+RX_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_ee", "E_OMG1", "E_OMG2", "S_total", "E_P_OMG1",
+            "E_P_OMG2", "S_P_OMG1", "E_BE_OMG1", "S_BE_OMG1", "dDA", "dDBE", "dDP", "micro")
+
+
+def rx_scf(s: NeoSystem, kind: str, nae: int = 0, nalp: int = 0, nbet: int = 0,
+           nucst: int = 1, maxit: int = 100) -> dict:
+    """One-special-electron RXCHF SCF on the device (rxchfne_scf.f
+    xcrxchfne, rxcuhfne_scf.f xcrxcuhfne): kind "rxchf_ne" (nae closed-shell
+    regular electrons), "rxcuhf_ne" or "rxcuhf_ae" (nalp alpha, nbet beta;
+    EXCHLEV 0 / 1).  Returns the initial and final energy slots (RX_SLOTS),
+    the densities, the history and the iteration count."""
+    ne, np_ = s.nebf, s.npbf
+    DA, DB, DBE, DP = np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(np_ * np_)
+    Ei, Ef = np.zeros(16), np.zeros(16)
+    hist = np.zeros(3 * maxit)
+    nit, conv = C.c_int64(0), C.c_int64(0)
+    keep, ptrs = _sysargs(s)
+    _check(lib().neoxc_rx_scf(RX_KINDS[kind], nae, nalp, nbet, nucst, ne, s.npebf, np_, s.nat,
+                              s.ngtg, s.pmass, *ptrs, maxit, _p(DA), _p(DB), _p(DBE), _p(DP),
+                              _p(Ei), _p(Ef), _p(hist), C.byref(nit), C.byref(conv)))
+    n = nit.value
+    return {"initial": dict(zip(RX_SLOTS, Ei)), "final": dict(zip(RX_SLOTS, Ef)),
+            "DA": DA.reshape(ne, ne, order="F"), "DAbet": DB.reshape(ne, ne, order="F"),
+            "DBE": DBE.reshape(ne, ne, order="F"), "DP": DP.reshape(np_, np_, order="F"),
+            "history": hist[:3 * n].reshape(n, 3), "niter": n, "converged": bool(conv.value)}
 
 
 SCF_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_gam1", "E_gam2",

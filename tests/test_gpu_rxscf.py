@@ -1,0 +1,93 @@
+"""The one-special-electron RXCHF SCF on the device (neoxc_rx_scf) pinned to
+the reference's example logs, and its RXCHF GAM_1 table to the oracle:
+
+* examples/rxchf/one_special_electron (RXCHF-ne, NAE = 2): RXCHF.log
+  initial components :302-308, converged -7.4810462989 after 14 iterations;
+* examples/rxcuhf/rxchf-ne (RXCUHF, EXCHLEV 0, NAalpE = 1, NAbetE = 2):
+  RXCHF-ne.log :290-296, -7.6404271066 after 8 iterations;
+* examples/rxcuhf/rxchf-ae (RXCUHF, EXCHLEV 1: the RXCUHFne_*_OMG2 exchange
+  contractions; 19 primitives on 2 nuclei): RXCHF-ae.log :315-321,
+  -7.9746613535 after 12 iterations.
+
+Tolerances: E_NUC, E_ECORE, E_EE, S_TOTAL within 6e-11 Eh of the printed
+10 decimals.  E_OMG1, E_OMG2 and E_TOTAL of the RXCHF-ne guess are
+ill-conditioned: GAM_1 entries reach 1.4e6 (geminal exponents up to 1088)
+and cancel to E_P_OMG1 = 0.041, which S_total = 0.027 then divides.  The
+device GAM_1 agrees with the oracle's to 1.3e-15 of its largest entry
+(about 6 ulps, from summing the geminal terms in another order), and that
+alone moves E_OMG1 by 5e-10; the measured gaps to the log are 7.5e-10
+(E_OMG1) and 1.3e-9 (E_TOTAL), against 4e-10 for the oracle, which keeps
+the reference's summation order.  Those three components carry 2e-9.  The
+converged energies (S_total 2-48) are within 1e-9 Eh of the logs (measured
+3e-11 to 7e-11) in the logs' iteration counts.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES = {"rxchf_ne": dict(nae=2), "rxcuhf_ne": dict(nalp=1, nbet=2),
+         "rxcuhf_ae": dict(nalp=1, nbet=2)}
+NAMES = {"E_NUC": "E_nuc", "E_ECORE": "E_ecore", "E_EE": "E_ee", "E_OMG1": "E_OMG1",
+         "E_OMG2": "E_OMG2", "S_TOTAL": "S_total", "E_TOTAL": "E_total"}
+TIGHT = ("E_NUC", "E_ECORE", "E_EE", "S_TOTAL")
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def rx_gpu(request, nx, golden_rx):
+    from neoxc import basis
+    name = request.param
+    g = golden_rx[name]
+    s = basis.parse_inp(g["inp"], name=name)
+    return name, g, s, nx.rx_scf(s, name, **CASES[name])
+
+
+def test_rx_initial_energetics_match_log(rx_gpu):
+    name, g, s, r = rx_gpu
+    for k, mine in NAMES.items():
+        tol = 6e-11 if k in TIGHT else 2e-9
+        assert abs(r["initial"][mine] - g["initial"][k]) <= tol, (name, k, r["initial"][mine])
+
+
+def test_rx_scf_converges_to_log_energy(nx, rx_gpu):
+    name, g, s, r = rx_gpu
+    assert r["converged"], (name, r["history"])
+    assert abs(r["final"]["E_total"] - g["final_energy"]) <= 1e-9, (name, r["final"]["E_total"])
+    assert r["niter"] == g["iterations"], (name, r["niter"])
+    for k in ("E_ECORE", "E_EE", "E_OMG1", "E_OMG2"):
+        ref = g["final"][k]
+        assert abs(r["final"][NAMES[k]] - ref) <= 1e-6 * max(1.0, abs(ref)), (name, k)
+    # the special electron's density is that of one normalised orbital
+    Se = nx.onebody_integrals(s, which=("Se",))["Se"].reshape(s.nebf, s.nebf)
+    assert abs(float((r["DBE"] * Se).sum()) - 1.0) <= 1e-10
+
+
+def test_rx_matches_oracle_iterations(nx, orc, golden_rx):
+    """RXCUHF-ne: the same macro-iterations (micro-iteration counts and
+    energies) as the oracle's restatement."""
+    import rxne
+    from neoxc import basis
+    g = golden_rx["rxcuhf_ne"]
+    s = basis.parse_inp(g["inp"], name="rxcuhf_ne")
+    ints = rxne.RxIntegrals(s)
+    _, fin, hist, ok = rxne.rx_scf(ints, nalp=1, nbet=2)
+    r = nx.rx_scf(s, "rxcuhf_ne", nalp=1, nbet=2)
+    assert ok and r["converged"] and r["niter"] == len(hist)
+    for k, (it, micro, E) in enumerate(hist):
+        assert int(r["history"][k, 1]) == micro, (it, r["history"][k], micro)
+        assert abs(r["history"][k, 0] - E) <= 1e-9, (it, r["history"][k, 0], E)
+
+
+def test_rxchf_gam1_matches_oracle(nx, orc, golden_rx):
+    from neoxc import basis
+    for s in (basis.parse_inp(golden_rx["rxcuhf_ne"]["inp"], name="rxcuhf_ne"),
+              basis.synthetic(seed=412, nat=2, nebf=4, nprim=2, npbf=3, ngtg=2, lmax_e=2,
+                              lmax_p=1, nelec=3)):
+        g, gs = nx.rxchf_gam1(s)
+        L, h = orc.lib(), orc.SystemHandle(s)
+        r, rs = np.zeros(s.ng1), np.zeros(s.ng1)
+        L.orc_rxchf_gam1(h.ref, orc.ptr(r), orc.ptr(rs))
+        for a, b in ((g, r), (gs, rs)):
+            assert float(np.abs(a - b).max()) <= 1e-12 * max(1.0, float(np.abs(b).max()))
