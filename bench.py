@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--nebf", type=int, default=NEBF)
     ap.add_argument("--npbf", type=int, default=NPBF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf"], default=None,
+    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf"], default=None,
                     help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
 
@@ -440,6 +440,53 @@ def xcuhf_scf_section(neoxc):
     return out
 
 
+RX_BENCH = (("rxchf_ne", dict(nae=2)), ("rxcuhf_ne", dict(nalp=1, nbet=2)),
+            ("rxcuhf_ae", dict(nalp=1, nbet=2)))
+
+
+def rx_scf_section(neoxc, with_cpu: bool):
+    """One-special-electron RXCHF SCF (neoxc_rx_scf) on the reference's
+    examples/rxchf/one_special_electron and examples/rxcuhf/rxchf-{ne,ae}
+    (fixture tests/golden/rx_examples.json): every integral on the GPU,
+    UROOTHAN + OCBSE2 iterations there.  The converged energies are compared
+    with the logs'.  The CPU leg times the oracle's restatement of the
+    RXCHF-ne solve (C tables with OpenMP + the numpy SCF) on the host cores."""
+    from neoxc import basis
+    with open(os.path.join(ROOT, "tests", "golden", "rx_examples.json")) as f:
+        g = json.load(f)
+    out = {"api": "neoxc_rx_scf (host arrays; integrals and SCF on the GPU)"}
+    for name, kw in RX_BENCH:
+        s = basis.parse_inp(g[name]["inp"], name=name)
+        neoxc.rx_scf(s, name, **kw)   # warm-up
+        t0 = time.perf_counter()
+        r = neoxc.rx_scf(s, name, **kw)
+        dt = time.perf_counter() - t0
+        out[name] = {"workload": "%s (nebf=%d, npebf=%d, npbf=%d, NG=%d)" % (
+                         g[name]["source"], s.nebf, s.npebf, s.npbf, s.ngtg),
+                     "solves_per_s": 1.0 / dt, "ms_per_solve": 1e3 * dt,
+                     "iterations": r["niter"], "converged": r["converged"],
+                     "micro_iterations": int(r["history"][:, 1].sum()),
+                     "E_total": r["final"]["E_total"],
+                     "E_err_vs_log": r["final"]["E_total"] - g[name]["final_energy"]}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        import rxne
+        O.build()
+        s = basis.parse_inp(g["rxchf_ne"]["inp"], name="rxchf_ne")
+        t0 = time.perf_counter()
+        ints = rxne.RxIntegrals(s)
+        _, fin, hist, ok = rxne.rx_scf(ints, nae=2)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "cores": os.cpu_count(),
+                               "sample": "one full RXCHF-ne solve of "
+                                         "examples/rxchf/one_special_electron",
+                               "solves_per_s": 1.0 / dt, "seconds": dt,
+                               "E_err_vs_log": fin["E_total"] - g["rxchf_ne"]["final_energy"]}
+        out["gpu_vs_cpu_rxchf_ne"] = out["rxchf_ne"]["solves_per_s"] / (1.0 / dt)
+    return out
+
+
 def scf_section(neoxc, with_cpu: bool):
     """XCHF RHF SCF solves/s on the reference's examples/xchf system (inputs
     from the committed fixture tests/golden/xchf_example.json: exam_xchf.inp
@@ -484,6 +531,7 @@ def scf_section(neoxc, with_cpu: bool):
         else:
             E_fp64 = r["final"]["E_total"]
     out["xcuhf"] = xcuhf_scf_section(neoxc)
+    out["rx"] = rx_scf_section(neoxc, with_cpu)
     out["batch"] = scf_batch_section(neoxc, s, DE)
     out["serving"] = scf_serving_section(neoxc, s, DE)
     if with_cpu:
@@ -591,6 +639,9 @@ def main():
         return
     if args.only == "xcuhf_scf":
         print(json.dumps(xcuhf_scf_section(neoxc)))
+        return
+    if args.only == "rx_scf":
+        print(json.dumps(rx_scf_section(neoxc, not args.no_cpu_baseline)))
         return
     ne, np_ = args.nebf, args.npbf
     ng4 = ne ** 8 * np_ ** 2

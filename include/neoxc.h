@@ -519,6 +519,25 @@ int neoxc_xcuhf_scf(int64_t nelec, int64_t NAE, int64_t NBE, int64_t nucst,
  * regular / special / proton density change, 15 micro-iterations of the
  * last iteration; history [3*maxit]: E_TOTAL, micro-iterations, proton
  * density change per iteration.  Limits: nebf, npbf <= 64. */
+/* rxchfne/rxchfne_fock.f:2-250 RXCHFne_FOCK (open_shell = 0: DA = DAE of
+ * NAE closed-shell regular electrons, FA = FAE) or rxchfne/rxcuhfne_fock.f
+ * RXCUHFne_FOCK (open_shell = 1: DA / DAbet = DAalpE / DAbetE with NAalpE /
+ * NAbetE electrons, FA / FAbet = FAalpE / FAbetE; addexch = LADDEXCH adds
+ * the RXCUHFne_*_OMG2 exchange terms from GM2exICR) in one device pass.
+ * GAM_1 / GAM_1s are arguments (the reference's RXCHF_FP_OMG1 and
+ * RXCHF_FBE_OMG1 read GAM_1.ufm / GAM_1s.ufm); GM2exICR is read only with
+ * addexch.  Outputs overwritten: FP, FA, FAbet (open shell), FBE and the
+ * routine's energies (E_total without E_nuc, as the routine returns it).
+ * Limits: nebf, npbf <= 64. */
+int neoxc_rxchfne_fock(int64_t open_shell, int64_t addexch, int64_t NAE,
+                       int64_t NAalpE, int64_t NAbetE, int64_t nebf, int64_t npbf,
+                       const double* DA, const double* DAbet, const double* DBE,
+                       const double* DP, const double* GAM_ecore, const double* GAM_ee,
+                       const double* GAM_1, const double* GAM_1s, const double* GM2ICR,
+                       const double* GM2exICR, double* FP, double* FA, double* FAbet,
+                       double* FBE, double* E_ecore, double* E_GAMee, double* E_OMG1,
+                       double* E_OMG2, double* E_total, double* S_total);
+
 #define NEOXC_RX_NE 0
 #define NEOXC_RX_CU_NE 1
 #define NEOXC_RX_CU_AE 2
@@ -1099,6 +1118,33 @@ void xchf1_fock_(const int64_t* LNEOHF, const int64_t* LGAM4, const int64_t* LG4
                  const double* E_nuc, double* E_ecore, double* E_pcore, double* E_ep,
                  double* E_ee, double* E_gam1, double* E_gam2, double* E_gam3,
                  double* E_gam4, double* S_total, double* S_gam1, double* S_gam2);
+/* RXCHFne_FOCK / RXCUHFne_FOCK with the reference's argument lists;
+ * GAM_1.ufm and GAM_1s.ufm are read from the working directory as
+ * RXCHF_FP_OMG1 does, LOGICAL*8 switches by their low bit; LCMF's printed
+ * checks are not reproduced. */
+void rxchfne_fock_(const int64_t* LCMF, const int64_t* LNEOHF, const int64_t* nelec,
+                   const int64_t* NAE, const int64_t* NBE, const int64_t* nebf,
+                   const int64_t* nebf2, const int64_t* npbf, const int64_t* npbf2,
+                   const int64_t* ngee, const int64_t* ng1, const int64_t* ng2,
+                   const int64_t* ng3, const int64_t* ng4, const int64_t* SZG2ICR,
+                   const int64_t* NG2CHK, const double* DAE, const double* DBE,
+                   const double* DP, const double* GAM_ecore, const double* GAM_pcore,
+                   const double* GAM_ep, const double* GAM_ee, const double* GM2ICR,
+                   double* FP, double* FAE, double* FBE, double* E_ecore,
+                   double* E_GAMee, double* E_OMG1, double* E_OMG2, double* E_total,
+                   double* S_total);
+void rxcuhfne_fock_(const int64_t* LCMF, const int64_t* LNEOHF, const int64_t* LADDEXCH,
+                    const int64_t* nelec, const int64_t* NBE, const int64_t* NAalpE,
+                    const int64_t* NAbetE, const int64_t* nebf, const int64_t* nebf2,
+                    const int64_t* npbf, const int64_t* npbf2, const int64_t* ngee,
+                    const int64_t* ng1, const int64_t* ng2, const int64_t* ng3,
+                    const int64_t* ng4, const int64_t* SZG2ICR, const int64_t* NG2CHK,
+                    const double* DAalpE, const double* DAbetE, const double* DBE,
+                    const double* DP, const double* GAM_ecore, const double* GAM_pcore,
+                    const double* GAM_ep, const double* GAM_ee, const double* GM2ICR,
+                    const double* GM2exICR, double* FP, double* FAalpE, double* FAbetE,
+                    double* FBE, double* E_ecore, double* E_GAMee, double* E_OMG1,
+                    double* E_OMG2, double* E_total, double* S_total);
 #ifdef __cplusplus
 }
 #endif

@@ -2514,6 +2514,71 @@ extern "C" int neoxc_xcuhf_scf(int64_t nelec, int64_t NAE, int64_t NBE, int64_t 
 // branch with UROOTHAN for the regular electrons.
 namespace {
 
+// One RXCHFne_FOCK / RXCUHFne_FOCK on device buffers: the regular
+// electrons' one-body and GAMee terms, RXCHF_FP/FBE_OMG1 with the special
+// electron's density, the OMG2 contractions (RXCHFne_* in one fused pass,
+// or RXCUHFne_* with GM2exICR when exch), then the corrections and energy
+// slots (launch_rx_assemble).  Scratch and partial matrices live in the
+// struct; `en` holds E_nuc in slot 1 on entry.
+struct RxFock {
+  int ne = 0, np = 0, open = 0, exch = 0, with_ee = 0;
+  const double *Hce = nullptr, *Gee = nullptr, *G1 = nullptr, *G1s = nullptr,
+               *G2 = nullptr, *G2x = nullptr;
+  DBuf dT, XFA1, XFB1, XFA2, XFB2, XFP, XSP, XFBE, XSBE, feo, fpo, part, scr, dumE;
+  int alloc(cudaStream_t s) {
+    const size_t e2 = (size_t)ne * ne, p2 = (size_t)np * np;
+    for (DBuf* b : {&dT, &XFA1, &XFB1, &XFA2, &XFB2, &XFBE, &XSBE})
+      RC(dalloc(*b, sizeof(double) * e2, s));
+    for (DBuf* b : {&XFP, &XSP}) RC(dalloc(*b, sizeof(double) * p2, s));
+    RC(dalloc(feo, sizeof(double) * 2 * e2, s));
+    RC(dalloc(fpo, sizeof(double) * 2 * p2, s));
+    RC(dalloc(part, sizeof(double) * rx_fock1_part_doubles(ne), s));
+    RC(dalloc(scr, sizeof(double) * std::max(omg2_partial_doubles(ne, np),
+                                             rx_scratch_doubles(ne, np)), s));
+    RC(dalloc(dumE, sizeof(double) * 4, s));
+    return NEOXC_OK;
+  }
+  // DA (closed: DAE; open: DAalpE), DB (open: DAbetE), DBE, DP in; FA, FB
+  // (open), FP, FBE out; en[2..11] written, en[0] = E_total + en[1].
+  int build(const double* DA, const double* DB, const double* DBE, const double* DP,
+            double* FA, double* FB, double* FP, double* FBE, double* en, cudaStream_t s) {
+    const size_t e2 = (size_t)ne * ne, p2 = (size_t)np * np;
+    CU(launch_rx_fock1(ne, open, with_ee, Hce, Gee, DA, open ? DB : nullptr,
+                       XFA1.as<double>(), open ? XFB1.as<double>() : nullptr,
+                       open ? dT.as<double>() : nullptr, part.as<double>(), en, s));
+    for (DBuf* b : {&XFA2, &XFB2, &XFBE}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * e2, s));
+    CU(cudaMemsetAsync(XFP.p, 0, sizeof(double) * p2, s));
+    // RXCHF_FP_OMG1 / RXCHF_FBE_OMG1 with the special electron's density
+    CU(launch_omg1(ne, np, G1, G1s, DBE, DP, feo.as<double>(), fpo.as<double>(), s));
+    CU(launch_spin_finish(np, fpo.as<double>(), fpo.as<double>() + p2, DP, 1.0,
+                          XFP.as<double>(), XSP.as<double>(), en + 7, en + 9, s));
+    CU(launch_spin_finish(ne, feo.as<double>(), feo.as<double>() + e2, DBE, 1.0,
+                          XFBE.as<double>(), XSBE.as<double>(), en + 10, en + 11, s));
+    const double* DT = open ? dT.as<double>() : nullptr;
+    if (exch) {   // RXCUHFne_FE/FP/FBE_OMG2 (LADDEXCH)
+      CU(launch_rx(RxRoutine::CuhfneFE2, ne, np, G2, G2x, nullptr, DA, nullptr, DT, DBE, DP,
+                   scr.as<double>(), XFA2.as<double>(), XFB2.as<double>(), nullptr,
+                   dumE.as<double>(), s));
+      CU(launch_rx(RxRoutine::CuhfneFP2, ne, np, G2, G2x, nullptr, DA, nullptr, DT, DBE, DP,
+                   scr.as<double>(), XFP.as<double>(), nullptr, nullptr, en + 8, s));
+      CU(launch_rx(RxRoutine::CuhfneFBE2, ne, np, G2, G2x, nullptr, DA, nullptr, DT, DBE, DP,
+                   scr.as<double>(), XFBE.as<double>(), nullptr, nullptr, dumE.as<double>(), s));
+    } else {
+      // RXCHFne_FAE/FP/FBE_OMG2 in one pass; the FAE part depends on DBE and
+      // DP only, so the open-shell alpha and beta matrices are the same one
+      CU(launch_rxchfne_omg2(ne, np, open ? DT : DA, DBE, DP, G2, scr.as<double>(),
+                             XFA2.as<double>(), XFP.as<double>(), XFBE.as<double>(), en + 8,
+                             s));
+    }
+    CU(launch_rx_assemble(ne, np, en, XFA1.as<double>(), XFA2.as<double>(),
+                          open ? XFB1.as<double>() : nullptr,
+                          open ? (exch ? XFB2.as<double>() : XFA2.as<double>()) : nullptr,
+                          XFP.as<double>(), XSP.as<double>(), XFBE.as<double>(),
+                          XSBE.as<double>(), FA, FB, FP, FBE, s));
+    return NEOXC_OK;
+  }
+};
+
 int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t NAbetE,
               int64_t nucst, int64_t nebf, int64_t npebf, int64_t npbf, int64_t nat,
               int64_t ngtg1, double pmass, const double* cat, const double* zan,
@@ -2561,23 +2626,28 @@ int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t
   CU(launch_gam2_raw(u.d, 1, G2.as<double>(), G2x.as<double>(), s));
   CU(launch_gam2_symmetrize(ne, np, 1, G2.as<double>(), G2x.as<double>(), s));
   // SCF state
-  DBuf dA, dB, dT, dBE, dP, A0, B0, BE0, P0, CA, CBE, Ctmp, FA, FB, FP, FBE, XFA1, XFB1,
-      XFA2, XFB2, XFP, XSP, XFBE, XSBE, feo, fpo, part, scr, ocb, en, info, st, dumE;
-  for (DBuf* b : {&dA, &dB, &dT, &dBE, &A0, &B0, &BE0, &CA, &CBE, &Ctmp, &FA, &FB, &FBE,
-                  &XFA1, &XFB1, &XFA2, &XFB2, &XFBE, &XSBE})
+  DBuf dA, dB, dBE, dP, A0, B0, BE0, P0, CA, CBE, Ctmp, FA, FB, FP, FBE, ocb, en, info, st;
+  for (DBuf* b : {&dA, &dB, &dBE, &A0, &B0, &BE0, &CA, &CBE, &Ctmp, &FA, &FB, &FBE})
     RC(dalloc(*b, sizeof(double) * e2, s));
-  for (DBuf* b : {&dP, &P0, &FP, &XFP, &XSP}) RC(dalloc(*b, sizeof(double) * p2, s));
-  RC(dalloc(feo, sizeof(double) * 2 * e2, s));
-  RC(dalloc(fpo, sizeof(double) * 2 * p2, s));
-  RC(dalloc(part, sizeof(double) * rx_fock1_part_doubles(ne), s));
-  RC(dalloc(scr, sizeof(double) * std::max(omg2_partial_doubles(ne, np),
-                                           rx_scratch_doubles(ne, np)), s));
+  for (DBuf* b : {&dP, &P0, &FP}) RC(dalloc(*b, sizeof(double) * p2, s));
   RC(dalloc(ocb, sizeof(double) * ocbse_scratch_doubles(ne), s));
   RC(dalloc(en, sizeof(double) * kRxSlots, s));
   RC(dalloc(info, sizeof(double) * 4, s));
   RC(dalloc(st, sizeof(int) * 16, s));
-  RC(dalloc(dumE, sizeof(double) * 4, s));
-  for (DBuf* b : {&A0, &B0, &BE0, &CBE, &dB, &dT})
+  RxFock rf;
+  rf.ne = ne;
+  rf.np = np;
+  rf.open = open ? 1 : 0;
+  rf.exch = kind == NEOXC_RX_CU_AE ? 1 : 0;
+  rf.with_ee = nreg > 1 ? 1 : 0;
+  rf.Hce = Hce.as<double>();
+  rf.Gee = Gee.as<double>();
+  rf.G1 = G1.as<double>();
+  rf.G1s = G1s.as<double>();
+  rf.G2 = G2.as<double>();
+  rf.G2x = G2x.as<double>();
+  RC(rf.alloc(s));
+  for (DBuf* b : {&A0, &B0, &BE0, &CBE, &dB})
     CU(cudaMemsetAsync(b->p, 0, sizeof(double) * e2, s));
   CU(cudaMemsetAsync(P0.p, 0, sizeof(double) * p2, s));
   CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kRxSlots, s));
@@ -2602,47 +2672,10 @@ int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t
                      cudaMemcpyDeviceToDevice, s));
   CU(launch_roothan(np, Hcp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
                     dP.as<double>(), nullptr, nullptr, sts + 5, s));
-  const bool exch = kind == NEOXC_RX_CU_AE;
   auto fock = [&]() -> int {
-    CU(launch_rx_fock1(ne, open ? 1 : 0, nreg > 1 ? 1 : 0, Hce.as<double>(), Gee.as<double>(),
-                       dA.as<double>(), open ? dB.as<double>() : nullptr, XFA1.as<double>(),
-                       open ? XFB1.as<double>() : nullptr, open ? dT.as<double>() : nullptr,
-                       part.as<double>(), d_en, s));
-    for (DBuf* b : {&XFA2, &XFB2, &XFBE}) CU(cudaMemsetAsync(b->p, 0, sizeof(double) * e2, s));
-    CU(cudaMemsetAsync(XFP.p, 0, sizeof(double) * p2, s));
-    // RXCHF_FP_OMG1 / RXCHF_FBE_OMG1 with the special electron's density
-    CU(launch_omg1(ne, np, G1.as<double>(), G1s.as<double>(), dBE.as<double>(),
-                   dP.as<double>(), feo.as<double>(), fpo.as<double>(), s));
-    CU(launch_spin_finish(np, fpo.as<double>(), fpo.as<double>() + p2, dP.as<double>(), 1.0,
-                          XFP.as<double>(), XSP.as<double>(), d_en + 7, d_en + 9, s));
-    CU(launch_spin_finish(ne, feo.as<double>(), feo.as<double>() + e2, dBE.as<double>(), 1.0,
-                          XFBE.as<double>(), XSBE.as<double>(), d_en + 10, d_en + 11, s));
-    if (exch) {   // RXCUHFne_FE/FP/FBE_OMG2 (LADDEXCH)
-      CU(launch_rx(RxRoutine::CuhfneFE2, ne, np, G2.as<double>(), G2x.as<double>(), nullptr,
-                   dA.as<double>(), nullptr, dT.as<double>(), dBE.as<double>(), dP.as<double>(),
-                   scr.as<double>(), XFA2.as<double>(), XFB2.as<double>(), nullptr,
-                   dumE.as<double>(), s));
-      CU(launch_rx(RxRoutine::CuhfneFP2, ne, np, G2.as<double>(), G2x.as<double>(), nullptr,
-                   dA.as<double>(), nullptr, dT.as<double>(), dBE.as<double>(), dP.as<double>(),
-                   scr.as<double>(), XFP.as<double>(), nullptr, nullptr, d_en + 8, s));
-      CU(launch_rx(RxRoutine::CuhfneFBE2, ne, np, G2.as<double>(), G2x.as<double>(), nullptr,
-                   dA.as<double>(), nullptr, dT.as<double>(), dBE.as<double>(), dP.as<double>(),
-                   scr.as<double>(), XFBE.as<double>(), nullptr, nullptr, dumE.as<double>(), s));
-    } else {
-      // RXCHFne_FAE/FP/FBE_OMG2 in one pass; the FAE part depends on DBE and
-      // DP only, so the open-shell alpha and beta matrices are the same one
-      CU(launch_rxchfne_omg2(ne, np, open ? dT.as<double>() : dA.as<double>(),
-                             dBE.as<double>(), dP.as<double>(), G2.as<double>(),
-                             scr.as<double>(), XFA2.as<double>(), XFP.as<double>(),
-                             XFBE.as<double>(), d_en + 8, s));
-    }
-    CU(launch_rx_assemble(ne, np, d_en, XFA1.as<double>(), XFA2.as<double>(),
-                          open ? XFB1.as<double>() : nullptr,
-                          open ? (exch ? XFB2.as<double>() : XFA2.as<double>()) : nullptr,
-                          XFP.as<double>(), XSP.as<double>(), XFBE.as<double>(),
-                          XSBE.as<double>(), FA.as<double>(), FB.as<double>(),
-                          FP.as<double>(), FBE.as<double>(), s));
-    return NEOXC_OK;
+    return rf.build(dA.as<double>(), open ? dB.as<double>() : nullptr, dBE.as<double>(),
+                    dP.as<double>(), FA.as<double>(), FB.as<double>(), FP.as<double>(),
+                    FBE.as<double>(), d_en, s);
   };
   auto check_eig = [&](int n_status) -> int {
     int hs[16];
@@ -2736,4 +2769,78 @@ extern "C" int neoxc_rx_scf(int64_t kind, int64_t NAE, int64_t NAalpE, int64_t N
                    cat, zan, bcoef1, gamma1, KPESTR, KPEEND, AGEBFCC, AGNBFCC, ELCEX, NUCEX,
                    ELCAM, NUCAM, ELCBFC, NUCBFC, maxit, DA, DAbet, DBE, DP, E_init, E_final,
                    history, niter, converged);
+}
+
+// rxchfne/rxchfne_fock.f:2-250 RXCHFne_FOCK and rxchfne/rxcuhfne_fock.f
+// RXCUHFne_FOCK from host arrays: one RxFock::build on uploaded copies.
+extern "C" int neoxc_rxchfne_fock(int64_t open_shell, int64_t addexch, int64_t NAE,
+                                  int64_t NAalpE, int64_t NAbetE, int64_t nebf,
+                                  int64_t npbf, const double* DA, const double* DAbet,
+                                  const double* DBE, const double* DP,
+                                  const double* GAM_ecore, const double* GAM_ee,
+                                  const double* GAM_1, const double* GAM_1s,
+                                  const double* GM2ICR, const double* GM2exICR, double* FP,
+                                  double* FA, double* FAbet, double* FBE, double* E_ecore,
+                                  double* E_GAMee, double* E_OMG1, double* E_OMG2,
+                                  double* E_total, double* S_total) {
+  RC(need(nebf >= 1 && npbf >= 1 && nebf <= kScfMaxN && npbf <= kScfMaxN,
+          "1 <= nebf, npbf <= 64"));
+  RC(need(open_shell == 0 || open_shell == 1, "open_shell is 0 or 1"));
+  RC(need(addexch == 0 || (open_shell == 1 && addexch == 1), "addexch only with open_shell"));
+  const bool open = open_shell == 1;
+  const int64_t nreg = open ? NAalpE + NAbetE : NAE;
+  RC(need(nreg >= 1 && (!open || (NAalpE >= 0 && NAbetE >= 0)), "regular electron counts"));
+  RC(need(DA && DBE && DP && GAM_ecore && GAM_1 && GAM_1s && GM2ICR && FP && FA && FBE &&
+              E_ecore && E_GAMee && E_OMG1 && E_OMG2 && E_total && S_total &&
+              (!open || (DAbet && FAbet)) && (!addexch || GM2exICR) && (nreg < 2 || GAM_ee),
+          "pointers"));
+  cudaStream_t s;
+  RC(get_stream(&s));
+  const size_t e2 = (size_t)nebf * nebf, p2 = (size_t)npbf * npbf;
+  const size_t ng1 = e2 * p2, ng2 = e2 * e2 * p2;
+  DBuf hce, gee, g1, g1s, g2, g2x, da, db, dbe, dp, fa, fb, fp, fbe, en;
+  RC(upload(hce, GAM_ecore, sizeof(double) * e2, s));
+  if (nreg > 1) RC(upload(gee, GAM_ee, sizeof(double) * e2 * e2, s));
+  RC(upload(g1, GAM_1, sizeof(double) * ng1, s));
+  RC(upload(g1s, GAM_1s, sizeof(double) * ng1, s));
+  RC(upload(g2, GM2ICR, sizeof(double) * ng2, s));
+  if (addexch) RC(upload(g2x, GM2exICR, sizeof(double) * ng2, s));
+  RC(upload(da, DA, sizeof(double) * e2, s));
+  if (open) RC(upload(db, DAbet, sizeof(double) * e2, s));
+  RC(upload(dbe, DBE, sizeof(double) * e2, s));
+  RC(upload(dp, DP, sizeof(double) * p2, s));
+  for (DBuf* b : {&fa, &fb, &fbe}) RC(dalloc(*b, sizeof(double) * e2, s));
+  RC(dalloc(fp, sizeof(double) * p2, s));
+  RC(dalloc(en, sizeof(double) * kRxSlots, s));
+  CU(cudaMemsetAsync(en.p, 0, sizeof(double) * kRxSlots, s));   // E_nuc = 0
+  RxFock rf;
+  rf.ne = (int)nebf;
+  rf.np = (int)npbf;
+  rf.open = open ? 1 : 0;
+  rf.exch = addexch ? 1 : 0;
+  rf.with_ee = nreg > 1 ? 1 : 0;
+  rf.Hce = hce.as<double>();
+  rf.Gee = gee.as<double>();
+  rf.G1 = g1.as<double>();
+  rf.G1s = g1s.as<double>();
+  rf.G2 = g2.as<double>();
+  rf.G2x = g2x.as<double>();
+  RC(rf.alloc(s));
+  RC(rf.build(da.as<double>(), db.as<double>(), dbe.as<double>(), dp.as<double>(),
+              fa.as<double>(), fb.as<double>(), fp.as<double>(), fbe.as<double>(),
+              en.as<double>(), s));
+  double h[kRxSlots];
+  CU(cudaMemcpyAsync(FA, fa.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  if (open) CU(cudaMemcpyAsync(FAbet, fb.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(FBE, fbe.p, sizeof(double) * e2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(FP, fp.p, sizeof(double) * p2, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(h, en.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  RC(finish(s));
+  *E_ecore = h[2];
+  *E_GAMee = h[3];
+  *E_OMG1 = h[4];
+  *E_OMG2 = h[5];
+  *S_total = h[6];
+  *E_total = h[0];
+  return NEOXC_OK;
 }

@@ -810,4 +810,59 @@ void xchf1_fock_(const int64_t* LNEOHF, const int64_t* LGAM4, const int64_t* LG4
                           E_gam2, E_gam3, E_gam4, S_total, S_gam1, S_gam2));
 }
 
+// rxchfne/rxchfne_fock.f:2-250 RXCHFne_FOCK
+void rxchfne_fock_(const int64_t* LCMF, const int64_t* LNEOHF, const int64_t* nelec,
+                   const int64_t* NAE, const int64_t* NBE, const int64_t* nebf,
+                   const int64_t* nebf2, const int64_t* npbf, const int64_t* npbf2,
+                   const int64_t* ngee, const int64_t* ng1, const int64_t* ng2,
+                   const int64_t* ng3, const int64_t* ng4, const int64_t* SZG2ICR,
+                   const int64_t* NG2CHK, const double* DAE, const double* DBE,
+                   const double* DP, const double* GAM_ecore, const double* GAM_pcore,
+                   const double* GAM_ep, const double* GAM_ee, const double* GM2ICR,
+                   double* FP, double* FAE, double* FBE, double* E_ecore,
+                   double* E_GAMee, double* E_OMG1, double* E_OMG2, double* E_total,
+                   double* S_total) {
+  (void)LCMF; (void)LNEOHF; (void)nelec; (void)NBE; (void)nebf2; (void)npbf2; (void)ngee;
+  (void)ng2; (void)ng3; (void)ng4; (void)SZG2ICR; (void)NG2CHK; (void)GAM_pcore;
+  (void)GAM_ep;
+  std::vector<double> g1, g1s;
+  if (!read_ufm("GAM_1.ufm", *ng1, g1) || !read_ufm("GAM_1s.ufm", *ng1, g1s)) {
+    std::fprintf(stderr, "neoxc: RXCHFne_FOCK: cannot read GAM_1.ufm/GAM_1s.ufm\n");
+    return;
+  }
+  report("RXCHFne_FOCK",
+         neoxc_rxchfne_fock(0, 0, *NAE, 0, 0, *nebf, *npbf, DAE, nullptr, DBE, DP, GAM_ecore,
+                            GAM_ee, g1.data(), g1s.data(), GM2ICR, nullptr, FP, FAE, nullptr,
+                            FBE, E_ecore, E_GAMee, E_OMG1, E_OMG2, E_total, S_total));
+}
+
+// rxchfne/rxcuhfne_fock.f RXCUHFne_FOCK
+void rxcuhfne_fock_(const int64_t* LCMF, const int64_t* LNEOHF, const int64_t* LADDEXCH,
+                    const int64_t* nelec, const int64_t* NBE, const int64_t* NAalpE,
+                    const int64_t* NAbetE, const int64_t* nebf, const int64_t* nebf2,
+                    const int64_t* npbf, const int64_t* npbf2, const int64_t* ngee,
+                    const int64_t* ng1, const int64_t* ng2, const int64_t* ng3,
+                    const int64_t* ng4, const int64_t* SZG2ICR, const int64_t* NG2CHK,
+                    const double* DAalpE, const double* DAbetE, const double* DBE,
+                    const double* DP, const double* GAM_ecore, const double* GAM_pcore,
+                    const double* GAM_ep, const double* GAM_ee, const double* GM2ICR,
+                    const double* GM2exICR, double* FP, double* FAalpE, double* FAbetE,
+                    double* FBE, double* E_ecore, double* E_GAMee, double* E_OMG1,
+                    double* E_OMG2, double* E_total, double* S_total) {
+  (void)LCMF; (void)LNEOHF; (void)nelec; (void)NBE; (void)nebf2; (void)npbf2; (void)ngee;
+  (void)ng2; (void)ng3; (void)ng4; (void)SZG2ICR; (void)NG2CHK; (void)GAM_pcore;
+  (void)GAM_ep;
+  std::vector<double> g1, g1s;
+  if (!read_ufm("GAM_1.ufm", *ng1, g1) || !read_ufm("GAM_1s.ufm", *ng1, g1s)) {
+    std::fprintf(stderr, "neoxc: RXCUHFne_FOCK: cannot read GAM_1.ufm/GAM_1s.ufm\n");
+    return;
+  }
+  const int64_t exch = (*LADDEXCH & 1) ? 1 : 0;
+  report("RXCUHFne_FOCK",
+         neoxc_rxchfne_fock(1, exch, 0, *NAalpE, *NAbetE, *nebf, *npbf, DAalpE, DAbetE, DBE,
+                            DP, GAM_ecore, GAM_ee, g1.data(), g1s.data(), GM2ICR,
+                            exch ? GM2exICR : nullptr, FP, FAalpE, FAbetE, FBE, E_ecore,
+                            E_GAMee, E_OMG1, E_OMG2, E_total, S_total));
+}
+
 }  // extern "C"

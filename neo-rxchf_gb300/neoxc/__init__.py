@@ -31,7 +31,7 @@ __all__ = [
     "fae_omg1", "ufp_omg1", "fae_omg2", "ufp_omg2", "fae_omg3", "ufp_omg3", "fae_omg4",
     "ufp_omg4", "omg4_icr", "dev_xcuhf_omg", "dev_omg4_icr",
     "rxcuhfne_omg2", "rxchf_omg", "rxcuhf_omg", "rxchf_omg1", "xcuhf_scf", "XCUHF_SLOTS",
-    "onebody_integrals", "class_nuc_rep", "xchf1_fock", "FOCK", "rx_scf", "RX_SLOTS", "rxchf_gam1",
+    "onebody_integrals", "class_nuc_rep", "xchf1_fock", "FOCK", "rx_scf", "RX_SLOTS", "rxchf_gam1", "rxchfne_fock",
 ]
 
 LIB_PATH = _build.LIB
@@ -127,6 +127,7 @@ def _declare(L):
         "neoxc_rxchf_gam1": (I, [i64] * 7 + [d] + [vp] * 15),
         "neoxc_xchf1_fock": (I, [i64] * 13 + [vp] * 13 + [i64] * 4 + [d] + [vp] * 32),
         "neoxc_rx_scf": (I, [i64] * 10 + [d] + [vp] * 15 + [i64] + [vp] * 9),
+        "neoxc_rxchfne_fock": (I, [i64] * 7 + [vp] * 20),
         "neoxc_probe_fp64": (I, [vp]),
         "neoxc_dev_gam4_dscf": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_dev_gam4_dscf_noalloc": (I, [vp, i64, i64] + [vp] * 7),
@@ -396,6 +397,34 @@ def rx_scf(s: NeoSystem, kind: str, nae: int = 0, nalp: int = 0, nbet: int = 0,
             "DA": DA.reshape(ne, ne, order="F"), "DAbet": DB.reshape(ne, ne, order="F"),
             "DBE": DBE.reshape(ne, ne, order="F"), "DP": DP.reshape(np_, np_, order="F"),
             "history": hist[:3 * n].reshape(n, 3), "niter": n, "converged": bool(conv.value)}
+
+
+def rxchfne_fock(ne, np_, DA, DBE, DP, tables: dict, NAE=0, NAalpE=0, NAbetE=0, DAbet=None,
+                 addexch=False) -> dict:
+    """RXCHFne_FOCK (DAbet None) or RXCUHFne_FOCK on the device; ``tables``
+    holds GAM_ecore, GAM_ee, GAM_1, GAM_1s, GM2ICR (and GM2exICR)."""
+    open_ = DAbet is not None
+    t = {k: None if tables.get(k) is None else np.ascontiguousarray(tables[k], dtype=np.float64)
+         for k in ("GAM_ecore", "GAM_ee", "GAM_1", "GAM_1s", "GM2ICR", "GM2exICR")}
+    da, dbe, dp = _fmat(DA), _fmat(DBE), _fmat(DP)
+    db = _fmat(DAbet) if open_ else None
+    FP, FA, FB, FBE = np.zeros(np_ * np_), np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(ne * ne)
+    en = [np.zeros(1) for _ in range(6)]
+
+    def pp(a):
+        return None if a is None else _p(a)
+    _check(lib().neoxc_rxchfne_fock(int(open_), int(addexch), NAE, NAalpE, NAbetE, ne, np_,
+                                    _p(da), pp(db), _p(dbe), _p(dp), pp(t["GAM_ecore"]),
+                                    pp(t["GAM_ee"]), pp(t["GAM_1"]), pp(t["GAM_1s"]),
+                                    pp(t["GM2ICR"]), pp(t["GM2exICR"]), _p(FP), _p(FA),
+                                    _p(FB), _p(FBE), *[_p(e) for e in en]))
+    r = dict(zip(("E_ecore", "E_ee", "E_OMG1", "E_OMG2", "E_total", "S_total"),
+                 [float(e[0]) for e in en]))
+    r["FP"], r["FAE"] = FP.reshape(np_, np_, order="F"), FA.reshape(ne, ne, order="F")
+    r["FBE"] = FBE.reshape(ne, ne, order="F")
+    if open_:
+        r["FAbetE"] = FB.reshape(ne, ne, order="F")
+    return r
 
 
 SCF_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_gam1", "E_gam2",

@@ -91,3 +91,48 @@ def test_rxchf_gam1_matches_oracle(nx, orc, golden_rx):
         L.orc_rxchf_gam1(h.ref, orc.ptr(r), orc.ptr(rs))
         for a, b in ((g, r), (gs, rs)):
             assert float(np.abs(a - b).max()) <= 1e-12 * max(1.0, float(np.abs(b).max()))
+
+
+@pytest.mark.parametrize("variant", ["rxchf_ne", "rxcuhf_ne", "rxcuhf_ae"])
+def test_rx_fock_entry_matches_oracle(nx, orc, golden_rx, variant):
+    """neoxc_rxchfne_fock (RXCHFne_FOCK / RXCUHFne_FOCK) against the oracle's
+    restatement on the same tables (the device's), at the guess densities
+    and at perturbed ones.  Fock matrices within 1e-9 of their largest
+    element, energies within 1e-9 relative: the contractions sum in another
+    order, and in the RXCHF-ne guess S_total = 0.027 is itself a cancelling
+    sum (GAM_1s entries up to 4e3), known to ~1e-10 relative, which the
+    corrections FP = XFP / S - E / S^2 XSP amplify (measured 1.1e-10 of the
+    largest FP element)."""
+    import rxne
+    from neoxc import basis
+    src = "rxchf_ne" if variant == "rxchf_ne" else "rxcuhf_ne"
+    s = basis.parse_inp(golden_rx[src]["inp"], name=src)
+    G2, G2x = nx.rxchfne_gam2_ic1(s)
+    ints = rxne.RxIntegrals(s, G2=G2, G2ex=G2x)
+    ints.G1, ints.G1s = nx.rxchf_gam1(s)
+    tables = {"GAM_ecore": ints.Gecore, "GAM_ee": ints.Gee, "GAM_1": ints.G1,
+              "GAM_1s": ints.G1s, "GM2ICR": G2, "GM2exICR": G2x}
+    ne, np_ = s.nebf, s.npbf
+    rng = np.random.default_rng(5)
+    closed = variant == "rxchf_ne"
+    st = rxne.guess(ints, nae=2) if closed else rxne.guess(ints, nalp=1, nbet=2)
+    for step in range(2):
+        if step:
+            for k in ("DAE", "DBE", "DP") + (() if closed else ("DAbetE",)):
+                X = 1e-3 * rng.standard_normal(st[k].shape)
+                st[k] = st[k] + X + X.T
+        if closed:
+            ref = rxne.rxchfne_fock(ints, 2, st["DAE"], st["DBE"], st["DP"])
+            got = nx.rxchfne_fock(ne, np_, st["DAE"], st["DBE"], st["DP"], tables, NAE=2)
+            mats = ("FAE", "FP", "FBE")
+        else:
+            ex = variant == "rxcuhf_ae"
+            ref = rxne.rxcuhfne_fock(ints, 1, 2, st["DAE"], st["DAbetE"], st["DBE"], st["DP"], ex)
+            got = nx.rxchfne_fock(ne, np_, st["DAE"], st["DBE"], st["DP"], tables, NAalpE=1,
+                                  NAbetE=2, DAbet=st["DAbetE"], addexch=ex)
+            mats = ("FAE", "FAbetE", "FP", "FBE")
+        for m in mats:
+            a, b = got[m], ref[m]
+            assert float(np.abs(a - b).max()) <= 1e-9 * max(1.0, float(np.abs(b).max())), (m, step)
+        for k in ("E_ecore", "E_ee", "E_OMG1", "E_OMG2", "S_total", "E_total"):
+            assert abs(got[k] - ref[k]) <= 1e-9 * max(1.0, abs(ref[k])), (k, step, got[k], ref[k])
