@@ -394,8 +394,9 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
 #define NEOXC_SCF_GAM4_ELEMENT 4   /* element-wise GAM4_DSCF for gam_4     */
 #define NEOXC_SCF_MIXED 8          /* gam_3 MD integrals in FP32 (new)     */
 #define NEOXC_SCF_MIXED_GAM2 16    /* gam_1, gam_2 MD integrals in FP32 (new) */
-#define NEOXC_SCF_GUESS_ELEC 32    /* XCUHF: DAE, DBE from the electronic core
-                                      Hamiltonian (guess_A_elec) */
+#define NEOXC_SCF_GUESS_ELEC 32    /* DE (XCHF: guess_elec, xcscf.f:660) or
+                                      DAE, DBE (XCUHF: guess_A_elec) from the
+                                      electronic core Hamiltonian */
 int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
                    const double* cat, const double* zan, const double* bcoef1,

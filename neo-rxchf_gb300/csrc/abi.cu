@@ -1362,7 +1362,7 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
   RC(need(DE && DP && E_init && E_final && niter && converged, "pointers"));
   RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_DIIS |
                                 NEOXC_SCF_GAM4_ELEMENT | NEOXC_SCF_MIXED |
-                                NEOXC_SCF_MIXED_GAM2)) == 0,
+                                NEOXC_SCF_MIXED_GAM2 | NEOXC_SCF_GUESS_ELEC)) == 0,
           "options"));
   const int mixed = (options & NEOXC_SCF_MIXED) ? 1 : 0;
   const int mixed_gam2 = (options & NEOXC_SCF_MIXED_GAM2) ? 1 : 0;
@@ -1451,6 +1451,9 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
   CU(launch_inv_sqrt(np, Sp.as<double>(), Xp.as<double>(), sts + 1, s));
   const int noccE = nelec > 1 ? (int)(nelec / 2) : 1;
   const double prefE = nelec > 1 ? 2.0 : 1.0;
+  if (options & NEOXC_SCF_GUESS_ELEC)   // guess_elec (xcscf.f:660-670)
+    CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), 0, noccE, prefE,
+                      dDE.as<double>(), nullptr, nullptr, sts + 2, s));
   if (options & NEOXC_SCF_GUESS_PROT) {
     // guess_prot (xcscf.f:683-716): diagonalise the nuclear core Hamiltonian
     CU(launch_roothan(np, Hcp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1,

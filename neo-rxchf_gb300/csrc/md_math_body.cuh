@@ -267,6 +267,15 @@ struct GK3 {
 };
 NX_BIG void dgauss3(const GK3& g, const real* X, int N1, int N2, int N3,
                    real* D /* [TD][TD][TD] */) {
+  if ((N1 | N2 | N3) == 0) {   // s shells: the base value only
+    real expo = R_(0.0);
+    for (int k = 0; k < g.nk; k++) {
+      const real u = g.c[k][0] * X[0] + g.c[k][1] * X[1] + g.c[k][2] * X[2];
+      expo -= g.xi[k] * u * u;
+    }
+    D[0] = exp(expo);
+    return;
+  }
   real grad[3] = {0, 0, 0}, H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   real expo = R_(0.0);   // prod_k exp(-xi_k u_k^2) as one exponential
   for (int k = 0; k < g.nk; k++) {
@@ -305,6 +314,16 @@ struct GK4 {
 // D[n1][n2][n3][n4], extents T4D each
 constexpr int T4D = 2 * LP + 1;
 NX_BIG void dgauss4(const GK4& g, const real* X, const int* N, real* D) {
+  if ((N[0] | N[1] | N[2] | N[3]) == 0) {   // s shells: the base value only
+    real expo = R_(0.0);
+    for (int k = 0; k < g.nk; k++) {
+      const real u = g.c[k][0] * X[0] + g.c[k][1] * X[1] + g.c[k][2] * X[2] +
+                     g.c[k][3] * X[3];
+      expo -= g.xi[k] * u * u;
+    }
+    D[0] = exp(expo);
+    return;
+  }
   real grad[4] = {0, 0, 0, 0}, H[4][4];
   for (int i = 0; i < 4; i++)
     for (int j = 0; j < 4; j++) H[i][j] = R_(0.0);
@@ -568,6 +587,31 @@ NX_BIG real contract_wr(const real* Wx, int nx, const real* Wy, int ny,
 }
 
 // G3_MD_xgVxCg (XC1_G3_MD.f:711-1088): attraction of particle 1 to C
+// Coulomb factor of a G3 kernel, C0 C3 sum W_x W_y W_z R_tuv: for s shells
+// every Hermite expansion is E_0 = K, so W_d = K1 K2 K3 D_d(0,0,0) and only
+// R_000 = F_0(T) enters -- the same products in the same order as the
+// general contraction, without its tables.
+NX_BIG real g3_coulomb(const G3& s, real C0, real C3, real bf, real bg, real bh, real T,
+                       real alpha, const real* Rv) {
+  bool all_s = true;
+  for (int i = 0; i < 3; i++)
+    for (int d = 0; d < 3; d++) all_s = all_s && s.T[i][d] == 0;
+  if (all_s) {
+    real w = R_(1.0);
+    for (int d = 0; d < 3; d++) {
+      const real wd = ((s.pr[0].K[d] * s.pr[1].K[d]) * s.pr[2].K[d]) * s.D[d][0];
+      w = d == 0 ? wd : w * wd;
+    }
+    real F[1];
+    boys(0, T, F);
+    return C0 * C3 * (w * F[0]);
+  }
+  real W[3][LTOT + 1];
+  int n[3];
+  for (int d = 0; d < 3; d++) g3_wvec(s, d, bf, bg, bh, W[d], &n[d]);
+  return C0 * C3 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], T, alpha, Rv);
+}
+
 NX_BIG real g3_vxc(const G3& s, const real* C) {
   const real s1 = s.S1, s2 = s.S2, g = s.gam12;
   const real p1 = s.pr[0].p, p2 = s.pr[1].p, c1 = s.C1, c2 = s.C2;
@@ -588,10 +632,7 @@ NX_BIG real g3_vxc(const G3& s, const real* C) {
     R2 += Rv[d] * Rv[d];
   }
   const real alpha = tv3, T = alpha * R2;
-  real W[3][LTOT + 1];
-  int n[3];
-  for (int d = 0; d < 3; d++) g3_wvec(s, d, bf, bg, bh, W[d], &n[d]);
-  return C0 * C3 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], T, alpha, Rv);
+  return g3_coulomb(s, C0, C3, bf, bg, bh, T, alpha, Rv);
 }
 
 // G3_MD_xgVeeg (XC1_G3_MD.f:1376-1675): 1/|r1 - r2|
@@ -611,11 +652,7 @@ NX_BIG real g3_vee(const G3& s) {
     R2 += dd * dd;
   }
   const real T = alpha * R2;
-  real W[3][LTOT + 1];
-  int n[3];
-  for (int d = 0; d < 3; d++)
-    g3_wvec(s, d, s.gk.c[2][0], s.gk.c[2][1], s.gk.c[2][2], W[d], &n[d]);
-  return C0 * C3 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], T, alpha, Rv);
+  return g3_coulomb(s, C0, C3, s.gk.c[2][0], s.gk.c[2][1], s.gk.c[2][2], T, alpha, Rv);
 }
 
 // ======================================================================

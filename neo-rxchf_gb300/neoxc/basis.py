@@ -233,19 +233,74 @@ def parse_inp(text: str, name: str = "input") -> NeoSystem:
     bgem = np.array([float(gem["bgem"][k]) for k in range(1, ngtg + 1)])
     ggem = np.array([float(gem["ggem"][k]) for k in range(1, ngtg + 1)])
     at = _card_lines(text, "ATOMS", nat)
-    zan = np.array([float(r[0]) for r in at])
-    cat = np.array([[A2BOHR * float(r[d]) for r in at] for d in (1, 2, 3)])
     eb = _card_lines(text, "EBASIS", npebf)
+    pb = _card_lines(text, "PBASIS", npbf)
+    return _system(name, nebf, npebf, npbf, nat, ngtg, pmass, nelec, nucst, bgem, ggem,
+                   at, eb, pb)
+
+
+def _fnum(tok: str) -> float:
+    return float(tok.replace("d", "e").replace("D", "E"))
+
+
+def parse_positional_inp(text: str, name: str = "input"):
+    """Parse the older positional ``basis_definition.inp`` decks of the
+    reference's tests/ directories: NGTG, NGTG rows of (b_k, gamma_k), NAT,
+    NAT atom rows (Z, x, y, z in Angstrom, label), NEBF, NPEBF, NPEBF
+    primitive rows (index, contracted index, l, m, n, exponent, coefficient,
+    x, y, z in Angstrom), NPBF, NPBF nuclear rows alike, then one value per
+    row tagged ``=NAME`` (PMASS, nelec, NAE, NBE, NUCST, the logical switches,
+    EXCHLEV, NAalpE, NAbetE ...).  The logs of those runs echo the same
+    parameters (coordinates converted to bohr).  Returns the normalised
+    system and the tagged values keyed by lower-case name (strings)."""
+    rows = [ln.split() for ln in text.splitlines() if ln.strip()]
+    k = 0
+
+    def take():
+        nonlocal k
+        k += 1
+        return rows[k - 1]
+
+    ngtg = int(take()[0])
+    gem = [take() for _ in range(ngtg)]
+    bgem = np.array([_fnum(r[0]) for r in gem])
+    ggem = np.array([_fnum(r[1]) for r in gem])
+    nat = int(take()[0])
+    at = [take() for _ in range(nat)]
+    nebf = int(take()[0])
+    npebf = int(take()[0])
+    eb = [take() for _ in range(npebf)]
+    npbf = int(take()[0])
+    pb = [take() for _ in range(npbf)]
+    tags = {}
+    for r in rows[k:]:
+        line = " ".join(r)
+        m = re.match(r"(\S+)\s*=\s*([A-Za-z_][A-Za-z_0-9]*)", line)
+        if m and m.group(2).lower() not in tags:
+            tags[m.group(2).lower()] = m.group(1)
+    pmass = _fnum(tags.get("pmass", "1836.0"))
+    nelec = int(tags.get("nelec", "2"))
+    nucst = int(tags.get("nucst", "1"))
+    sysm = _system(name, nebf, npebf, npbf, nat, ngtg, pmass, nelec, nucst, bgem, ggem,
+                   at, eb, pb)
+    return sysm, tags
+
+
+def _system(name, nebf, npebf, npbf, nat, ngtg, pmass, nelec, nucst, bgem, ggem, at, eb,
+            pb) -> NeoSystem:
+    """Arrays of the driver (xcneo_HYBRID.f:375-445) from the ATOMS, EBASIS
+    and PBASIS rows, with ELCNORM3 / NUCNORM applied."""
+    zan = np.array([_fnum(r[0]) for r in at])
+    cat = np.array([[A2BOHR * _fnum(r[d]) for r in at] for d in (1, 2, 3)])
     ampeb2c = np.array([int(r[1]) for r in eb], np.int64)
     elcam = np.array([[int(r[2]), int(r[3]), int(r[4])] for r in eb], np.int64)
-    elcex = np.array([float(r[5]) for r in eb])
-    agebfcc = np.array([float(r[6]) for r in eb])
-    elcbfc = np.array([[A2BOHR * float(r[7 + d]) for d in range(3)] for r in eb])
-    pb = _card_lines(text, "PBASIS", npbf)
+    elcex = np.array([_fnum(r[5]) for r in eb])
+    agebfcc = np.array([_fnum(r[6]) for r in eb])
+    elcbfc = np.array([[A2BOHR * _fnum(r[7 + d]) for d in range(3)] for r in eb])
     nucam = np.array([[int(r[2]), int(r[3]), int(r[4])] for r in pb], np.int64)
-    nucex = np.array([float(r[5]) for r in pb])
-    agnbfcc = np.array([float(r[6]) for r in pb])
-    nucbfc = np.array([[A2BOHR * float(r[7 + d]) for d in range(3)] for r in pb])
+    nucex = np.array([_fnum(r[5]) for r in pb])
+    agnbfcc = np.array([_fnum(r[6]) for r in pb])
+    nucbfc = np.array([[A2BOHR * _fnum(r[7 + d]) for d in range(3)] for r in pb])
     kpestr, kpeend = make_kpe(nebf, ampeb2c)
     agebfcc = elcnorm3(ampeb2c, agebfcc, elcex, elcam, elcbfc)
     agnbfcc = nucnorm(agnbfcc, nucex, nucam)

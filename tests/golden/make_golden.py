@@ -18,6 +18,11 @@ Writes, next to this script:
                       examples/rxcuhf/rxchf-{ne,ae} (RXCUHF, EXCHLEV 0 / 1):
                       input decks and the energy components of their logs
                       for the initial guess and at convergence;
+  ref_tests.json      tests/TEST_RXCHFmult/*/answer (XCHF RHF runs) and
+                      tests/TEST_XCUHF/XCUHF_TEST_0{2..6,8} (XCUHF runs):
+                      the positional input decks, the MO guess files the
+                      read_CE runs start from, and the energy components of
+                      their logs for the initial guess and at convergence;
   spot_check.json     CS_Integrals/Spot_Check/TEST_G{2,3,4}: the single-
                       primitive inputs (first record block, as SCI.f:114-152
                       reads them) and the MD values printed in each ``out``.
@@ -124,6 +129,42 @@ def rx_examples(ref: str) -> dict:
     return out
 
 
+REF_TESTS = {   # name: (directory under tests/, log, kind)
+    "xchf_mult01_321g": ("TEST_RXCHFmult/RXCHFmult_TEST_01/3-21G/answer/PsH", "XCHF.log", "xchf"),
+    "xchf_mult01_6311g": ("TEST_RXCHFmult/RXCHFmult_TEST_01/6-311G/answer/PsH", "XCHF.log",
+                          "xchf"),
+    "xchf_mult02_lips": ("TEST_RXCHFmult/RXCHFmult_TEST_02/answer/LiPs_xchf", "XCHF.log", "xchf"),
+    "xchf_mult03": ("TEST_RXCHFmult/RXCHFmult_TEST_03/answer", "XCHF.log", "xchf"),
+    "xchf_mult04": ("TEST_RXCHFmult/RXCHFmult_TEST_04/answer", "XCHF.log", "xchf"),
+    "xchf_mult05": ("TEST_RXCHFmult/RXCHFmult_TEST_05/answer", "XCHF.log", "xchf"),
+    "xcuhf_02": ("TEST_XCUHF/XCUHF_TEST_02", "answer/xcOMPout.log", "xcuhf"),
+    "xcuhf_03": ("TEST_XCUHF/XCUHF_TEST_03", "answer/xcOMPout.log", "xcuhf"),
+    "xcuhf_04": ("TEST_XCUHF/XCUHF_TEST_04", "answer/xcOMPout.log", "xcuhf"),
+    "xcuhf_05": ("TEST_XCUHF/XCUHF_TEST_05", "answer/xcOMPout.log", "xcuhf"),
+    "xcuhf_06": ("TEST_XCUHF/XCUHF_TEST_06", "answer/xcOMPout.log", "xcuhf"),
+    "xcuhf_08": ("TEST_XCUHF/XCUHF_TEST_08", "answer/xcOMPout.log", "xcuhf"),
+}
+
+
+def ref_tests(ref: str) -> dict:
+    out = {}
+    for name, (sub, logname, kind) in REF_TESTS.items():
+        d = os.path.join(ref, "tests", sub)
+        log = open(os.path.join(d, logname)).read()
+        keys = XCHF_KEYS if kind == "xchf" else XCUHF_KEYS
+        m = re.search(r"FINAL NEO\w* ENERGY IS\s+(-?[0-9.]+)\s+AFTER\s+(\d+)", log)
+        entry = {"source": "tests/%s/basis_definition.inp, %s" % (sub, logname), "kind": kind,
+                 "inp": open(os.path.join(d, "basis_definition.inp")).read(),
+                 "initial": _components(log, "INITIAL GUESS ENERGETICS", keys),
+                 "final": _components(log, m.group(0), keys),
+                 "final_energy": float(m.group(1)), "iterations": int(m.group(2))}
+        for g in ("guessCE.inp", "guessCP.inp", "guessCAE.inp", "guessCBE.inp"):
+            if os.path.exists(os.path.join(d, g)):
+                entry[g] = open(os.path.join(d, g)).read()
+        out[name] = entry
+    return out
+
+
 def _first_block(path: str):
     rows = [l.split() for l in open(path).read().splitlines()]
     k = 0
@@ -168,6 +209,8 @@ def main(ref: str):
         json.dump(spot_check(ref), f, indent=1)
     with open(os.path.join(HERE, "rx_examples.json"), "w") as f:
         json.dump(rx_examples(ref), f, indent=1)
+    with open(os.path.join(HERE, "ref_tests.json"), "w") as f:
+        json.dump(ref_tests(ref), f, indent=1)
 
 
 if __name__ == "__main__":
