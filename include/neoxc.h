@@ -542,6 +542,10 @@ int neoxc_rxchfne_fock(int64_t open_shell, int64_t addexch, int64_t NAE,
 #define NEOXC_RX_NE 0
 #define NEOXC_RX_CU_NE 1
 #define NEOXC_RX_CU_AE 2
+#define NEOXC_RX_NO_OCBSE 16   /* or-ed into kind: the reference's LOCBSE =
+   .false. branch -- RXCHF_guess_A/B_elec (rxchf/rxchf_scf.f:733-784), a Fock
+   build at the top of every micro-iteration and UROOTHAN of FBE for the
+   special electron's lowest orbital instead of RXCHF_OCBSE2 */
 int neoxc_rx_scf(int64_t kind, int64_t NAE, int64_t NAalpE, int64_t NAbetE,
                  int64_t nucst, int64_t nebf, int64_t npebf, int64_t npbf,
                  int64_t nat, int64_t ngtg1, double pmass, const double* cat,

@@ -2592,6 +2592,8 @@ int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t
               int64_t maxit, double* DA, double* DAbet, double* DBE, double* DP,
               double* E_init, double* E_final, double* history, int64_t* niter,
               int64_t* converged) {
+  const bool ocbse = (kind & NEOXC_RX_NO_OCBSE) == 0;
+  kind &= ~(int64_t)NEOXC_RX_NO_OCBSE;
   RC(need(kind == NEOXC_RX_NE || kind == NEOXC_RX_CU_NE || kind == NEOXC_RX_CU_AE, "kind"));
   const bool open = kind != NEOXC_RX_NE;
   if (open)
@@ -2669,8 +2671,9 @@ int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t
   if (open && NAbetE > 0)
     CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), 0, (int)NAbetE, 1.0,
                       dB.as<double>(), nullptr, nullptr, sts + 3, s));
-  CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), nocca, 1, 1.0, dBE.as<double>(),
-                    nullptr, Ctmp.as<double>(), sts + 4, s));
+  // RXCHF_guess_B_elec (plain branch): the lowest core orbital
+  CU(launch_roothan(ne, Hce.as<double>(), Xe.as<double>(), ocbse ? nocca : 0, 1, 1.0,
+                    dBE.as<double>(), nullptr, Ctmp.as<double>(), sts + 4, s));
   CU(cudaMemcpyAsync(CBE.p, Ctmp.as<double>() + (size_t)ne * nocca, sizeof(double) * ne,
                      cudaMemcpyDeviceToDevice, s));
   CU(launch_roothan(np, Hcp.as<double>(), Xp.as<double>(), (int)nucst - 1, 1, 1.0,
@@ -2706,7 +2709,7 @@ int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t
     int micro = 0;
     double dreg = 0.0;
     for (micro = 1; micro <= maxmicro; micro++) {
-      if (micro == 1) RC(fock());
+      if (micro == 1 || !ocbse) RC(fock());
       CU(launch_roothan(ne, FA.as<double>(), Xe.as<double>(), 0, nocca, prefA, dA.as<double>(),
                         nullptr, CA.as<double>(), sts + 7, s));
       CU(launch_rx_dendif(ne, dA.as<double>(), A0.as<double>(), d_en + 12, s));
@@ -2717,16 +2720,20 @@ int rx_scf_on(cudaStream_t s, int64_t kind, int64_t NAE, int64_t NAalpE, int64_t
       }
       // RXCHF_OCBSE2 / RXCUHF_OCBSE2 with the Fock matrix of the densities
       // before this micro-iteration's regular update
-      CU(launch_ocbse2(ne, nocca, CA.as<double>(), CBE.as<double>(), FBE.as<double>(),
-                       Se.as<double>(), ocb.as<double>(), CBE.as<double>(), dBE.as<double>(),
-                       info.as<double>(), sts + 9, s));
+      if (ocbse)
+        CU(launch_ocbse2(ne, nocca, CA.as<double>(), CBE.as<double>(), FBE.as<double>(),
+                         Se.as<double>(), ocb.as<double>(), CBE.as<double>(),
+                         dBE.as<double>(), info.as<double>(), sts + 9, s));
+      else   // UROOTHAN of FBE, the lowest orbital (RXCHF_construct_DBE)
+        CU(launch_roothan(ne, FBE.as<double>(), Xe.as<double>(), 0, 1, 1.0, dBE.as<double>(),
+                          nullptr, nullptr, sts + 9, s));
       CU(launch_rx_dendif(ne, dBE.as<double>(), BE0.as<double>(), d_en + 13, s));
-      RC(fock());
+      if (ocbse) RC(fock());
       double hi[4];
       CU(cudaMemcpyAsync(h, d_en, sizeof(h), cudaMemcpyDeviceToHost, s));
       CU(cudaMemcpyAsync(hi, info.p, sizeof(hi), cudaMemcpyDeviceToHost, s));
       RC(check_eig(11));
-      if (!(hi[1] > 0.0))
+      if (ocbse && !(hi[1] > 0.0))
         return set_err(NEOXC_ERR_CUDA, "OCBSE2: the projected special orbital vanished");
       dreg = (open && NAbetE > 0) ? std::max(h[12], hi[2]) : h[12];
       if (dreg < tolE && h[13] < tolE) break;

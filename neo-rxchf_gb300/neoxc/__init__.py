@@ -377,11 +377,12 @@ RX_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_ee", "E_OMG1", "E_OMG2", "S_total"
 
 
 def rx_scf(s: NeoSystem, kind: str, nae: int = 0, nalp: int = 0, nbet: int = 0,
-           nucst: int = 1, maxit: int = 100) -> dict:
+           nucst: int = 1, maxit: int = 100, ocbse: bool = True) -> dict:
     """One-special-electron RXCHF SCF on the device (rxchfne_scf.f
     xcrxchfne, rxcuhfne_scf.f xcrxcuhfne): kind "rxchf_ne" (nae closed-shell
     regular electrons), "rxcuhf_ne" or "rxcuhf_ae" (nalp alpha, nbet beta;
-    EXCHLEV 0 / 1).  Returns the initial and final energy slots (RX_SLOTS),
+    EXCHLEV 0 / 1); ocbse=False selects the reference's LOCBSE = .false.
+    branch.  Returns the initial and final energy slots (RX_SLOTS),
     the densities, the history and the iteration count."""
     ne, np_ = s.nebf, s.npbf
     DA, DB, DBE, DP = np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(ne * ne), np.zeros(np_ * np_)
@@ -389,7 +390,8 @@ def rx_scf(s: NeoSystem, kind: str, nae: int = 0, nalp: int = 0, nbet: int = 0,
     hist = np.zeros(3 * maxit)
     nit, conv = C.c_int64(0), C.c_int64(0)
     keep, ptrs = _sysargs(s)
-    _check(lib().neoxc_rx_scf(RX_KINDS[kind], nae, nalp, nbet, nucst, ne, s.npebf, np_, s.nat,
+    _check(lib().neoxc_rx_scf(RX_KINDS[kind] | (0 if ocbse else 16), nae, nalp, nbet, nucst,
+                              ne, s.npebf, np_, s.nat,
                               s.ngtg, s.pmass, *ptrs, maxit, _p(DA), _p(DB), _p(DBE), _p(DP),
                               _p(Ei), _p(Ef), _p(hist), C.byref(nit), C.byref(conv)))
     n = nit.value

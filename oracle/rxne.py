@@ -275,13 +275,21 @@ def ocbse2(ints: RxIntegrals, nocca, CAE, CBE0, FBE):
 
 
 def rx_scf(ints: RxIntegrals, nae=None, nalp=None, nbet=None, addexch=False, nucst=1,
-           maxit=100, maxmicro=200, tole=1.0e-6, tolp=1.0e-4):
-    """The LOCBSE2 SCF of rxchfne_scf.f / rxcuhfne_scf.f with UROOTHAN for
-    the regular electrons.  Returns (initial energetics, final energetics,
-    history of (iteration, micro-iterations, E_total), converged)."""
+           maxit=100, maxmicro=200, tole=1.0e-6, tolp=1.0e-4, ocbse=True):
+    """The SCF of rxchfne_scf.f / rxcuhfne_scf.f with UROOTHAN for the
+    regular electrons: the LOCBSE2 branch (ocbse=True: OCBSE guess, one Fock
+    build per micro-iteration after RXCHF_OCBSE2) or the plain branch
+    (ocbse=False: RXCHF_guess_A/B_elec, rxchf_scf.f:733-784, a Fock build at
+    the top of every micro-iteration and UROOTHAN for the special electron's
+    lowest orbital).  Returns (initial energetics, final energetics, history
+    of (iteration, micro-iterations, E_total), converged)."""
     open_shell = nae is None
     st = guess(ints, nae=nae, nalp=nalp, nbet=nbet, nucst=nucst)
     nocca = nalp if open_shell else (nae // 2 if nae > 1 else nae)
+    if not ocbse:   # RXCHF_guess_B_elec: the lowest core orbital
+        C, _ = uroothan(ints.ecore(), ints.S_e())
+        st["CBE"] = C.copy()
+        st["DBE"] = occ_density(C, 1)
 
     def fock():
         if open_shell:
@@ -305,7 +313,7 @@ def rx_scf(ints: RxIntegrals, nae=None, nalp=None, nbet=None, addexch=False, nuc
         diffP = float(np.abs(D0["DP"] - st["DP"]).max())
         D0["DP"] = st["DP"].copy()
         for micro in range(1, maxmicro + 1):
-            if micro == 1:
+            if micro == 1 or not ocbse:
                 r = fock()
             C, _ = uroothan(r["FAE"], ints.S_e())
             st["CAE"] = C
@@ -317,11 +325,15 @@ def rx_scf(ints: RxIntegrals, nae=None, nalp=None, nbet=None, addexch=False, nuc
                 st["DAbetE"] = occ_density(Cb, nbet)
                 diffA = max(diffA, float(np.abs(D0["DAbetE"] - st["DAbetE"]).max()))
                 D0["DAbetE"] = st["DAbetE"].copy()
-            st["CBE"], _ = ocbse2(ints, nocca, st["CAE"], st["CBE"], r["FBE"])
+            if ocbse:
+                st["CBE"], _ = ocbse2(ints, nocca, st["CAE"], st["CBE"], r["FBE"])
+            else:
+                st["CBE"], _ = uroothan(r["FBE"], ints.S_e())
             st["DBE"] = occ_density(st["CBE"], 1)
             diffB = float(np.abs(D0["DBE"] - st["DBE"]).max())
             D0["DBE"] = st["DBE"].copy()
-            r = fock()
+            if ocbse:
+                r = fock()
             if diffA < tole and diffB < tole:
                 break
         hist.append((it, micro, r["E_total"]))

@@ -55,6 +55,12 @@ def golden_rx():
 
 
 @pytest.fixture(scope="session")
+def golden_rx_ref_tests():
+    with open(os.path.join(GOLDEN, "rx_ref_tests.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
 def golden_ref_tests():
     with open(os.path.join(GOLDEN, "ref_tests.json")) as f:
         return json.load(f)

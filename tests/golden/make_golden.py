@@ -23,6 +23,10 @@ Writes, next to this script:
                       the positional input decks, the MO guess files the
                       read_CE runs start from, and the energy components of
                       their logs for the initial guess and at convergence;
+  rx_ref_tests.json   tests/TEST_RXCHF and tests/TEST_RXCUHF one-special-
+                      electron decks (RXCHF-ne, RXCUHF-ne / -ae) with the
+                      converged energies and iteration counts their READMEs
+                      record;
   spot_check.json     CS_Integrals/Spot_Check/TEST_G{2,3,4}: the single-
                       primitive inputs (first record block, as SCI.f:114-152
                       reads them) and the MD values printed in each ``out``.
@@ -146,6 +150,41 @@ REF_TESTS = {   # name: (directory under tests/, log, kind)
 }
 
 
+# one-special-electron RX decks and the README line that records each
+# run's converged energy: name -> (deck directory, README, section, label)
+RX_REF_TESTS = {
+    "rxchf_t01": ("TEST_RXCHF/RXCHF_TEST_01", "TEST_RXCHF/README", "TEST01", "RXCHF:"),
+    "rxchf_t02": ("TEST_RXCHF/RXCHF_TEST_02", "TEST_RXCHF/README", "TEST02", "RXCHF:"),
+    "rxcuhf_t01_ae": ("TEST_RXCUHF/RXCUHF_TEST_01/rxchf-ae", "TEST_RXCUHF/README", "TEST01",
+                      "RXCHF-ae:"),
+    "rxcuhf_t01_ne": ("TEST_RXCUHF/RXCUHF_TEST_01/rxchf-ne", "TEST_RXCUHF/README", "TEST01",
+                      "RXCHF-ne:"),
+    "rxcuhf_t02_ae": ("TEST_RXCUHF/RXCUHF_TEST_02/rxchf-ae", "TEST_RXCUHF/README", "TEST02",
+                      "RXCHF-ae:"),
+    "rxcuhf_t03_ae": ("TEST_RXCUHF/RXCUHF_TEST_03/rxchf-ae", "TEST_RXCUHF/README", "TEST03",
+                      "RXCHF-ae:"),
+    "rxcuhf_t04": ("TEST_RXCUHF/RXCUHF_TEST_04", "TEST_RXCUHF/README", "TEST04", "RXCUHF:"),
+    "rxcuhf_t05": ("TEST_RXCUHF/RXCUHF_TEST_05", "TEST_RXCUHF/README", "TEST05", "RXCHF:"),
+    "rxcuhf_t06": ("TEST_RXCUHF/RXCUHF_TEST_06", "TEST_RXCUHF/README", "TEST06", "RXCHF:"),
+}
+
+
+def rx_ref_tests(ref: str) -> dict:
+    out = {}
+    for name, (sub, readme, section, label) in RX_REF_TESTS.items():
+        text = open(os.path.join(ref, "tests", readme)).read()
+        i = text.index("\n" + section + "\n")
+        j = text.find("======\n" + "TEST", i + len(section) + 10)
+        block = text[i:j if j > 0 else len(text)]
+        m = re.search(re.escape(label) + r"\s+FINAL NEO\w* ENERGY IS\s+(-?[0-9.]+)\s+AFTER\s+"
+                      r"(\d+)", block)
+        out[name] = {"source": "tests/%s/basis_definition.inp, tests/%s %s %s" % (
+                         sub, readme, section, label),
+                     "inp": open(os.path.join(ref, "tests", sub, "basis_definition.inp")).read(),
+                     "final_energy": float(m.group(1)), "iterations": int(m.group(2))}
+    return out
+
+
 def ref_tests(ref: str) -> dict:
     out = {}
     for name, (sub, logname, kind) in REF_TESTS.items():
@@ -211,6 +250,8 @@ def main(ref: str):
         json.dump(rx_examples(ref), f, indent=1)
     with open(os.path.join(HERE, "ref_tests.json"), "w") as f:
         json.dump(ref_tests(ref), f, indent=1)
+    with open(os.path.join(HERE, "rx_ref_tests.json"), "w") as f:
+        json.dump(rx_ref_tests(ref), f, indent=1)
 
 
 if __name__ == "__main__":

@@ -39,3 +39,36 @@ def test_oracle_initial_energetics_of_a_reference_run(orc, golden_ref_tests):
              "E_TOTAL": "E_total"}
     for k, mine in names.items():
         assert abs(r[mine] - g["initial"][k]) <= 6e-11, (k, r[mine], g["initial"][k])
+
+
+def _true(tag):
+    return tag is not None and tag.strip(".").lower().startswith("t")
+
+
+def rx_case(tags, name):
+    """rx_scf arguments of one RX regression deck: RXCHF-ne (NAE closed-shell
+    regular electrons) or RXCUHF (NAalpE / NAbetE, EXCHLEV 1 = ae), and the
+    LOCBSE switch."""
+    ocbse = _true(tags.get("locbse"))
+    if name.startswith("rxchf"):
+        return "rxchf_ne", dict(nae=int(tags["nae"])), ocbse
+    kind = "rxcuhf_ae" if int(tags["exchlev"]) == 1 else "rxcuhf_ne"
+    return kind, dict(nalp=int(tags["naalpe"]), nbet=int(tags["nabete"])), ocbse
+
+
+def test_oracle_rx_reference_runs(orc, golden_rx_ref_tests):
+    """tests/TEST_RXCHF/RXCHF_TEST_01 (RXCHF-ne with LOCBSE = .false., the
+    plain branch) and tests/TEST_RXCUHF/RXCUHF_TEST_03/rxchf-ae: the oracle
+    reaches the READMEs' converged energies (-0.6666367359, -7.4259664751)
+    within 1e-9 Eh in their iteration counts (7, 4)."""
+    import rxne
+    from neoxc import basis
+    for name in ("rxchf_t01", "rxcuhf_t03_ae"):
+        g = golden_rx_ref_tests[name]
+        s, tags = basis.parse_positional_inp(g["inp"], name=name)
+        kind, kw, ocbse = rx_case(tags, name)
+        if kind == "rxcuhf_ae":
+            kw["addexch"] = True
+        _, fin, hist, ok = rxne.rx_scf(rxne.RxIntegrals(s), ocbse=ocbse, **kw)
+        assert ok and len(hist) == g["iterations"], (name, len(hist))
+        assert abs(fin["E_total"] - g["final_energy"]) <= 1e-9, (name, fin["E_total"])
