@@ -1530,7 +1530,9 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
     RC(finish(s));
     for (int k = 0; k < 4; k++)
       if (hs[k] > 40)
-        return set_err(NEOXC_ERR_CUDA, "ROOTHAN: Jacobi eigensolver did not converge");
+        return set_err(NEOXC_ERR_CUDA,
+                       "ROOTHAN: Jacobi eigensolver %s (status slot %d, iteration %lld)",
+                       hs[k] > 41 ? "met a NaN" : "did not converge", k, (long long)it);
     if (history) {
       history[4 * (it - 1) + 0] = h[0];
       history[4 * (it - 1) + 1] = h[0] - Eold;

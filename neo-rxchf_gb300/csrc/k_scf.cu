@@ -499,6 +499,7 @@ __device__ int jacobi_eig(int n, double* A, double* V, double* rc, double* rs,
     V[k] = (k / n == k % n) ? 1.0 : 0.0;
   __syncthreads();
   int sweep = 0;
+  double prev_off = 0.0;
   for (; sweep < kJacobiMaxSweeps; sweep++) {
     // convergence: off-diagonal vs diagonal squared norms
     double off = 0.0, dia = 0.0;
@@ -511,7 +512,15 @@ __device__ int jacobi_eig(int n, double* A, double* V, double* rc, double* rs,
     __syncthreads();
     dia = block_sum(dia, sw);
     __syncthreads();
+    if (!(off == off) || !(dia == dia)) return kJacobiMaxSweeps + 2;   // NaN input
     if (off <= 1e-30 * dia || off == 0.0) break;
+    // at the rounding floor (n^2 eps^2 of the diagonal mass can exceed
+    // 1e-30 for n >= 5 when the eigenvalues span several decades) a sweep
+    // no longer shrinks the off-diagonal mass: stop there once it is below
+    // 1e-24 of the diagonal (off-diagonal norm 1e-12 relative)
+    if (sweep > 0 && off <= 1e-24 * dia && off >= 0.25 * prev_off) break;
+    if (sweep >= 8 && off <= 1e-24 * dia) break;
+    prev_off = off;
     for (int step = 0; step < m - 1; step++) {
       // round robin: slot 0 fixed, the other m-1 rotate
       for (int k = threadIdx.x; k < m / 2; k += blockDim.x) {

@@ -18,8 +18,9 @@ Writes, next to this script:
                       examples/rxcuhf/rxchf-{ne,ae} (RXCUHF, EXCHLEV 0 / 1):
                       input decks and the energy components of their logs
                       for the initial guess and at convergence;
-  ref_tests.json      tests/TEST_RXCHFmult/*/answer (XCHF RHF runs) and
-                      tests/TEST_XCUHF/XCUHF_TEST_0{2..6,8} (XCUHF runs):
+  ref_tests.json      tests/TEST_RXCHFmult/*/answer and tests/TEST_XCRHF
+                      (XCHF RHF runs) and tests/TEST_XCUHF/XCUHF_TEST_0{2..6,8}
+                      (XCUHF runs):
                       the positional input decks, the MO guess files the
                       read_CE runs start from, and the energy components of
                       their logs for the initial guess and at convergence;
@@ -141,6 +142,13 @@ REF_TESTS = {   # name: (directory under tests/, log, kind)
     "xchf_mult03": ("TEST_RXCHFmult/RXCHFmult_TEST_03/answer", "XCHF.log", "xchf"),
     "xchf_mult04": ("TEST_RXCHFmult/RXCHFmult_TEST_04/answer", "XCHF.log", "xchf"),
     "xchf_mult05": ("TEST_RXCHFmult/RXCHFmult_TEST_05/answer", "XCHF.log", "xchf"),
+    "xcrhf_02": ("TEST_XCRHF/TEST_02", "xcOMP_MD_out.log", "xchf"),
+    "xcrhf_03": ("TEST_XCRHF/TEST_03", "xcOMP_MD_out.log_ST4", "xchf"),
+    "xcrhf_04md": ("TEST_XCRHF/TEST_04/TEST_MD", "xcOMP_MD_out.log", "xchf"),
+    "xcrhf_05": ("TEST_XCRHF/TEST_05", "xcOMP_MD_out.log", "xchf"),
+    "xcrhf_06": ("TEST_XCRHF/TEST_06", "xcOMP_MD_out.log", "xchf"),
+    "xcrhf_07": ("TEST_XCRHF/TEST_07", "xcOMP_MD_out.log", "xchf"),
+    "xcrhf_nucst": ("TEST_XCRHF/TEST_NUCST", "xcOMP_MD_out.log", "xchf"),
     "xcuhf_02": ("TEST_XCUHF/XCUHF_TEST_02", "answer/xcOMPout.log", "xcuhf"),
     "xcuhf_03": ("TEST_XCUHF/XCUHF_TEST_03", "answer/xcOMPout.log", "xcuhf"),
     "xcuhf_04": ("TEST_XCUHF/XCUHF_TEST_04", "answer/xcOMPout.log", "xcuhf"),

@@ -5,7 +5,10 @@ positional basis_definition.inp decks (neoxc.basis.parse_positional_inp):
 * XCHF RHF (neoxc_xchf_scf) on tests/TEST_RXCHFmult/*/answer: PsH (3-21G and
   6-311G runs, 2 electrons + positron), LiPs (4 electrons, 8 geminal
   terms), RXCHFmult_TEST_03/04/05 (He-based, 2 and 4 electrons, contracted
-  s/p basis, 11 primitives), from the core-Hamiltonian guesses;
+  s/p basis, 11 primitives), from the core-Hamiltonian guesses; and on
+  tests/TEST_XCRHF (TEST_02, 03 with NUCST = 4 and 38 nuclear functions,
+  04/TEST_MD, 05 with NUCST = 2, 06, 07, TEST_NUCST), mostly started from
+  the runs' guessCE / guessCP files;
 * XCUHF (neoxc_xcuhf_scf) on tests/TEST_XCUHF/XCUHF_TEST_0{2,3,4,5}: e+Li
   and LiPs with 1-8 geminal terms, started from the runs' guessCAE /
   guessCBE / guessCP files where the deck sets read_CE / read_CP.  The two
@@ -24,7 +27,13 @@ second-order SCF steps, the device with Roothaan + DIIS, so the iteration
 counts are not compared; RXCHFmult_TEST_03 is pinned at its initial guess
 only: its reference run wandered (proton density changes up to 292 per
 iteration) until the second-order steps brought it to -2.7643081827 after
-37 iterations, and Roothaan + DIIS does not settle it within 200.
+37 iterations, and Roothaan + DIIS does not settle it within 200; nor
+TEST_XCRHF/TEST_06 (3 contracted electronic functions, 2 occupied):
+Roothaan + DIIS falls into a two-cycle between -5.4306 and -5.4164 where
+the reference's second-order steps reach -5.4788705945.  TEST_NUCST's log
+predates the current GAM_1 for p-type nuclear functions: E_GAM1 and
+S_TOTAL carry 2e-8 of their size there (the oracle's restatement of the
+current source differs from the log by the same 4.6e-9 and 1.9e-9).
 """
 from __future__ import annotations
 
@@ -36,10 +45,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 XCHF_CASES = ("xchf_mult01_321g", "xchf_mult01_6311g", "xchf_mult02_lips", "xchf_mult03",
-              "xchf_mult04", "xchf_mult05")
+              "xchf_mult04", "xchf_mult05", "xcrhf_02", "xcrhf_03", "xcrhf_04md", "xcrhf_05",
+              "xcrhf_06", "xcrhf_07", "xcrhf_nucst")
 XCUHF_CASES = ("xcuhf_02", "xcuhf_03", "xcuhf_04", "xcuhf_05")
 XCUHF_SLOW = ("xcuhf_06", "xcuhf_08")
-NOT_CONVERGED_HERE = ("xchf_mult03",)
+NOT_CONVERGED_HERE = ("xchf_mult03", "xcrhf_06")
+# TEST_NUCST's log predates the current GAM_1 for p-type nuclear functions:
+# the oracle's restatement of the current source and the device agree with
+# each other and differ from the log by 4.6e-9 (E_GAM1) and 1.9e-9
+# (S_TOTAL); every other component matches it
+LOG_PREDATES = {"xcrhf_nucst": ("E_GAM1", "S_TOTAL")}
 BIG_SUMS = ("E_GAM4", "E_OMG4")
 
 
@@ -62,10 +77,19 @@ def test_xchf_reference_runs(nx, golden_ref_tests, name):
     from neoxc import basis
     g = golden_ref_tests[name]
     s, tags = basis.parse_positional_inp(g["inp"], name=name)
-    assert not _true(tags.get("read_ce")) and not _true(tags.get("read_cp"))
-    r = nx.xchf_scf(s, None, None, diis=True, maxit=200)
+    DE = DP = None
+    if _true(tags.get("read_ce")):   # read_elec_density (GAM_IO.f)
+        nocc, pref = (s.nelec // 2, 2.0) if s.nelec > 1 else (1, 1.0)
+        DE = basis.density(basis.read_mo_file(g["guessCE.inp"], s.nebf), nocc, pref)
+    if _true(tags.get("read_cp")):   # read_nuc_density (GAM_IO.f)
+        C = basis.read_mo_file(g["guessCP.inp"], s.npbf)
+        DP = np.outer(C[:, s.nucst - 1], C[:, s.nucst - 1])
+    r = nx.xchf_scf(s, DE, DP, diis=True, maxit=200)
     for k, mine in XCHF_NAMES.items():
         ref = g["initial"][k]
+        if k in LOG_PREDATES.get(name, ()):
+            assert abs(r["initial"][mine] - ref) <= 2e-8 * abs(ref), (name, k, r["initial"][mine])
+            continue
         assert abs(r["initial"][mine] - ref) <= _tol(k, ref), (name, k, r["initial"][mine])
     if name in NOT_CONVERGED_HERE:
         return
