@@ -13,9 +13,9 @@ import re
 import numpy as np
 
 
-def test_positional_parser_reads_the_decks(golden_ref_tests):
+def test_positional_parser_reads_the_decks(golden_ref_tests, golden_rx_ref_tests):
     from neoxc import basis
-    for name, g in golden_ref_tests.items():
+    for name, g in list(golden_ref_tests.items()) + list(golden_rx_ref_tests.items()):
         s, tags = basis.parse_positional_inp(g["inp"], name=name)
         assert s.nebf >= 1 and s.npbf >= 1 and s.ngtg >= 1
         assert int(tags["nelec"]) == s.nelec
