@@ -2,7 +2,10 @@
 // GPU and usable as plain C++ (every function is __host__ __device__).
 // Included by md_math.cuh (real = double, namespace md: the FP64 path that
 // matches the reference) and md_math32.cuh (real = float, namespace md32:
-// the mixed-precision path; the Boys function stays FP64 in both).
+// the mixed-precision path).  In both instances the Boys function and the
+// R_tuv recursion seeds (-2 alpha)^j F_j(T) are evaluated in FP64; md32
+// narrows each seed to FP32 before the recursion, and its Gaussian-product
+// set-up, Hermite and derivative tables, recursion and contraction are FP32.
 //
 // The reference evaluates each primitive integral as a 9- or 12-deep loop
 // over Hermite indices, and inside every iteration re-derives the Boys'
@@ -19,10 +22,15 @@
 //     the binomial split between the Gaussian part and the Coulomb part,
 //     and the chain-rule powers of the Coulomb-centre coefficients;
 //   * one R_tuv table per call, and  I = C * sum_{n,l,m} Wx Wy Wz R_nlm.
-// The Boys function keeps the reference's branches (XGAMMAF, common.f:
-// 317-348): asymptotic form without the exp(-T) term for T > 20, series
-// truncated at 1e-12 otherwise, so results agree with the reference to
-// rounding.  Constants: pi truncated to 3.14159265358979 in the MD kernels
+// The Boys function keeps the branch structure of the reference's XGAMMAF
+// (common.f:317-348): for T > 20 the asymptotic form without the exp(-T)
+// term and upward recursion, exactly as there; for T <= 20 the reference
+// sums the series to a 1e-12 cutoff, and here F_M(T) comes from a
+// pretabulated seven-term Taylor expansion (the standard grid method, e.g.
+// Helgaker, Jorgensen, Olsen, Molecular Electronic-Structure Theory, 9.8.5)
+// followed by the same downward recursion; the two agree to ~2.4e-12
+// relative (the series' truncation; the table itself is exact to ~1e-15).
+// Constants: pi truncated to 3.14159265358979 in the MD kernels
 // (XC1_G3_MD.f, XC1_G4_MD.f, XC1_G2_MD.f), acos(-1) in the two-centre
 // integrals (AC_Integrals vee.f, vec.f, ovlap.f, ke.f).
 #include <math.h>
@@ -107,6 +115,63 @@ NX_HD double boys_rinv(int j) {
   return kBoysRinvHost[j];
 #endif
 }
+
+// F_m(T_g), m = 0..22, and exp(-T_g) on the grid T_g = g/16, g = 0..320
+// (boys_table.inc, written by gen_boys_table.py from the integral definition
+// at 40 digits).
+constexpr int kBoysCols = 24, kBoysRows = 321;
+#if defined(__CUDACC__)
+static __device__ const double kBoysTabDev[kBoysRows * kBoysCols] = {
+#include "boys_table.inc"
+};
+#endif
+static const double kBoysTabHost[kBoysRows * kBoysCols] = {
+#include "boys_table.inc"
+};
+NX_HD double boys_tab(int i) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&kBoysTabDev[i]);
+#else
+  return kBoysTabHost[i];
+#endif
+}
+
+// F[0..M](T) in FP64 for both instances (M <= 16).  T > 20 (and NaN): the
+// asymptotic branch of XGAMMAF (common.f:327-333), F_0 = sqrt(pi/T)/2 and
+// F_L = F_(L-1) (L - 1/2) / T.  T <= 20: F_M from the Taylor expansion about
+// the nearest grid point, F_M(T) = sum_{k<=6} F_(M+k)(T_g) d^k / k!,
+// d = T_g - T (|d| <= 1/32, truncation < 1e-14 relative), exp(-T) likewise
+// from exp(-T_g), then the downward recursion F_L = (2T F_(L+1) + exp(-T)) /
+// (2L + 1) as in XGAMMAF (common.f:336-346).
+NX_BIG void boys(int M, double T, double* F) {
+  if (!(T <= 20.0)) {
+    const double rT = 1.0 / T;
+    double f = 0.88622692545275801365 / sqrt(T);
+    F[0] = f;
+    for (int L = 1; L <= M; L++) {
+      f = f * (1.0 * L - 0.5) * rT;
+      F[L] = f;
+    }
+    return;
+  }
+  int g = (int)(T * 16.0 + 0.5);
+  g = g < 0 ? 0 : (g > kBoysRows - 1 ? kBoysRows - 1 : g);
+  const double d = (double)g * 0.0625 - T;
+  const int row = g * kBoysCols;
+  const double inv[6] = {1.0, 0.5, 1.0 / 3.0, 0.25, 0.2, 1.0 / 6.0};
+  double f = boys_tab(row + M + 6);
+  for (int k = 6; k >= 1; k--) f = fma(d * inv[k - 1], f, boys_tab(row + M + k - 1));
+  F[M] = f;
+  if (M == 0) return;
+  double e = 1.0;
+  for (int k = 6; k >= 1; k--) e = fma(d * inv[k - 1], e, 1.0);
+  const double ex = boys_tab(row + kBoysCols - 1) * e;
+  const double t2 = 2.0 * T;
+  for (int L = M - 1; L >= 0; L--) {
+    f = (f * t2 + ex) * (0.5 * boys_rinv(L));
+    F[L] = f;
+  }
+}
 }  // namespace neoxc
 #endif
 
@@ -132,89 +197,6 @@ struct Prim {
   real c[3];
   int l[3];
 };
-
-// ---------------------------------------------------------------- Boys
-// F[0..M] (common.f:317-348 XGAMMAF; T>20 upward, else series at M and
-// downward recursion)
-NX_BIG void boys(int M, real Tr, real* F) {
-  if (M == 0 && (double)Tr <= 20.0) {
-    // F0(T) = sqrt(pi/T) erf(sqrt(T)) / 2 (the T <= 20 series sums to this
-    // to its 1e-12 cutoff); the T > 20 branch below keeps XGAMMAF's
-    // asymptotic form.
-    if (sizeof(real) == sizeof(double)) {
-      const double T = (double)Tr;
-      F[0] = (real)(T < 1.0e-12 ? 1.0 - T / 3.0
-                                : 0.5 * sqrt(3.14159265358979323846 / T) * erf(sqrt(T)));
-    } else {
-      const float T = (float)Tr;
-      F[0] = (real)(T < 1.0e-6f ? 1.0f - T / 3.0f
-                                : 0.5f * sqrtf(3.14159265f / T) * erff(sqrtf(T)));
-    }
-    return;
-  }
-  if (sizeof(real) == sizeof(double)) {
-    // FP64: XGAMMAF's branches and cutoff; the series divisors 1/(m+1/2)
-    // and the downward-recursion divisors 1/(2L+1) = (1/2)/(L+1/2) come from
-    // a reciprocal table (one multiply instead of one FP64 division).
-    const double T = (double)Tr;
-    if (T > 20.0) {
-      const double rT = 1.0 / T;
-      double f = 0.88622692545275801365 / sqrt(T);
-      F[0] = (real)f;
-      for (int L = 1; L <= M; L++) {
-        f = f * (1.0 * L - 0.5) * rT;
-        F[L] = (real)f;
-      }
-    } else {
-      const double pt5 = 0.5 + M;
-      double term = 0.5 / pt5, sum = term;
-      for (int k = 1; k <= 1000; k++) {
-        const double r = M + k < kBoysRinv ? boys_rinv(M + k) : 1.0 / (pt5 + k);
-        term = term * T * r;
-        sum = sum + term;
-        if (term < 1.0e-12) break;
-      }
-      const double ex = exp(-T);
-      double f = ex * sum;
-      F[M] = (real)f;
-      const double t2 = 2.0 * T;
-      for (int L = M - 1; L >= 0; L--) {
-        f = (f * t2 + ex) * (0.5 * boys_rinv(L));
-        F[L] = (real)f;
-      }
-    }
-  } else {
-    // FP32 (mixed path): same branches, series cut when a term falls below
-    // 1e-8 of the partial sum (the FP32 resolution).
-    const float T = (float)Tr;
-    if (T > 20.0f) {
-      const float rT = 1.0f / T;
-      float f = 0.886226925f / sqrtf(T);
-      F[0] = (real)f;
-      for (int L = 1; L <= M; L++) {
-        f = f * ((float)L - 0.5f) * rT;
-        F[L] = (real)f;
-      }
-    } else {
-      const float pt5 = 0.5f + M;
-      float term = 0.5f / pt5, sum = term;
-      for (int k = 1; k <= 1000; k++) {
-        const float r = M + k < kBoysRinv ? (float)boys_rinv(M + k) : 1.0f / (pt5 + k);
-        term = term * T * r;
-        sum = sum + term;
-        if (term < 1.0e-8f * sum) break;
-      }
-      const float ex = expf(-T);
-      float f = ex * sum;
-      F[M] = (real)f;
-      const float t2 = 2.0f * T;
-      for (int L = M - 1; L >= 0; L--) {
-        f = (f * t2 + ex) * (0.5f * (float)boys_rinv(L));
-        F[L] = (real)f;
-      }
-    }
-  }
-}
 
 // ------------------------------------------------------- Hermite E^{ij}_t
 // out[t], t = 0..i+j (XC1_int_tools.f:136-227 ghec; common.f hecod)
@@ -372,12 +354,13 @@ constexpr int kTetMax = (LTOT + 1) * (LTOT + 2) * (LTOT + 3) / 6;
 
 NX_BIG void rtuv_table(int L, real T, real alpha, const real* R3,
                       real* R /* >= tet_size(L) */) {
-  real F[LTOT + 1], pw[LTOT + 1];
-  boys(L, T, F);
-  const real m2a = -R_(2.0) * alpha;
-  pw[0] = R_(1.0);
+  // seeds R^(j)_000 = (-2 alpha)^j F_j(T) in FP64, narrowed once
+  double F[LTOT + 1], pw[LTOT + 1];
+  boys(L, (double)T, F);
+  const double m2a = -2.0 * (double)alpha;
+  pw[0] = 1.0;
   for (int k = 1; k <= L; k++) pw[k] = pw[k - 1] * m2a;
-  R[0] = pw[L] * F[L];
+  R[0] = (real)(pw[L] * F[L]);
   // In place: layer j is built from layer j+1 by decreasing t+u+v, so every
   // entry read still holds its layer-(j+1) value.
   for (int j = L - 1; j >= 0; j--) {
@@ -394,7 +377,7 @@ NX_BIG void rtuv_table(int L, real T, real alpha, const real* R3,
             r = (v > 1 ? (v - 1) * R[tet(t, u, v - 2)] : R_(0.0)) + R3[2] * R[tet(t, u, v - 1)];
           R[tet(t, u, v)] = r;
         }
-    R[0] = pw[j] * F[j];
+    R[0] = (real)(pw[j] * F[j]);
   }
 }
 
@@ -602,9 +585,9 @@ NX_BIG real g3_coulomb(const G3& s, real C0, real C3, real bf, real bg, real bh,
       const real wd = ((s.pr[0].K[d] * s.pr[1].K[d]) * s.pr[2].K[d]) * s.D[d][0];
       w = d == 0 ? wd : w * wd;
     }
-    real F[1];
-    boys(0, T, F);
-    return C0 * C3 * (w * F[0]);
+    double F[1];
+    boys(0, (double)T, F);
+    return C0 * C3 * (w * (real)F[0]);
   }
   real W[3][LTOT + 1];
   int n[3];
@@ -722,9 +705,9 @@ NX_BIG real g4_coulomb(const G4& s, const GK4& gk, const real* cof,
       w *= s.pr[0].K[d] * s.pr[1].K[d] * s.pr[2].K[d] * s.pr[3].K[d];
     }
     w *= exp(expo);
-    real F[1];
-    boys(0, T, F);
-    return pref * (w * F[0]);
+    double F[1];
+    boys(0, (double)T, F);
+    return pref * (w * (real)F[0]);
   }
   real W[3][LTOT + 1];
   int nmax[3];

@@ -24,7 +24,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 UNITS = ["abi.cu", "abi_fortran.cu", "abi_io.cu", "k_gam4.cu", "k_gam4f.cu", "k_contract.cu",
          "k_md.cu", "k_scf.cu", "k_spin.cu", "k_rx.cu", "k_rxscf.cu", "k_probe.cu",
          "k_noalloc.cu"]
-HEADERS = ["neoxc_internal.h", "md_math.cuh", "md_math32.cuh", "md_math_body.cuh"]
+HEADERS = ["neoxc_internal.h", "md_math.cuh", "md_math32.cuh", "md_math_body.cuh",
+           "boys_table.inc"]
 
 
 def nvcc() -> str:

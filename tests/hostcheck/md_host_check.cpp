@@ -3,6 +3,7 @@
 // algorithm the GPU kernels run can be compared with the CPU oracle on any
 // machine.  Only the tests load this library.
 #include "../../neo-rxchf_gb300/csrc/md_math.cuh"
+#include "../../neo-rxchf_gb300/csrc/md_math32.cuh"
 
 using namespace neoxc::md;
 
@@ -60,5 +61,36 @@ double hc_gfvee(const HP* A1, const HP* A2, const HP* B1, const HP* B2) {
 }
 double hc_gfke(const HP* A, const HP* B, double m) { return gfke(cv(*A), cv(*B), m); }
 double hc_gfvec(const HP* A, const HP* B, const double* C) { return gfvec(cv(*A), cv(*B), C); }
-double hc_boys(int m, double T) { double F[64]; boys(m, T, F); return F[m]; }
+double hc_boys(int m, double T) { double F[64]; neoxc::boys(m, T, F); return F[m]; }
+
+// the FP32 instance (mixed path): same integrals, FP32 tables, FP64 Boys
+static neoxc::md32::Prim cv32(const HP& h) {
+  neoxc::md32::Prim p;
+  p.a = (float)h.a;
+  for (int d = 0; d < 3; d++) { p.l[d] = h.l[d]; p.c[d] = (float)h.c[d]; }
+  return p;
+}
+double hc32_g4(int kind, const HP* A, const HP* B, double g1, double g2) {
+  neoxc::md32::G4 s;
+  neoxc::md32::Prim a[4], b[4];
+  for (int i = 0; i < 4; i++) { a[i] = cv32(A[i]); b[i] = cv32(B[i]); }
+  neoxc::md32::g4_pairs(s, a, b);
+  return kind == 0 ? neoxc::md32::g4_vee(s, (float)g1, (float)g2)
+                   : neoxc::md32::g4_vep(s, (float)g1, (float)g2);
+}
+double hc32_g3(int kind, const HP* A, const HP* B, const double* gam,
+               const double* C, double xmass) {
+  neoxc::md32::Prim a[3], b[3];
+  for (int i = 0; i < 3; i++) { a[i] = cv32(A[i]); b[i] = cv32(B[i]); }
+  float g[6], c[3] = {(float)C[0], (float)C[1], (float)C[2]};
+  for (int k = 0; k < 6; k++) g[k] = (float)gam[k];
+  static thread_local neoxc::md32::G3 s;
+  neoxc::md32::g3_setup(s, a, b, g, kind == 1 ? 2 : 0);
+  switch (kind) {
+    case 0: return neoxc::md32::g3_overlap(s);
+    case 1: return neoxc::md32::g3_ke(s, g[4], (float)xmass);
+    case 2: return neoxc::md32::g3_vxc(s, c);
+    default: return neoxc::md32::g3_vee(s);
+  }
+}
 }

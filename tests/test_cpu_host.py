@@ -188,6 +188,73 @@ def test_md_math_matches_oracle(orc, hostcheck):
         check(H.hc_gfvec(r[0], r[2], O.ptr(Cm)), L.orc_gfvec(r[0], r[2], O.ptr(Cm)), "gfvec")
 
 
+def test_boys_function_matches_xgammaf(orc, hostcheck):
+    """The kernels' FP64 Boys function (pretabulated Taylor expansion for
+    T <= 20, XGAMMAF's asymptotic branch above) against the oracle's
+    restatement of XGAMMAF (common.f:317-348), every order the kernels use.
+    The table is exact to ~1e-15; XGAMMAF's series stops at a 1e-12 term,
+    which leaves up to ~2.4e-12 relative in its values for T <= 20.  Above
+    T = 20 both take XGAMMAF's asymptotic branch."""
+    L, H = orc.lib(), hostcheck
+    H.hc_boys.restype = C.c_double
+    H.hc_boys.argtypes = [C.c_int, C.c_double]
+    rng = np.random.default_rng(5)
+    Ts = np.concatenate([[0.0, 1e-14, 1e-6, 0.03125, 19.97, 20.0, 20.0001, 35.0, 300.0],
+                         rng.uniform(0, 22, 400), np.exp(rng.uniform(-20, 3, 100))])
+    F = np.zeros(17)
+    worst = 0.0
+    for T in Ts:
+        L.orc_xgammaf(orc.ptr(F), float(T), 16)
+        for m in range(17):
+            got = H.hc_boys(m, float(T))
+            worst = max(worst, abs(got - F[m]) / F[m])
+    assert worst < 5e-12, worst
+
+
+def test_md32_instance_within_fp32_error(orc, hostcheck):
+    """The mixed path's FP32 instance (md_math32.cuh: FP32 tables and
+    recursions, FP64 Boys function and seeds) against the oracle's FP64
+    four- and three-particle integrals on random s/p/d primitives: the
+    relative error stays at the FP32 level (bound 2e-4 on significant
+    values, 3e-5 on the median)."""
+    O, L, H = orc, orc.lib(), hostcheck
+    P = C.POINTER(O.Prim)
+    d = C.c_double
+    H.hc32_g4.restype = d
+    H.hc32_g4.argtypes = [C.c_int, P, P, d, d]
+    H.hc32_g3.restype = d
+    H.hc32_g3.argtypes = [C.c_int, P, P, C.c_void_p, C.c_void_p, d]
+    rng = np.random.default_rng(11)
+    AMS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (1, 1, 0), (0, 2, 0),
+           (1, 0, 1), (0, 1, 1), (0, 0, 2)]
+
+    def rp():
+        l = AMS[rng.integers(0, len(AMS))]
+        return O.prim(*l, float(np.exp(rng.uniform(np.log(0.1), np.log(20)))),
+                      *rng.uniform(-1.5, 1.5, 3))
+    errs = []
+    for trial in range(60):
+        A = O.prims([rp() for _ in range(4)])
+        B = O.prims([rp() for _ in range(4)])
+        g1, g2 = np.exp(rng.uniform(np.log(0.5), np.log(20), 2))
+        g = np.zeros(6)
+        g[1], g[5] = g1, g2
+        Cm = rng.uniform(-1.5, 1.5, 3)
+        A3, B3 = O.prims([A[0], A[1], A[2]]), O.prims([B[0], B[1], B[2]])
+        pairs = [(H.hc32_g4(0, A, B, g1, g2), L.orc_g4_xgveeg(A, B, g1, g2)),
+                 (H.hc32_g4(1, A, B, g1, g2), L.orc_g4_xgvepg(A, B, g1, g2)),
+                 (H.hc32_g3(3, A3, B3, O.ptr(g), O.ptr(Cm), 1.0),
+                  L.orc_g3_xgveeg(A3, B3, O.ptr(g))),
+                 (H.hc32_g3(2, A3, B3, O.ptr(g), O.ptr(Cm), 1.0),
+                  L.orc_g3_xgvxcg(A3, B3, O.ptr(g), O.ptr(Cm)))]
+        scale = max(abs(b) for _, b in pairs)
+        for a, b in pairs:
+            if abs(b) > 1e-6 * scale and abs(b) > 1e-30:
+                errs.append(abs(a - b) / abs(b))
+    errs = np.array(errs)
+    assert errs.max() < 2e-4 and np.median(errs) < 3e-5, (errs.max(), np.median(errs))
+
+
 # ------------------------------------------------------- C-ABI library (no GPU)
 def _header_symbols():
     txt = open(os.path.join(ROOT, "include", "neoxc.h")).read()
