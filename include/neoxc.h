@@ -35,6 +35,8 @@ extern "C" {
 #define NEOXC_ERR_NOMEM 3        /* device allocation failed             */
 #define NEOXC_ERR_UNSUPPORTED 4  /* shape outside the supported range    */
 #define NEOXC_ERR_IO 5           /* integral file could not be read      */
+#define NEOXC_ERR_TIMEOUT 6      /* server wait ran out (job still runs) */
+#define NEOXC_ERR_NUMERIC 7      /* non-finite energy or Fock matrix     */
 
 const char* neoxc_last_error(void);
 int neoxc_version(void);
@@ -312,16 +314,18 @@ int neoxc_dev_gam4_dscf(void* stream, int64_t ne, int64_t np,
                         double* d_focke, double* d_fockp, double* d_E_gam4);
 /* No counterpart in the reference.  Same computation as
  * neoxc_dev_gam4_dscf, for callers that cannot allocate device memory
- * (memory handed to their own pool, an SCF loop recorded once and
- * replayed, a fixed memory budget): the call allocates nothing and uses a
- * scratch array built into the library (264,192 doubles per GPU, held until
- * the process exits).  Limit: npbf^2*nebf^3 + npbf^2 <= 264,192 (e.g.
- * nebf=12/npbf=8 or nebf=16/npbf=8); larger systems return
- * NEOXC_ERR_UNSUPPORTED.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  All calls share the one array, so
- * calls whose work overlaps on the GPU (e.g. on two streams at once) race;
- * serialise them on one stream. */
+ * (all of it handed to their own pool allocator, or a strict memory budget
+ * where a transient allocation could fail in the middle of an SCF
+ * iteration): the call allocates nothing and uses a scratch array built
+ * into the library (264,192 doubles per GPU, held until the process exits).
+ * Limit: npbf^2*nebf^3 + npbf^2 <= 264,192 (e.g. nebf=12/npbf=8 or
+ * nebf=16/npbf=8); larger systems return NEOXC_ERR_UNSUPPORTED.  The
+ * stream must belong to the current device (else NEOXC_ERR_ARG).  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the one array, so calls whose
+ * work overlaps on the GPU (e.g. on two streams at once) race; serialise
+ * them on one stream. */
 int neoxc_dev_gam4_dscf_noalloc(void* stream, int64_t ne, int64_t np,
                                 const double* d_GAM_ee,
                                 const double* d_GAM_2s, const double* d_DE,
@@ -414,9 +418,10 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
  * One job = the arguments of neoxc_xchf_scf for one system; the outputs are
  * written into the job.  neoxc_xchf_scf_batch runs the jobs on nworkers
  * host threads, each with its own CUDA stream: a worker takes the next job
- * as soon as it is free, and a job starts only when its device footprint
- * fits in 80 % of the memory free at entry (one at a time if a single job is
- * larger).  Each job's result equals a separate neoxc_xchf_scf call.
+ * as soon as it is free, and a job starts when neoxc_admit (below) starts
+ * it, with the device's free memory re-read at each admission; a job that
+ * can never fit ends with NEOXC_ERR_NOMEM, unstarted, and the others go on.
+ * Each job's result equals a separate neoxc_xchf_scf call.
  * Returns NEOXC_OK, or the first failing job's code (every job's own code is
  * in its status field). */
 typedef struct neoxc_xchf_job {
@@ -446,19 +451,45 @@ int neoxc_xchf_scf_job(neoxc_xchf_job* job, int64_t options, int64_t maxit);
 int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
                          int64_t options, int64_t maxit);
 
+/* Admission by device memory (no reference counterpart), the rule the
+ * batch driver and the server apply each time a job is about to start,
+ * with free_bytes re-read from the device at that moment:
+ *   limit = 0.8 * (free_bytes + in_use_bytes), lowered to cap_bytes if
+ *           cap_bytes > 0 (in_use_bytes: footprints of the jobs running);
+ *   need > limit                                -> NEOXC_ADMIT_REFUSE (the
+ *            job can never fit; it ends with NEOXC_ERR_NOMEM, unstarted);
+ *   in_use + need <= limit, need <= 0.9 free    -> NEOXC_ADMIT_START;
+ *   otherwise                                   -> NEOXC_ADMIT_WAIT (until
+ *            a running job ends).  With nothing running a job never waits.
+ * Pure host arithmetic; negative arguments -> NEOXC_ADMIT_REFUSE. */
+#define NEOXC_ADMIT_START 0
+#define NEOXC_ADMIT_WAIT 1
+#define NEOXC_ADMIT_REFUSE 2
+int neoxc_admit(int64_t need_bytes, int64_t free_bytes, int64_t in_use_bytes,
+                int64_t cap_bytes);
+/* Device bytes one XCHF solve holds at its peak (integral tensors, SCF
+ * state, contraction scratch): the footprint neoxc_admit weighs. */
+int64_t neoxc_xchf_job_bytes(const neoxc_xchf_job* job, int64_t options);
+
 /* ---- serving loop for XCHF solves (no reference counterpart) -------------------
  * Continuous batching: requests are queued with submit (non-blocking) and
  * taken by nworkers threads, each with its own CUDA stream, as soon as a
- * worker is free and the request's device footprint fits in the memory
- * budget (80 % of the memory free at start); a request may arrive while
- * others run and its work overlaps theirs on the GPU.  The job struct and
- * its arrays must stay valid until wait() reports it done; the job's
- * t_submit / t_start / t_end record the request's life.  wait() returns the
- * job's status, or NEOXC_ERR_CUDA with "timeout" after timeout_s seconds
- * (the job keeps running).  stop() drains the queue and joins the workers. */
+ * worker is free and neoxc_admit starts the request (free memory re-read at
+ * each admission; set_budget caps the bytes the server's running jobs may
+ * hold together, 0 = no cap); a request may arrive while others run and its
+ * work overlaps theirs on the GPU.  A request that can never fit ends with
+ * status NEOXC_ERR_NOMEM without starting; one whose energy or Fock matrix
+ * turns non-finite ends with NEOXC_ERR_NUMERIC; one that reaches maxit ends
+ * with status NEOXC_OK and converged = 0.  The job struct and its arrays
+ * must stay valid until wait() reports it done; the job's t_submit /
+ * t_start / t_end record the request's life.  wait() returns the job's
+ * status, or NEOXC_ERR_TIMEOUT after timeout_s seconds (the job stays
+ * queued or running; wait again).  stop() drains the queue and joins the
+ * workers. */
 typedef struct neoxc_xchf_server neoxc_xchf_server;
 neoxc_xchf_server* neoxc_xchf_server_start(int64_t nworkers, int64_t options,
                                            int64_t maxit);
+int neoxc_xchf_server_set_budget(neoxc_xchf_server* srv, int64_t cap_bytes);
 int neoxc_xchf_server_submit(neoxc_xchf_server* srv, neoxc_xchf_job* job);
 int neoxc_xchf_server_wait(neoxc_xchf_server* srv, neoxc_xchf_job* job,
                            double timeout_s);

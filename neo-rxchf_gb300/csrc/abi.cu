@@ -492,9 +492,10 @@ int neoxc_dev_gam4_dscf(void* stream, int64_t ne, int64_t np,
                         const double* d_DE, const double* d_DP,
                         double* d_focke, double* d_fockp, double* d_E) {
   RC(need(ne >= 1 && np >= 1, "sizes"));
-  if (ne > kGam4MaxNE)
-    return set_err(NEOXC_ERR_UNSUPPORTED, "gam_4 element kernels: ne <= %d",
-                   kGam4MaxNE);
+  if (ne > kGam4MaxNE || np > kGam4MaxNP)
+    return set_err(NEOXC_ERR_UNSUPPORTED,
+                   "gam_4 element kernels: ne <= %d, np <= %lld", kGam4MaxNE,
+                   (long long)kGam4MaxNP);
   cudaStream_t s = (cudaStream_t)stream;
   DBuf scr;
   RC(dalloc(scr, sizeof(double) * gam4_partial_doubles((int)ne, (int)np), s));
@@ -1530,9 +1531,12 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
     RC(finish(s));
     for (int k = 0; k < 4; k++)
       if (hs[k] > 40)
-        return set_err(NEOXC_ERR_CUDA,
+        return set_err(hs[k] > 41 ? NEOXC_ERR_NUMERIC : NEOXC_ERR_CUDA,
                        "ROOTHAN: Jacobi eigensolver %s (status slot %d, iteration %lld)",
                        hs[k] > 41 ? "met a NaN" : "did not converge", k, (long long)it);
+    if (!std::isfinite(h[0]))
+      return set_err(NEOXC_ERR_NUMERIC, "XCHF SCF: non-finite total energy at iteration %lld",
+                     (long long)it);
     if (history) {
       history[4 * (it - 1) + 0] = h[0];
       history[4 * (it - 1) + 1] = h[0] - Eold;
@@ -1609,12 +1613,47 @@ static size_t xchf_job_bytes(const neoxc_xchf_job& j, int64_t options) {
   return sizeof(double) * d + (1u << 20);
 }
 
+int neoxc_admit(int64_t need_b, int64_t free_b, int64_t in_use, int64_t cap) {
+  if (need_b < 0 || free_b < 0 || in_use < 0 || cap < 0) return NEOXC_ADMIT_REFUSE;
+  double limit = 0.8 * ((double)free_b + (double)in_use);
+  if (cap > 0 && (double)cap < limit) limit = (double)cap;
+  if ((double)need_b > limit) return NEOXC_ADMIT_REFUSE;
+  if ((double)in_use + (double)need_b <= limit && (double)need_b <= 0.9 * (double)free_b)
+    return NEOXC_ADMIT_START;
+  return NEOXC_ADMIT_WAIT;
+}
+
+int64_t neoxc_xchf_job_bytes(const neoxc_xchf_job* j, int64_t options) {
+  if (!j || j->nebf < 1 || j->npbf < 1 || j->nebf > kScfMaxN || j->npbf > kScfMaxN) return -1;
+  return (int64_t)xchf_job_bytes(*j, options);
+}
+
+// One admission decision for a job of need_b bytes: re-reads the device's
+// free memory each time and waits (on cv, woken when a job ends, or every
+// 50 ms) while neoxc_admit says wait.  Called with mu held by lk; returns
+// NEOXC_ADMIT_START (in_use and running updated) or NEOXC_ADMIT_REFUSE.
+static int admit_job(std::unique_lock<std::mutex>& lk, std::condition_variable& cv,
+                     size_t need_b, size_t& in_use, int& running, int64_t cap) {
+  for (;;) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+    const int d = neoxc_admit((int64_t)need_b, (int64_t)free_b, (int64_t)in_use, cap);
+    if (d == NEOXC_ADMIT_REFUSE) return d;
+    if (d == NEOXC_ADMIT_START) {
+      in_use += need_b;
+      running++;
+      return d;
+    }
+    cv.wait_for(lk, std::chrono::milliseconds(50));
+  }
+}
+
 // Independent XCHF solves (geometry or proton-position scans, many small
 // molecules) on nworkers host threads, each with its own CUDA stream.  Jobs
-// are taken in order as workers free up, and a job starts only when its
-// device footprint fits in 80 % of the memory free at entry (one job at a
-// time if a single job exceeds that).  Every job gives the same result as a
-// separate neoxc_xchf_scf call (same kernels, same order on its stream).
+// are taken in order as workers free up and admitted by neoxc_admit against
+// the memory free at that moment; a job that can never fit is refused with
+// NEOXC_ERR_NOMEM.  Every job gives the same result as a separate
+// neoxc_xchf_scf call (same kernels, same order on its stream).
 int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
                          int64_t options, int64_t maxit) {
   RC(need(jobs != nullptr && njobs >= 0 && nworkers >= 1, "jobs, njobs, nworkers"));
@@ -1623,9 +1662,6 @@ int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
   RC(get_stream(&s0));   // checks the device and fixes it for the workers
   int dev = 0;
   CU(cudaGetDevice(&dev));
-  size_t free_b = 0, total_b = 0;
-  CU(cudaMemGetInfo(&free_b, &total_b));
-  const size_t budget = (size_t)(0.8 * (double)free_b);
   std::mutex mu;
   std::condition_variable cv;
   size_t in_use = 0;
@@ -1648,11 +1684,14 @@ int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
           continue;
         }
         const size_t need_b = xchf_job_bytes(j, options);
+        int decision;
         {
           std::unique_lock<std::mutex> lk(mu);
-          cv.wait(lk, [&] { return running == 0 || in_use + need_b <= budget; });
-          in_use += need_b;
-          running++;
+          decision = admit_job(lk, cv, need_b, in_use, running, 0);
+        }
+        if (decision == NEOXC_ADMIT_REFUSE) {
+          j.status = NEOXC_ERR_NOMEM;
+          continue;
         }
         j.status = xchf_scf_on(st, j.nelec, j.nucst, j.nebf, j.npebf, j.npbf, j.nat,
                                j.ngtg1, j.pmass, j.cat, j.zan, j.bcoef1, j.gamma1,
@@ -1689,7 +1728,8 @@ int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
 struct neoxc_xchf_server {
   int dev = 0;
   int64_t options = 0, maxit = 100;
-  size_t budget = 0, in_use = 0;
+  int64_t cap = 0;   // neoxc_xchf_server_set_budget (0 = none)
+  size_t in_use = 0;
   int running = 0;
   bool stopping = false;
   std::mutex mu;
@@ -1717,11 +1757,19 @@ static void server_worker(neoxc_xchf_server* S) {
       S->queue.pop_front();
     }
     const size_t need_b = xchf_job_bytes(*j, S->options);
+    int decision;
     {
       std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_mem.wait(lk, [&] { return S->running == 0 || S->in_use + need_b <= S->budget; });
-      S->in_use += need_b;
-      S->running++;
+      decision = admit_job(lk, S->cv_mem, need_b, S->in_use, S->running, S->cap);
+      if (decision == NEOXC_ADMIT_REFUSE) {
+        j->status = NEOXC_ERR_NOMEM;
+        j->t_start = j->t_end = S->now();
+        j->reserved = 1;
+      }
+    }
+    if (decision == NEOXC_ADMIT_REFUSE) {
+      S->cv_done.notify_all();
+      continue;
     }
     j->t_start = S->now();
     j->status = ok ? xchf_scf_on(st, j->nelec, j->nucst, j->nebf, j->npebf, j->npbf,
@@ -1761,14 +1809,21 @@ neoxc_xchf_server* neoxc_xchf_server_start(int64_t nworkers, int64_t options,
   if (get_stream(&s0) != NEOXC_OK) return nullptr;
   auto* S = new neoxc_xchf_server();
   cudaGetDevice(&S->dev);
-  size_t free_b = 0, total_b = 0;
-  cudaMemGetInfo(&free_b, &total_b);
-  S->budget = (size_t)(0.8 * (double)free_b);
   S->options = options;
   S->maxit = maxit;
   S->t0 = std::chrono::steady_clock::now();
   for (int64_t w = 0; w < nworkers; w++) S->workers.emplace_back(server_worker, S);
   return S;
+}
+
+int neoxc_xchf_server_set_budget(neoxc_xchf_server* S, int64_t cap_bytes) {
+  RC(need(S != nullptr && cap_bytes >= 0, "server, cap_bytes >= 0"));
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->cap = cap_bytes;
+  }
+  S->cv_mem.notify_all();
+  return NEOXC_OK;
 }
 
 int neoxc_xchf_server_submit(neoxc_xchf_server* S, neoxc_xchf_job* job) {
@@ -1791,7 +1846,7 @@ int neoxc_xchf_server_wait(neoxc_xchf_server* S, neoxc_xchf_job* job,
   std::unique_lock<std::mutex> lk(S->mu);
   const bool done = S->cv_done.wait_for(
       lk, std::chrono::duration<double>(timeout_s), [&] { return job->reserved == 1; });
-  if (!done) return set_err(NEOXC_ERR_CUDA, "server wait: timeout");
+  if (!done) return set_err(NEOXC_ERR_TIMEOUT, "server wait: timeout after %g s", timeout_s);
   return job->status;
 }
 

@@ -4,13 +4,14 @@
 // The regular device entry point (neoxc_dev_gam4_dscf) obtains its scratch
 // buffer -- one partial Fock row per CTA plus one partial per proton pair --
 // from cudaMallocAsync on every call.  Some callers cannot allow that: a
-// host code that has handed all device memory to its own pool allocator,
-// an SCF loop recorded once and replayed where any allocation would break
-// the recording, or a caller that runs inside a strict memory budget where
-// a transient allocation can fail at the worst moment.  This variant keeps
-// its scratch in a fixed array compiled into the library instead, so a
-// call allocates nothing: the caller passes the inputs and outputs and the
-// library uses only memory that exists from load time.
+// host code that has handed all device memory to its own pool allocator
+// (a Fortran SCF driver sharing the GPU with a memory-hungry integral
+// phase), or one that runs inside a strict memory budget where a transient
+// allocation can fail at the worst moment, in the middle of an SCF
+// iteration.  This variant keeps its scratch in a fixed array compiled into
+// the library instead, so a call allocates nothing: the caller passes the
+// inputs and outputs and the library uses only memory that exists from load
+// time.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,8 +36,10 @@ double* g_scratch_addr[64] = {nullptr};
 
 // Device address of the scratch array on the current device.  The array's
 // name is only a host-side handle, so its device address is looked up once
-// per device (with that device current) and cached.
-int scratch_on_current_device(double** out) {
+// per device (with that device current) and cached.  The stream must belong
+// to the current device: the address is that device's copy, and kernels on
+// another device's stream would write that other GPU's array.
+int scratch_on_current_device(cudaStream_t stream, double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess)
@@ -44,6 +47,15 @@ int scratch_on_current_device(double** out) {
                           cudaGetErrorString(e));
   if (dev < 0 || dev >= 64)
     return set_last_error(NEOXC_ERR_CUDA, "device id %d out of range", dev);
+  int sdev = dev;
+  e = cudaStreamGetDevice(stream, &sdev);
+  if (e != cudaSuccess)
+    return set_last_error(NEOXC_ERR_ARG, "stream: %s", cudaGetErrorString(e));
+  if (sdev != dev)
+    return set_last_error(NEOXC_ERR_ARG,
+                          "neoxc_dev_gam4_dscf_noalloc: the stream belongs to "
+                          "device %d but device %d is current; make the "
+                          "stream's device current", sdev, dev);
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
@@ -72,9 +84,10 @@ extern "C" int neoxc_dev_gam4_dscf_noalloc(void* stream, int64_t ne,
   if (ne < 1 || np < 1 || !d_gee || !d_g2s || !d_DE || !d_DP || !d_focke ||
       !d_fockp || !d_E)
     return set_last_error(NEOXC_ERR_ARG, "argument check failed: sizes/pointers");
-  if (ne > kGam4MaxNE)
+  if (ne > kGam4MaxNE || np > kGam4MaxNP)
     return set_last_error(NEOXC_ERR_UNSUPPORTED,
-                          "gam_4 element kernels: ne <= %d", kGam4MaxNE);
+                          "gam_4 element kernels: ne <= %d, np <= %lld",
+                          kGam4MaxNE, (long long)kGam4MaxNP);
   const size_t need = gam4_partial_doubles((int)ne, (int)np);
   if (need > kNoAllocScratchDoubles)
     return set_last_error(
@@ -84,7 +97,7 @@ extern "C" int neoxc_dev_gam4_dscf_noalloc(void* stream, int64_t ne,
         "must not exceed it); use neoxc_dev_gam4_dscf for larger systems",
         (long long)ne, (long long)np, need, kNoAllocScratchDoubles);
   double* scratch = nullptr;
-  int rc = scratch_on_current_device(&scratch);
+  int rc = scratch_on_current_device((cudaStream_t)stream, &scratch);
   if (rc) return rc;
   // Every scratch element the kernels read is written earlier in the same
   // call, so nothing needs clearing between calls.

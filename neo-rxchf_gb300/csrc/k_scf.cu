@@ -645,20 +645,27 @@ __global__ void roothan_kernel(int n, const double* __restrict__ F,
   }
   __syncthreads();
   const int sw = jacobi_eig(n, m.A, m.V, m.rc, m.rs, m.rp, m.rq, m.sw);
-  // ascending order: rank of each eigenvalue (ties by index)
+  // ascending order: rank of each eigenvalue (ties by index).  The order is
+  // total even for NaN eigenvalues (a NaN Fock matrix, reported through
+  // status): NaNs sort last, among themselves by index, so the ranks are a
+  // permutation and every rank slot is written.
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double w = m.A[i * n + i];
+    const bool wn = isnan(w);
     int r = 0;
     for (int j = 0; j < n; j++) {
       const double v = m.A[j * n + j];
-      r += (v < w) || (v == w && j < i);
+      const bool vn = isnan(v);
+      r += (vn || wn) ? ((!vn && wn) || (vn && wn && j < i))
+                      : ((v < w) || (v == w && j < i));
     }
-    m.rank[r] = i;   // rank -> eigen index
+    m.rank[r < n ? r : n - 1] = i;   // rank -> eigen index
   }
   __syncthreads();
   // C = X V in sorted order (T reused, row-major T[i][k])
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    const int i = e / n, k = e - i * n, col = m.rank[k];
+    const int i = e / n, k = e - i * n;
+    const int col = min(max(m.rank[k], 0), n - 1);
     double acc = 0.0;
     for (int l = 0; l < n; l++) acc += X[i + n * l] * m.V[l * n + col];
     m.T[e] = acc;
@@ -672,7 +679,8 @@ __global__ void roothan_kernel(int n, const double* __restrict__ F,
     if (Cout) Cout[i + n * j] = m.T[e];
   }
   if (evals)
-    for (int k = threadIdx.x; k < n; k += blockDim.x) evals[k] = m.A[m.rank[k] * (n + 1)];
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+      evals[k] = m.A[min(max(m.rank[k], 0), n - 1) * (n + 1)];
   if (threadIdx.x == 0) status[0] = sw;
 }
 

@@ -99,6 +99,7 @@ cudaError_t launch_rx(RxRoutine r, int ne, int np, const double* T1, const doubl
 
 // ---- gam_4 (gam_4_OMP.f, gam4_DSCF_OMP.f, gam4_ICR_OMP.f) --------------
 constexpr int kGam4MaxNE = 24;   // shared-memory tables: 25*ne^2 doubles
+constexpr int64_t kGam4MaxNP = 4096;   // npbf bound checked before any int cast
 size_t gam4_partial_doubles(int ne, int np);   // scratch the DSCF path uses
 cudaError_t launch_gam4_dscf(int ne, int np, const double* gee,
                              const double* g2s, const double* DE,

@@ -111,6 +111,9 @@ def _declare(L):
         "neoxc_xchf_scf_batch": (I, [vp, i64, i64, i64, i64]),
         "neoxc_xchf_server_start": (vp, [i64, i64, i64]),
         "neoxc_xchf_server_submit": (I, [vp, vp]),
+        "neoxc_xchf_server_set_budget": (I, [vp, i64]),
+        "neoxc_admit": (I, [i64, i64, i64, i64]),
+        "neoxc_xchf_job_bytes": (i64, [vp, i64]),
         "neoxc_xchf_server_wait": (I, [vp, vp, d]),
         "neoxc_xchf_server_stop": (I, [vp]),
         "neoxc_dev_gam4_fock_factored": (I, [vp, i64, i64] + [vp] * 7),
@@ -158,6 +161,10 @@ def lib(build_if_missing: bool = False):
             _declare(L)
             _lib = L
     return _lib
+
+
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED, ERR_IO, ERR_TIMEOUT, ERR_NUMERIC = 1, 2, 3, 4, 5, 6, 7
+ADMIT_START, ADMIT_WAIT, ADMIT_REFUSE = 0, 1, 2
 
 
 def _check(rc: int):
@@ -596,16 +603,30 @@ class XchfServer:
         if not self._h:
             raise NeoxcError(lib().neoxc_last_error().decode())
 
+    def set_budget(self, cap_bytes: int):
+        """Cap the device bytes the server's running jobs may hold together
+        (0 = no cap beyond the free-memory rule of neoxc_admit)."""
+        _check(lib().neoxc_xchf_server_set_budget(self._h, int(cap_bytes)))
+
     def submit(self, s: NeoSystem, DE, DP=None):
         job = XchfJob()
         bufs = _fill_job(job, s, DE, None if self.guess_prot else DP, self.maxit)
         _check(lib().neoxc_xchf_server_submit(self._h, C.byref(job)))
         return (job, bufs)
 
-    def wait(self, ticket, timeout: float = 600.0):
+    def wait(self, ticket, timeout: float = 600.0, raise_on_error: bool = True):
+        """The result dict once the request is done.  raise_on_error=False
+        returns the dict with its "status" (NEOXC_ERR_NOMEM: refused,
+        NEOXC_ERR_NUMERIC: non-finite energy) instead of raising; a timeout
+        (NEOXC_ERR_TIMEOUT) always raises, and the request stays queued or
+        running."""
         job, bufs = ticket
-        _check(lib().neoxc_xchf_server_wait(self._h, C.byref(job), timeout))
-        return _job_result(job, bufs)
+        rc = lib().neoxc_xchf_server_wait(self._h, C.byref(job), timeout)
+        if rc == ERR_TIMEOUT or (rc != 0 and raise_on_error):
+            _check(rc)
+        r = _job_result(job, bufs)
+        r["status"] = int(job.status)
+        return r
 
     def stop(self):
         if self._h:

@@ -1,8 +1,9 @@
 """Generate the golden fixtures of the parity tests from the reference tree.
 
-Run in a container where the reference is mounted (it reads files only):
+Run where the reference tree is available (it reads files only), giving
+the tree's root as the one required argument:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path-to-NEO-RXCHF>
 
 Writes, next to this script:
   xchf_example.json   examples/xchf: input deck, initial MO guess
@@ -263,4 +264,6 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path-to-NEO-RXCHF>")
+    main(sys.argv[1])

@@ -321,6 +321,40 @@ def test_proton_scan_moves_only_the_proton_basis():
         assert np.array_equal(t.ELCBFC, s.ELCBFC) and np.array_equal(t.cat, s.cat)
 
 
+def test_admission_rule():
+    """neoxc_admit, the memory-admission rule of the batch driver and the
+    server: limit = 0.8 (free + in_use), lowered to the cap; a job above the
+    limit is refused, one that fits starts, anything else waits; with
+    nothing running a job never waits (no deadlock)."""
+    import neoxc
+    L = neoxc.lib(build_if_missing=True)
+    S, W, R = neoxc.ADMIT_START, neoxc.ADMIT_WAIT, neoxc.ADMIT_REFUSE
+    assert L.neoxc_admit(10, 100, 0, 0) == S
+    assert L.neoxc_admit(90, 100, 0, 0) == R          # > 0.8 of everything
+    assert L.neoxc_admit(30, 50, 50, 0) == S          # 50 + 30 <= 0.8 * 100
+    assert L.neoxc_admit(40, 50, 50, 0) == W          # fits once a job ends
+    assert L.neoxc_admit(10, 10 ** 12, 0, 5) == R     # above the cap
+    assert L.neoxc_admit(10, 10 ** 12, 10, 15) == W   # cap shared with running jobs
+    assert L.neoxc_admit(-1, 100, 0, 0) == R
+    rng = np.random.default_rng(3)
+    for need, free in rng.integers(0, 10 ** 11, size=(200, 2)):
+        assert L.neoxc_admit(int(need), int(free), 0, 0) in (S, R)
+
+
+def test_job_footprint_counts_the_tensors():
+    """neoxc_xchf_job_bytes: the footprint neoxc_admit weighs holds at least
+    the stored gam_2 and gam_3 tensors of the job's system."""
+    import neoxc
+    from neoxc import basis
+    L = neoxc.lib(build_if_missing=True)
+    s = basis.synthetic(seed=1, nebf=12, npbf=8)
+    job = neoxc.XchfJob()
+    keep = neoxc._fill_job(job, s, np.eye(12), None, 5)
+    b = L.neoxc_xchf_job_bytes(C.byref(job), 0)
+    assert b >= 8 * (2 * s.ng2 + s.ng3)
+    assert keep["ne"] == 12
+
+
 def test_argument_checks_need_no_gpu():
     """Size validation happens on the host before any device work, and a
     shape outside the supported range is an error, never a CPU fallback."""
@@ -337,6 +371,11 @@ def test_argument_checks_need_no_gpu():
     assert L.neoxc_index_map(7, 2, 2, 4, p) == 1
     # host index maps are plain arithmetic
     assert L.neoxc_index_gam_2pk(3, 2, 2, 2, 3, 3, 3, 3) == 3 ** 4 * 4
+    # an npbf beyond int range is refused before any narrowing (2^32 + 2
+    # would otherwise wrap to 2), by both gam_4 device entry points
+    for fn in (L.neoxc_dev_gam4_dscf, L.neoxc_dev_gam4_dscf_noalloc):
+        assert fn(None, 12, 2 ** 32 + 2, *([p] * 7)) == 4
+        assert b"np <=" in L.neoxc_last_error()
     # no device here: compute calls report a CUDA error instead of running
     if not L.neoxc_device_ok():
         assert b"CUDA" in L.neoxc_last_error() or b"device" in L.neoxc_last_error()

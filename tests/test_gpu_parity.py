@@ -295,7 +295,13 @@ def test_rxchfne_gam2_ic1(nx, orc, kw):
     assert_close_scaled(gx, T.get("rx2ex"), RTOL, "GM2exICR")
 
 
-@pytest.mark.parametrize("kw", SMALL[:2])
+# gam_3 cases: the s/p systems above and one with an electronic d shell
+# (nebf=5 cycles s, px, py, pz, dxx; the oracle needs ~10 s of CPU for it)
+GAM3_CASES = SMALL[:2] + [dict(seed=105, nat=2, nebf=5, nprim=1, npbf=1, ngtg=2,
+                               lmax_e=2, lmax_p=0)]
+
+
+@pytest.mark.parametrize("kw", GAM3_CASES)
 def test_gam3_ic1(nx, orc, kw):
     s = _system(**kw)
     T = OracleTensors(orc, s)

@@ -163,6 +163,42 @@ def test_server_requests_match_separate_solves(nx, xchf):
         assert r["t_submit"] <= r["t_start"] <= r["t_end"]
 
 
+def test_server_failure_modes(nx, xchf):
+    """Failures made on the host, reported per request while the other
+    requests go on: a request whose start density holds a NaN ends with
+    NEOXC_ERR_NUMERIC; with the server's budget capped below a request's
+    footprint the request is refused with NEOXC_ERR_NOMEM without starting;
+    a wait that runs out returns NEOXC_ERR_TIMEOUT and the request still
+    completes; a request that reaches maxit ends with status 0 and
+    converged = False."""
+    DE0 = xchf["DE0"]
+    bad = np.array(DE0, copy=True)
+    bad[1, 2] = np.nan
+    srv = nx.XchfServer(nworkers=1, diis=True, mixed=False)
+    try:
+        t_ok = srv.submit(xchf["sys"], DE0)
+        with pytest.raises(nx.NeoxcError, match="error 6"):
+            srv.wait(t_ok, timeout=0.0)          # still queued or running
+        r_ok = srv.wait(t_ok)
+        assert r_ok["status"] == 0 and r_ok["converged"]
+        r_nan = srv.wait(srv.submit(xchf["sys"], bad), raise_on_error=False)
+        assert r_nan["status"] == nx.ERR_NUMERIC
+        srv.set_budget(1 << 20)                  # 1 MiB: below any XCHF footprint
+        r_big = srv.wait(srv.submit(xchf["sys"], DE0), raise_on_error=False)
+        assert r_big["status"] == nx.ERR_NOMEM and r_big["t_start"] == r_big["t_end"]
+        srv.set_budget(0)
+        r_again = srv.wait(srv.submit(xchf["sys"], DE0))
+        assert r_again["final"]["E_total"] == r_ok["final"]["E_total"]
+    finally:
+        srv.stop()
+    srv = nx.XchfServer(nworkers=1, maxit=2, diis=False, mixed=False)
+    try:
+        r = srv.wait(srv.submit(xchf["sys"], DE0))
+    finally:
+        srv.stop()
+    assert r["status"] == 0 and not r["converged"] and r["niter"] == 2
+
+
 def test_xchf_scf_job_returns_final_mos(nx, xchf, xchf_gpu_scf, tmp_path):
     """neoxc_xchf_scf_job: the same solve as neoxc_xchf_scf plus the final
     MOs and orbital energies.  C^T S C = 1; the occupied MOs rebuild the

@@ -1,8 +1,9 @@
 """The allocation-free gam_4 direct-SCF entry point.
 
 neoxc_dev_gam4_dscf_noalloc serves callers that cannot allocate device
-memory during a Fock build (memory handed to their own pool, a recorded and
-replayed SCF loop, a fixed memory budget).  It keeps its scratch in an array
+memory during a Fock build (all of it handed to their own pool allocator, or
+a strict memory budget where a transient allocation could fail in the middle
+of an SCF iteration).  It keeps its scratch in an array
 built into the library; these tests call it through the C-ABI twice in a
 row with different inputs and compare each result with the allocating entry
 point neoxc_dev_gam4_dscf, and check that a system too large for the
