@@ -401,6 +401,10 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
 #define NEOXC_SCF_GUESS_ELEC 32    /* DE (XCHF: guess_elec, xcscf.f:660) or
                                       DAE, DBE (XCUHF: guess_A_elec) from the
                                       electronic core Hamiltonian */
+#define NEOXC_SCF_SCREEN 64        /* skip gam_3 (bra, ket) primitive pairs
+                                      whose Schwarz-type estimate is below
+                                      1e-12 (new; the reference evaluates
+                                      every tuple) */
 int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t npbf, int64_t nat, int64_t ngtg1, double pmass,
                    const double* cat, const double* zan, const double* bcoef1,

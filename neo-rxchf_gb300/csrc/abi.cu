@@ -140,7 +140,7 @@ int need(bool ok, const char* what) {
 // ---- basis staging for the MD builders ------------------------------------
 struct SysUpload {
   DevSystem d{};
-  DBuf eprim, pprim, kps, kpe, zan, cat, bgem, ggem;
+  DBuf eprim, pprim, kps, kpe, zan, cat, bgem, ggem, g3i, g3rec;
 };
 
 int stage_system(SysUpload& u, cudaStream_t s, int64_t nebf, int64_t npebf,
@@ -224,6 +224,69 @@ int stage_system(SysUpload& u, cudaStream_t s, int64_t nebf, int64_t npebf,
   u.d.cat = u.cat.as<double>();
   u.d.bgem = u.bgem.as<double>();
   u.d.ggem = u.ggem.as<double>();
+  int le = 0, lp = 0;
+  for (const DevPrim& q : ep) le = std::max(le, q.l[0] + q.l[1] + q.l[2]);
+  for (const DevPrim& q : pp) lp = std::max(lp, q.l[0] + q.l[1] + q.l[2]);
+  u.d.lmax_e = le;
+  u.d.lmax_p = lp;
+  // gam_3 pair tables (k_gam3.cu): the primitive pairs of every canonical
+  // contracted pair (i >= j, P = i(i+1)/2 + j) in P order, tiles of whole
+  // pairs with at most kG3MaxTileKets kets, and within a tile the kets
+  // ordered by angular class (so the lanes of a warp take alike kets)
+  {
+    const int ne = (int)nebf;
+    const int nPe = ne * (ne + 1) / 2;
+    std::vector<int> ab, kofs(nPe + 1, 0), tk, tp, perm, cls;
+    for (int i = 0; i < ne; i++)
+      for (int j = 0; j <= i; j++) {
+        const int P = i * (i + 1) / 2 + j;
+        kofs[P] = (int)ab.size() / 2;
+        for (int a = ks[i]; a <= ke[i]; a++)
+          for (int b = ks[j]; b <= ke[j]; b++) {
+            ab.push_back(a);
+            ab.push_back(b);
+            int key = 0;
+            for (int d = 0; d < 3; d++) key = key * 8 + ep[a].l[d] + ep[b].l[d];
+            cls.push_back(key);
+          }
+      }
+    const int nket = (int)ab.size() / 2;
+    kofs[nPe] = nket;
+    bool ok = true;
+    tk.push_back(0);
+    tp.push_back(0);
+    for (int P = 0; P < nPe; P++) {
+      if (kofs[P + 1] - kofs[P] > kG3MaxTileKets) ok = false;
+      if (kofs[P + 1] - tk.back() > kG3MaxTileKets) {
+        tk.push_back(kofs[P]);
+        tp.push_back(P);
+      }
+    }
+    tk.push_back(nket);
+    tp.push_back(nPe);
+    const int ntile = (int)tk.size() - 1;
+    perm.resize(nket);
+    for (int t = 0; t < ntile; t++) {
+      std::vector<int> idx;
+      for (int k = tk[t]; k < tk[t + 1]; k++) idx.push_back(k);
+      std::stable_sort(idx.begin(), idx.end(),
+                       [&](int x, int y) { return cls[x] < cls[y]; });
+      for (size_t q = 0; q < idx.size(); q++) perm[tk[t] + q] = idx[q];
+    }
+    std::vector<int> g3i;
+    g3i.insert(g3i.end(), ab.begin(), ab.end());
+    g3i.insert(g3i.end(), kofs.begin(), kofs.end());
+    g3i.insert(g3i.end(), tk.begin(), tk.end());
+    g3i.insert(g3i.end(), tp.begin(), tp.end());
+    g3i.insert(g3i.end(), perm.begin(), perm.end());
+    RC(upload(u.g3i, g3i.data(), sizeof(int) * g3i.size(), s));
+    u.d.g3_nket = nket;
+    u.d.g3_ntile = ok ? ntile : 0;
+    u.d.g3i = u.g3i.as<int>();
+    RC(dalloc(u.g3rec, sizeof(double) * g3_record_doubles(nket, (int)npbf), s));
+    u.d.g3rec = u.g3rec.as<double>();
+    CU(launch_g3_records(u.d, const_cast<double*>(u.d.g3rec), s));
+  }
   return NEOXC_OK;
 }
 
@@ -855,6 +918,7 @@ static int gam3_dscf_dev(const SysUpload& u, cudaStream_t s, const double* dde,
   RC(dalloc(part, sizeof(double) * eg3_partial_doubles(ne, np), s));
   RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
   CU(launch_gam3_aux(u.d, aux.as<double>(), s));
+  CU(launch_gam3_pairs(u.d, aux.as<double>(), s, 0, 0.0));
   for (int64_t pp = 0; pp < (int64_t)np * np; pp++) {
     CU(launch_gam3_raw_range(u.d, aux.as<double>(), pp * n6, n6,
                              slice.as<double>(), s));
@@ -1363,7 +1427,8 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
   RC(need(DE && DP && E_init && E_final && niter && converged, "pointers"));
   RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_DIIS |
                                 NEOXC_SCF_GAM4_ELEMENT | NEOXC_SCF_MIXED |
-                                NEOXC_SCF_MIXED_GAM2 | NEOXC_SCF_GUESS_ELEC)) == 0,
+                                NEOXC_SCF_MIXED_GAM2 | NEOXC_SCF_GUESS_ELEC |
+                                NEOXC_SCF_SCREEN)) == 0,
           "options"));
   const int mixed = (options & NEOXC_SCF_MIXED) ? 1 : 0;
   const int mixed_gam2 = (options & NEOXC_SCF_MIXED_GAM2) ? 1 : 0;
@@ -1410,7 +1475,8 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
     RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
     // GAM_ee and the core Hamiltonian (Hce, pack_2D order) are already built
     CU(launch_gam3_aux(u.d, aux.as<double>(), s, Gee.as<double>(), Hce.as<double>()));
-    CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed));
+    CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed,
+                       (options & NEOXC_SCF_SCREEN) ? kScreenThreshold : 0.0));
     CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
   }
   // SCF state
@@ -2412,7 +2478,8 @@ int xcuhf_scf_on(cudaStream_t s, int64_t nelec, int64_t NAE, int64_t NBE, int64_
     DBuf aux;
     RC(dalloc(aux, sizeof(double) * gam3_aux_doubles(ne, np), s));
     CU(launch_gam3_aux(u.d, aux.as<double>(), s, Gee.as<double>(), Hce.as<double>()));
-    CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed));
+    CU(launch_gam3_raw(u.d, aux.as<double>(), G3.as<double>(), s, mixed,
+                       (options & NEOXC_SCF_SCREEN) ? kScreenThreshold : 0.0));
     CU(launch_gam3_symmetrize(ne, np, G3.as<double>(), s));
   }
   if (nelec > 3)

@@ -9,8 +9,9 @@
 //   rxchfne/rxchfne_gam2_IC1_OMP.f:245-340       -> gam2_raw_kernel<RX, F32>
 //   gam2_IC1_OMP.f:136-185, rxchfne_gam2_IC1_OMP.f:184-201
 //                                                -> gam2_sym_kernel
-//   gam_3_OMP.f:617-984 (xcalc_GAM3_MD),
-//   gam3_CONV_OMP.f:479-705, gam3_IC1_OMP.f:299-431 -> gam3_raw_kernel
+//   gam_3_OMP.f:617-984 (xcalc_GAM3_MD) separable terms
+//                                                -> gam3_w1/w3/hcore_kernel
+//     (the four-particle terms: k_gam3.cu)
 //   gam3_IC1_OMP.f:143-262                       -> gam3_sym_kernel
 //
 // Work decomposition: one warp per contracted tuple (its packed index is
@@ -190,39 +191,6 @@ __device__ void xcalc_gam2_rx_item(const Prim* A, const Prim* B, const DevSystem
   double xgVEEg2 = md::underflow(md::g3_vee(st));
   ansE1 = bb * xgVEPg2 + bb * xgVEEg1;
   ansE2 = bb * xgVEEg2;
-}
-
-// gam_3_OMP.f:617-984 xcalc_GAM3_MD, particles (e1, e2, e3, p):
-//   ans = gVEE + gHEg + gVEEg1/2 + 2 gVEEg2 (:964) with
-//   gVEE   = sum_k b_k G2xggs(e1,p; g_k, 0) (e2 e2'|e3 e3')            (:720-753)
-//   gHEg   = sum_kl b_k b_l [h(e3) G3xggs(e1,e2,p; g_k, g_l) - G4Vep]    (:760-872)
-//   gVEEg1 = sum_kl b_k b_l G2xggs(e1,p; g_k, g_l) (e2 e2'|e3 e3')      (:877-902)
-//   gVEEg2 = sum_kl b_k b_l G4Vee                                      (:907-930)
-// with h(e3) the electronic core Hamiltonian.  Three of the terms are
-// products of factors on disjoint particles, so their contracted sums are
-// built once as small tensors (W1(p,e1) x GAM_ee(e2,e3) and
-// W3(p,e1,e2) x Hcore(e3), gam3_aux) instead of per primitive 8-tuple; the
-// primitive loop keeps only the four-particle Coulomb integrals:
-//   g4part = sum_kl b_k b_l (2 G4Vee - G4Vep).
-template <class G4T, class P>
-__device__ double gam3_g4part(const P* A, const P* B, const DevSystem& S,
-                              G4T& s4) {
-  using R = typename std::remove_cv<decltype(P::a)>::type;
-  const int ng = S.ngtg;
-  const double* b = S.bgem;
-  const double* gm = S.ggem;
-  g4_pairs(s4, A, B);
-  double zsum = 0.0, vsum = 0.0;
-  for (int ik = 0; ik < ng; ik++)
-    for (int il = 0; il < ng; il++) {
-      const R gk = (R)gm[ik], gl = (R)gm[il];
-      const double bb = b[ik] * b[il];
-      const double zz = md::underflow((double)g4_vep(s4, gk, gl));
-      const double vv = (double)g4_vee(s4, gk, gl);
-      zsum = zsum + bb * zz;
-      vsum = vsum + bb * vv;
-    }
-  return 2.0 * vsum - zsum;
 }
 
 __device__ __forceinline__ md32::Prim to_prim32(const DevPrim& d) {
@@ -464,76 +432,6 @@ __global__ void gam3_hcore_kernel(DevSystem S, double* __restrict__ Hc) {
   Hc[t] = h;
 }
 
-// ---- gam_3 raw tensor: warp per contracted tuple ----------------------------
-template <bool F32>
-__global__ void __launch_bounds__(64, F32 ? 16 : 8)
-gam3_raw_kernel(DevSystem S, const double* __restrict__ aux,
-                double* __restrict__ x3, long long t0, long long ntup) {
-  const int ne = S.nebf, np = S.npbf;
-  const int lane = threadIdx.x & 31;
-  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  if (w >= ntup) return;
-  long long r = w + t0;   // packed index - 1 of the tuple; outputs from t0
-  int c[6];
-  for (int k = 5; k >= 0; k--) {
-    c[k] = (int)(r % ne);
-    r /= ne;
-  }
-  const int jp = (int)(r % np);
-  const int ip = (int)(r / np);
-  // c = (ic1, jc1, ic2, jc2, ic3, jc3)
-  int st0[6], cnt[6], nq = 1;
-  for (int k = 0; k < 6; k++) {
-    st0[k] = S.kpestr[c[k]];
-    cnt[k] = S.kpeend[c[k]] - st0[k] + 1;
-    nq *= cnt[k];
-  }
-  const DevPrim& pa = S.pprim[ip];
-  const DevPrim& pb = S.pprim[jp];
-  const double cp = pa.coef * pb.coef;
-  typename std::conditional<F32, md32::G4, G4>::type s4;
-  double o = 0.0;
-  for (int q = lane; q < nq; q += 32) {
-    int qq = q, idx[6];
-    for (int k = 5; k >= 0; k--) {
-      idx[k] = st0[k] + qq % cnt[k];
-      qq /= cnt[k];
-    }
-    double ans;
-    if constexpr (F32) {
-      md32::Prim A[4] = {to_prim32(S.eprim[idx[0]]), to_prim32(S.eprim[idx[2]]),
-                         to_prim32(S.eprim[idx[4]]), to_prim32(pa)};
-      md32::Prim B[4] = {to_prim32(S.eprim[idx[1]]), to_prim32(S.eprim[idx[3]]),
-                         to_prim32(S.eprim[idx[5]]), to_prim32(pb)};
-      ans = gam3_g4part(A, B, S, s4);
-    } else {
-      Prim A[4] = {to_prim(S.eprim[idx[0]]), to_prim(S.eprim[idx[2]]),
-                   to_prim(S.eprim[idx[4]]), to_prim(pa)};
-      Prim B[4] = {to_prim(S.eprim[idx[1]]), to_prim(S.eprim[idx[3]]),
-                   to_prim(S.eprim[idx[5]]), to_prim(pb)};
-      ans = gam3_g4part(A, B, S, s4);
-    }
-    double cc = cp;
-    for (int k = 0; k < 6; k++) cc = cc * S.eprim[idx[k]].coef;
-    o = o + ans * cc;
-  }
-  o = warp_sum(o);
-  if (lane == 0) {
-    // separable terms: W1(p,e1) GAM_ee(e2,e3) + W3(p,e1,e2) Hcore(e3)
-    const long long n2 = (long long)ne * ne, n4 = n2 * n2;
-    const double* gee = aux;
-    const double* hc = gee + n4;
-    const double* W1 = hc + n2;
-    const double* W3 = W1 + (long long)np * np * n2;
-    const long long pp = (long long)ip * np + jp;
-    const double w1 = W1[(pp * ne + c[0]) * ne + c[1]];
-    const double w3 = W3[(((pp * ne + c[0]) * ne + c[1]) * ne + c[2]) * ne + c[3]];
-    const double ee = gee[((c[2] * (long long)ne + c[3]) * ne + c[4]) * ne + c[5]];
-    const double h = hc[c[4] * ne + c[5]];
-    x3[w] = o + w1 * ee + w3 * h;
-  }
-}
-
 // Six-permutation symmetrisation in place: each orbit is handled by the
 // tuple with the largest packed index (the reference's last writer), which
 // averages in its own permutation order and writes the whole orbit.
@@ -608,11 +506,6 @@ cudaError_t launch_gam2_symmetrize(int ne, int np, int rx, double* x1,
   return cudaGetLastError();
 }
 
-size_t gam3_aux_doubles(int ne, int np) {
-  const size_t n2 = (size_t)ne * ne;
-  return n2 * n2 + n2 + (size_t)np * np * n2 + (size_t)np * np * n2 * n2;
-}
-
 cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s,
                             const double* gee_in, const double* hc_in) {
   const int ne = sys.nebf, np = sys.npbf;
@@ -634,24 +527,6 @@ cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s,
   gam3_w1_kernel<<<(unsigned)((w1 * 32 + 127) / 128), 128, 0, s>>>(sys, W1);
   gam3_w3_kernel<<<(unsigned)((w3 * 32 + 63) / 64), 64, 0, s>>>(sys, W3);
   return cudaGetLastError();
-}
-
-cudaError_t launch_gam3_raw_range(const DevSystem& sys, const double* aux,
-                                  long long t0, long long ntup, double* x3,
-                                  cudaStream_t s, int fp32) {
-  const long long threads = ntup * 32;
-  const unsigned blocks = (unsigned)((threads + 63) / 64);
-  if (ntup <= 0) return cudaSuccess;
-  if (fp32) gam3_raw_kernel<true><<<blocks, 64, 0, s>>>(sys, aux, x3, t0, ntup);
-  else gam3_raw_kernel<false><<<blocks, 64, 0, s>>>(sys, aux, x3, t0, ntup);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_gam3_raw(const DevSystem& sys, const double* aux, double* x3,
-                            cudaStream_t s, int fp32) {
-  const long long n6 = (long long)sys.nebf * sys.nebf * sys.nebf * sys.nebf *
-                       sys.nebf * sys.nebf;
-  return launch_gam3_raw_range(sys, aux, 0, n6 * sys.npbf * sys.npbf, x3, s, fp32);
 }
 
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,

@@ -30,6 +30,15 @@ struct DevSystem {
   const double* cat;        // [3*nat]
   const double* bgem;       // [ngtg]
   const double* ggem;       // [ngtg]
+  int lmax_e, lmax_p;       // largest total l of an electronic / nuclear primitive
+  // gam_3 pair tables (k_gam3.cu), built by stage_system: g3i holds
+  // ket_ab[2 nket] (primitive pairs of the canonical contracted pairs, in
+  // canonical order), kofs[nPe+1], tile_k[ntile+1], tile_P[ntile+1],
+  // kperm[nket] (kets of each tile ordered by angular class); g3rec the
+  // FP64 pair records of the kets and of the canonical nuclear pairs.
+  int g3_nket, g3_ntile;
+  const int* g3i;
+  const double* g3rec;
 };
 
 // Largest per-Cartesian angular momentum supported by the MD kernels.
@@ -172,25 +181,38 @@ cudaError_t launch_gam_ee(const DevSystem& sys, double* gee, cudaStream_t s);
 cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
                                   long long ntup, double* x1, double* x2,
                                   cudaStream_t s, int fp32 = 0);
-// gam_3 raw tensor = W1(p,e1) GAM_ee(e2,e3) + W3(p,e1,e2) Hcore(e3) + the
-// primitive sum of the four-particle terms.  aux (gam3_aux_doubles) holds
-// GAM_ee, Hcore, W1, W3 from launch_gam3_aux (FP64).  fp32 = 1: the
-// four-particle integrals in FP32 (md_math32.cuh), sums in FP64 (mixed path).
+// gam_3 raw tensor = W1(p,e1) GAM_ee(e2,e3) + W3(p,e1,e2) Hcore(e3) + R4,
+// R4 the contracted primitive sum of the four-particle terms, stored once
+// per pair-canonical tuple (k_gam3.cu).  aux (gam3_aux_doubles) holds
+// GAM_ee, Hcore, W1, W3 (launch_gam3_aux, FP64) and R4 (launch_gam3_pairs).
 size_t gam3_aux_doubles(int ne, int np);
+size_t gam3_r4_doubles(int ne, int np);
 // gee_in / hc_in (optional, device): GAM_ee and Hcore already built by the
 // caller (C-order [i][j][k][l] and [i][j]); copied instead of recomputed.
 cudaError_t launch_gam3_aux(const DevSystem& sys, double* aux, cudaStream_t s,
                             const double* gee_in = nullptr,
                             const double* hc_in = nullptr);
+// R4 into aux.  fp32 = 1: the four-particle integrals in FP32 with FP64
+// Boys function, seeds and sums (mixed path).  screen > 0: (bra, ket)
+// pairs whose Schwarz-type estimate is below it are skipped.
+cudaError_t launch_gam3_pairs(const DevSystem& sys, double* aux, cudaStream_t s,
+                              int fp32, double screen);
+// raw tensor of packed tuples [t0, t0+ntup) into x3, after launch_gam3_pairs
 cudaError_t launch_gam3_raw_range(const DevSystem& sys, const double* aux,
                                   long long t0, long long ntup, double* x3,
-                                  cudaStream_t s, int fp32 = 0);
+                                  cudaStream_t s);
+// pair records of the gam_3 builder (sys.g3i must be set)
+size_t g3_record_doubles(int nket, int np);
+cudaError_t launch_g3_records(const DevSystem& sys, double* rec, cudaStream_t s);
+constexpr int kG3MaxTileKets = 1024;
+constexpr double kScreenThreshold = 1.0e-12;   // NEOXC_SCF_SCREEN
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rxchfne, double* x1,
                             double* x2, cudaStream_t s, int fp32 = 0);
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rxchfne, double* x1,
                                    double* x2, cudaStream_t s);
-cudaError_t launch_gam3_raw(const DevSystem& sys, const double* aux, double* x3,
-                            cudaStream_t s, int fp32 = 0);
+// launch_gam3_pairs + launch_gam3_raw_range over every tuple
+cudaError_t launch_gam3_raw(const DevSystem& sys, double* aux, double* x3,
+                            cudaStream_t s, int fp32 = 0, double screen = 0.0);
 cudaError_t launch_gam3_symmetrize(int ne, int np, double* g3,
                                    cudaStream_t s);
 

@@ -4,6 +4,7 @@
 // machine.  Only the tests load this library.
 #include "../../neo-rxchf_gb300/csrc/md_math.cuh"
 #include "../../neo-rxchf_gb300/csrc/md_math32.cuh"
+#include "../../neo-rxchf_gb300/csrc/g3_fatbra.cuh"
 
 using namespace neoxc::md;
 
@@ -92,5 +93,43 @@ double hc32_g3(int kind, const HP* A, const HP* B, const double* gam,
     case 2: return neoxc::md32::g3_vxc(s, c);
     default: return neoxc::md32::g3_vee(s);
   }
+}
+}  // extern "C"
+
+// the gam_3 builder's composite-bra form (g3_fatbra.cuh) of G4_MD_xgVeeg
+// (kind 0: bra e1, e3, p / ket e2) and G4_MD_xgVepg (kind 1: bra e1, e2, p /
+// ket e3), in precision R, for the general s/p/d class
+template <class R>
+static double fb_one(int kind, const HP* A, const HP* B, double g1, double g2) {
+  namespace g3 = neoxc::g3;
+  double rec[4][g3::kRLen];
+  for (int i = 0; i < 4; i++) g3::fill_pair_record(cv(A[i]), cv(B[i]), 1.0, 1.0, rec[i]);
+  g3::Bra<R, 12> b;
+  int ket;
+  if (kind == 1) {
+    g3::build_bra_vep<R, 2, 2, 12>(rec[0], rec[1], rec[3], (R)g1, (R)g2, b);
+    ket = 2;
+  } else {
+    g3::build_bra_vee<R, 2, 2, 12>(rec[0], rec[2], rec[3], (R)g1, (R)g2, b);
+    ket = 1;
+  }
+  const double* rk = rec[ket];
+  R Xk[3], Ek[3][5];
+  int tk[3];
+  for (int d = 0; d < 3; d++) {
+    Xk[d] = (R)rk[g3::kRX + d];
+    tk[d] = (int)rk[g3::kRT + d];
+    for (int t = 0; t < 5; t++)
+      Ek[d][t] = (t & 1) ? -(R)rk[g3::kRE + 5 * d + t] : (R)rk[g3::kRE + 5 * d + t];
+  }
+  return g3::fb_eval<R, 12, 4>(b, (R)rk[g3::kRP], Xk, Ek, tk);
+}
+
+extern "C" {
+double hc_fb(int kind, const HP* A, const HP* B, double g1, double g2) {
+  return fb_one<double>(kind, A, B, g1, g2);
+}
+double hc32_fb(int kind, const HP* A, const HP* B, double g1, double g2) {
+  return fb_one<float>(kind, A, B, g1, g2);
 }
 }

@@ -211,6 +211,45 @@ def test_boys_function_matches_xgammaf(orc, hostcheck):
     assert worst < 5e-12, worst
 
 
+def test_composite_bra_form_matches_g4_integrals(orc, hostcheck):
+    """The gam_3 builder evaluates G4_MD_xgVeeg / G4_MD_xgVepg as a Coulomb
+    integral between a composite bra (three pair densities, both geminals
+    integrated out) and the free electron's pair density, with the factorised
+    Hermite-Coulomb sum (g3_fatbra.cuh).  FP64: the oracle's restatement of
+    the reference's 12-deep loops (XC1_G4_MD.f) to 1e-10 relative; FP32 (the
+    mixed path, FP64 Boys function and seeds): at the FP32 level."""
+    O, L, H = orc, orc.lib(), hostcheck
+    P = C.POINTER(O.Prim)
+    d = C.c_double
+    for f in ("hc_fb", "hc32_fb"):
+        getattr(H, f).restype = d
+        getattr(H, f).argtypes = [C.c_int, P, P, d, d]
+    rng = np.random.default_rng(21)
+    AMS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (1, 1, 0), (0, 2, 0),
+           (1, 0, 1), (0, 1, 1), (0, 0, 2)]
+
+    def rp(lmax):
+        ams = [a for a in AMS if sum(a) <= lmax]
+        l = ams[rng.integers(0, len(ams))]
+        return O.prim(*l, float(np.exp(rng.uniform(np.log(0.1), np.log(20)))),
+                      *rng.uniform(-1.5, 1.5, 3))
+    errs32 = []
+    for trial in range(80):
+        lm = (0, 1, 2)[trial % 3]
+        A = O.prims([rp(lm) for _ in range(4)])
+        B = O.prims([rp(lm) for _ in range(4)])
+        g1, g2 = np.exp(rng.uniform(np.log(0.5), np.log(20), 2))
+        for kind, ref in ((0, L.orc_g4_xgveeg(A, B, g1, g2)),
+                          (1, L.orc_g4_xgvepg(A, B, g1, g2))):
+            got = H.hc_fb(kind, A, B, g1, g2)
+            assert abs(got - ref) <= 1e-10 * abs(ref) + 1e-14, (trial, kind, got, ref)
+            g32 = H.hc32_fb(kind, A, B, g1, g2)
+            if abs(ref) > 1e-12:
+                errs32.append(abs(g32 - ref) / abs(ref))
+    errs32 = np.array(errs32)
+    assert errs32.max() < 2e-4 and np.median(errs32) < 3e-5, (errs32.max(), np.median(errs32))
+
+
 def test_md32_instance_within_fp32_error(orc, hostcheck):
     """The mixed path's FP32 instance (md_math32.cuh: FP32 tables and
     recursions, FP64 Boys function and seeds) against the oracle's FP64
