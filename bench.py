@@ -61,7 +61,8 @@ def parse():
     ap.add_argument("--nebf", type=int, default=NEBF)
     ap.add_argument("--npbf", type=int, default=NPBF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf"], default=None,
+    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1"],
+                    default=None,
                     help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
 
@@ -295,6 +296,10 @@ def factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
         neoxc.gam4_fock_factored(ne, np_, gee, g2s, DE, DP)
     e2e_ms = 1e3 * (time.perf_counter() - t0) / n_e2e
     out = {"api": "neoxc_dev_gam4_fock_factored (device), neoxc_gam4_fock_factored (host arrays)",
+           "label": ("algorithm change, not the reference's loop: the same focke, fockp and "
+                     "E_gam4 as GAM4_DSCF for pair-symmetric tables, from O(nebf^4 npbf^2 + "
+                     "nebf^5) contractions instead of nebf^8 npbf^2 elements; the "
+                     "'equivalent' rate divides the element count by this time"),
            "nebf": ne, "npbf": np_, "ms_per_build": ms, "e2e_ms_per_build": e2e_ms,
            "equivalent_gam4_integrals_per_s": ne ** 8 * np_ ** 2 / (ms * 1e-3),
            "speedup_vs_element_kernel": elem_ms / ms,
@@ -530,12 +535,52 @@ def scf_section(neoxc, with_cpu: bool):
                                       % ("gam_3" if mixed == "gam3" else "gam_1, gam_2, gam_3"))
         else:
             E_fp64 = r["final"]["E_total"]
+    out["config1"] = config1_section(neoxc)
     out["xcuhf"] = xcuhf_scf_section(neoxc)
     out["rx"] = rx_scf_section(neoxc, with_cpu)
     out["batch"] = scf_batch_section(neoxc, s, DE)
     out["serving"] = scf_serving_section(neoxc, s, DE)
     if with_cpu:
         out["cpu_baseline"] = scf_cpu_baseline(s, DE, out["roothan"]["iterations"])
+    return out
+
+
+CONFIG1 = dict(seed=2024, nat=3, nebf=12, nprim=3, npbf=8, ngtg=3, lmax_e=1, lmax_p=2)
+
+
+def config1_section(neoxc):
+    """The seeded XCHF RHF system of the first configuration: 3 nuclei in
+    [-1.5,1.5]^3 bohr, 4 electrons, the proton on nucleus 0, 12 contracted
+    s/p electronic functions of 3 primitives (exponents log-uniform in
+    [0.1,20]), 8 even-tempered s/p/d nuclear primitives (4-32), NG=3.  One
+    solve = every integral built on the GPU (gam_2 and the 1.9e8-element
+    gam_3 tensor included) from core-Hamiltonian guesses and DIIS SCF to
+    the reference's convergence rule, through neoxc_xchf_scf with host
+    arrays.  FP64, then mixed (FP32 McMurchie-Davidson tables for gam_1,
+    gam_2, gam_3 with FP64 Boys function, seeds, sums, Fock assembly and
+    diagonalisation); the mixed energy is reported against the FP64 one."""
+    from neoxc import basis
+    s = basis.synthetic(**CONFIG1)
+    out = {"workload": "XCHF RHF, seeded synthetic system (seed %d): nebf=%d (s/p, 3 primitives), "
+                       "npbf=%d (s/p/d), NG=%d, nelec=%d; ng3=%.3g" % (
+                           CONFIG1["seed"], s.nebf, s.npbf, s.ngtg, s.nelec, s.ng3),
+           "api": "neoxc_xchf_scf (host arrays; core-Hamiltonian guesses, DIIS)"}
+    E = {}
+    for name, mixed in (("mixed", True), ("fp64", False)):
+        t0 = time.perf_counter()
+        r = neoxc.xchf_scf(s, None, diis=True, mixed=mixed)
+        dt = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        neoxc.xchf_scf(s, None, maxit=1, diis=True, mixed=mixed)
+        dt1 = time.perf_counter() - t1
+        E[name] = r["final"]["E_total"]
+        out[name] = {"solves_per_s": 1.0 / dt, "ms_per_solve": 1e3 * dt,
+                     "ms_integrals_plus_first_iteration": 1e3 * dt1,
+                     "iterations": r["niter"], "converged": r["converged"],
+                     "E_total": r["final"]["E_total"],
+                     "E_init": r["initial"]["E_total"]}
+    out["mixed"]["E_err_vs_fp64_Eh"] = E["mixed"] - E["fp64"]
+    out["mixed_over_fp64_solves_per_s"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
     return out
 
 
@@ -594,8 +639,8 @@ def scf_batch_section(neoxc, s, DE, njobs=48):
 
 def scf_cpu_baseline(s, DE, niter):
     """The oracle's restatement (C integrals with OpenMP + numpy xcscf) of the
-    same solve: integrals timed in full, the Roothaan loop timed over 3
-    iterations and scaled to the GPU run's iteration count."""
+    same solve, timed in full: every integral and every Roothaan iteration
+    to convergence."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import xchf_scf as X
@@ -604,13 +649,13 @@ def scf_cpu_baseline(s, DE, niter):
     ints = X.XchfIntegrals(s)
     t_int = time.perf_counter() - t0
     t1 = time.perf_counter()
-    X.xchf_scf(ints, DE, maxit=3)
-    t_it = (time.perf_counter() - t1) / 3
-    total = t_int + niter * t_it
+    hist, _, _, _, ok = X.xchf_scf(ints, DE)
+    t_scf = time.perf_counter() - t1
+    total = t_int + t_scf
     return {"solves_per_s": 1.0 / total, "unit": "SCF solves/s", "kind": "port",
-            "cores": int(O.lib().orc_num_threads()),
-            "sample": "integrals in full (%.1f s) + 3 of %d Roothaan iterations "
-                      "(%.2f s each), scaled" % (t_int, niter, t_it)}
+            "cores": int(O.lib().orc_num_threads()), "converged": bool(ok),
+            "sample": "one full solve: integrals %.1f s + %d Roothaan iterations %.1f s "
+                      "(the GPU run took %d)" % (t_int, len(hist) - 1, t_scf, niter)}
 
 
 def read_hbm_peak():
@@ -642,6 +687,9 @@ def main():
         return
     if args.only == "rx_scf":
         print(json.dumps(rx_scf_section(neoxc, not args.no_cpu_baseline)))
+        return
+    if args.only == "config1":
+        print(json.dumps(config1_section(neoxc)))
         return
     ne, np_ = args.nebf, args.npbf
     ng4 = ne ** 8 * np_ ** 2
@@ -723,7 +771,9 @@ def main():
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "peak_source": "neoxc_probe_fp64 on this GPU (measured DFMA rate); "
+                     "peak_source": "neoxc_probe_fp64 on this GPU (measured DFMA rate, a "
+                                    "builder-measured lower bound of the FP64 peak: the "
+                                    "kernel can exceed it); "
                                     "MEASURED_PEAKS.json has no FP64 figure",
                      "flop_per_element": FLOP_PER_ELEMENT,
                      "kernel_ms_mean": mean_ms},

@@ -366,6 +366,19 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
                                  const double* d_GAM_2s, const double* d_DE,
                                  const double* d_DP, double* d_focke,
                                  double* d_fockp, double* d_E_gam4);
+/* Mixed-precision form of neoxc_dev_gam4_fock_factored (gam_4_OMP.f:712-1192
+ * element, gam4_DSCF_OMP.f:266-307 contraction; the factorisation is new):
+ * the one-index transforms and the focke contraction run on the tensor
+ * cores (tcgen05.mma kind::tf32, each FP64 operand split into two TF32
+ * halves, three products, FP32 accumulation, FP64 results: ~1e-6
+ * relative); the two passes over GAM_2s, the traces, gradients and every
+ * reduction are FP64.  Same accumulate/overwrite contract; returns after
+ * the stream has drained (it checks the kernels' bounded-wait flag). */
+int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
+                                    const double* d_GAM_ee,
+                                    const double* d_GAM_2s, const double* d_DE,
+                                    const double* d_DP, double* d_focke,
+                                    double* d_fockp, double* d_E_gam4);
 
 /* ---- XCHF RHF SCF on the device ----------------------------------------------
  * xchf1_independent/xcscf.f:2-658 xcscf (the plain Roothaan branch; SOSCF is

@@ -598,6 +598,31 @@ int neoxc_gam4_dscf(int64_t NG4CHK, int64_t ne, int64_t np, int64_t ngee,
 }
 
 // ---- factorised gam_4 Fock build ----------------------------------------------
+int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
+                                    const double* d_gee, const double* d_g2s,
+                                    const double* d_DE, const double* d_DP,
+                                    double* d_focke, double* d_fockp, double* d_E) {
+  RC(need(ne >= 1 && np >= 1, "sizes"));
+  if (ne > kGam4FactMaxNE || np > 255)
+    return set_err(NEOXC_ERR_UNSUPPORTED,
+                   "factorised gam_4 Fock build: ne <= %d, np <= 255",
+                   kGam4FactMaxNE);
+  cudaStream_t s = (cudaStream_t)stream;
+  DBuf scr;
+  const size_t nd = gam4f_tc_scratch_doubles((int)ne, (int)np);
+  RC(dalloc(scr, sizeof(double) * nd, s));
+  CU(launch_gam4_factored_tc((int)ne, (int)np, d_gee, d_g2s, d_DE, d_DP,
+                             scr.as<double>(), d_focke, d_fockp, d_E, 1, s));
+  int flag = 0;   // the tensor-core waits' error flag, last word of the scratch
+  CU(cudaMemcpyAsync(&flag, scr.as<double>() + nd - 2, sizeof(int),
+                     cudaMemcpyDeviceToHost, s));
+  RC(finish(s));
+  if (flag)
+    return set_err(NEOXC_ERR_CUDA, "factorised gam_4 (tensor cores): an MMA completion "
+                                   "wait ran out; results not written");
+  return NEOXC_OK;
+}
+
 int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
                                  const double* d_gee, const double* d_g2s,
                                  const double* d_DE, const double* d_DP,

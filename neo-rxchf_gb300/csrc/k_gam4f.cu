@@ -35,6 +35,7 @@
 // index_GAM_2PK), so a table read is a linear offset.  All arithmetic is
 // FP64; table reads pass through the reference's underflow (|x|<1e-100 -> 0).
 #include "neoxc_internal.h"
+#include "tc_gemm.cuh"
 
 namespace neoxc {
 namespace {
@@ -423,6 +424,190 @@ int grid_for(long long work, int tb) {
   return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
+// out = underflow(in), element by element
+__global__ void flush_copy_kernel(long long n, const double* __restrict__ in,
+                                  double* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = flush(in[i]);
+}
+
+// ---- mixed-precision variant: the transforms and focke on tensor cores -----
+// C[m*ldc + n] = alpha sum_{k in split} A[m*lda + k] B[n*ldb + k]
+// grid (ceil(M/128), ceil(N/64), nsplit); split z covers K range
+// [z*kchunk, min(K, (z+1)*kchunk)) and writes C + z*split_stride.
+__global__ void __launch_bounds__(tc::kThreads, 1)
+tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
+               const double* __restrict__ B, long long ldb, long long N, long long K,
+               long long kchunk, double alpha, double* __restrict__ C, long long ldc,
+               long long split_stride, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_sm[];
+  unsigned char* a_hi = tc_sm;
+  unsigned char* a_lo = tc_sm + tc::kABytes;
+  unsigned char* b_hi = tc_sm + 2 * tc::kABytes;
+  unsigned char* b_lo = b_hi + tc::kBBytes;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(b_lo + tc::kBBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(b_lo + tc::kBBytes + 8);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long m0 = (long long)blockIdx.x * tc::kTileM;
+  const long long n0 = (long long)blockIdx.y * tc::kTileN;
+  const long long kbeg = (long long)blockIdx.z * kchunk;
+  const long long kend = kbeg + kchunk < K ? kbeg + kchunk : K;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;"
+                 :: "r"(tc::smem_u32(tmem_slot)) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(tc::smem_u32(mbar))
+                 : "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t mb = tc::smem_u32(mbar);
+  uint32_t phase = 0;
+  bool ok = true;
+  const uint32_t idesc = tc::instr_desc();
+  for (long long kt = kbeg; kt < kend && ok; kt += tc::kTileK) {
+    for (int e = tid; e < tc::kTileM * tc::kTileK; e += tc::kThreads) {
+      const int r = e / tc::kTileK, k = e - r * tc::kTileK;
+      const long long gm = m0 + r, gk = kt + k;
+      const double v = (gm < M && gk < kend) ? A[gm * lda + gk] : 0.0;
+      uint32_t hi, lo;
+      tc::split_tf32(v, hi, lo);
+      const int off = tc::canon_off(r, k);
+      *reinterpret_cast<uint32_t*>(a_hi + off) = hi;
+      *reinterpret_cast<uint32_t*>(a_lo + off) = lo;
+    }
+    for (int e = tid; e < tc::kTileN * tc::kTileK; e += tc::kThreads) {
+      const int r = e / tc::kTileK, k = e - r * tc::kTileK;
+      const long long gn = n0 + r, gk = kt + k;
+      const double v = (gn < N && gk < kend) ? B[gn * ldb + gk] : 0.0;
+      uint32_t hi, lo;
+      tc::split_tf32(v, hi, lo);
+      const int off = tc::canon_off(r, k);
+      *reinterpret_cast<uint32_t*>(b_hi + off) = hi;
+      *reinterpret_cast<uint32_t*>(b_lo + off) = lo;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t ah = tc::smem_u32(a_hi), al = tc::smem_u32(a_lo);
+      const uint32_t bh = tc::smem_u32(b_hi), bl = tc::smem_u32(b_lo);
+      for (int st = 0; st < tc::kTileK / 8; st++) {
+        const uint32_t o = st * 256;   // two 128-byte core matrices per K step
+        tc::mma_tf32(tmem, tc::smem_desc(ah + o), tc::smem_desc(bh + o), idesc,
+                     (kt > kbeg || st > 0) ? 1 : 0);
+        tc::mma_tf32(tmem, tc::smem_desc(ah + o), tc::smem_desc(bl + o), idesc, 1);
+        tc::mma_tf32(tmem, tc::smem_desc(al + o), tc::smem_desc(bh + o), idesc, 1);
+      }
+      tc::mma_commit(mb);
+    }
+    ok = __syncthreads_and(tc::mbar_wait(mb, phase) ? 1 : 0) != 0;
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    const long long row = m0 + warp * 32 + lane;
+    double* out = C + (long long)blockIdx.z * split_stride;
+    const bool any = kend > kbeg;
+    for (int c = 0; c < tc::kTileN / 16; c++) {
+      float v[16];
+      if (any) {
+        tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+      } else {
+        for (int i = 0; i < 16; i++) v[i] = 0.0f;
+      }
+      if (row < M)
+        for (int i = 0; i < 16; i++) {
+          const long long n = n0 + c * 16 + i;
+          if (n < N) out[row * ldc + n] = alpha * (double)v[i];
+        }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" :: "r"(tmem)
+                 : "memory");
+  }
+}
+
+// out(i,j,k,l) = in(k,l,i,j) + beta in(i,j,k,l): a transpose of the
+// (n^2 x n^2) matrix view, through 32 x 32 shared-memory tiles.
+__global__ void pair_swap_kernel(int n2, const double* __restrict__ in, double beta,
+                                 double* __restrict__ out) {
+  __shared__ double t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = by + j, c = bx + threadIdx.x;
+    if (r < n2 && c < n2) t[j][threadIdx.x] = in[(long long)r * n2 + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = bx + j, c = by + threadIdx.x;   // out[r][c] = in[c][r]
+    if (r < n2 && c < n2) {
+      const long long o = (long long)r * n2 + c;
+      out[o] = t[threadIdx.x][j] + (beta != 0.0 ? beta * in[o] : 0.0);
+    }
+  }
+}
+
+// out(x,a,c,y) = in(a,x,c,y)
+__global__ void swap12_kernel(int n, const double* __restrict__ in, double* __restrict__ out) {
+  const long long n2 = (long long)n * n, total = n2 * n2;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
+       o += (long long)gridDim.x * blockDim.x) {
+    const long long j = o % n2, xa = o / n2;
+    const long long a = xa % n, x = xa / n;
+    out[o] = in[(a * n + x) * n2 + j];
+  }
+}
+
+// DEt[y*n + d] = DE(y,d) (column-major DE)
+__global__ void transpose_n_kernel(int n, const double* __restrict__ DE, double* __restrict__ t) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+    const int y = e / n, d = e - y * n;
+    t[e] = DE[y + n * d];
+  }
+}
+
+// focke(x,b) (+)= sum_split part[split][x*64 + b]
+__global__ void focke_tc_reduce_kernel(int n, int nsplit, const double* __restrict__ part,
+                                       int accumulate, double* __restrict__ focke) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+    const int x = e / n, b = e - x * n;
+    double s = 0.0;
+    for (int z = 0; z < nsplit; z++) s += part[(long long)z * 128 * 64 + x * 64 + b];
+    const int f = x + n * b;
+    focke[f] = accumulate ? focke[f] + s : s;
+  }
+}
+
+constexpr long long kFockeKChunk = 4096;
+
+cudaError_t tc_gemm(const double* A, long long lda, long long M, const double* B,
+                    long long ldb, long long N, long long K, long long kchunk, double alpha,
+                    double* C, long long ldc, long long split_stride, int* err,
+                    cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tc::kSmemBytes);
+  if (e != cudaSuccess) return e;
+  const long long nsplit = (K + kchunk - 1) / kchunk;
+  const dim3 grid((unsigned)((M + tc::kTileM - 1) / tc::kTileM),
+                  (unsigned)((N + tc::kTileN - 1) / tc::kTileN), (unsigned)(nsplit < 1 ? 1 : nsplit));
+  tc_gemm_kernel<<<grid, tc::kThreads, tc::kSmemBytes, s>>>(A, lda, M, B, ldb, N, K, kchunk,
+                                                           alpha, C, ldc, split_stride, err);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_pair_symmetry_check(int ne, int np, const double* gee,
@@ -503,6 +688,96 @@ cudaError_t launch_gam4_factored(int ne, int np, const double* gee,
   }
   focke_part_kernel<<<n * n, tbf, 2 * sm_second, s>>>(n, Wp, HG, Vp, HE, epart);
   focke_reduce_kernel<<<grid_for((long long)n * n, TB), TB, 0, s>>>(n, epart, accumulate, focke);
+  return cudaGetLastError();
+}
+
+size_t gam4f_tc_scratch_doubles(int ne, int np) {
+  const size_t n4 = (size_t)ne * ne * ne * ne;
+  const size_t nchunk = (n4 + kDotChunk - 1) / kDotChunk;
+  const size_t nsplit = (size_t)((n4 / ne + kFockeKChunk - 1) / kFockeKChunk);
+  // 8 n^4 tensors, DE^T, PT(2x6 n^2), ST(8), fockp partials, focke partials,
+  // error flag
+  return 8 * n4 + (size_t)ne * ne + 12 * (size_t)ne * ne + 8 + (size_t)np * np * nchunk +
+         2 * nsplit * 128 * 64 + 2;
+}
+
+// Same focke / fockp / E as launch_gam4_factored, with the one-index
+// transforms and the focke contraction on the tensor cores (tc_gemm.cuh:
+// 3xTF32 products, FP32 accumulation, FP64 results) and everything else
+// (the two passes over GAM_2s, traces, gradients, reductions) FP64.  The
+// second-index transforms use the pair-exchange symmetry of the tables:
+// sum_b T(a,b,c,d) DE(x,b) = H(c,d,a,x) with H the last-index transform, so
+// T' = last(swap(last(T))); likewise the back transform of the symmetrised
+// gradient.  *err (device int, optional) is set when a tensor-core wait ran
+// out; the call then returns cudaErrorLaunchTimeout after the stream drains.
+cudaError_t launch_gam4_factored_tc(int ne, int np, const double* gee,
+                                    const double* g2s, const double* DE,
+                                    const double* DP, double* scratch,
+                                    double* focke, double* fockp, double* E,
+                                    int accumulate, cudaStream_t s) {
+  if (ne < 1 || ne > 64 || np < 1 || np > 255) return cudaErrorInvalidValue;
+  const int n = ne;
+  const long long n2 = (long long)n * n, n3 = n2 * n, n4 = n2 * n2;
+  const int nchunk = (int)((n4 + kDotChunk - 1) / kDotChunk);
+  const long long nsplit = (n3 + kFockeKChunk - 1) / kFockeKChunk;
+  double* buf[8];
+  for (int i = 0; i < 8; i++) buf[i] = scratch + (size_t)i * n4;
+  double* DEt = scratch + 8 * n4;
+  double* PT = DEt + n2;
+  double* ST = PT + 12 * n2;
+  double* fpart = ST + 8;
+  double* epart = fpart + (size_t)np * np * nchunk;   // [2][nsplit][128*64]
+  int* err = reinterpret_cast<int*>(epart + 2 * nsplit * 128 * 64);
+  const int TB = 256;
+  const int g_n4 = grid_for(n4, TB);
+  const dim3 tgrid((unsigned)((n2 + 31) / 32), (unsigned)((n2 + 31) / 32));
+  const dim3 tblk(32, 8);
+  cudaError_t e;
+#define TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+  TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  transpose_n_kernel<<<grid_for(n2, TB), TB, 0, s>>>(n, DE, DEt);
+  // last-index transforms: T'(..,y) = sum_d T(..,d) DE(y,d)  [B = DE^T rows]
+  auto last_f = [&](const double* in, double* out) {
+    return tc_gemm(in, n, n3, DEt, n, n, n, n, 1.0, out, n, 0, err, s);
+  };
+  // back transforms: T'(..,d) = sum_y T(..,y) DE(y,d)  [B = DE rows]
+  auto last_b = [&](const double* in, double* out, double alpha) {
+    return tc_gemm(in, n, n3, DE, n, n, n, n, alpha, out, n, 0, err, s);
+  };
+  // 1. G = DP . GAM_2s (FP64, HBM)
+  dp_contract_kernel<<<g_n4, TB, 0, s>>>(n4, np, g2s, DP, buf[0]);
+  // 2. H_G, G' and H_E, E'
+  TRY(last_f(buf[0], buf[1]));                                        // H_G
+  pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[1], 0.0, buf[2]);
+  TRY(last_f(buf[2], buf[3]));                                        // G'
+  flush_copy_kernel<<<g_n4, TB, 0, s>>>(n4, gee, buf[0]);             // flushed GAM_ee
+  TRY(last_f(buf[0], buf[4]));                                        // H_E
+  pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[4], 0.0, buf[2]);
+  TRY(last_f(buf[2], buf[5]));                                        // E'
+  // 3-4. traces and gradients (FP64)
+  traces_kernel<<<dim3(grid_for(6LL * n * n, TB), 2), TB, 0, s>>>(n, buf[3], buf[5], PT);
+  dtraces_kernel<<<1, 64, 0, s>>>(n, PT, ST);
+  gam4f_grad_kernel<<<dim3(g_n4, 2), TB, 0, s>>>(n, buf[5], buf[3], PT, ST, buf[6], buf[7]);
+  // Ws = Wp + Wp^swap, Vs = Vp + Vp^swap
+  pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[6], 1.0, buf[0]);
+  pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[7], 1.0, buf[2]);
+  // 5. W = back(Ws / 2), fockp = <GAM_2s, W>, E
+  TRY(last_b(buf[0], buf[3], 0.5));
+  pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[3], 0.0, buf[5]);
+  TRY(last_b(buf[5], buf[6], 1.0));                                   // W
+  fockp_dot_kernel<<<dim3(nchunk, np * np), kDotTB, 0, s>>>(n4, nchunk, g2s, buf[6], fpart);
+  fockp_reduce_kernel<<<1, 256, 0, s>>>(np, nchunk, fpart, DP, accumulate, fockp, E);
+  // 6. focke(x,b) = sum_{a,c,y} Ws(a,x,c,y) H_G(a,b,c,y) + Vs(a,x,c,y) H_E(a,b,c,y)
+  swap12_kernel<<<g_n4, TB, 0, s>>>(n, buf[0], buf[3]);   // Ws  -> [x][a][c][y]
+  swap12_kernel<<<g_n4, TB, 0, s>>>(n, buf[1], buf[5]);   // H_G -> [b][a][c][y]
+  swap12_kernel<<<g_n4, TB, 0, s>>>(n, buf[2], buf[7]);   // Vs
+  swap12_kernel<<<g_n4, TB, 0, s>>>(n, buf[4], buf[1]);   // H_E
+  TRY(tc_gemm(buf[3], n3, n, buf[5], n3, n, n3, kFockeKChunk, 1.0, epart, 64, 128 * 64, err, s));
+  TRY(tc_gemm(buf[7], n3, n, buf[1], n3, n, n3, kFockeKChunk, 1.0, epart + nsplit * 128 * 64,
+              64, 128 * 64, err, s));
+  focke_tc_reduce_kernel<<<grid_for(n2, TB), TB, 0, s>>>(n, (int)(2 * nsplit), epart,
+                                                        accumulate, focke);
+#undef TRY
   return cudaGetLastError();
 }
 

@@ -132,6 +132,15 @@ cudaError_t launch_gam4_factored(int ne, int np, const double* gee,
                                  const double* DP, double* scratch,
                                  double* focke, double* fockp, double* E,
                                  int accumulate, cudaStream_t s);
+// The same build with the one-index transforms and the focke contraction on
+// the tensor cores (tcgen05, 3xTF32 products with FP32 accumulation, FP64
+// results); the passes over GAM_2s, traces and gradients stay FP64.
+size_t gam4f_tc_scratch_doubles(int ne, int np);
+cudaError_t launch_gam4_factored_tc(int ne, int np, const double* gee,
+                                    const double* g2s, const double* DE,
+                                    const double* DP, double* scratch,
+                                    double* focke, double* fockp, double* E,
+                                    int accumulate, cudaStream_t s);
 // Largest |T - T^swap| and |T| over GAM_ee (t=0) and GAM_2s (t=1), where
 // ^swap exchanges the two electron pairs; per-CTA maxima in out[4*grid],
 // returns the grid size used in *grid.

@@ -117,6 +117,7 @@ def _declare(L):
         "neoxc_xchf_server_wait": (I, [vp, vp, d]),
         "neoxc_xchf_server_stop": (I, [vp]),
         "neoxc_dev_gam4_fock_factored": (I, [vp, i64, i64] + [vp] * 7),
+        "neoxc_dev_gam4_fock_factored_tc": (I, [vp, i64, i64] + [vp] * 7),
         "neoxc_eg4icr": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg3ic1": (I, [i64] * 4 + [vp] * 6),
         "neoxc_eg2ic1": (I, [i64] * 4 + [vp] * 10),
@@ -951,6 +952,16 @@ def dev_gam4_fock_factored(stream, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_focke, d
     _check(lib().neoxc_dev_gam4_fock_factored(C.c_void_p(stream), ne, np_, _tptr(d_gee),
                                               _tptr(d_g2s), _tptr(d_DE), _tptr(d_DP),
                                               _tptr(d_focke), _tptr(d_fockp), _tptr(d_E)))
+
+
+def dev_gam4_fock_factored_tc(stream, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_focke, d_fockp,
+                              d_E):
+    """The factorised gam_4 Fock build with its transforms and focke
+    contraction on the tensor cores (3xTF32, FP32 accumulation, FP64
+    results); waits for the stream before returning."""
+    _check(lib().neoxc_dev_gam4_fock_factored_tc(C.c_void_p(stream), ne, np_, _tptr(d_gee),
+                                                 _tptr(d_g2s), _tptr(d_DE), _tptr(d_DP),
+                                                 _tptr(d_focke), _tptr(d_fockp), _tptr(d_E)))
 
 
 def dev_eg3ic1(stream, ne, np_, d_DE, d_DP, d_g3, d_focke, d_fockp, d_E):

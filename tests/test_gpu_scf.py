@@ -122,6 +122,39 @@ def test_mixed_precision_all_geminal_energy_error(nx, xchf, xchf_gpu_scf):
     assert abs(err) <= 1e-6
 
 
+# A reduced copy of the first configuration's seeded system: the same
+# generator (3 nuclei, s/p electronic shells of 3 primitives with exponents
+# in [0.1, 20], even-tempered s/p/d nuclear basis, NG = 3) at nebf = 6,
+# npbf = 4, so that both solves take seconds.
+SPD_SYSTEM = dict(seed=2024, nat=3, nebf=6, nprim=3, npbf=4, ngtg=3, lmax_e=1, lmax_p=2)
+
+
+def test_mixed_precision_spd_energy_error(nx):
+    """On an s/p electronic, s/p/d nuclear system the mixed path (FP32
+    McMurchie-Davidson tables for gam_1, gam_2 and gam_3, FP64 Boys function,
+    seeds, sums, Fock assembly and diagonalisation) converges within 1
+    microhartree of the FP64 path."""
+    from neoxc import basis
+    s = basis.synthetic(**SPD_SYSTEM)
+    a = nx.xchf_scf(s, None, diis=True)
+    b = nx.xchf_scf(s, None, diis=True, mixed=True)
+    assert a["converged"] and b["converged"]
+    err = b["final"]["E_total"] - a["final"]["E_total"]
+    print("mixed-precision s/p/d E error (Eh):", err, "E:", a["final"]["E_total"])
+    assert abs(err) <= 1e-6
+
+
+def test_screened_scf_matches_unscreened(nx):
+    """Schwarz-type screening at 1e-12 (NEOXC_SCF_SCREEN) moves the
+    converged energy of the s/p/d system by less than 1e-8 Eh."""
+    from neoxc import basis
+    s = basis.synthetic(**SPD_SYSTEM)
+    a = nx.xchf_scf(s, None, diis=True)
+    b = nx.xchf_scf(s, None, diis=True, screen=True)
+    assert a["converged"] and b["converged"]
+    assert abs(b["final"]["E_total"] - a["final"]["E_total"]) <= 1e-8
+
+
 def test_batch_matches_separate_solves(nx, xchf):
     """A proton-position scan of examples/xchf run as one batch on three
     worker streams gives, job by job, exactly the result of a separate
