@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--nebf", type=int, default=NEBF)
     ap.add_argument("--npbf", type=int, default=NPBF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1"],
+    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1", "gam3"],
                     default=None,
                     help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
@@ -584,6 +584,42 @@ def config1_section(neoxc):
     return out
 
 
+def gam3_section(neoxc, kw=None):
+    """The gam_3 builder (GAM3_IC1: the dense contracted gam_3 tensor, packed
+    index_GAM_3PK order, six-permutation symmetrised) on the seeded system of
+    the first configuration, FP64 and mixed (FP32 tables, FP64 Boys
+    function, seeds and sums).  Device time of the build from CUDA events
+    (the copy of the 1.5 GB tensor to the host excluded).  Units: contracted
+    gam_3 integrals/s (ng3 / t) and composite-bra x pair-ket Coulomb
+    evaluations/s (k_gam3.cu: 2 passes x pair-canonical (Pp, P1, P2) x
+    primitive bras x geminal pairs x primitive kets)."""
+    from neoxc import basis
+    kw = kw or CONFIG1
+    s = basis.synthetic(**kw)
+    nPe = s.nebf * (s.nebf + 1) // 2
+    nPp = s.npbf * (s.npbf + 1) // 2
+    k = np.array(s.KPEEND) - np.array(s.KPESTR) + 1
+    ket_pairs = sum(int(k[i] * k[j]) for i in range(s.nebf) for j in range(i + 1))
+    # per pass: CTAs (Pp, Pa, Pb) x bras (prim pairs of Pa x of Pb x NG^2) x kets
+    pp_of = [int(k[i] * k[j]) for i in range(s.nebf) for j in range(i + 1)]
+    evals = 2 * nPp * sum(pp_of) ** 2 * s.ngtg ** 2 * ket_pairs
+    out = {"workload": "GAM3_IC1 on the seeded nebf=%d (s/p, %d primitives), npbf=%d (s/p/d), "
+                       "NG=%d system: ng3=%d" % (s.nebf, s.npebf // s.nebf, s.npbf, s.ngtg, s.ng3),
+           "api": "neoxc_gam3_ic1_opts (device time from CUDA events)",
+           "canonical_tuples": nPp * nPe ** 3, "primitive_pair_kets": ket_pairs,
+           "coulomb_evaluations": evals}
+    for name, mixed in (("mixed", True), ("fp64", False)):
+        x, sec = neoxc.gam3_ic1(s, mixed=mixed, timing=True)
+        out[name] = {"seconds": sec, "gam3_integrals_per_s": s.ng3 / sec,
+                     "coulomb_evaluations_per_s": evals / sec, "absmax": float(np.abs(x).max())}
+        out[name + "_tensor"] = x
+    diff = float(np.abs(out["mixed_tensor"] - out["fp64_tensor"]).max())
+    out["mixed"]["max_abs_diff_vs_fp64"] = diff
+    out["mixed"]["max_rel_diff_vs_fp64"] = diff / max(out["fp64"]["absmax"], 1e-300)
+    del out["mixed_tensor"], out["fp64_tensor"]
+    return out
+
+
 def scf_serving_section(neoxc, s, DE):
     """Poisson arrivals of proton-scan requests (seeded) into the
     continuous-batching server (8 worker streams, DIIS): p50/p99 time from
@@ -690,6 +726,9 @@ def main():
         return
     if args.only == "config1":
         print(json.dumps(config1_section(neoxc)))
+        return
+    if args.only == "gam3":
+        print(json.dumps(gam3_section(neoxc)))
         return
     ne, np_ = args.nebf, args.npbf
     ng4 = ne ** 8 * np_ ** 2

@@ -102,6 +102,22 @@ int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
                    const double* NUCEX, const int64_t* ELCAM,
                    const int64_t* NUCAM, const double* ELCBFC,
                    const double* NUCBFC, double* GM3ICR);
+/* GAM3_IC1 with options (no reference counterpart for the options):
+ * NEOXC_SCF_MIXED computes the four-particle terms with FP32 tables and
+ * FP64 Boys function, seeds and sums; NEOXC_SCF_SCREEN skips primitive
+ * (bra, ket) pairs whose Schwarz-type estimate is below 1e-12.  seconds
+ * (optional) receives the device time of the build (CUDA events, the copy
+ * to GM3ICR excluded). */
+int neoxc_gam3_ic1_opts(int64_t options, int64_t Nchunks, int64_t nebf, int64_t npebf,
+                        int64_t npbf, int64_t ng3, int64_t ng3prm, int64_t nat,
+                        int64_t ngtg1, double pmass, const double* cat, const double* zan,
+                        const double* bcoef1, const double* gamma1,
+                        const int64_t* KPESTR, const int64_t* KPEEND,
+                        const int64_t* AMPEB2C, const double* AGEBFCC,
+                        const double* AGNBFCC, const double* ELCEX,
+                        const double* NUCEX, const int64_t* ELCAM,
+                        const int64_t* NUCAM, const double* ELCBFC,
+                        const double* NUCBFC, double* GM3ICR, double* seconds);
 
 /* gam3_DSCF_OMP.f:2-137 GAM3_DSCF: builds gam_3 one proton pair at a time
  * and contracts it on the fly; focke, fockp accumulate (add2fock), E_gam3

@@ -491,17 +491,18 @@ int neoxc_rxchfne_gam2_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf,
                      NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, GM2ICR, GM2exICR);
 }
 
-int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
-                   int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
-                   double pmass, const double* cat, const double* zan,
-                   const double* bcoef1, const double* gamma1,
-                   const int64_t* KPESTR, const int64_t* KPEEND,
-                   const int64_t* AMPEB2C, const double* AGEBFCC,
-                   const double* AGNBFCC, const double* ELCEX,
-                   const double* NUCEX, const int64_t* ELCAM,
-                   const int64_t* NUCAM, const double* ELCBFC,
-                   const double* NUCBFC, double* GM3ICR) {
+int neoxc_gam3_ic1_opts(int64_t options, int64_t Nchunks, int64_t nebf, int64_t npebf,
+                        int64_t npbf, int64_t ng3, int64_t ng3prm, int64_t nat,
+                        int64_t ngtg1, double pmass, const double* cat, const double* zan,
+                        const double* bcoef1, const double* gamma1,
+                        const int64_t* KPESTR, const int64_t* KPEEND,
+                        const int64_t* AMPEB2C, const double* AGEBFCC,
+                        const double* AGNBFCC, const double* ELCEX,
+                        const double* NUCEX, const int64_t* ELCAM,
+                        const int64_t* NUCAM, const double* ELCBFC,
+                        const double* NUCBFC, double* GM3ICR, double* seconds) {
   (void)AMPEB2C;
+  RC(need((options & ~(int64_t)(NEOXC_SCF_MIXED | NEOXC_SCF_SCREEN)) == 0, "options"));
   RC(need(Nchunks >= 1, "Nchunks >= 1"));
   int64_t n6 = nebf * nebf * nebf * nebf * nebf * nebf;
   RC(need(ng3 == n6 * npbf * npbf, "ng3 == nebf**6 * npbf**2"));
@@ -517,12 +518,45 @@ int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
   DBuf d, aux;
   RC(dalloc(d, sizeof(double) * ng3, s));
   RC(dalloc(aux, sizeof(double) * gam3_aux_doubles((int)nebf, (int)npbf), s));
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  if (seconds) {
+    CU(cudaEventCreate(&ev[0]));
+    CU(cudaEventCreate(&ev[1]));
+    CU(cudaEventRecord(ev[0], s));
+  }
   CU(launch_gam3_aux(u.d, aux.as<double>(), s));
-  CU(launch_gam3_raw(u.d, aux.as<double>(), d.as<double>(), s));
+  CU(launch_gam3_raw(u.d, aux.as<double>(), d.as<double>(), s,
+                     (options & NEOXC_SCF_MIXED) ? 1 : 0,
+                     (options & NEOXC_SCF_SCREEN) ? kScreenThreshold : 0.0));
   CU(launch_gam3_symmetrize((int)nebf, (int)npbf, d.as<double>(), s));
+  if (seconds) CU(cudaEventRecord(ev[1], s));
   CU(cudaMemcpyAsync(GM3ICR, d.p, sizeof(double) * ng3, cudaMemcpyDeviceToHost,
                      s));
-  return finish(s);
+  const int rc = finish(s);
+  if (seconds) {
+    float ms = 0.0f;
+    if (rc == NEOXC_OK) cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    *seconds = 1e-3 * ms;
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+  }
+  return rc;
+}
+
+int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
+                   int64_t ng3, int64_t ng3prm, int64_t nat, int64_t ngtg1,
+                   double pmass, const double* cat, const double* zan,
+                   const double* bcoef1, const double* gamma1,
+                   const int64_t* KPESTR, const int64_t* KPEEND,
+                   const int64_t* AMPEB2C, const double* AGEBFCC,
+                   const double* AGNBFCC, const double* ELCEX,
+                   const double* NUCEX, const int64_t* ELCAM,
+                   const int64_t* NUCAM, const double* ELCBFC,
+                   const double* NUCBFC, double* GM3ICR) {
+  return neoxc_gam3_ic1_opts(0, Nchunks, nebf, npebf, npbf, ng3, ng3prm, nat, ngtg1, pmass,
+                             cat, zan, bcoef1, gamma1, KPESTR, KPEEND, AMPEB2C, AGEBFCC,
+                             AGNBFCC, ELCEX, NUCEX, ELCAM, NUCAM, ELCBFC, NUCBFC, GM3ICR,
+                             nullptr);
 }
 
 int neoxc_gam4_icr(int64_t Nchunks, int64_t ne, int64_t np, int64_t ngee,

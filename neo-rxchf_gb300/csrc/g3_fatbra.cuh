@@ -204,40 +204,6 @@ G3_HD void build_bra_vee(const double* r1, const double* r3, const double* rp,
   b.pref = C0 * CB0;
 }
 
-// C(t,i) 2^(2i-t) = t! 2^(2i-t) / ((2i-t)! (t-i)!) for t, i <= 16 (zero
-// outside ceil(t/2) <= i <= t): d^t/dX^t f(a X^2) = sum_i C(t,i) (2aX)^(2i-t)
-// a^(t-i) f^(i)(a X^2).
-#define G3_HERMC_VALUES \
-    1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 2, 4, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 12, 8, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 12, 48, 16, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 120, 160, 32, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 120, 720, 480, 64, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 0, 1680, 3360, 1344, 128, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 0, 1680, 13440, 13440, 3584, 256, 0, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 0, 0, 30240, 80640, 48384, 9216, 512, 0, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 0, 0, 30240, 302400, 403200, 161280, 23040, 1024, 0, 0, 0, 0, 0, 0, \
-    0, 0, 0, 0, 0, 0, 665280, 2217600, 1774080, 506880, 56320, 2048, 0, 0, 0, 0, 0, \
-    0, 0, 0, 0, 0, 0, 665280, 7983360, 13305600, 7096320, 1520640, 135168, 4096, 0, 0, 0, 0, \
-    0, 0, 0, 0, 0, 0, 0, 17297280, 69189120, 69189120, 26357760, 4392960, 319488, 8192, 0, 0, 0, \
-    0, 0, 0, 0, 0, 0, 0, 17297280, 242161920, 484323840, 322882560, 92252160, 12300288, 745472, 16384, 0, 0, \
-    0, 0, 0, 0, 0, 0, 0, 0, 518918400, 2421619200, 2905943040, 1383782400, 307507200, 33546240, 1720320, 32768, 0, \
-    0, 0, 0, 0, 0, 0, 0, 0, 518918400, 8302694400, 19372953600, 15498362880, 5535129600, 984023040, 89456640, 3932160, 65536
-#if defined(__CUDACC__)
-static __device__ const double kHermCDev[17 * 17] = {G3_HERMC_VALUES};
-#endif
-static const double kHermCHost[17 * 17] = {G3_HERMC_VALUES};
-#undef G3_HERMC_VALUES
-G3_HD double hermc(int t, int i) {
-#if defined(__CUDA_ARCH__)
-  return __ldg(&kHermCDev[t * 17 + i]);
-#else
-  return kHermCHost[t * 17 + i];
-#endif
-}
-
 // One (bra, ket) Coulomb integral, pref C4 sum_tuv W_x W_y W_z R_tuv, with
 // W_d = W'_d (*) Ek_d (Ek: the ket's Hermite coefficients times (-1)^t) and
 // the Hermite-Coulomb sum in factorised form:
@@ -273,7 +239,7 @@ G3_HD double fb_eval(const Bra<R, NW>& b, R pk, const R* Xk, const R (*Ek)[NK + 
     for (int k = 1; k <= n; k++) xp[k] = xp[k - 1] * Rv[d];
     for (int i = 0; i <= n; i++) A[d][i] = R(0);
     for (int t = 0; t <= n; t++)
-      for (int i = (t + 1) / 2; i <= t; i++) A[d][i] += W[t] * (R)hermc(t, i) * xp[2 * i - t];
+      for (int i = (t + 1) / 2; i <= t; i++) A[d][i] += W[t] * (R)neoxc::hermc(t, i) * xp[2 * i - t];
     L += n;
   }
   const int nx = b.N[0] + tk[0], ny = b.N[1] + tk[1], nz = b.N[2] + tk[2];

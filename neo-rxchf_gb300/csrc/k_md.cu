@@ -94,19 +94,24 @@ __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
   perm3(pr, 2, 0, 1, pr312);
   R g[6];
   const R zero = R(0.0), one = R(1.0);
-  // centre of classical nucleus ia in the working precision
-  auto vxc = [&](int ia) {
-    const R C3[3] = {(R)S.cat[3 * ia], (R)S.cat[3 * ia + 1], (R)S.cat[3 * ia + 2]};
-    return md::underflow((double)g3_vxc(st, C3));
+  // sum over the classical nuclei of sign * zan * underflow(G3_MD_xgVxCg),
+  // in the reference's order; the Hermite fold is shared by all nuclei
+  R vx[kMaxNat];
+  auto vxc_sum = [&](double sign) {
+    g3_vxc_multi(st, nat, S.cat, vx);
+    double acc = 0.0;
+    for (int ia = 0; ia < nat; ia++) {
+      const double v = md::underflow((double)vx[ia]);
+      acc = sign < 0.0 ? acc - S.zan[ia] * v : acc + S.zan[ia] * v;
+    }
+    return acc;
   };
   if (gi < ng) {
     const int ik = gi;
     gam6(g, A23, (R)gm[ik], -1, zero);
     g3_setup_pairs(st, A, B, pr, g, 2);
     double xgTE = (double)g3_ke(st, zero, one);
-    double xgVEC = 0.0;
-    for (int ia = 0; ia < nat; ia++)
-      xgVEC = xgVEC - S.zan[ia] * vxc(ia);
+    double xgVEC = vxc_sum(-1.0);
     double xgVEE = md::underflow((double)g3_vee(st));
     g3_setup_pairs(st, A132, B132, pr132, g, 0);
     double xgVEP = -md::underflow((double)g3_vee(st));
@@ -122,16 +127,12 @@ __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
   gam6(g, A12, gk, B13, gl);
   g3_setup_pairs(st, A312, B312, pr312, g, 2);
   double xgTPg = (double)g3_ke(st, gl, (R)S.pmass);
-  double xgVPCg = 0.0;
-  for (int ia = 0; ia < nat; ia++)
-    xgVPCg = xgVPCg + S.zan[ia] * vxc(ia);
+  double xgVPCg = vxc_sum(1.0);
   // order (e1, e2, p): A13, B23
   gam6(g, A13, gk, B23, gl);
   g3_setup_pairs(st, A, B, pr, g, 2);
   double xgTEg1 = (double)g3_ke(st, zero, one);
-  double xgVECg1 = 0.0;
-  for (int ia = 0; ia < nat; ia++)
-    xgVECg1 = xgVECg1 - S.zan[ia] * vxc(ia);
+  double xgVECg1 = vxc_sum(-1.0);
   double xgVEEg2 = md::underflow((double)g3_vee(st));
   double xgsg = (double)g3_overlap(st);
   // A23, B13
@@ -142,9 +143,7 @@ __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
   gam6(g, A23, gk, B23, gl);
   g3_setup_pairs(st, A, B, pr, g, 2);
   double xgTEg3 = (double)g3_ke(st, zero, one);
-  double xgVECg2 = 0.0;
-  for (int ia = 0; ia < nat; ia++)
-    xgVECg2 = xgVECg2 - S.zan[ia] * vxc(ia);
+  double xgVECg2 = vxc_sum(-1.0);
   // A13, B13
   gam6(g, A13, gk, B13, gl);
   g3_setup_pairs(st, A, B, pr, g, 0);

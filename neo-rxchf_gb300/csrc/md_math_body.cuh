@@ -21,7 +21,9 @@
 //   * per direction a vector W_d[n] that folds the Hermite coefficients,
 //     the binomial split between the Gaussian part and the Coulomb part,
 //     and the chain-rule powers of the Coulomb-centre coefficients;
-//   * one R_tuv table per call, and  I = C * sum_{n,l,m} Wx Wy Wz R_nlm.
+//   * I = C * sum_{n,l,m} Wx Wy Wz R_nlm evaluated in factorised form
+//     (contract_wr: the derivatives of F_0(alpha |R|^2) split per
+//     direction, so no R_tuv table is built).
 // The Boys function keeps the branch structure of the reference's XGAMMAF
 // (common.f:317-348): for T > 20 the asymptotic form without the exp(-T)
 // term and upward recursion, exactly as there; for T <= 20 the reference
@@ -116,6 +118,41 @@ NX_HD double boys_rinv(int j) {
 #endif
 }
 
+// C(t,i) 2^(2i-t) = t! 2^(2i-t) / ((2i-t)! (t-i)!) for t, i <= 16 (zero
+// outside ceil(t/2) <= i <= t): d^t/dX^t f(a X^2) = sum_i C(t,i) (2aX)^(2i-t)
+// a^(t-i) f^(i)(a X^2), the coefficients of the factorised Hermite-Coulomb
+// sum (contract_wr).
+#define NX_HERMC_VALUES \
+    1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 2, 4, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 12, 8, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 12, 48, 16, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 120, 160, 32, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 120, 720, 480, 64, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 0, 1680, 3360, 1344, 128, 0, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 0, 1680, 13440, 13440, 3584, 256, 0, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 0, 0, 30240, 80640, 48384, 9216, 512, 0, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 0, 0, 30240, 302400, 403200, 161280, 23040, 1024, 0, 0, 0, 0, 0, 0, \
+    0, 0, 0, 0, 0, 0, 665280, 2217600, 1774080, 506880, 56320, 2048, 0, 0, 0, 0, 0, \
+    0, 0, 0, 0, 0, 0, 665280, 7983360, 13305600, 7096320, 1520640, 135168, 4096, 0, 0, 0, 0, \
+    0, 0, 0, 0, 0, 0, 0, 17297280, 69189120, 69189120, 26357760, 4392960, 319488, 8192, 0, 0, 0, \
+    0, 0, 0, 0, 0, 0, 0, 17297280, 242161920, 484323840, 322882560, 92252160, 12300288, 745472, 16384, 0, 0, \
+    0, 0, 0, 0, 0, 0, 0, 0, 518918400, 2421619200, 2905943040, 1383782400, 307507200, 33546240, 1720320, 32768, 0, \
+    0, 0, 0, 0, 0, 0, 0, 0, 518918400, 8302694400, 19372953600, 15498362880, 5535129600, 984023040, 89456640, 3932160, 65536
+#if defined(__CUDACC__)
+static __device__ const double kHermCDev[17 * 17] = {NX_HERMC_VALUES};
+#endif
+static const double kHermCHost[17 * 17] = {NX_HERMC_VALUES};
+#undef NX_HERMC_VALUES
+NX_HD double hermc(int t, int i) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&kHermCDev[t * 17 + i]);
+#else
+  return kHermCHost[t * 17 + i];
+#endif
+}
+
 // F_m(T_g), m = 0..22, and exp(-T_g) on the grid T_g = g/16, g = 0..320
 // (boys_table.inc, written by gen_boys_table.py from the integral definition
 // at 40 digits).
@@ -158,17 +195,24 @@ NX_BIG void boys(int M, double T, double* F) {
   g = g < 0 ? 0 : (g > kBoysRows - 1 ? kBoysRows - 1 : g);
   const double d = (double)g * 0.0625 - T;
   const int row = g * kBoysCols;
-  const double inv[6] = {1.0, 0.5, 1.0 / 3.0, 0.25, 0.2, 1.0 / 6.0};
-  double f = boys_tab(row + M + 6);
-  for (int k = 6; k >= 1; k--) f = fma(d * inv[k - 1], f, boys_tab(row + M + k - 1));
+  // e_k = d^k / k!, shared by F_M and exp(d)
+  double e[7];
+  e[0] = 1.0;
+  e[1] = d;
+  e[2] = e[1] * d * 0.5;
+  e[3] = e[2] * d * (1.0 / 3.0);
+  e[4] = e[3] * d * 0.25;
+  e[5] = e[4] * d * 0.2;
+  e[6] = e[5] * d * (1.0 / 6.0);
+  double f = boys_tab(row + M + 6) * e[6];
+  for (int k = 5; k >= 0; k--) f = fma(boys_tab(row + M + k), e[k], f);
   F[M] = f;
   if (M == 0) return;
-  double e = 1.0;
-  for (int k = 6; k >= 1; k--) e = fma(d * inv[k - 1], e, 1.0);
-  const double ex = boys_tab(row + kBoysCols - 1) * e;
+  const double ex =
+      boys_tab(row + kBoysCols - 1) * (((((e[6] + e[5]) + e[4]) + e[3]) + e[2]) + e[1] + 1.0);
   const double t2 = 2.0 * T;
   for (int L = M - 1; L >= 0; L--) {
-    f = (f * t2 + ex) * (0.5 * boys_rinv(L));
+    f = fma(f, t2, ex) * (0.5 * boys_rinv(L));   // (2T F_(L+1) + e^-T) / (2L + 1)
     F[L] = f;
   }
 }
@@ -342,45 +386,12 @@ NX_BIG void dgauss4(const GK4& g, const real* X, const int* N, real* D) {
 }
 
 // ------------------------------------------------------------- R_tuv
-// R^{(0)}_{tuv} for t+u+v <= L (tetrahedral storage, R[tet(t,u,v)]),
-// R^{(j)}_{000} = (-2 alpha)^j F_j(T), standard MD recursion.
 NX_HD int tet_size(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
 NX_HD int tet(int t, int u, int v) {
   int n = t + u + v;               // entries with t+u+v < n precede
   int k = u + v;                   // within shell n: order by (u+v), then v
   return n * (n + 1) * (n + 2) / 6 + k * (k + 1) / 2 + v;
 }
-constexpr int kTetMax = (LTOT + 1) * (LTOT + 2) * (LTOT + 3) / 6;
-
-NX_BIG void rtuv_table(int L, real T, real alpha, const real* R3,
-                      real* R /* >= tet_size(L) */) {
-  // seeds R^(j)_000 = (-2 alpha)^j F_j(T) in FP64, narrowed once
-  double F[LTOT + 1], pw[LTOT + 1];
-  boys(L, (double)T, F);
-  const double m2a = -2.0 * (double)alpha;
-  pw[0] = 1.0;
-  for (int k = 1; k <= L; k++) pw[k] = pw[k - 1] * m2a;
-  R[0] = (real)(pw[L] * F[L]);
-  // In place: layer j is built from layer j+1 by decreasing t+u+v, so every
-  // entry read still holds its layer-(j+1) value.
-  for (int j = L - 1; j >= 0; j--) {
-    for (int n = L - j; n >= 1; n--)
-      for (int k = 0; k <= n; k++)
-        for (int v = 0; v <= k; v++) {
-          const int u = k - v, t = n - k;
-          real r;
-          if (t > 0)
-            r = (t > 1 ? (t - 1) * R[tet(t - 2, u, v)] : R_(0.0)) + R3[0] * R[tet(t - 1, u, v)];
-          else if (u > 0)
-            r = (u > 1 ? (u - 1) * R[tet(t, u - 2, v)] : R_(0.0)) + R3[1] * R[tet(t, u - 1, v)];
-          else
-            r = (v > 1 ? (v - 1) * R[tet(t, u, v - 2)] : R_(0.0)) + R3[2] * R[tet(t, u, v - 1)];
-          R[tet(t, u, v)] = r;
-        }
-    R[0] = (real)(pw[j] * F[j]);
-  }
-}
-
 NX_HD real binom(int n, int k) {
   real r = R_(1.0);
   for (int i = 1; i <= k; i++) r = r * (real)(n - k + i) / (real)i;
@@ -554,19 +565,46 @@ NX_BIG void g3_wvec(const G3& s, int d, real bf, real bg, real bh,
   *nmax = N;
 }
 
+// I = sum_{t,u,v} Wx[t] Wy[u] Wz[v] R_tuv(alpha, R3) in factorised form:
+// R_tuv = d^t/dX^t d^u/dY^u d^v/dZ^v F_0(alpha |R|^2), and because F_0's
+// argument is additive over directions the derivatives factorise,
+//   I = sum_m (-alpha)^m F_m(T) sum_{i+j+k=m} A_x[i] A_y[j] A_z[k],
+//   A_d[i] = sum_t W_d[t] C(t,i) 2^(2i-t) R_d^(2i-t)  (hermc),
+// O(L^2) work and no R_tuv table; equal to the MD recursion of the
+// reference's RTUV (XC1_int_tools.f:341-464) to rounding.  The seeds
+// (-alpha)^m F_m(T) and the final sum are FP64 in both instances.
 NX_BIG real contract_wr(const real* Wx, int nx, const real* Wy, int ny,
-                         const real* Wz, int nz, real T, real alpha,
-                         const real* R3) {
+                        const real* Wz, int nz, real T, real alpha,
+                        const real* R3) {
+  const real* W[3] = {Wx, Wy, Wz};
+  const int n[3] = {nx, ny, nz};
+  real A[3][LTOT + 1];
+  for (int d = 0; d < 3; d++) {
+    real xp[LTOT + 1];
+    xp[0] = R_(1.0);
+    for (int k = 1; k <= n[d]; k++) xp[k] = xp[k - 1] * R3[d];
+    for (int i = 0; i <= n[d]; i++) A[d][i] = R_(0.0);
+    for (int t = 0; t <= n[d]; t++)
+      for (int i = (t + 1) / 2; i <= t; i++)
+        A[d][i] += W[d][t] * (real)hermc(t, i) * xp[2 * i - t];
+  }
+  real Bxy[2 * LTOT + 1];
+  for (int m = 0; m <= nx + ny; m++) Bxy[m] = R_(0.0);
+  for (int i = 0; i <= nx; i++)
+    for (int j = 0; j <= ny; j++) Bxy[i + j] += A[0][i] * A[1][j];
   const int L = nx + ny + nz;
-  real R[kTetMax];
-  rtuv_table(L, T, alpha, R3, R);
-  real acc = R_(0.0);
-  for (int t = 0; t <= nx; t++)
-    for (int u = 0; u <= ny; u++) {
-      real wxy = Wx[t] * Wy[u];
-      for (int v = 0; v <= nz; v++) acc += wxy * Wz[v] * R[tet(t, u, v)];
-    }
-  return acc;
+  double F[LTOT + 1];
+  boys(L, (double)T, F);
+  const double ma = -(double)alpha;
+  double s = 0.0, pw = 1.0;
+  for (int m = 0; m <= L; m++) {
+    real bm = R_(0.0);
+    const int lo = m - nz > 0 ? m - nz : 0, hi = m < nx + ny ? m : nx + ny;
+    for (int i = lo; i <= hi; i++) bm += Bxy[i] * A[2][m - i];
+    s += pw * F[m] * (double)bm;
+    pw *= ma;
+  }
+  return (real)s;
 }
 
 // G3_MD_xgVxCg (XC1_G3_MD.f:711-1088): attraction of particle 1 to C
@@ -616,6 +654,56 @@ NX_BIG real g3_vxc(const G3& s, const real* C) {
   }
   const real alpha = tv3, T = alpha * R2;
   return g3_coulomb(s, C0, C3, bf, bg, bh, T, alpha, Rv);
+}
+
+// G3_MD_xgVxCg for nat classical centres at once (cat: 3 x nat bohr):
+// the Hermite vectors W_d do not depend on the attracting centre, so they
+// are folded once and only the Coulomb sum runs per centre; out[ia] equals
+// g3_vxc(s, C_ia).
+NX_BIG void g3_vxc_multi(const G3& s, int nat, const double* cat, real* out) {
+  const real s1 = s.S1, s2 = s.S2, g = s.gam12;
+  const real p1 = s.pr[0].p, p2 = s.pr[1].p, c1 = s.C1, c2 = s.C2;
+  const real tv1 = s2 + g;
+  const real tv2 = s1 * s2 + s1 * g + s2 * g;
+  const real tv3 = tv2 / tv1;
+  const real x = kPiT / tv1;
+  const real C3 = sqrt(x * x * x) * (R_(2.0) * kPiT / tv3);
+  const real C0 = pow(kPiT / s.xsum, R_(1.5));
+  const real bf = (s1 * s2 + s1 * g) / tv2 * (p1 / (p1 + c1));
+  const real bg = (s2 * g) / tv2 * (p2 / (p2 + c2));
+  const real bh = (s1 * s2 + s1 * g) / tv2 * (c1 / (p1 + c1)) +
+                    (s2 * g) / tv2 * (c2 / (p2 + c2));
+  const real alpha = tv3;
+  bool all_s = true;
+  for (int i = 0; i < 3; i++)
+    for (int d = 0; d < 3; d++) all_s = all_s && s.T[i][d] == 0;
+  real W[3][LTOT + 1];
+  int n[3] = {0, 0, 0};
+  real w = R_(1.0);
+  if (all_s) {
+    for (int d = 0; d < 3; d++) {
+      const real wd = ((s.pr[0].K[d] * s.pr[1].K[d]) * s.pr[2].K[d]) * s.D[d][0];
+      w = d == 0 ? wd : w * wd;
+    }
+  } else {
+    for (int d = 0; d < 3; d++) g3_wvec(s, d, bf, bg, bh, W[d], &n[d]);
+  }
+  for (int ia = 0; ia < nat; ia++) {
+    real Rv[3], R2 = R_(0.0);
+    for (int d = 0; d < 3; d++) {
+      real sm = ((s1 * s2 + s1 * g) / tv2) * s.Sm1[d] + ((s2 * g) / tv2) * s.Sm2[d];
+      Rv[d] = sm - (real)cat[3 * ia + d];
+      R2 += Rv[d] * Rv[d];
+    }
+    const real T = alpha * R2;
+    if (all_s) {
+      double F[1];
+      boys(0, (double)T, F);
+      out[ia] = C0 * C3 * (w * (real)F[0]);
+    } else {
+      out[ia] = C0 * C3 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], T, alpha, Rv);
+    }
+  }
 }
 
 // G3_MD_xgVeeg (XC1_G3_MD.f:1376-1675): 1/|r1 - r2|

@@ -60,6 +60,7 @@ def _declare(L):
         "neoxc_calc_gam_ee": (I, [i64, i64, i64, vp, vp, vp, vp, vp, vp]),
         "neoxc_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
         "neoxc_gam3_ic1": (I, [i64] * 8 + [d] + [vp] * 16),
+        "neoxc_gam3_ic1_opts": (I, [i64] * 9 + [d] + [vp] * 17),
         "neoxc_rxchfne_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
         "neoxc_gam3_dscf": (I, [i64] * 8 + [d] + [vp] * 20),
         "neoxc_gam2_dscf": (I, [i64] * 8 + [d] + [vp] * 23),
@@ -262,13 +263,19 @@ def rxchfne_gam2_ic1(s: NeoSystem, nchunks: int = 1):
     return g, gx
 
 
-def gam3_ic1(s: NeoSystem, nchunks: int = 1) -> np.ndarray:
-    """gam3_IC1_OMP.f GAM3_IC1 -> GM3ICR."""
+def gam3_ic1(s: NeoSystem, nchunks: int = 1, mixed: bool = False, screen: bool = False,
+             timing: bool = False):
+    """gam3_IC1_OMP.f GAM3_IC1 -> GM3ICR.  mixed: four-particle terms with
+    FP32 tables (FP64 Boys, seeds, sums); screen: skip primitive pairs below
+    the 1e-12 Schwarz-type estimate; timing: also return the device seconds
+    of the build."""
     g = np.empty(s.ng3)
     keep, ptrs = _sysargs(s)
-    _check(lib().neoxc_gam3_ic1(nchunks, s.nebf, s.npebf, s.npbf, s.ng3, s.ng3prm,
-                                s.nat, s.ngtg, s.pmass, *ptrs, _p(g)))
-    return g
+    sec = np.zeros(1)
+    opts = (8 if mixed else 0) | (64 if screen else 0)
+    _check(lib().neoxc_gam3_ic1_opts(opts, nchunks, s.nebf, s.npebf, s.npbf, s.ng3, s.ng3prm,
+                                     s.nat, s.ngtg, s.pmass, *ptrs, _p(g), _p(sec)))
+    return (g, float(sec[0])) if timing else g
 
 
 def gam3_dscf(s: NeoSystem, DE, DP, focke=None, fockp=None, nchunks: int = 1):
