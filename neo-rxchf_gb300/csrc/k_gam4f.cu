@@ -470,6 +470,12 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
   uint32_t phase = 0;
   bool ok = true;
   const uint32_t idesc = tc::instr_desc();
+  // each 64-wide K tile is accumulated in TMEM (FP32) and then folded into
+  // this thread's FP64 row of the result
+  double acc[tc::kTileN];
+#pragma unroll
+  for (int i = 0; i < tc::kTileN; i++) acc[i] = 0.0;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
   for (long long kt = kbeg; kt < kend && ok; kt += tc::kTileK) {
     for (int e = tid; e < tc::kTileM * tc::kTileK; e += tc::kThreads) {
       const int r = e / tc::kTileK, k = e - r * tc::kTileK;
@@ -500,7 +506,7 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
       for (int st = 0; st < tc::kTileK / 8; st++) {
         const uint32_t o = st * 256;   // two 128-byte core matrices per K step
         tc::mma_tf32(tmem, tc::smem_desc(ah + o), tc::smem_desc(bh + o), idesc,
-                     (kt > kbeg || st > 0) ? 1 : 0);
+                     st > 0 ? 1 : 0);
         tc::mma_tf32(tmem, tc::smem_desc(ah + o), tc::smem_desc(bl + o), idesc, 1);
         tc::mma_tf32(tmem, tc::smem_desc(al + o), tc::smem_desc(bh + o), idesc, 1);
       }
@@ -509,26 +515,30 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
     ok = __syncthreads_and(tc::mbar_wait(mb, phase) ? 1 : 0) != 0;
     phase ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+#pragma unroll
+      for (int c = 0; c < tc::kTileN / 16; c++) {
+        float v[16];
+        tc::tmem_ld16(trow + (uint32_t)(c * 16), v);
+#pragma unroll
+        for (int i = 0; i < 16; i++) acc[c * 16 + i] += (double)v[i];
+      }
+    }
+    // every lane's reads are done before the next tile's MMA overwrites TMEM
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
   }
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);
   } else {
     const long long row = m0 + warp * 32 + lane;
     double* out = C + (long long)blockIdx.z * split_stride;
-    const bool any = kend > kbeg;
-    for (int c = 0; c < tc::kTileN / 16; c++) {
-      float v[16];
-      if (any) {
-        tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
-      } else {
-        for (int i = 0; i < 16; i++) v[i] = 0.0f;
+    if (row < M)
+#pragma unroll
+      for (int i = 0; i < tc::kTileN; i++) {
+        const long long n = n0 + i;
+        if (n < N) out[row * ldc + n] = alpha * acc[i];
       }
-      if (row < M)
-        for (int i = 0; i < 16; i++) {
-          const long long n = n0 + c * 16 + i;
-          if (n < N) out[row * ldc + n] = alpha * (double)v[i];
-        }
-    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
