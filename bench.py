@@ -61,7 +61,10 @@ def parse():
     ap.add_argument("--nebf", type=int, default=NEBF)
     ap.add_argument("--npbf", type=int, default=NPBF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1", "gam3"],
+    ap.add_argument("--small", action="store_true",
+                    help="with --only gam3 / factored_tc: a small case (for ncu captures)")
+    ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1", "gam3",
+                                       "factored_tc"],
                     default=None,
                     help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
@@ -266,19 +269,20 @@ FACTORED_LAUNCHES = 14      # kernels of one factorised build (k_gam4f.cu)
 
 
 def time_factored(neoxc, torch, dev, stream, ne, np_, d_gee, d_g2s, d_DE, d_DP,
-                  warmup=2, steps=5):
+                  warmup=2, steps=5, fn=None):
     f64 = torch.float64
+    fn = fn or neoxc.dev_gam4_fock_factored
     d_fe = torch.zeros(ne * ne, dtype=f64, device=dev)
     d_fp = torch.zeros(np_ * np_, dtype=f64, device=dev)
     d_E = torch.zeros(1, dtype=f64, device=dev)
     sp = stream.cuda_stream
     for _ in range(warmup):
-        neoxc.dev_gam4_fock_factored(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
+        fn(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
     torch.cuda.synchronize(dev)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
     for _ in range(steps):
-        neoxc.dev_gam4_fock_factored(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
+        fn(sp, ne, np_, d_gee, d_g2s, d_DE, d_DP, d_fe, d_fp, d_E)
     b.record(stream)
     torch.cuda.synchronize(dev)
     return a.elapsed_time(b) / steps, float(d_E.item())
@@ -330,6 +334,8 @@ def factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
     lDP = torch.tensor(np.ascontiguousarray(basis.random_density(pl, 1, 12, 1.0).ravel(order="F")),
                        dtype=f64, device=dev)
     lms, lE = time_factored(neoxc, torch, dev, stream, nl, pl, lgee, lg2s, lDE, lDP)
+    tms, tE = time_factored(neoxc, torch, dev, stream, nl, pl, lgee, lg2s, lDE, lDP,
+                            fn=neoxc.dev_gam4_fock_factored_tc)
     table_bytes = 8 * n4 * pl * pl
     # GAM_2s is read twice (G = DP.GAM_2s, fockp = GAM_2s.W): the HBM floor
     hbm_bytes = 2 * table_bytes
@@ -342,10 +348,52 @@ def factored_section(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
                                  "peak": peak,
                                  "frac": (hbm_bytes / (lms * 1e-3) / 1e9) / peak if peak else None,
                                  "note": "whole build timed; bytes = the two passes over GAM_2s"},
-                    "E": lE}
+                    "E": lE,
+                    "tensor_core": {
+                        "api": "neoxc_dev_gam4_fock_factored_tc (tcgen05 kind::tf32, 3xTF32 "
+                               "products, FP32 accumulation per 64-wide K tile, FP64 across "
+                               "tiles; GAM_2s passes, traces, gradients FP64)",
+                        "ms_per_build": tms,
+                        "speedup_vs_fp64_build": lms / tms,
+                        "E": tE, "E_rel_err_vs_fp64": abs(tE - lE) / max(abs(lE), 1e-300),
+                        "roofline": {"bound": "hbm", "algorithmic_bytes": hbm_bytes,
+                                     "achieved": hbm_bytes / (tms * 1e-3) / 1e9, "unit": "GB/s",
+                                     "peak": peak,
+                                     "frac": (hbm_bytes / (tms * 1e-3) / 1e9) / peak
+                                     if peak else None}}}
     del lg2s, lgee
     torch.cuda.empty_cache()
     return out
+
+
+def factored_tc_only(neoxc, torch, dev, ne, np_):
+    """FP64 and tensor-core factorised gam_4 builds on device-generated
+    pair-symmetric tables (ne^4 np^2 GAM_2s), timed with CUDA events."""
+    f64 = torch.float64
+    stream = torch.cuda.current_stream(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2025)
+    n4 = ne ** 4
+    g2s = torch.empty(n4 * np_ * np_, dtype=f64, device=dev)
+    for p in range(np_ * np_):
+        t = torch.rand((ne,) * 4, generator=gen, dtype=f64, device=dev)
+        g2s[p * n4:(p + 1) * n4].view((ne,) * 4).copy_(0.5 * (t + t.permute(2, 3, 0, 1)))
+    t = torch.rand((ne,) * 4, generator=gen, dtype=f64, device=dev)
+    gee = (0.5 * (t + t.permute(2, 3, 0, 1))).contiguous().view(-1)
+    from neoxc import basis
+    DE = torch.tensor(np.ascontiguousarray(basis.random_density(ne, 5, 11, 2.0).ravel(order="F")),
+                      dtype=f64, device=dev)
+    DP = torch.tensor(np.ascontiguousarray(basis.random_density(np_, 1, 12, 1.0).ravel(order="F")),
+                      dtype=f64, device=dev)
+    ms, E = time_factored(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP)
+    tms, tE = time_factored(neoxc, torch, dev, stream, ne, np_, gee, g2s, DE, DP,
+                            fn=neoxc.dev_gam4_fock_factored_tc)
+    hbm = 2 * 8 * n4 * np_ * np_
+    peak = read_hbm_peak()
+    return {"nebf": ne, "npbf": np_, "fp64_ms": ms, "tc_ms": tms, "E_fp64": E, "E_tc": tE,
+            "E_rel_err": abs(tE - E) / max(abs(E), 1e-300),
+            "hbm_floor_ms": hbm / (peak * 1e9) * 1e3,
+            "tc_frac_of_hbm_floor": (hbm / (peak * 1e9) * 1e3) / tms}
 
 
 def open_shell_section(neoxc, torch, dev, stream):
@@ -728,7 +776,12 @@ def main():
         print(json.dumps(config1_section(neoxc)))
         return
     if args.only == "gam3":
-        print(json.dumps(gam3_section(neoxc)))
+        kw = dict(CONFIG1, nebf=6, npbf=4) if args.small else None
+        print(json.dumps(gam3_section(neoxc, kw)))
+        return
+    if args.only == "factored_tc":
+        print(json.dumps(factored_tc_only(neoxc, torch, dev, 24 if args.small else 60,
+                                          8 if args.small else 24)))
         return
     ne, np_ = args.nebf, args.npbf
     ng4 = ne ** 8 * np_ ** 2

@@ -430,6 +430,10 @@ int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
 #define NEOXC_SCF_GUESS_ELEC 32    /* DE (XCHF: guess_elec, xcscf.f:660) or
                                       DAE, DBE (XCUHF: guess_A_elec) from the
                                       electronic core Hamiltonian */
+#define NEOXC_SCF_SOSCF 128        /* second-order steps on the electronic
+                                      orbitals (soscf.f, xcscf.f:459-485)
+                                      once the orbital gradient is below 1;
+                                      exclusive with NEOXC_SCF_DIIS */
 #define NEOXC_SCF_SCREEN 64        /* skip gam_3 (bra, ket) primitive pairs
                                       whose Schwarz-type estimate is below
                                       1e-12 (new; the reference evaluates

@@ -1487,8 +1487,11 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
   RC(need((options & ~(int64_t)(NEOXC_SCF_GUESS_PROT | NEOXC_SCF_DIIS |
                                 NEOXC_SCF_GAM4_ELEMENT | NEOXC_SCF_MIXED |
                                 NEOXC_SCF_MIXED_GAM2 | NEOXC_SCF_GUESS_ELEC |
-                                NEOXC_SCF_SCREEN)) == 0,
+                                NEOXC_SCF_SCREEN | NEOXC_SCF_SOSCF)) == 0,
           "options"));
+  const bool soscf = (options & NEOXC_SCF_SOSCF) != 0 && nelec > 1 && nelec / 2 < nebf;
+  RC(need(!((options & NEOXC_SCF_SOSCF) && (options & NEOXC_SCF_DIIS)),
+          "NEOXC_SCF_SOSCF and NEOXC_SCF_DIIS are exclusive"));
   const int mixed = (options & NEOXC_SCF_MIXED) ? 1 : 0;
   const int mixed_gam2 = (options & NEOXC_SCF_MIXED_GAM2) ? 1 : 0;
   if (nebf > kScfMaxN || npbf > kScfMaxN)
@@ -1588,9 +1591,16 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
     CU(cudaMemcpyAsync(dDP.p, DP, sizeof(double) * p2, cudaMemcpyHostToDevice, s));
   }
   double* d_en = en.as<double>();
-  // final MOs and orbital energies (ROOTHAN's VECE/EE, VECP/EP) when asked
-  const bool want_mo = CE || CP || EE || EP;
+  // final MOs and orbital energies (ROOTHAN's VECE/EE, VECP/EP) when asked,
+  // and always for the second-order steps (they rotate VECE)
+  const bool want_mo = CE || CP || EE || EP || soscf;
   DBuf dCE, dCP, dEE, dEP;
+  DBuf sow, sost;
+  if (soscf) {
+    RC(dalloc(sow, sizeof(double) * soscf_doubles(ne, (int)(nelec / 2), (int)maxit), s));
+    RC(dalloc(sost, sizeof(int) * 4, s));
+    CU(cudaMemsetAsync(sost.p, 0, sizeof(int) * 4, s));
+  }
   if (want_mo) {
     RC(dalloc(dCE, sizeof(double) * e2, s));
     RC(dalloc(dCP, sizeof(double) * p2, s));
@@ -1644,9 +1654,16 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
     if (diis)
       CU(launch_diis(ne, fe.as<double>(), dDE.as<double>(), Se.as<double>(),
                      dwork.as<double>(), sts + 4, nullptr, s));
+    // second-order step (xcscf.f:459-485) from the second iteration on; when
+    // it moves the orbitals, the diagonalisation below is skipped on the
+    // device (state[1])
+    if (soscf && it > 1)
+      CU(launch_soscf(ne, noccE, fe.as<double>(), dCE.as<double>(), dEE.as<double>(), prefE,
+                      dDE.as<double>(), sost.as<int>(), sow.as<double>(), (int)maxit, s));
     CU(launch_roothan(ne, fe.as<double>(), Xe.as<double>(), 0, noccE, prefE,
                       dDE.as<double>(), want_mo ? dEE.as<double>() : nullptr,
-                      want_mo ? dCE.as<double>() : nullptr, sts + 0, s));
+                      want_mo ? dCE.as<double>() : nullptr, sts + 0, s,
+                      soscf ? sost.as<int>() + 1 : nullptr));
     CU(launch_dendif(ne, np, dDE.as<double>(), DE0.as<double>(), dDP.as<double>(),
                      DP0.as<double>(), d_en, s));
     double h[kScfSlots];

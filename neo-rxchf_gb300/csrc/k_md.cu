@@ -74,6 +74,14 @@ __device__ __forceinline__ void perm3(const P* X, int a, int b, int c, P* Y) {
 // so one primitive tuple is split into ng + ng^2 independent work items
 // (gi < ng: single-geminal term k = gi; else the pair (k,l)) that the lanes
 // of a warp share.
+//
+// Four of the terms have no geminal on electron 1 -- xgTE and xgVEC (bra
+// geminal e2-p), xgTEg3 and xgVECg2 (both geminals e2-p) -- so they factor
+// exactly into electron 1's core Hamiltonian times a two-particle geminal
+// overlap of (e2, p): their contracted sum is H1(i1,j1) W2(i2,j2,ip,jp) with
+//   W2 = sum c^4 [2 sum_k b_k G2xggs(g_k, 0) + sum_kl b_k b_l G2xggs(g_k, g_l)],
+// which gam2_raw_kernel adds once per contracted tuple, in FP64 on both
+// paths (separable_gam2); the per-primitive items below omit them.
 template <class P, class G3T>
 __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
                                 G3T& st, int gi, double& ansE, double& ansS) {
@@ -109,14 +117,12 @@ __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
   if (gi < ng) {
     const int ik = gi;
     gam6(g, A23, (R)gm[ik], -1, zero);
-    g3_setup_pairs(st, A, B, pr, g, 2);
-    double xgTE = (double)g3_ke(st, zero, one);
-    double xgVEC = vxc_sum(-1.0);
+    g3_setup_pairs(st, A, B, pr, g, 0);
     double xgVEE = md::underflow((double)g3_vee(st));
     g3_setup_pairs(st, A132, B132, pr132, g, 0);
     double xgVEP = -md::underflow((double)g3_vee(st));
-    // 2 (gTE + gVEC + gVEP) + 4 gVEE / 2
-    ansE = 2.0 * (b[ik] * xgTE + b[ik] * xgVEC + b[ik] * xgVEP) + 4.0 * (b[ik] * xgVEE) * 0.5;
+    // 2 (gTE + gVEC + gVEP) + 4 gVEE / 2, gTE and gVEC in separable_gam2
+    ansE = 2.0 * (b[ik] * xgVEP) + 4.0 * (b[ik] * xgVEE) * 0.5;
     ansS = 0.0;
     return;
   }
@@ -139,11 +145,7 @@ __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
   gam6(g, A23, gk, B13, gl);
   g3_setup_pairs(st, A, B, pr, g, 2);
   double xgTEg2 = (double)g3_ke(st, gl, one);
-  // A23, B23
-  gam6(g, A23, gk, B23, gl);
-  g3_setup_pairs(st, A, B, pr, g, 2);
-  double xgTEg3 = (double)g3_ke(st, zero, one);
-  double xgVECg2 = vxc_sum(-1.0);
+  // A23, B23: xgTEg3 and xgVECg2 are separable (separable_gam2)
   // A13, B13
   gam6(g, A13, gk, B13, gl);
   g3_setup_pairs(st, A, B, pr, g, 0);
@@ -156,10 +158,10 @@ __device__ void xcalc_gam2_item(const P* A, const P* B, const DevSystem& S,
   g3_setup_pairs(st, A132, B132, pr132, g, 0);
   double xgVEPg2 = -md::underflow((double)g3_vee(st));
   // gTPg + gVPCg + gTEg1 + gTEg3 + 2 (gVEPg1 + gVECg1) + gTEg2 + gVEPg2 +
-  // gVECg2 + 2 gVEEg1 / 2 + 2 gVEEg2 / 2
-  ansE = bb * xgTPg + bb * xgVPCg + bb * xgTEg1 + bb * xgTEg3 +
+  // gVECg2 + 2 gVEEg1 / 2 + 2 gVEEg2 / 2, gTEg3 and gVECg2 in separable_gam2
+  ansE = bb * xgTPg + bb * xgVPCg + bb * xgTEg1 +
          2.0 * (bb * xgVEPg1 + bb * xgVECg1) + bb * xgTEg2 + bb * xgVEPg2 +
-         bb * xgVECg2 + 2.0 * (bb * xgVEEg1) * 0.5 + 2.0 * (bb * xgVEEg2) * 0.5;
+         2.0 * (bb * xgVEEg1) * 0.5 + 2.0 * (bb * xgVEEg2) * 0.5;
   ansS = bb * xgsg;
 }
 
@@ -200,6 +202,44 @@ __device__ __forceinline__ md32::Prim to_prim32(const DevPrim& d) {
     p.l[k] = d.l[k];
   }
   return p;
+}
+
+// The separable part of one contracted XCHF gam_2 tuple (see
+// xcalc_gam2_item): H1(i1,j1) W2(i2,j2,ip,jp), FP64, summed by the warp.
+// H1 = sum c c [T - sum_C Z V_C] (gfke, gfvec), W2 as above (G2_MD_xggs).
+__device__ double separable_gam2(const DevSystem& S, int ic1, int jc1, int ic2, int jc2,
+                                 int ip, int jp, int lane) {
+  const int s1 = S.kpestr[ic1], n1 = S.kpeend[ic1] - s1 + 1;
+  const int t1 = S.kpestr[jc1], m1 = S.kpeend[jc1] - t1 + 1;
+  const int s2 = S.kpestr[ic2], n2 = S.kpeend[ic2] - s2 + 1;
+  const int t2 = S.kpestr[jc2], m2 = S.kpeend[jc2] - t2 + 1;
+  const int ng = S.ngtg;
+  double h = 0.0, w = 0.0;
+  for (int q = lane; q < n1 * m1; q += 32) {
+    const int a = s1 + q / m1, bq = t1 + q % m1;
+    const Prim A = to_prim(S.eprim[a]), B = to_prim(S.eprim[bq]);
+    double v = md::gfke(A, B, 1.0);
+    for (int ia = 0; ia < S.nat; ia++) v = v - S.zan[ia] * md::gfvec(A, B, S.cat + 3 * ia);
+    h = h + v * (S.eprim[a].coef * S.eprim[bq].coef);
+  }
+  const Prim Pa = to_prim(S.pprim[ip]), Pb = to_prim(S.pprim[jp]);
+  const int nit = ng + ng * ng;
+  for (int q = lane; q < n2 * m2 * nit; q += 32) {
+    const int it = q / (n2 * m2), u = q - it * (n2 * m2);
+    const int a = s2 + u / m2, bq = t2 + u % m2;
+    const Prim A = to_prim(S.eprim[a]), B = to_prim(S.eprim[bq]);
+    double v;
+    if (it < ng) {
+      v = 2.0 * S.bgem[it] * md::g2_xggs(A, Pa, B, Pb, S.ggem[it], 0.0);
+    } else {
+      const int k = (it - ng) / ng, l = (it - ng) - k * ng;
+      v = S.bgem[k] * S.bgem[l] * md::g2_xggs(A, Pa, B, Pb, S.ggem[k], S.ggem[l]);
+    }
+    w = w + v * (S.eprim[a].coef * S.eprim[bq].coef);
+  }
+  h = warp_sum(h);
+  w = warp_sum(w);
+  return h * w * (S.pprim[ip].coef * S.pprim[jp].coef);
 }
 
 // ---- GAM_ee: warp per contracted (iec1,jec1,iec2,jec2) ----------------------
@@ -295,6 +335,7 @@ gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
   }
   o1 = warp_sum(o1);
   o2 = warp_sum(o2);
+  if (!RX) o1 += separable_gam2(S, ic1, jc1, ic2, jc2, ip, jp, lane);
   if (lane == 0) {
     x1[w] = o1;
     x2[w] = o2;

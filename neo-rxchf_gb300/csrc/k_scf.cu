@@ -624,7 +624,9 @@ __global__ void roothan_kernel(int n, const double* __restrict__ F,
                                const double* __restrict__ X, int first, int nocc,
                                double prefac, double* __restrict__ D,
                                double* __restrict__ evals,
-                               double* __restrict__ Cout, int* status) {
+                               double* __restrict__ Cout, int* status,
+                               const int* __restrict__ skip) {
+  if (skip && *skip) return;   // a second-order step already gave D (soscf_kernel)
   extern __shared__ double smem[];
   EigSmem m = carve(n, smem);
   // T = F X  (row-major T[i][j])
@@ -844,6 +846,223 @@ __global__ void diis_kernel(int n, double* __restrict__ F,
   }
 }
 
+// ---- second-order SCF step (soscf.f SOGRAD / SOHESS / SONEWT / SOTRAN,
+// driven as in xcscf.f:459-485) ---------------------------------------------
+// One CTA.  F: electronic Fock matrix (column-major; its lower triangle is
+// used, as pack_LT does), C: the current MO coefficients (column-major,
+// orbitals by ascending energy; rotated in place), EE: the orbital energies
+// of the last diagonalisation.  state[0] = ITSO (second-order steps taken
+// since the last reset), state[1] = 1 when this call replaced the
+// diagonalisation (D then holds prefac C_occ C_occ^T), else 0.  work:
+// GRAD, PGRAD, DISPLI, HSTART, DISPLN, DGRADI, UPDTI (NPR each) and the
+// (DISPL, DGRAD, UPDT) history the reference keeps on unit 15.
+__device__ double block_dot(const double* a, const double* b, int n, double* red) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v += a[i] * b[i];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) t += red[w];
+  __syncthreads();
+  return t;   // every thread
+}
+
+__global__ void soscf_kernel(int n, int na, const double* __restrict__ F,
+                             double* __restrict__ C, const double* __restrict__ EE,
+                             double prefac, double* __restrict__ D, int* __restrict__ state,
+                             double* __restrict__ work, int maxit) {
+  extern __shared__ double sm[];
+  double* G = sm;                  // [n][n] rotation, G[i*n + j] = G(i,j)
+  double* T = G + n * n;           // [n][n] scratch
+  double* FC = T + n * n;          // [n][na] F C_occ
+  double* red = FC + n * na;       // 64 reduction slots
+  const int nv = n - na, npr = na * nv;
+  double* grad = work;
+  double* pgrad = grad + npr;
+  double* displ = pgrad + npr;     // DISPLI
+  double* hst = displ + npr;       // HSTART
+  double* dn = hst + npr;          // DISPLN
+  double* dg = dn + npr;           // DGRADI
+  double* up = dg + npr;           // UPDTI
+  double* hist = up + npr;         // [k][3][npr]
+  const int tid = threadIdx.x;
+  auto Fs = [&](int i, int k) { return i >= k ? F[i + n * k] : F[k + n * i]; };
+  // SOGRAD: GRAD(jo, jv) = -C_jv^T F C_jo, ORBGRD = max |GRAD|
+  for (int e = tid; e < n * na; e += blockDim.x) {
+    const int i = e / na, jo = e - i * na;
+    double acc = 0.0;
+    for (int k = 0; k < n; k++) acc += Fs(i, k) * C[k + n * jo];
+    FC[e] = acc;
+  }
+  __syncthreads();
+  double gmax = 0.0;
+  for (int q = tid; q < npr; q += blockDim.x) {
+    const int jo = q / nv, jv = na + (q - jo * nv);
+    double acc = 0.0;
+    for (int i = 0; i < n; i++) acc += FC[i * na + jo] * C[i + n * jv];
+    grad[q] = -acc;
+    gmax = fmax(gmax, fabs(acc));
+  }
+  for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_down_sync(0xffffffffu, gmax, o));
+  __syncthreads();
+  if ((tid & 31) == 0) red[tid >> 5] = gmax;
+  __syncthreads();
+  double orbgrd = 0.0;
+  for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) orbgrd = fmax(orbgrd, red[w]);
+  __syncthreads();
+  int itso = state[0];
+  const double sogtol = 1.0;        // xcscf.f:330
+  if (!(orbgrd < sogtol || itso > 0)) {
+    if (tid == 0) state[1] = 0;
+    return;
+  }
+  // SOHESS on the first step: HSTART = 1/(e_v - e_o), capped at 200
+  if (itso == 0)
+    for (int q = tid; q < npr; q += blockDim.x) {
+      const int jo = q / nv, jv = na + (q - jo * nv);
+      const double de = EE[jv] - EE[jo];
+      hst[q] = de > 0.5e-2 ? 1.0 / de : 200.0;
+    }
+  itso += 1;
+  __syncthreads();
+  // SONEWT
+  for (int q = tid; q < npr; q += blockDim.x) dn[q] = hst[q] * grad[q];
+  __syncthreads();
+  const double small = 1.0e-3 * 1.0e-5;
+  bool update = itso != 1;
+  if (update && orbgrd < small) {
+    itso -= 1;
+    update = false;
+  }
+  if (update) {
+    for (int q = tid; q < npr; q += blockDim.x) {
+      dg[q] = grad[q] - pgrad[q];
+      up[q] = hst[q] * dg[q];
+    }
+    __syncthreads();
+    for (int k = 0; k < itso - 2 && k < maxit; k++) {
+      const double* Dk = hist + (size_t)k * 3 * npr;
+      const double* Gk = Dk + npr;
+      const double* Uk = Gk + npr;
+      double s1 = block_dot(Dk, Gk, npr, red), s2 = block_dot(Gk, Uk, npr, red);
+      const double s3 = block_dot(Dk, grad, npr, red), s4 = block_dot(Uk, grad, npr, red);
+      const double s5 = block_dot(Dk, dg, npr, red), s6 = block_dot(Uk, dg, npr, red);
+      s1 = 1.0 / s1;
+      s2 = 1.0 / s2;
+      const double t = 1.0 + s1 / s2, t2 = s1 * s3, t4 = s1 * s5;
+      const double t1 = t * t2 - s1 * s4, t3 = t * t4 - s1 * s6;
+      for (int q = tid; q < npr; q += blockDim.x) {
+        dn[q] += t1 * Dk[q] - t2 * Uk[q];
+        up[q] += t3 * Dk[q] - t4 * Uk[q];
+      }
+      __syncthreads();
+    }
+    double s1 = block_dot(displ, dg, npr, red), s2 = block_dot(dg, up, npr, red);
+    const double s3 = block_dot(displ, grad, npr, red), s4 = block_dot(up, grad, npr, red);
+    s1 = 1.0 / s1;
+    s2 = 1.0 / s2;
+    const double t = 1.0 + s1 / s2, t2 = s1 * s3, t1 = t * t2 - s1 * s4;
+    for (int q = tid; q < npr; q += blockDim.x) dn[q] += t1 * displ[q] - t2 * up[q];
+    // the history entry of this step: the previous displacement, the
+    // gradient change and its Hessian-updated image
+    const int slot = itso - 2;
+    if (slot >= 0 && slot <= maxit) {
+      double* Hk = hist + (size_t)slot * 3 * npr;
+      for (int q = tid; q < npr; q += blockDim.x) {
+        Hk[q] = displ[q];
+        Hk[npr + q] = dg[q];
+        Hk[2 * npr + q] = up[q];
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = tid; q < npr; q += blockDim.x) displ[q] = -dn[q];
+  __syncthreads();
+  const double sqcdf = sqrt(block_dot(displ, displ, npr, red) / npr);
+  if (sqcdf > 1.0 && itso > 5) itso = 0;     // reset on a huge rotation
+  if (sqcdf > 0.1) {
+    const double scal = sqrt(0.1 / sqcdf);
+    for (int q = tid; q < npr; q += blockDim.x) displ[q] *= scal;
+  }
+  __syncthreads();
+  // SOTRAN: G = 1 + X (X antisymmetric from the displacement), columns
+  // orthonormalised in order, C <- C G
+  for (int e = tid; e < n * n; e += blockDim.x) G[e] = 0.0;
+  __syncthreads();
+  for (int q = tid; q < npr; q += blockDim.x) {
+    const int j = q / nv, i = na + (q - j * nv);
+    G[j * n + i] = displ[q];
+    G[i * n + j] = -displ[q];
+  }
+  __syncthreads();
+  if (orbgrd <= 1.0e-20) {   // second-order term of the exponential (SOTRAN)
+    for (int e = tid; e < na * na; e += blockDim.x) {
+      const int i = e / na, j = e - i * na;
+      if (j < i) continue;
+      double dum = 0.0;
+      for (int k = 0; k < nv; k++) dum += displ[nv * i + k] * displ[nv * j + k];
+      dum *= -0.5;
+      G[i * n + j] += dum;   // G(I,J) and G(J,I): twice on the diagonal, as SOTRAN
+      G[j * n + i] += dum;
+    }
+    for (int e = tid; e < nv * nv; e += blockDim.x) {
+      const int i = e / nv, j = e - i * nv;
+      if (j < i) continue;
+      double dum = 0.0;
+      for (int k = 0; k < na; k++) dum += displ[nv * k + i] * displ[nv * k + j];
+      dum *= -0.5;
+      G[(na + i) * n + na + j] += dum;
+      G[(na + j) * n + na + i] += dum;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += blockDim.x) G[i * n + i] += 1.0;
+  __syncthreads();
+  for (int i = 0; i < n; i++) {   // Gram-Schmidt on the columns G(:, i)
+    if (tid == 0) {
+      double d = 0.0;
+      for (int k = 0; k < n; k++) d += G[k * n + i] * G[k * n + i];
+      red[0] = 1.0 / sqrt(d);
+    }
+    __syncthreads();
+    const double sc = red[0];
+    for (int k = tid; k < n; k += blockDim.x) G[k * n + i] *= sc;
+    __syncthreads();
+    for (int j = i + 1 + tid; j < n; j += blockDim.x) {
+      double d = 0.0;
+      for (int k = 0; k < n; k++) d += G[k * n + i] * G[k * n + j];
+      for (int k = 0; k < n; k++) G[k * n + j] -= d * G[k * n + i];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;    // T(i,j) = sum_k C(i,k) G(k,j)
+    double acc = 0.0;
+    for (int k = 0; k < n; k++) acc += C[i + n * k] * G[k * n + j];
+    T[e] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;
+    C[i + n * j] = T[e];
+  }
+  for (int q = tid; q < npr; q += blockDim.x) pgrad[q] = grad[q];
+  __syncthreads();
+  // make_density: D = prefac sum_occ C_o C_o^T
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;
+    double acc = 0.0;
+    for (int o = 0; o < na; o++) acc += prefac * T[i * n + o] * T[j * n + o];
+    D[i + n * j] = acc;
+  }
+  if (tid == 0) {
+    state[0] = itso;
+    state[1] = 1;
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_scf_onebody(const DevSystem& S, double* Se, double* Sp,
@@ -913,14 +1132,31 @@ cudaError_t launch_inv_sqrt(int n, const double* S, double* X, int* status,
 
 cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
                            int nocc, double prefac, double* D, double* evals,
-                           double* C, int* status, cudaStream_t s) {
+                           double* C, int* status, cudaStream_t s, const int* skip) {
   if (n < 1 || n > kScfMaxN || first < 0 || nocc < 1 || first + nocc > n)
     return cudaErrorInvalidValue;
   const size_t smem = eig_smem_bytes(n);
   cudaError_t e = eig_attr((const void*)roothan_kernel, smem);
   if (e != cudaSuccess) return e;
   roothan_kernel<<<1, 256, smem, s>>>(n, F, X, first, nocc, prefac, D, evals, C,
-                                      status);
+                                      status, skip);
+  return cudaGetLastError();
+}
+
+size_t soscf_doubles(int n, int na, int maxit) {
+  const size_t npr = (size_t)na * (n - na);
+  return 7 * npr + 3 * npr * (size_t)(maxit + 1);
+}
+
+cudaError_t launch_soscf(int n, int na, const double* F, double* C, const double* EE,
+                         double prefac, double* D, int* state, double* work, int maxit,
+                         cudaStream_t s) {
+  if (n < 2 || n > kScfMaxN || na < 1 || na >= n) return cudaErrorInvalidValue;
+  const size_t smem = sizeof(double) * (2 * (size_t)n * n + (size_t)n * na) + 64 * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(soscf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  soscf_kernel<<<1, 256, smem, s>>>(n, na, F, C, EE, prefac, D, state, work, maxit);
   return cudaGetLastError();
 }
 

@@ -1160,7 +1160,8 @@ NX_BIG real pgike1(const Prim& A1, const Prim& A2, const Prim& B1,
   return (T[0] * S[1] * S[2]) + (S[0] * T[1] * S[2]) + (S[0] * S[1] * T[2]);
 }
 
-NX_HD real underflow(real x) { return fabs(x) < R_(1.0e-100) ? R_(0.0) : x; }
+// |x| < 1e-100 -> 0 (underflow.f:2-11); below FP32's range in the md32 instance
+NX_HD real underflow(real x) { return fabs((double)x) < 1.0e-100 ? R_(0.0) : x; }
 
 #undef R_
 }  // namespace MD_NS

@@ -255,7 +255,15 @@ cudaError_t launch_inv_sqrt(int n, const double* S, double* X, int* status,
                             cudaStream_t s);
 cudaError_t launch_roothan(int n, const double* F, const double* X, int first,
                            int nocc, double prefac, double* D, double* evals,
-                           double* C, int* status, cudaStream_t s);
+                           double* C, int* status, cudaStream_t s,
+                           const int* skip = nullptr);
+// One second-order SCF step on the electronic orbitals (soscf.f, as xcscf.f
+// drives it); state[1] = 1 when it replaced the diagonalisation (pass
+// state + 1 as launch_roothan's skip).  work = soscf_doubles(n, na, maxit).
+size_t soscf_doubles(int n, int na, int maxit);
+cudaError_t launch_soscf(int n, int na, const double* F, double* C, const double* EE,
+                         double prefac, double* D, int* state, double* work, int maxit,
+                         cudaStream_t s);
 // XCUHF (UHF_FOCK): one-body / HF terms of both spins and the proton
 // (energies into en[2..6], en[11]; en[7..9], en[12] zeroed), the
 // normalisation + UHF_Fock_correction, and DENDIF of alpha, beta, proton

@@ -450,20 +450,22 @@ SCF_SLOTS = ("E_total", "E_nuc", "E_ecore", "E_pcore", "E_ep", "E_ee", "E_gam1",
 
 def xchf_scf(s: NeoSystem, DE, DP=None, nucst=None, maxit: int = 100,
              gam4_element: bool = False, diis: bool = False, mixed=False,
-             screen: bool = False):
+             screen: bool = False, soscf: bool = False):
     """xcscf.f XCHF RHF SCF on the GPU (plain Roothaan, or DIIS).  DE: initial
     electronic density, or None for the core-Hamiltonian guess (guess_elec);
     DP: initial nuclear density, or None for the core-Hamiltonian guess
     (guess_prot).  mixed: False (all FP64), "gam3"
     (FP32 MD integrals for gam_3), True (FP32 for gam_1, gam_2 and gam_3).
     screen: skip gam_3 primitive (bra, ket) pairs whose Schwarz-type
-    estimate is below 1e-12 (NEOXC_SCF_SCREEN).  Returns a dict with the initial and
+    estimate is below 1e-12 (NEOXC_SCF_SCREEN).  soscf: the reference's
+    second-order steps on the electronic orbitals (NEOXC_SCF_SOSCF; not with
+    diis).  Returns a dict with the initial and
     final energetics (SCF_SLOTS names), the per-iteration history, the
     converged densities, the iteration count and the convergence flag."""
     ne, np_ = s.nebf, s.npbf
     opts = ((1 if DP is None else 0) | (2 if diis else 0) | (4 if gam4_element else 0)
             | (8 if mixed else 0) | (16 if mixed is True else 0) | (32 if DE is None else 0)
-            | (64 if screen else 0))
+            | (64 if screen else 0) | (128 if soscf else 0))
     de = np.zeros(ne * ne) if DE is None else _fmat(DE).copy()
     dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
     Ei, Ef = np.zeros(16), np.zeros(16)

@@ -91,6 +91,24 @@ def test_synthetic_scf_matches_oracle(nx, orc, kw):
         assert abs(g["final"]["E_total"] - r["E_total"]) <= 1e-9
 
 
+# examples/xchf/answer/XCHF.log:325-333: the reference's iteration energies
+# with its second-order steps (LSOSCF), iteration 1 .. 8
+XCHF_LOG_ITERATIONS = (-5.7303165793, -5.7737887409, -5.7779417176, -5.7800627999,
+                       -5.7800664080, -5.7800665092, -5.7800665094, -5.7800665094)
+
+
+def test_soscf_reproduces_reference_iterations(nx, xchf, golden_xchf):
+    """With the second-order steps (soscf.f SOGRAD / SOHESS / SONEWT /
+    SOTRAN, driven as xcscf.f:459-485) the device SCF follows the
+    reference's own iteration sequence: the same 8 iterations and every
+    printed energy of XCHF.log:325-333 to 1e-8 Eh."""
+    r = nx.xchf_scf(xchf["sys"], xchf["DE0"], soscf=True)
+    assert r["converged"] and r["niter"] == len(XCHF_LOG_ITERATIONS), r["niter"]
+    for k, E in enumerate(XCHF_LOG_ITERATIONS):
+        assert abs(r["history"][k, 0] - E) <= 1e-8, (k + 1, r["history"][k, 0], E)
+    assert abs(r["final"]["E_total"] - golden_xchf["final"]["E_TOTAL"]) <= 1e-9
+
+
 def test_diis_converges_to_same_state_faster(nx, xchf, xchf_gpu_scf, golden_xchf):
     """Pulay DIIS on the electronic Fock matrix (no reference counterpart):
     same converged energy, fewer iterations than plain Roothaan."""
