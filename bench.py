@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--small", action="store_true",
                     help="with --only gam3 / factored_tc: a small case (for ncu captures)")
     ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1", "gam3",
-                                       "factored_tc"],
+                                       "factored_tc", "gam3_batch"],
                     default=None,
                     help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
@@ -587,6 +587,7 @@ def scf_section(neoxc, with_cpu: bool):
     out["xcuhf"] = xcuhf_scf_section(neoxc)
     out["rx"] = rx_scf_section(neoxc, with_cpu)
     out["batch"] = scf_batch_section(neoxc, s, DE)
+    out["gam3_batch"] = gam3_batch_section(neoxc)
     out["serving"] = scf_serving_section(neoxc, s, DE)
     if with_cpu:
         out["cpu_baseline"] = scf_cpu_baseline(s, DE, out["roothan"]["iterations"])
@@ -666,6 +667,39 @@ def gam3_section(neoxc, kw=None):
     out["mixed"]["max_rel_diff_vs_fp64"] = diff / max(out["fp64"]["absmax"], 1e-300)
     del out["mixed_tensor"], out["fp64_tensor"]
     return out
+
+
+def gam3_batch_section(neoxc, nsys=48):
+    """Many uneven systems' gam_3 in persistent launches
+    (neoxc_gam3_ic1_batch): seeded molecules of 3-6 nuclei with the proton
+    basis on nucleus 0, nebf 4-7 (s/p, 2-3 primitives), npbf 2-4 (s/p/d),
+    NG 3-4, mixed precision.  Device time of the batched build against the
+    sum of the per-system builds' device times (neoxc_gam3_ic1_opts), the
+    autotuner's choices, and the largest deviation of a batched tensor from
+    its separate build."""
+    from neoxc import basis
+    rng = np.random.Generator(np.random.PCG64(44))
+    systems = []
+    for k in range(nsys):
+        systems.append(basis.synthetic(seed=1000 + k, nat=int(rng.integers(3, 7)),
+                                       nebf=int(rng.integers(4, 8)), nprim=(2, 3),
+                                       npbf=int(rng.integers(2, 5)), ngtg=int(rng.integers(3, 5)),
+                                       lmax_e=1, lmax_p=2, name="batch%d" % k))
+    neoxc.gam3_ic1_batch(systems[:2], mixed=True)            # warm-up (tunes the class)
+    outs, t_batch = neoxc.gam3_ic1_batch(systems, mixed=True)
+    t_sep, dev = 0.0, 0.0
+    for s, x in zip(systems, outs):
+        y, t = neoxc.gam3_ic1(s, mixed=True, timing=True)
+        t_sep += t
+        dev = max(dev, float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300)))
+    return {"workload": "%d seeded systems, nebf 4-7 (s/p), npbf 2-4 (s/p/d), NG 3-4, mixed" % nsys,
+            "api": "neoxc_gam3_ic1_batch (one persistent launch per angular class)",
+            "total_ng3": int(sum(s.ng3 for s in systems)),
+            "batched_s": t_batch, "separate_builds_s": t_sep,
+            "speedup": t_sep / t_batch if t_batch > 0 else None,
+            "systems_per_s": nsys / t_batch if t_batch > 0 else None,
+            "max_rel_dev_vs_separate": dev,
+            "autotuner": neoxc.gam3_batch_tuning()}
 
 
 def scf_serving_section(neoxc, s, DE):
@@ -778,6 +812,9 @@ def main():
     if args.only == "gam3":
         kw = dict(CONFIG1, nebf=6, npbf=4) if args.small else None
         print(json.dumps(gam3_section(neoxc, kw)))
+        return
+    if args.only == "gam3_batch":
+        print(json.dumps(gam3_batch_section(neoxc, 8 if args.small else 48)))
         return
     if args.only == "factored_tc":
         print(json.dumps(factored_tc_only(neoxc, torch, dev, 24 if args.small else 60,

@@ -119,6 +119,7 @@ int neoxc_gam3_ic1_opts(int64_t options, int64_t Nchunks, int64_t nebf, int64_t 
                         const int64_t* NUCAM, const double* ELCBFC,
                         const double* NUCBFC, double* GM3ICR, double* seconds);
 
+
 /* gam3_DSCF_OMP.f:2-137 GAM3_DSCF: builds gam_3 one proton pair at a time
  * and contracts it on the fly; focke, fockp accumulate (add2fock), E_gam3
  * overwritten.  Limit: nebf <= 20. */
@@ -397,8 +398,9 @@ int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
                                     double* d_fockp, double* d_E_gam4);
 
 /* ---- XCHF RHF SCF on the device ----------------------------------------------
- * xchf1_independent/xcscf.f:2-658 xcscf (the plain Roothaan branch; SOSCF is
- * not provided) with xchf1_fock.f:2-361 as the Fock build: builds every
+ * xchf1_independent/xcscf.f:2-658 xcscf (the Roothaan branch, and the
+ * second-order branch with NEOXC_SCF_SOSCF) with xchf1_fock.f:2-361 as the
+ * Fock build: builds every
  * integral on the GPU (overlaps and core Hamiltonians, pure_ovlap.f and
  * gam_epcore.f; GAM_ep, gam_ep.f; GAM_1/GAM_1s, gam_1_OMP.f; GAM_ee,
  * gam_ee.f; GM2ICR/GM2sICR and GM3ICR in core), then iterates: Fock build
@@ -412,6 +414,9 @@ int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
  * NEOXC_SCF_MIXED (no reference counterpart) evaluates the gam_3 primitive
  * integrals with FP32 McMurchie-Davidson recursions (FP64 Boys function,
  * FP64 sums over primitives and geminal pairs); everything else stays FP64.
+ * NEOXC_SCF_MIXED_GAM2 does the same for the gam_2 primitive items, with
+ * dynamic precision: an item whose FP32 contribution exceeds the threshold
+ * of neoxc_set_mixed_threshold is re-evaluated in FP64 (gam_1 is FP64).
  *   DE (in: initial electronic density, e.g. from guessCE; out: converged)
  *   DP (in: initial nuclear density unless NEOXC_SCF_GUESS_PROT; out)
  *   E_init[16], E_final[16]: energy slots 0 E_total 1 E_nuc 2 E_ecore
@@ -426,7 +431,8 @@ int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
 #define NEOXC_SCF_DIIS 2           /* Pulay DIIS on the electronic Fock (new) */
 #define NEOXC_SCF_GAM4_ELEMENT 4   /* element-wise GAM4_DSCF for gam_4     */
 #define NEOXC_SCF_MIXED 8          /* gam_3 MD integrals in FP32 (new)     */
-#define NEOXC_SCF_MIXED_GAM2 16    /* gam_1, gam_2 MD integrals in FP32 (new) */
+#define NEOXC_SCF_MIXED_GAM2 16    /* gam_2 MD integrals in FP32, the large
+                                      items in FP64 (new) */
 #define NEOXC_SCF_GUESS_ELEC 32    /* DE (XCHF: guess_elec, xcscf.f:660) or
                                       DAE, DBE (XCUHF: guess_A_elec) from the
                                       electronic core Hamiltonian */
@@ -450,6 +456,17 @@ int neoxc_xchf_scf(int64_t nelec, int64_t nucst, int64_t nebf, int64_t npebf,
                    int64_t maxit, double* DE, double* DP, double* E_init,
                    double* E_final, double* history, int64_t* niter,
                    int64_t* converged);
+
+/* Dynamic-precision threshold of the mixed gam_2 build (NEOXC_SCF_MIXED_GAM2
+ * in every entry point that takes it; no reference counterpart).  Each
+ * primitive item is first evaluated with the FP32 tables (FP64 Boys
+ * function, seeds and sums); an item whose contribution to a contracted
+ * gam_2 element exceeds tau in magnitude is re-evaluated entirely in FP64.
+ * tau = 0 re-evaluates every item, INFINITY none.  Default 1e-5.
+ * Process-wide; NEOXC_ERR_ARG for tau < 0 or NaN.  neoxc_get_mixed_threshold
+ * returns the current value. */
+int neoxc_set_mixed_threshold(double tau);
+double neoxc_get_mixed_threshold(void);
 
 /* ---- batched XCHF solves (no reference counterpart) ----------------------------
  * One job = the arguments of neoxc_xchf_scf for one system; the outputs are
@@ -487,6 +504,24 @@ int64_t neoxc_xchf_job_size(void);   /* sizeof(neoxc_xchf_job), for bindings */
 int neoxc_xchf_scf_job(neoxc_xchf_job* job, int64_t options, int64_t maxit);
 int neoxc_xchf_scf_batch(neoxc_xchf_job* jobs, int64_t njobs, int64_t nworkers,
                          int64_t options, int64_t maxit);
+/* GAM3_IC1 for many systems at once (no reference counterpart; the batched
+ * form of the reference's per-system call, for proton-position or geometry
+ * scans): each job's basis arrays are read from a neoxc_xchf_job (its other
+ * fields are unused) and GM3ICR[k] receives job k's tensor.  The
+ * four-particle terms of all systems of one angular class run in ONE
+ * persistent launch over a device work queue (an atomic counter over every
+ * system's work items, so uneven systems balance across the SMs); the
+ * persistent grid (CTAs per SM, items per grab) is chosen per class and
+ * precision by a built-in autotuner on the first call (timed samples of the
+ * real work), whose choices neoxc_gam3_batch_tuning reports.  options:
+ * NEOXC_SCF_MIXED, NEOXC_SCF_SCREEN as neoxc_gam3_ic1_opts.  seconds
+ * (optional): device time of the build (copies excluded).  Every system's
+ * tensor equals its neoxc_gam3_ic1 result.  nebf <= 20 per job. */
+int neoxc_gam3_ic1_batch(const neoxc_xchf_job* jobs, int64_t njobs, int64_t options,
+                         double* const* GM3ICR, double* seconds);
+/* The autotuner's choices so far as a JSON array (written into buf up to len
+ * bytes, NUL-terminated); returns the full length. */
+int64_t neoxc_gam3_batch_tuning(char* buf, int64_t len);
 
 /* Admission by device memory (no reference counterpart), the rule the
  * batch driver and the server apply each time a job is about to start,

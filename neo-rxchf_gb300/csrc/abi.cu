@@ -12,6 +12,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <map>
 #include <thread>
 #include <cmath>
 #include <cstdarg>
@@ -541,6 +542,203 @@ int neoxc_gam3_ic1_opts(int64_t options, int64_t Nchunks, int64_t nebf, int64_t 
     cudaEventDestroy(ev[1]);
   }
   return rc;
+}
+
+}  // extern "C"
+
+// ---- many systems' gam_3 in persistent launches ----------------------------
+// The autotuner's choices per (angular class, precision): CTAs per SM of the
+// persistent grid and work items per queue grab, with the sample rate that
+// chose them (items/s); read back by neoxc_gam3_batch_tuning.
+struct G3Tune {
+  int ctas_per_sm = 0, chunk = 0;
+  double items_per_s = 0.0;
+  std::string trials;
+};
+static std::mutex g_tune_mu;
+static std::map<int, G3Tune> g_tune;   // key: (lmax_e * 3 + lmax_p) * 2 + fp32
+
+static int g3_tune_key(const DevSystem& S, int fp32) {
+  return ((S.lmax_e * 3 + (S.lmax_p == 0 ? 0 : 2)) * 2) + fp32;
+}
+
+// Time candidate (ctas_per_sm, chunk) pairs on a sample of the batch's work
+// items (the first ~8 CTA-waves) and keep the fastest.  The candidates run
+// the real kernel on the real inputs; the sample's outputs are overwritten
+// by the full launch that follows.
+static int g3_autotune(const std::vector<G3BatchSys>& hs, int fp32, double screen,
+                       void* scratch, cudaStream_t s, G3Tune* out) {
+  static const int kCtas[] = {1, 2, 3, 4};
+  static const int kChunks[] = {1, 4, 16};
+  int dev = 0, nsm = 0;
+  CU(cudaGetDevice(&dev));
+  CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  G3Tune best;
+  char buf[160];
+  for (int c : kCtas)
+    for (int ch : kChunks) {
+      const long long sample = 8LL * nsm * c * ch;
+      long long total = 0;
+      CU(cudaEventRecord(a, s));
+      CU(launch_gam3_batch_pairs(hs.data(), (int)hs.size(), fp32, screen, scratch, c, ch, sample,
+                                 &total, s));
+      CU(cudaEventRecord(b, s));
+      CU(cudaEventSynchronize(b));
+      float ms = 0.0f;
+      CU(cudaEventElapsedTime(&ms, a, b));
+      const long long done = sample < total ? sample : total;
+      const double rate = ms > 0.0f ? done / (1e-3 * ms) : 0.0;
+      snprintf(buf, sizeof(buf), "%s{\"ctas_per_sm\":%d,\"chunk\":%d,\"items_per_s\":%.4g}",
+               best.trials.empty() ? "" : ",", c, ch, rate);
+      best.trials += buf;
+      if (rate > best.items_per_s) {
+        best.items_per_s = rate;
+        best.ctas_per_sm = c;
+        best.chunk = ch;
+      }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *out = best;
+  return NEOXC_OK;
+}
+
+extern "C" {
+
+int neoxc_gam3_ic1_batch(const neoxc_xchf_job* jobs, int64_t njobs, int64_t options,
+                         double* const* GM3ICR, double* seconds) {
+  RC(need(jobs != nullptr && GM3ICR != nullptr && njobs >= 1, "jobs, GM3ICR, njobs >= 1"));
+  RC(need((options & ~(int64_t)(NEOXC_SCF_MIXED | NEOXC_SCF_SCREEN)) == 0, "options"));
+  const int fp32 = (options & NEOXC_SCF_MIXED) ? 1 : 0;
+  const double screen = (options & NEOXC_SCF_SCREEN) ? kScreenThreshold : 0.0;
+  for (int64_t k = 0; k < njobs; k++) {
+    RC(need(GM3ICR[k] != nullptr, "GM3ICR[k]"));
+    if (jobs[k].nebf > 20)
+      return set_err(NEOXC_ERR_UNSUPPORTED, "gam_3 batch: nebf <= 20 (job %lld)", (long long)k);
+  }
+  cudaStream_t s;
+  RC(get_stream(&s));
+  std::vector<SysUpload> up((size_t)njobs);
+  std::vector<DBuf> aux((size_t)njobs), r4b((size_t)njobs), g3((size_t)njobs);
+  for (int64_t k = 0; k < njobs; k++) {
+    const neoxc_xchf_job& j = jobs[k];
+    RC(stage_system(up[k], s, j.nebf, j.npebf, j.npbf, j.nat, j.ngtg1, j.pmass, j.cat, j.zan,
+                    j.bcoef1, j.gamma1, j.KPESTR, j.KPEEND, j.AGEBFCC, j.AGNBFCC, j.ELCEX,
+                    j.NUCEX, j.ELCAM, j.NUCAM, j.ELCBFC, j.NUCBFC));
+    if (up[k].d.g3_ntile < 1)
+      return set_err(NEOXC_ERR_UNSUPPORTED, "gam_3 batch: a contracted pair has more than %d "
+                                            "primitive pairs (job %lld)", kG3MaxTileKets,
+                     (long long)k);
+    const int ne = (int)j.nebf, np = (int)j.npbf;
+    RC(dalloc(aux[k], sizeof(double) * gam3_aux_doubles(ne, np), s));
+    RC(dalloc(r4b[k], sizeof(double) * gam3_r4_doubles(ne, np), s));
+    const size_t ng3 = (size_t)ne * ne * ne * ne * ne * ne * np * np;
+    RC(dalloc(g3[k], sizeof(double) * ng3, s));
+  }
+  DBuf scr;
+  RC(dalloc(scr, gam3_batch_scratch_bytes((int)njobs), s));
+  cudaEvent_t ev[2];
+  CU(cudaEventCreate(&ev[0]));
+  CU(cudaEventCreate(&ev[1]));
+  RC(finish(s));
+  CU(cudaEventRecord(ev[0], s));
+  for (int64_t k = 0; k < njobs; k++) CU(launch_gam3_aux(up[k].d, aux[k].as<double>(), s));
+  // one persistent launch per angular class
+  std::map<int, std::vector<int64_t>> classes;
+  for (int64_t k = 0; k < njobs; k++) classes[g3_tune_key(up[k].d, fp32)].push_back(k);
+  for (auto& kv : classes) {
+    std::vector<G3BatchSys> hs;
+    for (int64_t k : kv.second) {
+      G3BatchSys b;
+      b.S = up[k].d;
+      b.erec = up[k].d.g3rec;
+      b.prec = up[k].d.g3rec + (size_t)32 * up[k].d.g3_nket;
+      const size_t n2 = (size_t)up[k].d.nebf * up[k].d.nebf;
+      const size_t p2 = (size_t)up[k].d.npbf * up[k].d.npbf;
+      b.r4a = aux[k].as<double>() + n2 * n2 + n2 + p2 * n2 + p2 * n2 * n2;
+      b.r4b = r4b[k].as<double>();
+      hs.push_back(b);
+    }
+    G3Tune t;
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(kv.first);
+      if (it != g_tune.end()) {
+        t = it->second;
+        have = true;
+      }
+    }
+    if (!have) {
+      RC(g3_autotune(hs, fp32, screen, scr.p, s, &t));
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[kv.first] = t;
+    }
+    CU(launch_gam3_batch_pairs(hs.data(), (int)hs.size(), fp32, screen, scr.p, t.ctas_per_sm,
+                               t.chunk, -1, nullptr, s));
+  }
+  for (int64_t k = 0; k < njobs; k++) {
+    const int ne = up[k].d.nebf, np = up[k].d.npbf;
+    const size_t n2 = (size_t)ne * ne, p2 = (size_t)np * np;
+    double* r4a = aux[k].as<double>() + n2 * n2 + n2 + p2 * n2 + p2 * n2 * n2;
+    CU(launch_gam3_add((long long)gam3_r4_doubles(ne, np), r4a, r4b[k].as<double>(), s));
+    const long long ng3 = (long long)(n2 * n2 * n2 * p2);
+    CU(launch_gam3_raw_range(up[k].d, aux[k].as<double>(), 0, ng3, g3[k].as<double>(), s));
+    CU(launch_gam3_symmetrize(ne, np, g3[k].as<double>(), s));
+  }
+  CU(cudaEventRecord(ev[1], s));
+  for (int64_t k = 0; k < njobs; k++) {
+    const int ne = up[k].d.nebf, np = up[k].d.npbf;
+    const size_t ng3 = (size_t)ne * ne * ne * ne * ne * ne * np * np;
+    CU(cudaMemcpyAsync(GM3ICR[k], g3[k].p, sizeof(double) * ng3, cudaMemcpyDeviceToHost, s));
+  }
+  const int rc = finish(s);
+  if (seconds) {
+    float ms = 0.0f;
+    if (rc == NEOXC_OK) cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    *seconds = 1e-3 * ms;
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  return rc;
+}
+
+int neoxc_set_mixed_threshold(double tau) {
+  if (!(tau >= 0.0)) return set_err(NEOXC_ERR_ARG, "mixed threshold: tau >= 0");
+  set_mixed_recompute_tau(tau);
+  return NEOXC_OK;
+}
+
+double neoxc_get_mixed_threshold(void) { return mixed_recompute_tau(); }
+
+int64_t neoxc_gam3_batch_tuning(char* buf, int64_t len) {
+  std::string out = "[";
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    bool first = true;
+    for (auto& kv : g_tune) {
+      const int fp32 = kv.first & 1, cls = kv.first >> 1;
+      char line[256];
+      snprintf(line, sizeof(line),
+               "%s{\"lmax_e\":%d,\"lmax_p_class\":%d,\"fp32\":%d,\"ctas_per_sm\":%d,"
+               "\"chunk\":%d,\"items_per_s\":%.4g,\"trials\":[",
+               first ? "" : ",", cls / 3, cls % 3, fp32, kv.second.ctas_per_sm, kv.second.chunk,
+               kv.second.items_per_s);
+      out += line;
+      out += kv.second.trials + "]}";
+      first = false;
+    }
+  }
+  out += "]";
+  if (buf && len > 0) {
+    const size_t n = out.size() < (size_t)(len - 1) ? out.size() : (size_t)(len - 1);
+    memcpy(buf, out.data(), n);
+    buf[n] = 0;
+  }
+  return (int64_t)out.size();
 }
 
 int neoxc_gam3_ic1(int64_t Nchunks, int64_t nebf, int64_t npebf, int64_t npbf,
@@ -1525,7 +1723,7 @@ static int xchf_scf_on(cudaStream_t s, int64_t nelec, int64_t nucst, int64_t neb
   CU(launch_scf_onebody(u.d, Se.as<double>(), Sp.as<double>(), Hce.as<double>(),
                         Hcp.as<double>(), s));
   CU(launch_gam_ep(u.d, Gep.as<double>(), s));
-  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, mixed_gam2));
+  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, 0));
   CU(launch_gam_ee(u.d, Gee.as<double>(), s));
   if (nelec > 1) {
     CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s,
@@ -2544,7 +2742,7 @@ int xcuhf_scf_on(cudaStream_t s, int64_t nelec, int64_t NAE, int64_t NBE, int64_
   CU(launch_scf_onebody(u.d, Se.as<double>(), Sp.as<double>(), Hce.as<double>(),
                         Hcp.as<double>(), s));
   CU(launch_gam_ep(u.d, Gep.as<double>(), s));
-  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, mixed_gam2));
+  CU(launch_gam1(u.d, G1.as<double>(), G1s.as<double>(), s, 0));
   CU(launch_gam_ee(u.d, Gee.as<double>(), s));
   if (nelec > 1) {
     CU(launch_gam2_raw(u.d, 0, G2.as<double>(), G2s.as<double>(), s, mixed_gam2));

@@ -19,6 +19,13 @@
 namespace neoxc {
 namespace g3 {
 
+// C(t,i) 2^(2i-t) in the precision of the contraction
+template <class R>
+G3_HD R hermc_r(int t, int i) {
+  if constexpr (sizeof(R) == sizeof(float)) return hermc32(t, i);
+  else return (R)hermc(t, i);
+}
+
 // ---- pair records (FP64, 32 doubles each) ----------------------------------
 // [0] p  [1..3] P  [4] c_a c_b  [5..19] E[d][t] (t <= 4)  [20..22] t_max[d]
 // [23] S  [24] Q (screening magnitudes, see k_gam3.cu)
@@ -239,7 +246,7 @@ G3_HD double fb_eval(const Bra<R, NW>& b, R pk, const R* Xk, const R (*Ek)[NK + 
     for (int k = 1; k <= n; k++) xp[k] = xp[k - 1] * Rv[d];
     for (int i = 0; i <= n; i++) A[d][i] = R(0);
     for (int t = 0; t <= n; t++)
-      for (int i = (t + 1) / 2; i <= t; i++) A[d][i] += W[t] * (R)neoxc::hermc(t, i) * xp[2 * i - t];
+      for (int i = (t + 1) / 2; i <= t; i++) A[d][i] += W[t] * hermc_r<R>(t, i) * xp[2 * i - t];
     L += n;
   }
   const int nx = b.N[0] + tk[0], ny = b.N[1] + tk[1], nz = b.N[2] + tk[2];
@@ -247,18 +254,13 @@ G3_HD double fb_eval(const Bra<R, NW>& b, R pk, const R* Xk, const R (*Ek)[NK + 
   for (int m = 0; m <= nx + ny; m++) Bxy[m] = R(0);
   for (int i = 0; i <= nx; i++)
     for (int j = 0; j <= ny; j++) Bxy[i + j] += A[0][i] * A[1][j];
-  double F[md::LTOT + 1];
-  boys(L, (double)T, F);
   // seeds (-alpha)^m F_m(T) and the final sum in FP64
-  const double ma = -(double)alpha;
-  double s = 0.0, pw = 1.0;
-  for (int m = 0; m <= L; m++) {
+  const double s = boys_sum(L, (double)T, (double)alpha, [&](int m) {
     R bm = R(0);
     const int lo = m - nz > 0 ? m - nz : 0, hi = m < nx + ny ? m : nx + ny;
     for (int i = lo; i <= hi; i++) bm += Bxy[i] * A[2][m - i];
-    s += pw * F[m] * (double)bm;
-    pw *= ma;
-  }
+    return bm;
+  });
   return (double)(b.pref * C4) * s;
 }
 

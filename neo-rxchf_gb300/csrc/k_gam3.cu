@@ -55,6 +55,7 @@
 // (a bound for s functions, an estimate for p/d); a (bra, ket) whose
 // estimate times sum_kl |b_k b_l| falls below `screen` is skipped.
 #include <type_traits>
+#include <vector>
 
 #include "g3_fatbra.cuh"
 #include "neoxc_internal.h"
@@ -111,19 +112,21 @@ __global__ void g3_records_kernel(DevSystem S, double* __restrict__ erec,
 
 constexpr int kFbThreads = 128;   // threads (and bras per chunk) of a CTA
 
-// MODE 0: G4Vep, CTA (Pp, P1, P2), kets e3 -> R4[Pp][P1][P2][P3]  = -sum
-// MODE 1: G4Vee, CTA (Pp, P1, P3), kets e2 -> R4[Pp][P1][P2][P3] += 2 sum
-// (MODE 1 runs after MODE 0 on the same stream; each element has one owner
-// CTA per pass, so the result is deterministic.)
+// One CTA's work: block blk (Pp, Pa, Pb) and ket tile `tile` of one pass.
+// MODE 0: G4Vep, (Pp, P1, P2), kets e3 -> R4[Pp][P1][P2][P3]  = -sum
+// MODE 1: G4Vee, (Pp, P1, P3), kets e2 -> R4[Pp][P1][P2][P3] += 2 sum
+//         (or = 2 sum when store1: the batched launch keeps the two passes
+//         in separate arrays and adds them afterwards).
+// Each element has one owner CTA per pass, so results are deterministic.
 template <bool F32, int LE, int LN, int MODE>
-__global__ void __launch_bounds__(kFbThreads)
-gam3_fb_kernel(DevSystem S, const double* __restrict__ erec,
-               const double* __restrict__ prec, double screen,
-               double* __restrict__ r4) {
+__device__ __forceinline__ void fb_block(const DevSystem& S, const double* __restrict__ erec,
+                                         const double* __restrict__ prec, double screen,
+                                         double* __restrict__ r4, long long blk, int tile,
+                                         unsigned char* smraw, bool store1) {
   using R = typename std::conditional<F32, float, double>::type;
   constexpr int NW = 4 * LE + 2 * LN;   // bra Hermite order per direction
   constexpr int NK = 2 * LE;            // ket Hermite order per direction
-  extern __shared__ __align__(16) unsigned char smraw[];
+  __syncthreads();   // the previous block's reads of the shared tables are done
   Bra<R, NW>* bras = reinterpret_cast<Bra<R, NW>*>(smraw);
   double* acc_s = reinterpret_cast<double*>(smraw + sizeof(Bra<R, NW>) * kFbThreads);
 
@@ -133,11 +136,10 @@ gam3_fb_kernel(DevSystem S, const double* __restrict__ erec,
   const int* tile_k = kofs + nPe + 1;               // [ntile + 1]
   const int* tile_P = tile_k + S.g3_ntile + 1;      // [ntile + 1]
   const int* kperm = tile_P + S.g3_ntile + 1;       // [nket]
-  long long r = blockIdx.x;
+  long long r = blk;
   const int Pb = (int)(r % nPe); r /= nPe;
   const int Pa = (int)(r % nPe); r /= nPe;
   const int Pp = (int)r;
-  const int tile = blockIdx.y;
   const int k0 = tile_k[tile], nkt = tile_k[tile + 1] - k0;
   const int P0 = tile_P[tile], P1t = tile_P[tile + 1];
   const int ka = kofs[Pa], na = kofs[Pa + 1] - ka;
@@ -188,6 +190,7 @@ gam3_fb_kernel(DevSystem S, const double* __restrict__ erec,
           Ek[d][t] = (t & 1) ? -(R)rk[kRE + 5 * d + t] : (R)rk[kRE + 5 * d + t];
       }
       const double qk = rk[kRQ];
+      const double rkc = rk[kRC];
       double part = 0.0;
       for (int bi = 0; bi < nvalid; bi++) {
         const Bra<R, NW>& b = bras[bi];
@@ -196,7 +199,7 @@ gam3_fb_kernel(DevSystem S, const double* __restrict__ erec,
         if (MODE == 0) v = md::underflow(v);   // zz = underflow(G4_MD_xgVepg)
         part += b.wgt * v;
       }
-      acc_s[kid - k0] += part * rk[kRC];
+      acc_s[kid - k0] += part * rkc;
     }
   }
   __syncthreads();
@@ -206,10 +209,69 @@ gam3_fb_kernel(DevSystem S, const double* __restrict__ erec,
     for (int k = kofs[P]; k < kofs[P + 1]; k++) s += acc_s[k - k0];
     if (MODE == 0)
       r4[((Pp * nP + Pa) * nP + Pb) * nP + P] = s;
+    else if (store1)
+      r4[((Pp * nP + Pa) * nP + P) * nP + Pb] = s;
     else
       r4[((Pp * nP + Pa) * nP + P) * nP + Pb] += s;
   }
 }
+
+template <bool F32, int LE, int LN, int MODE>
+__global__ void __launch_bounds__(kFbThreads, 4)
+gam3_fb_kernel(DevSystem S, const double* __restrict__ erec,
+               const double* __restrict__ prec, double screen,
+               double* __restrict__ r4) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  fb_block<F32, LE, LN, MODE>(S, erec, prec, screen, r4, (long long)blockIdx.x, blockIdx.y,
+                              smraw, false);
+}
+
+// ---- many systems in one persistent launch ----------------------------------
+// Work items are numbered over groups g = 2 s + mode (system s, pass mode):
+// group g holds nblk_s x ntile_s items, first item prefix[g].  Each CTA
+// takes chunks of `chunk` consecutive items from an atomic counter until
+// the items run out (or `limit`, for the autotuner's samples).
+template <bool F32, int LE, int LN>
+__global__ void __launch_bounds__(kFbThreads, 4)
+gam3_fb_persistent(const G3BatchSys* __restrict__ sys, const long long* __restrict__ prefix,
+                   int ngroups, int chunk, long long limit, double screen,
+                   unsigned long long* __restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ long long s_item;
+  const long long total = prefix[ngroups] < limit ? prefix[ngroups] : limit;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ULL) * chunk;
+    __syncthreads();
+    const long long first = s_item;
+    if (first >= total) break;
+    const long long last = first + chunk < total ? first + chunk : total;
+    for (long long it = first; it < last; it++) {
+      int lo = 0, hi = ngroups - 1;   // the group holding item `it`
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= it) lo = mid; else hi = mid - 1;
+      }
+      const G3BatchSys& b = sys[lo >> 1];
+      const long long local = it - prefix[lo];
+      const int tile = (int)(local % b.S.g3_ntile);
+      const long long blk = local / b.S.g3_ntile;
+      if ((lo & 1) == 0)
+        fb_block<F32, LE, LN, 0>(b.S, b.erec, b.prec, screen, b.r4a, blk, tile, smraw, false);
+      else
+        fb_block<F32, LE, LN, 1>(b.S, b.erec, b.prec, screen, b.r4b, blk, tile, smraw, true);
+    }
+  }
+}
+
+// r4a += r4b (the two passes of the batched launch)
+__global__ void add_kernel(long long n, double* __restrict__ a, const double* __restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    a[i] += b[i];
+}
+
+
 
 // x3[w] = R4(canonical tuple of t0 + w) + W1(p,e1) GAM_ee(e2,e3) + W3(p,e1,e2) Hcore(e3)
 __global__ void gam3_expand_kernel(int ne, int np, const double* __restrict__ aux,
@@ -242,6 +304,49 @@ __global__ void gam3_expand_kernel(int ne, int np, const double* __restrict__ au
     const double h = hc[c[4] * ne + c[5]];
     x3[t] = R4[cr] + w1 * ee + w3 * h;
   }
+}
+
+template <bool F32, int LE, int LN>
+cudaError_t persistent_t(const G3BatchSys* d_sys, const long long* d_prefix, int ngroups,
+                         int chunk, long long limit, double screen,
+                         unsigned long long* d_counter, int ctas_per_sm, cudaStream_t s) {
+  using R = typename std::conditional<F32, float, double>::type;
+  constexpr int NW = 4 * LE + 2 * LN;
+  const size_t smem = sizeof(Bra<R, NW>) * kFbThreads + sizeof(double) * kG3MaxTileKets;
+  cudaError_t e = cudaFuncSetAttribute(gam3_fb_persistent<F32, LE, LN>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0, occ = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gam3_fb_persistent<F32, LE, LN>,
+                                                         kFbThreads, smem)) != cudaSuccess)
+    return e;
+  const int per_sm = ctas_per_sm < 1 ? 1 : (ctas_per_sm > occ ? (occ > 0 ? occ : 1) : ctas_per_sm);
+  gam3_fb_persistent<F32, LE, LN><<<nsm * per_sm, kFbThreads, smem, s>>>(
+      d_sys, d_prefix, ngroups, chunk, limit, screen, d_counter);
+  return cudaGetLastError();
+}
+
+template <bool F32>
+cudaError_t persistent_dispatch(int le, int lp, const G3BatchSys* d_sys,
+                                const long long* d_prefix, int ngroups, int chunk,
+                                long long limit, double screen, unsigned long long* d_counter,
+                                int ctas_per_sm, cudaStream_t s) {
+  const int LN = lp == 0 ? 0 : 2;
+#define PD(a, b) persistent_t<F32, a, b>(d_sys, d_prefix, ngroups, chunk, limit, screen, \
+                                         d_counter, ctas_per_sm, s)
+  switch (le * 3 + LN) {
+    case 0: return PD(0, 0);
+    case 2: return PD(0, 2);
+    case 3: return PD(1, 0);
+    case 5: return PD(1, 2);
+    case 6: return PD(2, 0);
+    case 8: return PD(2, 2);
+    default: return cudaErrorInvalidValue;
+  }
+#undef PD
 }
 
 template <bool F32, int LE, int LN>
@@ -295,6 +400,58 @@ size_t gam3_aux_doubles(int ne, int np) {
   const size_t n2 = (size_t)ne * ne;
   return n2 * n2 + n2 + (size_t)np * np * n2 + (size_t)np * np * n2 * n2 +
          gam3_r4_doubles(ne, np);
+}
+
+size_t gam3_batch_scratch_bytes(int nsys) {
+  return sizeof(G3BatchSys) * (size_t)nsys + sizeof(long long) * (2 * (size_t)nsys + 1) + 64;
+}
+
+cudaError_t launch_gam3_batch_pairs(const G3BatchSys* h_sys, int nsys, int fp32, double screen,
+                                    void* scratch, int ctas_per_sm, int chunk, long long limit,
+                                    long long* total_items, cudaStream_t s) {
+  if (nsys < 1 || chunk < 1) return cudaErrorInvalidValue;
+  const int le = h_sys[0].S.lmax_e, lp = h_sys[0].S.lmax_p;
+  std::vector<long long> prefix(2 * (size_t)nsys + 1, 0);
+  for (int k = 0; k < nsys; k++) {
+    const DevSystem& S = h_sys[k].S;
+    if (S.lmax_e != le || (S.lmax_p == 0) != (lp == 0) || S.g3_ntile < 1 || !S.g3i || !S.g3rec)
+      return cudaErrorInvalidValue;   // one angular class per launch
+    const long long nPe = (long long)S.nebf * (S.nebf + 1) / 2;
+    const long long nPp = (long long)S.npbf * (S.npbf + 1) / 2;
+    const long long items = nPp * nPe * nPe * S.g3_ntile;
+    prefix[2 * k + 1] = prefix[2 * k] + items;
+    prefix[2 * k + 2] = prefix[2 * k + 1] + items;
+  }
+  if (total_items) *total_items = prefix[2 * nsys];
+  unsigned char* p = static_cast<unsigned char*>(scratch);
+  G3BatchSys* d_sys = reinterpret_cast<G3BatchSys*>(p);
+  long long* d_prefix = reinterpret_cast<long long*>(p + sizeof(G3BatchSys) * (size_t)nsys);
+  unsigned long long* d_counter =
+      reinterpret_cast<unsigned long long*>(d_prefix + 2 * (size_t)nsys + 1);
+  cudaError_t e = cudaMemcpyAsync(d_sys, h_sys, sizeof(G3BatchSys) * (size_t)nsys,
+                                  cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(d_prefix, prefix.data(), sizeof(long long) * prefix.size(),
+                      cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  // the host vectors are released when this returns: make the copies land
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  const long long lim = limit < 0 ? prefix[2 * nsys] : limit;
+  return fp32 ? persistent_dispatch<true>(le, lp, d_sys, d_prefix, 2 * nsys, chunk, lim, screen,
+                                          d_counter, ctas_per_sm, s)
+              : persistent_dispatch<false>(le, lp, d_sys, d_prefix, 2 * nsys, chunk, lim, screen,
+                                           d_counter, ctas_per_sm, s);
+}
+
+cudaError_t launch_gam3_add(long long n, double* a, const double* b, cudaStream_t s) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  add_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, a, b);
+  return cudaGetLastError();
 }
 
 size_t g3_record_doubles(int nket, int np) {

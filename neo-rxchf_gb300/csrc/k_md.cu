@@ -21,6 +21,7 @@
 // per-primitive integrand with the factorised MD kernels of md_math.cuh,
 // re-using one Boys'-lemma/derivative setup for every integral that shares
 // a particle order and geminal assignment.
+#include <atomic>
 #include <type_traits>
 
 #include "md_math.cuh"
@@ -281,10 +282,64 @@ gam_ee_kernel(DevSystem S, double* __restrict__ gee) {
 }
 
 // ---- gam_2 raw tensors: warp per contracted tuple --------------------------
+// One primitive work item q2 of a tuple (geminal item fastest-varying over
+// the primitive combination, see below): its FP64 contribution to x1, x2.
+struct Gam2Tuple {
+  int s_i1, n_i1, s_j1, n_j1, s_i2, n_i2, s_j2, n_j2, nq;
+};
+
+template <bool F32>
+__device__ __forceinline__ void gam2_item(const DevSystem& S, const Gam2Tuple& t,
+                                          const DevPrim& pa, const DevPrim& pb, double cp,
+                                          int q2, double& v1, double& v2) {
+  const int gi = q2 / t.nq;
+  int qq = q2 - gi * t.nq;
+  const int j2 = t.s_j2 + qq % t.n_j2; qq /= t.n_j2;
+  const int i2 = t.s_i2 + qq % t.n_i2; qq /= t.n_i2;
+  const int j1 = t.s_j1 + qq % t.n_j1; qq /= t.n_j1;
+  const int i1 = t.s_i1 + qq;
+  double a1, a2;
+  if constexpr (F32) {
+    md32::G3 st;
+    md32::Prim A[3] = {to_prim32(S.eprim[i1]), to_prim32(S.eprim[i2]), to_prim32(pa)};
+    md32::Prim B[3] = {to_prim32(S.eprim[j1]), to_prim32(S.eprim[j2]), to_prim32(pb)};
+    xcalc_gam2_item(A, B, S, st, gi, a1, a2);
+  } else {
+    G3 st;
+    Prim A[3] = {to_prim(S.eprim[i1]), to_prim(S.eprim[i2]), to_prim(pa)};
+    Prim B[3] = {to_prim(S.eprim[j1]), to_prim(S.eprim[j2]), to_prim(pb)};
+    xcalc_gam2_item(A, B, S, st, gi, a1, a2);
+  }
+  const double c = cp * S.eprim[i1].coef * S.eprim[j1].coef *
+                   S.eprim[i2].coef * S.eprim[j2].coef;
+  v1 = a1 * c;
+  v2 = a2 * c;
+}
+
+// The FP64 re-evaluation of the mixed path, kept out of line so that it
+// does not change the register allocation of the FP32 loop.
+__device__ __noinline__ void gam2_item64(const DevSystem& S, const Gam2Tuple& t,
+                                         const DevPrim& pa, const DevPrim& pb, double cp,
+                                         int q2, double& v1, double& v2) {
+  gam2_item<false>(S, t, pa, pb, cp, q2, v1, v2);
+}
+
+// F32 (the mixed path) evaluates every item in FP32 first and uses that
+// value as its own magnitude estimate: an item whose contribution exceeds
+// `tau` in magnitude is discarded and re-evaluated in FP64 (dynamic
+// precision per primitive item, in the spirit of Luehr, Ufimtsev and
+// Martinez, J. Chem. Theory Comput. 7, 949 (2011), which selects the
+// precision per shell quartet from a Schwarz bound).  The contributions are
+// concentrated in few items (for the geminal Coulomb terms about 1% of the
+// items carry 95-99% of the sum), so the FP64 share of the work stays small
+// while the FP32 error left in the sum drops by one to two orders of
+// magnitude.  Each warp queues its large items in shared memory and
+// re-evaluates them 32 at a time, so that the FP64 work runs on full warps.
+// The result is deterministic (fixed lane order, fixed queue order).
 template <int RX, bool F32>
 __global__ void __launch_bounds__(64, F32 ? 16 : 8)
 gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
-                double* __restrict__ x2, long long t0, long long ntup) {
+                double* __restrict__ x2, long long t0, long long ntup, double tau) {
   const int ne = S.nebf, np = S.npbf;
   const int lane = threadIdx.x & 31;
   const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -296,42 +351,84 @@ gam2_raw_kernel(DevSystem S, double* __restrict__ x1,
   const int ic1 = (int)(r % ne); r /= ne;
   const int jp = (int)(r % np);
   const int ip = (int)(r / np);
-  const int s_i1 = S.kpestr[ic1], n_i1 = S.kpeend[ic1] - s_i1 + 1;
-  const int s_j1 = S.kpestr[jc1], n_j1 = S.kpeend[jc1] - s_j1 + 1;
-  const int s_i2 = S.kpestr[ic2], n_i2 = S.kpeend[ic2] - s_i2 + 1;
-  const int s_j2 = S.kpestr[jc2], n_j2 = S.kpeend[jc2] - s_j2 + 1;
-  const int nq = n_i1 * n_j1 * n_i2 * n_j2;
+  Gam2Tuple t;
+  t.s_i1 = S.kpestr[ic1]; t.n_i1 = S.kpeend[ic1] - t.s_i1 + 1;
+  t.s_j1 = S.kpestr[jc1]; t.n_j1 = S.kpeend[jc1] - t.s_j1 + 1;
+  t.s_i2 = S.kpestr[ic2]; t.n_i2 = S.kpeend[ic2] - t.s_i2 + 1;
+  t.s_j2 = S.kpestr[jc2]; t.n_j2 = S.kpeend[jc2] - t.s_j2 + 1;
+  t.nq = t.n_i1 * t.n_j1 * t.n_i2 * t.n_j2;
   const int ng = S.ngtg;
   const int nitem = RX ? ng * ng : ng + ng * ng;   // geminal work items
+  const int total = t.nq * nitem;
   const DevPrim& pa = S.pprim[ip];
   const DevPrim& pb = S.pprim[jp];
   const double cp = pa.coef * pb.coef;
-  typename std::conditional<F32, md32::G3, G3>::type st;
   double o1 = 0.0, o2 = 0.0;
   // lanes take (geminal item, primitive combination) pairs, the primitive
   // combination fastest so that neighbouring lanes share the geminal item
-  for (int q2 = lane; q2 < nq * nitem; q2 += 32) {
-    const int gi = q2 / nq;
-    int qq = q2 - gi * nq;
-    const int j2 = s_j2 + qq % n_j2; qq /= n_j2;
-    const int i2 = s_i2 + qq % n_i2; qq /= n_i2;
-    const int j1 = s_j1 + qq % n_j1; qq /= n_j1;
-    const int i1 = s_i1 + qq;
-    double a1, a2;
-    if constexpr (F32) {
-      md32::Prim A[3] = {to_prim32(S.eprim[i1]), to_prim32(S.eprim[i2]), to_prim32(pa)};
-      md32::Prim B[3] = {to_prim32(S.eprim[j1]), to_prim32(S.eprim[j2]), to_prim32(pb)};
-      xcalc_gam2_item(A, B, S, st, gi, a1, a2);
-    } else {
+  if constexpr (RX) {
+    for (int q2 = lane; q2 < total; q2 += 32) {
+      const int gi = q2 / t.nq;
+      int qq = q2 - gi * t.nq;
+      const int j2 = t.s_j2 + qq % t.n_j2; qq /= t.n_j2;
+      const int i2 = t.s_i2 + qq % t.n_i2; qq /= t.n_i2;
+      const int j1 = t.s_j1 + qq % t.n_j1; qq /= t.n_j1;
+      const int i1 = t.s_i1 + qq;
+      G3 st;
       Prim A[3] = {to_prim(S.eprim[i1]), to_prim(S.eprim[i2]), to_prim(pa)};
       Prim B[3] = {to_prim(S.eprim[j1]), to_prim(S.eprim[j2]), to_prim(pb)};
-      if (RX) xcalc_gam2_rx_item(A, B, S, st, gi, a1, a2);
-      else xcalc_gam2_item(A, B, S, st, gi, a1, a2);
+      double a1, a2;
+      xcalc_gam2_rx_item(A, B, S, st, gi, a1, a2);
+      const double c = cp * S.eprim[i1].coef * S.eprim[j1].coef *
+                       S.eprim[i2].coef * S.eprim[j2].coef;
+      o1 = o1 + a1 * c;
+      o2 = o2 + a2 * c;
     }
-    const double c = cp * S.eprim[i1].coef * S.eprim[j1].coef *
-                     S.eprim[i2].coef * S.eprim[j2].coef;
-    o1 = o1 + a1 * c;
-    o2 = o2 + a2 * c;
+  } else if constexpr (!F32) {
+    for (int q2 = lane; q2 < total; q2 += 32) {
+      double v1, v2;
+      gam2_item<false>(S, t, pa, pb, cp, q2, v1, v2);
+      o1 = o1 + v1;
+      o2 = o2 + v2;
+    }
+  } else {
+    __shared__ int queue[2][64];   // per warp of the 64-thread CTA
+    int* qw = queue[threadIdx.x >> 5];
+    int qn = 0;
+    for (int base = 0; base < total; base += 32) {
+      const int q2 = base + lane;
+      bool big = false;
+      if (q2 < total) {
+        double v1, v2;
+        gam2_item<true>(S, t, pa, pb, cp, q2, v1, v2);
+        if (fabs(v1) > tau || fabs(v2) > tau || !(v1 == v1) || !(v2 == v2)) {
+          big = true;
+        } else {
+          o1 = o1 + v1;
+          o2 = o2 + v2;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, big);
+      if (big) qw[qn + __popc(m & ((1u << lane) - 1u))] = q2;
+      qn += __popc(m);
+      __syncwarp();
+      if (qn >= 32) {   // 32 queued items: one full-warp FP64 pass
+        double v1, v2;
+        gam2_item64(S, t, pa, pb, cp, qw[lane], v1, v2);
+        o1 = o1 + v1;
+        o2 = o2 + v2;
+        __syncwarp();
+        if (lane < qn - 32) qw[lane] = qw[lane + 32];
+        __syncwarp();
+        qn -= 32;
+      }
+    }
+    if (lane < qn) {
+      double v1, v2;
+      gam2_item64(S, t, pa, pb, cp, qw[lane], v1, v2);
+      o1 = o1 + v1;
+      o2 = o2 + v2;
+    }
   }
   o1 = warp_sum(o1);
   o2 = warp_sum(o2);
@@ -524,11 +621,18 @@ cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
   const unsigned blocks = (unsigned)((threads + 63) / 64);
   if (ntup <= 0) return cudaSuccess;
   if (rx && fp32) return cudaErrorInvalidValue;   // FP32 path: XCHF gam_2 only
-  if (rx) gam2_raw_kernel<1, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
-  else if (fp32) gam2_raw_kernel<0, true><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
-  else gam2_raw_kernel<0, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup);
+  const double tau = mixed_recompute_tau();
+  if (rx) gam2_raw_kernel<1, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup, tau);
+  else if (fp32) gam2_raw_kernel<0, true><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup, tau);
+  else gam2_raw_kernel<0, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup, tau);
   return cudaGetLastError();
 }
+
+namespace {
+std::atomic<double> g_tau_gam2{kMixedTauGam2};
+}
+void set_mixed_recompute_tau(double tau) { g_tau_gam2.store(tau); }
+double mixed_recompute_tau() { return g_tau_gam2.load(); }
 
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rx, double* x1,
                             double* x2, cudaStream_t s, int fp32) {

@@ -2,10 +2,11 @@
 // GPU and usable as plain C++ (every function is __host__ __device__).
 // Included by md_math.cuh (real = double, namespace md: the FP64 path that
 // matches the reference) and md_math32.cuh (real = float, namespace md32:
-// the mixed-precision path).  In both instances the Boys function and the
-// R_tuv recursion seeds (-2 alpha)^j F_j(T) are evaluated in FP64; md32
-// narrows each seed to FP32 before the recursion, and its Gaussian-product
-// set-up, Hermite and derivative tables, recursion and contraction are FP32.
+// the mixed-precision path).  In both instances the Boys function, the
+// seeds (-alpha)^m F_m(T) and the final Hermite-Coulomb sum are FP64; md32's
+// Gaussian-product set-up, Hermite and derivative tables and the Hermite
+// folds are FP32.  The mixed gam_2 build re-evaluates every md32 result
+// whose contribution is large with md (dynamic precision, k_md.cu).
 //
 // The reference evaluates each primitive integral as a 9- or 12-deep loop
 // over Hermite indices, and inside every iteration re-derives the Boys'
@@ -144,12 +145,26 @@ NX_HD double boys_rinv(int j) {
 static __device__ const double kHermCDev[17 * 17] = {NX_HERMC_VALUES};
 #endif
 static const double kHermCHost[17 * 17] = {NX_HERMC_VALUES};
+// FP32 copy for the FP32 contractions (no double-to-float conversion in
+// their inner loops; the values are exact in FP32 up to t = 11 and rounded
+// to FP32 beyond)
+#if defined(__CUDACC__)
+static __device__ const float kHermC32Dev[17 * 17] = {NX_HERMC_VALUES};
+#endif
+static const float kHermC32Host[17 * 17] = {NX_HERMC_VALUES};
 #undef NX_HERMC_VALUES
 NX_HD double hermc(int t, int i) {
 #if defined(__CUDA_ARCH__)
   return __ldg(&kHermCDev[t * 17 + i]);
 #else
   return kHermCHost[t * 17 + i];
+#endif
+}
+NX_HD float hermc32(int t, int i) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&kHermC32Dev[t * 17 + i]);
+#else
+  return kHermC32Host[t * 17 + i];
 #endif
 }
 
@@ -215,6 +230,58 @@ NX_BIG void boys(int M, double T, double* F) {
     f = fma(f, t2, ex) * (0.5 * boys_rinv(L));   // (2T F_(L+1) + e^-T) / (2L + 1)
     F[L] = f;
   }
+}
+
+// sum_{m=0..L} (-alpha)^m F_m(T) b(m) in FP64 (L <= 16), with boys()'s
+// Boys function evaluated inside the sum and no F table: for T <= 20 the
+// downward recursion from F_L runs alongside a Horner evaluation in
+// (-alpha) (s <- s (-alpha) + F_m b(m)), F_L and exp(d) by Horner in d;
+// for T > 20 (and NaN) the asymptotic upward recursion runs alongside the
+// ascending sum.  b(m) is called once per m, from m = L down (T <= 20) or
+// from m = 0 up.  Equal to boys() followed by the sum to rounding.
+template <class BF>
+NX_HD double boys_sum(int L, double T, double alpha, BF&& b) {
+  const double ma = -alpha;
+  if (!(T <= 20.0)) {
+    const double rT = 1.0 / T;
+    double f = 0.88622692545275801365 / sqrt(T);
+    double s = f * (double)b(0), pw = 1.0;
+    for (int m = 1; m <= L; m++) {
+      f = f * ((double)m - 0.5) * rT;
+      pw *= ma;
+      s = fma(pw * f, (double)b(m), s);
+    }
+    return s;
+  }
+  int g = (int)(T * 16.0 + 0.5);
+  g = g < 0 ? 0 : (g > kBoysRows - 1 ? kBoysRows - 1 : g);
+  const double d = (double)g * 0.0625 - T;
+  const int row = g * kBoysCols;
+  const double d2 = d * 0.5, d3 = d * (1.0 / 3.0), d4 = d * 0.25, d5 = d * 0.2,
+               d6 = d * (1.0 / 6.0);
+  // F_L(T) = sum_k F_(L+k)(T_g) d^k / k!
+  double f = boys_tab(row + L + 6);
+  f = fma(f, d6, boys_tab(row + L + 5));
+  f = fma(f, d5, boys_tab(row + L + 4));
+  f = fma(f, d4, boys_tab(row + L + 3));
+  f = fma(f, d3, boys_tab(row + L + 2));
+  f = fma(f, d2, boys_tab(row + L + 1));
+  f = fma(f, d, boys_tab(row + L));
+  double s = f * (double)b(L);
+  if (L == 0) return s;
+  double ep = 1.0 + d6;   // exp(d), the same seven terms
+  ep = fma(ep, d5, 1.0);
+  ep = fma(ep, d4, 1.0);
+  ep = fma(ep, d3, 1.0);
+  ep = fma(ep, d2, 1.0);
+  ep = fma(ep, d, 1.0);
+  const double ex = boys_tab(row + kBoysCols - 1) * ep;
+  const double t2 = 2.0 * T;
+  for (int m = L - 1; m >= 0; m--) {
+    f = fma(f, t2, ex) * (0.5 * boys_rinv(m));
+    s = fma(s, ma, f * (double)b(m));
+  }
+  return s;
 }
 }  // namespace neoxc
 #endif
@@ -576,6 +643,7 @@ NX_BIG void g3_wvec(const G3& s, int d, real bf, real bg, real bh,
 NX_BIG real contract_wr(const real* Wx, int nx, const real* Wy, int ny,
                         const real* Wz, int nz, real T, real alpha,
                         const real* R3) {
+  constexpr bool k32 = sizeof(real) == sizeof(float);
   const real* W[3] = {Wx, Wy, Wz};
   const int n[3] = {nx, ny, nz};
   real A[3][LTOT + 1];
@@ -586,24 +654,19 @@ NX_BIG real contract_wr(const real* Wx, int nx, const real* Wy, int ny,
     for (int i = 0; i <= n[d]; i++) A[d][i] = R_(0.0);
     for (int t = 0; t <= n[d]; t++)
       for (int i = (t + 1) / 2; i <= t; i++)
-        A[d][i] += W[d][t] * (real)hermc(t, i) * xp[2 * i - t];
+        A[d][i] += W[d][t] * (k32 ? (real)hermc32(t, i) : (real)hermc(t, i)) * xp[2 * i - t];
   }
   real Bxy[2 * LTOT + 1];
   for (int m = 0; m <= nx + ny; m++) Bxy[m] = R_(0.0);
   for (int i = 0; i <= nx; i++)
     for (int j = 0; j <= ny; j++) Bxy[i + j] += A[0][i] * A[1][j];
   const int L = nx + ny + nz;
-  double F[LTOT + 1];
-  boys(L, (double)T, F);
-  const double ma = -(double)alpha;
-  double s = 0.0, pw = 1.0;
-  for (int m = 0; m <= L; m++) {
+  const double s = boys_sum(L, (double)T, (double)alpha, [&](int m) {
     real bm = R_(0.0);
     const int lo = m - nz > 0 ? m - nz : 0, hi = m < nx + ny ? m : nx + ny;
     for (int i = lo; i <= hi; i++) bm += Bxy[i] * A[2][m - i];
-    s += pw * F[m] * (double)bm;
-    pw *= ma;
-  }
+    return bm;
+  });
   return (real)s;
 }
 
@@ -623,9 +686,7 @@ NX_BIG real g3_coulomb(const G3& s, real C0, real C3, real bf, real bg, real bh,
       const real wd = ((s.pr[0].K[d] * s.pr[1].K[d]) * s.pr[2].K[d]) * s.D[d][0];
       w = d == 0 ? wd : w * wd;
     }
-    double F[1];
-    boys(0, (double)T, F);
-    return C0 * C3 * (w * (real)F[0]);
+    return C0 * C3 * (w * (real)boys_sum(0, (double)T, 0.0, [](int) { return 1.0; }));
   }
   real W[3][LTOT + 1];
   int n[3];
@@ -697,9 +758,7 @@ NX_BIG void g3_vxc_multi(const G3& s, int nat, const double* cat, real* out) {
     }
     const real T = alpha * R2;
     if (all_s) {
-      double F[1];
-      boys(0, (double)T, F);
-      out[ia] = C0 * C3 * (w * (real)F[0]);
+      out[ia] = C0 * C3 * (w * (real)boys_sum(0, (double)T, 0.0, [](int) { return 1.0; }));
     } else {
       out[ia] = C0 * C3 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], T, alpha, Rv);
     }
@@ -793,9 +852,7 @@ NX_BIG real g4_coulomb(const G4& s, const GK4& gk, const real* cof,
       w *= s.pr[0].K[d] * s.pr[1].K[d] * s.pr[2].K[d] * s.pr[3].K[d];
     }
     w *= exp(expo);
-    double F[1];
-    boys(0, (double)T, F);
-    return pref * (w * (real)F[0]);
+    return pref * (w * (real)boys_sum(0, (double)T, 0.0, [](int) { return 1.0; }));
   }
   real W[3][LTOT + 1];
   int nmax[3];

@@ -217,8 +217,34 @@ constexpr int kG3MaxTileKets = 1024;
 constexpr double kScreenThreshold = 1.0e-12;   // NEOXC_SCF_SCREEN
 cudaError_t launch_gam2_raw(const DevSystem& sys, int rxchfne, double* x1,
                             double* x2, cudaStream_t s, int fp32 = 0);
+// Dynamic precision of the mixed gam_2 build (process-wide): a primitive
+// item whose FP32 contribution to a contracted element exceeds this
+// magnitude is re-evaluated in FP64.
+constexpr double kMixedTauGam2 = 1.0e-5;
+void set_mixed_recompute_tau(double tau);
+double mixed_recompute_tau();
 cudaError_t launch_gam2_symmetrize(int ne, int np, int rxchfne, double* x1,
                                    double* x2, cudaStream_t s);
+// Many systems of one angular class in one persistent launch: both passes of
+// the four-particle terms of every system go through one device work queue
+// (an atomic counter over items numbered system by system), each CTA taking
+// `chunk` items at a time; r4a receives the G4Vep pass, r4b the G4Vee pass
+// (launch_gam3_add adds them).  Grid: ctas_per_sm CTAs per SM.  limit caps
+// the items processed (the autotuner's samples; < 0: all).  scratch:
+// gam3_batch_scratch_bytes(nsys) of device memory for the system table,
+// the item prefix sums and the counter.
+struct G3BatchSys {
+  DevSystem S;
+  const double* erec;
+  const double* prec;
+  double* r4a;
+  double* r4b;
+};
+size_t gam3_batch_scratch_bytes(int nsys);
+cudaError_t launch_gam3_batch_pairs(const G3BatchSys* h_sys, int nsys, int fp32, double screen,
+                                    void* scratch, int ctas_per_sm, int chunk, long long limit,
+                                    long long* total_items, cudaStream_t s);
+cudaError_t launch_gam3_add(long long n, double* a, const double* b, cudaStream_t s);
 // launch_gam3_pairs + launch_gam3_raw_range over every tuple
 cudaError_t launch_gam3_raw(const DevSystem& sys, double* aux, double* x3,
                             cudaStream_t s, int fp32 = 0, double screen = 0.0);

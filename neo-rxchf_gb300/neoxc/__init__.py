@@ -61,6 +61,10 @@ def _declare(L):
         "neoxc_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
         "neoxc_gam3_ic1": (I, [i64] * 8 + [d] + [vp] * 16),
         "neoxc_gam3_ic1_opts": (I, [i64] * 9 + [d] + [vp] * 17),
+        "neoxc_gam3_ic1_batch": (I, [vp, i64, i64, vp, vp]),
+        "neoxc_gam3_batch_tuning": (i64, [vp, i64]),
+        "neoxc_set_mixed_threshold": (I, [d]),
+        "neoxc_get_mixed_threshold": (d, []),
         "neoxc_rxchfne_gam2_ic1": (I, [i64] * 8 + [d] + [vp] * 17),
         "neoxc_gam3_dscf": (I, [i64] * 8 + [d] + [vp] * 20),
         "neoxc_gam2_dscf": (I, [i64] * 8 + [d] + [vp] * 23),
@@ -454,8 +458,9 @@ def xchf_scf(s: NeoSystem, DE, DP=None, nucst=None, maxit: int = 100,
     """xcscf.f XCHF RHF SCF on the GPU (plain Roothaan, or DIIS).  DE: initial
     electronic density, or None for the core-Hamiltonian guess (guess_elec);
     DP: initial nuclear density, or None for the core-Hamiltonian guess
-    (guess_prot).  mixed: False (all FP64), "gam3"
-    (FP32 MD integrals for gam_3), True (FP32 for gam_1, gam_2 and gam_3).
+    (guess_prot).  mixed: False (all FP64), "gam3" (FP32 MD integrals for
+    gam_3), "gam2" (FP32 for gam_2, its large items in FP64: see
+    set_mixed_threshold), True (both).
     screen: skip gam_3 primitive (bra, ket) pairs whose Schwarz-type
     estimate is below 1e-12 (NEOXC_SCF_SCREEN).  soscf: the reference's
     second-order steps on the electronic orbitals (NEOXC_SCF_SOSCF; not with
@@ -464,7 +469,7 @@ def xchf_scf(s: NeoSystem, DE, DP=None, nucst=None, maxit: int = 100,
     converged densities, the iteration count and the convergence flag."""
     ne, np_ = s.nebf, s.npbf
     opts = ((1 if DP is None else 0) | (2 if diis else 0) | (4 if gam4_element else 0)
-            | (8 if mixed else 0) | (16 if mixed is True else 0) | (32 if DE is None else 0)
+            | _mixed_bits(mixed) | (32 if DE is None else 0)
             | (64 if screen else 0) | (128 if soscf else 0))
     de = np.zeros(ne * ne) if DE is None else _fmat(DE).copy()
     dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
@@ -497,7 +502,7 @@ def xcuhf_scf(s: NeoSystem, nae: int, nbe: int, DAE=None, DBE=None, DP=None, nuc
     ne, np_ = s.nebf, s.npbf
     guess_e = DAE is None or DBE is None
     opts = ((1 if DP is None else 0) | (32 if guess_e else 0) | (2 if diis else 0)
-            | (8 if mixed else 0) | (16 if mixed is True else 0))
+            | _mixed_bits(mixed))
     da = np.zeros(ne * ne) if guess_e else _fmat(DAE).copy()
     db = np.zeros(ne * ne) if guess_e else _fmat(DBE).copy()
     dp = np.zeros(np_ * np_) if DP is None else _fmat(DP).copy()
@@ -532,6 +537,43 @@ class XchfJob(C.Structure):
                    ("t_end", C.c_double)])
 
 
+def gam3_ic1_batch(systems, mixed: bool = False, screen: bool = False):
+    """GAM3_IC1 for many systems through neoxc_gam3_ic1_batch (one
+    persistent launch per angular class over a device work queue, grid
+    chosen by the built-in autotuner).  Returns (list of GM3ICR arrays,
+    device seconds of the build)."""
+    n = len(systems)
+    jobs = (XchfJob * n)()
+    bufs = [_fill_job(jobs[k], s, np.eye(s.nebf), None, 1) for k, s in enumerate(systems)]
+    outs = [np.empty(s.ng3) for s in systems]
+    ptrs = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+    sec = np.zeros(1)
+    opts = (8 if mixed else 0) | (64 if screen else 0)
+    _check(lib().neoxc_gam3_ic1_batch(C.cast(jobs, C.c_void_p), n, opts, ptrs, _p(sec)))
+    del bufs
+    return outs, float(sec[0])
+
+
+def set_mixed_threshold(tau: float) -> None:
+    """neoxc_set_mixed_threshold: the contribution magnitude above which a
+    mixed gam_2 primitive item is re-evaluated in FP64 (0: all, inf: none)."""
+    _check(lib().neoxc_set_mixed_threshold(float(tau)))
+
+
+def get_mixed_threshold() -> float:
+    """neoxc_get_mixed_threshold."""
+    return float(lib().neoxc_get_mixed_threshold())
+
+
+def gam3_batch_tuning() -> list:
+    """The autotuner's choices so far (neoxc_gam3_batch_tuning)."""
+    import json
+    n = lib().neoxc_gam3_batch_tuning(None, 0)
+    buf = C.create_string_buffer(int(n) + 1)
+    lib().neoxc_gam3_batch_tuning(buf, n + 1)
+    return json.loads(buf.value.decode())
+
+
 def xchf_scf_batch(systems, DEs, DPs=None, nworkers: int = 8, maxit: int = 100,
                    diis: bool = False, mixed=False, gam4_element: bool = False):
     """Independent XCHF solves through neoxc_xchf_scf_batch (worker threads
@@ -549,9 +591,17 @@ def xchf_scf_batch(systems, DEs, DPs=None, nworkers: int = 8, maxit: int = 100,
     return [_job_result(jobs[k], b) for k, b in enumerate(bufs)]
 
 
+def _mixed_bits(mixed):
+    """NEOXC_SCF_MIXED (8: gam_3) and NEOXC_SCF_MIXED_GAM2 (16: gam_2) for
+    mixed = False, "gam3", "gam2" or True (both)."""
+    if mixed not in (False, None, True, "gam3", "gam2"):
+        raise ValueError("mixed: False, 'gam3', 'gam2' or True")
+    return (8 if mixed in (True, "gam3") else 0) | (16 if mixed in (True, "gam2") else 0)
+
+
 def _scf_options(guess_prot, diis, mixed, gam4_element):
     return ((1 if guess_prot else 0) | (2 if diis else 0) | (4 if gam4_element else 0)
-            | (8 if mixed else 0) | (16 if mixed is True else 0))
+            | _mixed_bits(mixed))
 
 
 def _fill_job(j, s, DE, DP, maxit):

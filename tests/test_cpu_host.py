@@ -217,7 +217,8 @@ def test_composite_bra_form_matches_g4_integrals(orc, hostcheck):
     integrated out) and the free electron's pair density, with the factorised
     Hermite-Coulomb sum (g3_fatbra.cuh).  FP64: the oracle's restatement of
     the reference's 12-deep loops (XC1_G4_MD.f) to 1e-10 relative; FP32 (the
-    mixed path, FP64 Boys function and seeds): at the FP32 level."""
+    mixed path: FP32 tables, FP64 Boys function, seeds and sum): at the FP32
+    level."""
     O, L, H = orc, orc.lib(), hostcheck
     P = C.POINTER(O.Prim)
     d = C.c_double
@@ -298,7 +299,7 @@ def test_md32_instance_within_fp32_error(orc, hostcheck):
 def _header_symbols():
     txt = open(os.path.join(ROOT, "include", "neoxc.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    names = re.findall(r"\b(?:int|int64_t|void|const char\*)\s+([a-z0-9_]+)\s*\(", txt)
+    names = re.findall(r"\b(?:int|int64_t|void|double|const char\*)\s+([a-z0-9_]+)\s*\(", txt)
     return sorted(set(names))
 
 
@@ -319,7 +320,7 @@ def _header_arg_counts():
     txt = open(os.path.join(ROOT, "include", "neoxc.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     out = {}
-    for m in re.finditer(r"\b(?:int|int64_t|void|const char\*)\s+([a-z0-9_]+)\s*\(([^)]*)\)",
+    for m in re.finditer(r"\b(?:int|int64_t|void|double|const char\*)\s+([a-z0-9_]+)\s*\(([^)]*)\)",
                          txt):
         args = m.group(2).strip()
         out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
@@ -341,6 +342,22 @@ def test_ctypes_signatures_match_header():
         assert len(f.argtypes) == n, (name, len(f.argtypes), n)
         checked += 1
     assert checked >= 30
+
+
+def test_mixed_threshold_argument_check():
+    """neoxc_set_mixed_threshold is host-only: it accepts tau >= 0 (and
+    infinity), refuses negative or NaN thresholds with NEOXC_ERR_ARG, and
+    neoxc_get_mixed_threshold reads the value back."""
+    import neoxc
+    old = neoxc.get_mixed_threshold()
+    assert old == 1e-5
+    for bad in (-1.0, float("nan")):
+        with pytest.raises(neoxc.NeoxcError):
+            neoxc.set_mixed_threshold(bad)
+    assert neoxc.get_mixed_threshold() == old
+    neoxc.set_mixed_threshold(float("inf"))
+    assert neoxc.get_mixed_threshold() == float("inf")
+    neoxc.set_mixed_threshold(old)
 
 
 def test_batch_job_struct_layout():

@@ -162,6 +162,30 @@ def test_mixed_precision_spd_energy_error(nx):
     assert abs(err) <= 1e-6
 
 
+def test_mixed_gam2_dynamic_precision(nx):
+    """The mixed gam_2 build re-evaluates in FP64 every primitive item whose
+    FP32 contribution exceeds the threshold: at threshold 0 every item is
+    FP64 and the first-iteration energy equals the FP64 path's to rounding;
+    at the default threshold the FP32 error left is at most half that of
+    the all-FP32 build (threshold infinity)."""
+    from neoxc import basis
+    s = basis.synthetic(**SPD_SYSTEM)
+    ref = nx.xchf_scf(s, None, maxit=1)["initial"]["E_total"]
+    old = nx.get_mixed_threshold()
+    try:
+        nx.set_mixed_threshold(0.0)
+        e_all64 = nx.xchf_scf(s, None, maxit=1, mixed="gam2")["initial"]["E_total"]
+        nx.set_mixed_threshold(float("inf"))
+        e_all32 = nx.xchf_scf(s, None, maxit=1, mixed="gam2")["initial"]["E_total"]
+    finally:
+        nx.set_mixed_threshold(old)
+    e_dyn = nx.xchf_scf(s, None, maxit=1, mixed="gam2")["initial"]["E_total"]
+    print("gam_2 E error all-FP32 %.3e dynamic %.3e all-FP64 %.3e"
+          % (e_all32 - ref, e_dyn - ref, e_all64 - ref))
+    assert abs(e_all64 - ref) <= 1e-11
+    assert abs(e_dyn - ref) <= max(0.5 * abs(e_all32 - ref), 1e-10)
+
+
 def test_screened_scf_matches_unscreened(nx):
     """Schwarz-type screening at 1e-12 (NEOXC_SCF_SCREEN) moves the
     converged energy of the s/p/d system by less than 1e-8 Eh."""
