@@ -327,6 +327,117 @@ __global__ void fockp_reduce_kernel(int np, int nchunk,
   if (threadIdx.x == 0) *E = t;
 }
 
+// ---- mixed-precision forms of the two GAM_2s passes (tensor-core build) ----
+// The FP64 forms above issue one FP64 FMA per GAM_2s element, which on this
+// GPU (FP64 at 1/64 of the FP32 rate) costs more than reading the element
+// from HBM.  These narrow each element to FP32 on the integer pipes
+// (tc::narrow_f64) and multiply in FP32; partial sums are FP32 over at most
+// kMixChunk terms and FP64 beyond, so the result carries ~1e-7 relative
+// rounding (the GAM_2s values themselves are FP64 in memory).
+constexpr int kMixChunk = 64;
+constexpr int kDpShared = 12288;   // np^2 up to this: DP staged in shared memory
+
+// G[r] = sum_p DP(p) GAM_2s[p][r]  (DP column-major, p = ip*np + jp as above);
+// two consecutive elements per thread (16-byte loads) when every row p * n4
+// stays 16-byte aligned, i.e. n4 even.
+__global__ void __launch_bounds__(256, 4)
+dp_contract_mixed_kernel(long long n4, int np, const double* __restrict__ g2s,
+                         const double* __restrict__ DP, double* __restrict__ G) {
+  extern __shared__ float sdp[];   // [np*np] in the loop order of g2s, if staged
+  const int np2 = np * np;
+  const bool staged = np2 <= kDpShared;
+  if (staged)
+    for (int p = threadIdx.x; p < np2; p += blockDim.x) {
+      const int ip = p / np, jp = p - ip * np;
+      sdp[p] = tc::narrow_f64(DP[ip + np * jp]);
+    }
+  __syncthreads();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long nv = (n4 & 1) ? n4 : n4 / 2;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += stride) {
+    double acc0 = 0.0, acc1 = 0.0;
+    for (int p0 = 0; p0 < np2; p0 += kMixChunk) {
+      const int p1 = p0 + kMixChunk < np2 ? p0 + kMixChunk : np2;
+      float a0 = 0.0f, a1 = 0.0f;
+      if (n4 & 1) {
+#pragma unroll 8
+        for (int p = p0; p < p1; p++) {
+          const float d = staged ? sdp[p] : tc::narrow_f64(DP[(p / np) + np * (p % np)]);
+          a0 = fmaf(d, tc::narrow_f64(__ldg(g2s + (long long)p * n4 + v)), a0);
+        }
+      } else {
+#pragma unroll 8
+        for (int p = p0; p < p1; p++) {
+          const float d = staged ? sdp[p] : tc::narrow_f64(DP[(p / np) + np * (p % np)]);
+          const double2 g = __ldg(reinterpret_cast<const double2*>(g2s + (long long)p * n4) + v);
+          a0 = fmaf(d, tc::narrow_f64(g.x), a0);
+          a1 = fmaf(d, tc::narrow_f64(g.y), a1);
+        }
+      }
+      acc0 += (double)a0;
+      acc1 += (double)a1;
+    }
+    if (n4 & 1) {
+      G[v] = acc0;
+    } else {
+      G[2 * v] = acc0;
+      G[2 * v + 1] = acc1;
+    }
+  }
+}
+
+// Wf[r] = narrow_f64(W[r])
+__global__ void narrow_kernel(long long n, const double* __restrict__ in,
+                              float* __restrict__ out) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x)
+    out[r] = tc::narrow_f64(in[r]);
+}
+
+// part[p*nchunk + chunk] = sum_{r in chunk} GAM_2s[p][r] Wf[r], FP32
+// products; each thread sums its kDotChunk / kDotTB (= kMixChunk) terms in
+// FP32, the block in FP64.  Wf: W narrowed once (narrow_kernel), so the
+// np^2 re-reads of it come from L2 at half the bytes.
+// A CTA takes kDotP consecutive p (grid (nchunk, ceil(np^2 / kDotP))) so
+// that each Wf element it loads serves kDotP products.
+static_assert(kDotChunk / kDotTB == kMixChunk, "one FP32 partial sum per thread");
+constexpr int kDotP = 2;
+__global__ void __launch_bounds__(kDotTB, 4)
+fockp_dot_mixed_kernel(long long n4, int nchunk, int np2,
+                       const double* __restrict__ g2s,
+                       const float* __restrict__ Wf,
+                       double* __restrict__ part) {
+  __shared__ double sw[kDotP][kDotTB / 32];
+  const int p0 = blockIdx.y * kDotP;
+  const int pn = np2 - p0 < kDotP ? np2 - p0 : kDotP;
+  const long long base = (long long)blockIdx.x * kDotChunk;
+  const long long end = base + kDotChunk < n4 ? base + kDotChunk : n4;
+  float a[kDotP];
+#pragma unroll
+  for (int j = 0; j < kDotP; j++) a[j] = 0.0f;
+#pragma unroll 4
+  for (long long r = base + threadIdx.x; r < end; r += blockDim.x) {
+    const float w = __ldg(Wf + r);
+#pragma unroll
+    for (int j = 0; j < kDotP; j++)
+      if (j < pn) a[j] = fmaf(tc::narrow_f64(__ldg(g2s + (long long)(p0 + j) * n4 + r)), w, a[j]);
+  }
+  // kDotP block sums in FP64: warp shuffles, then one warp over the warps
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < kDotP; j++) {
+    double v = (double)a[j];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sw[j][warp] = v;
+  }
+  __syncthreads();
+  if (warp < kDotP && warp < pn) {
+    double v = lane < kDotTB / 32 ? sw[warp][lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) part[(long long)(p0 + warp) * nchunk + blockIdx.x] = v;
+  }
+}
+
 // ---- 6. focke ---------------------------------------------------------------
 // CTA per (a,c): part[(a*n+c)][x*n+b] = sum_y Ws(a,x,c,y) H_G(a,b,c,y)
 //                                      + Vs(a,x,c,y) H_E(a,b,c,y),
@@ -470,13 +581,16 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
   uint32_t phase = 0;
   bool ok = true;
   const uint32_t idesc = tc::instr_desc();
-  // each 64-wide K tile is accumulated in TMEM (FP32) and then folded into
-  // this thread's FP64 row of the result
+  // kFoldTiles 64-wide K tiles are accumulated in TMEM (FP32) and then
+  // folded into this thread's FP64 row of the result
   double acc[tc::kTileN];
 #pragma unroll
   for (int i = 0; i < tc::kTileN; i++) acc[i] = 0.0;
   const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-  for (long long kt = kbeg; kt < kend && ok; kt += tc::kTileK) {
+  int tile = 0;
+  for (long long kt = kbeg; kt < kend && ok; kt += tc::kTileK, tile++) {
+    const bool first = tile % tc::kFoldTiles == 0;
+    const bool fold = (tile + 1) % tc::kFoldTiles == 0 || kt + tc::kTileK >= kend;
     for (int e = tid; e < tc::kTileM * tc::kTileK; e += tc::kThreads) {
       const int r = e / tc::kTileK, k = e - r * tc::kTileK;
       const long long gm = m0 + r, gk = kt + k;
@@ -506,7 +620,7 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
       for (int st = 0; st < tc::kTileK / 8; st++) {
         const uint32_t o = st * 256;   // two 128-byte core matrices per K step
         tc::mma_tf32(tmem, tc::smem_desc(ah + o), tc::smem_desc(bh + o), idesc,
-                     st > 0 ? 1 : 0);
+                     (st > 0 || !first) ? 1 : 0);
         tc::mma_tf32(tmem, tc::smem_desc(ah + o), tc::smem_desc(bl + o), idesc, 1);
         tc::mma_tf32(tmem, tc::smem_desc(al + o), tc::smem_desc(bh + o), idesc, 1);
       }
@@ -515,7 +629,7 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
     ok = __syncthreads_and(tc::mbar_wait(mb, phase) ? 1 : 0) != 0;
     phase ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
+    if (ok && fold) {
 #pragma unroll
       for (int c = 0; c < tc::kTileN / 16; c++) {
         float v[16];
@@ -531,14 +645,20 @@ tc_gemm_kernel(const double* __restrict__ A, long long lda, long long M,
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);
   } else {
-    const long long row = m0 + warp * 32 + lane;
-    double* out = C + (long long)blockIdx.z * split_stride;
-    if (row < M)
+    // every MMA has completed (last wait) and the operand tiles are dead:
+    // stage the 128 x 64 FP64 tile in their shared memory (row stride 65)
+    // and write it row-segment by row-segment, coalesced
+    double* sc = reinterpret_cast<double*>(tc_sm);
+    const int rloc = warp * 32 + lane;
 #pragma unroll
-      for (int i = 0; i < tc::kTileN; i++) {
-        const long long n = n0 + i;
-        if (n < N) out[row * ldc + n] = alpha * acc[i];
-      }
+    for (int i = 0; i < tc::kTileN; i++) sc[rloc * (tc::kTileN + 1) + i] = alpha * acc[i];
+    __syncthreads();
+    double* out = C + (long long)blockIdx.z * split_stride;
+    for (int e = tid; e < tc::kTileM * tc::kTileN; e += tc::kThreads) {
+      const int r = e / tc::kTileN, c = e - r * tc::kTileN;
+      const long long row = m0 + r, n = n0 + c;
+      if (row < M && n < N) out[row * ldc + n] = sc[r * (tc::kTileN + 1) + c];
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -600,7 +720,7 @@ __global__ void focke_tc_reduce_kernel(int n, int nsplit, const double* __restri
   }
 }
 
-constexpr long long kFockeKChunk = 4096;
+constexpr long long kFockeKChunk = 1024;
 
 cudaError_t tc_gemm(const double* A, long long lda, long long M, const double* B,
                     long long ldb, long long N, long long K, long long kchunk, double alpha,
@@ -754,8 +874,9 @@ cudaError_t launch_gam4_factored_tc(int ne, int np, const double* gee,
   auto last_b = [&](const double* in, double* out, double alpha) {
     return tc_gemm(in, n, n3, DE, n, n, n, n, alpha, out, n, 0, err, s);
   };
-  // 1. G = DP . GAM_2s (FP64, HBM)
-  dp_contract_kernel<<<g_n4, TB, 0, s>>>(n4, np, g2s, DP, buf[0]);
+  // 1. G = DP . GAM_2s (FP32 products, HBM)
+  dp_contract_mixed_kernel<<<g_n4, 256, np * np <= kDpShared ? sizeof(float) * np * np : 0, s>>>(
+      n4, np, g2s, DP, buf[0]);
   // 2. H_G, G' and H_E, E'
   TRY(last_f(buf[0], buf[1]));                                        // H_G
   pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[1], 0.0, buf[2]);
@@ -775,7 +896,10 @@ cudaError_t launch_gam4_factored_tc(int ne, int np, const double* gee,
   TRY(last_b(buf[0], buf[3], 0.5));
   pair_swap_kernel<<<tgrid, tblk, 0, s>>>((int)n2, buf[3], 0.0, buf[5]);
   TRY(last_b(buf[5], buf[6], 1.0));                                   // W
-  fockp_dot_kernel<<<dim3(nchunk, np * np), kDotTB, 0, s>>>(n4, nchunk, g2s, buf[6], fpart);
+  float* Wf = reinterpret_cast<float*>(buf[7]);   // free until swap12 below
+  narrow_kernel<<<g_n4, TB, 0, s>>>(n4, buf[6], Wf);
+  fockp_dot_mixed_kernel<<<dim3(nchunk, (np * np + kDotP - 1) / kDotP), kDotTB, 0, s>>>(
+      n4, nchunk, np * np, g2s, Wf, fpart);
   fockp_reduce_kernel<<<1, 256, 0, s>>>(np, nchunk, fpart, DP, accumulate, fockp, E);
   // 6. focke(x,b) = sum_{a,c,y} Ws(a,x,c,y) H_G(a,b,c,y) + Vs(a,x,c,y) H_E(a,b,c,y)
   swap12_kernel<<<g_n4, TB, 0, s>>>(n, buf[0], buf[3]);   // Ws  -> [x][a][c][y]

@@ -622,6 +622,14 @@ cudaError_t launch_gam2_raw_range(const DevSystem& sys, int rx, long long t0,
   if (ntup <= 0) return cudaSuccess;
   if (rx && fp32) return cudaErrorInvalidValue;   // FP32 path: XCHF gam_2 only
   const double tau = mixed_recompute_tau();
+  // the builders keep their integral set-ups in local memory: prefer the
+  // largest L1 share of the unified L1 / shared-memory array (a hint)
+  if (rx) cudaFuncSetAttribute(gam2_raw_kernel<1, false>,
+                               cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  else if (fp32) cudaFuncSetAttribute(gam2_raw_kernel<0, true>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  else cudaFuncSetAttribute(gam2_raw_kernel<0, false>,
+                            cudaFuncAttributePreferredSharedMemoryCarveout, 0);
   if (rx) gam2_raw_kernel<1, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup, tau);
   else if (fp32) gam2_raw_kernel<0, true><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup, tau);
   else gam2_raw_kernel<0, false><<<blocks, 64, 0, s>>>(sys, x1, x2, t0, ntup, tau);

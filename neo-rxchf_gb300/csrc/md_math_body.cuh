@@ -380,7 +380,7 @@ NX_BIG void dgauss3(const GK3& g, const real* X, int N1, int N2, int N3,
     }
   }
   const real base = exp(expo);
-#define D3(a, b, c) D[((a) * TD + (b)) * TD + (c)]
+#define D3(a, b, c) D[((a) * (N2 + 1) + (b)) * (N3 + 1) + (c)]
   for (int n1 = 0; n1 <= N1; n1++)
     for (int n2 = 0; n2 <= N2; n2++)
       for (int n3 = 0; n3 <= N3; n3++) {
@@ -475,7 +475,7 @@ struct G3 {
   real C1, C2, S1, S2, Sm1[3], Sm2[3];
   GK3 gk;
   int T[3][3];                 // [particle][dim] max t incl. KE shift
-  real D[3][TD * TD * TD];   // per dimension
+  real D[3][TD * TD * TD];   // per dimension, compact [T[0]+1][T[1]+1][T[2]+1]
 };
 
 // pairs: the Gaussian products of (A[i], B[i]), which do not depend on the
@@ -538,11 +538,12 @@ NX_BIG real g3_ovl1d(const G3& s, int d, int L1, int L3) {
   hermite_e(I1, L1, pr[0].K[d], s.A[0].a, s.B[0].a, pr[0].p, pr[0].q, pr[0].Q[d], E1);
   hermite_e(I2, L2, pr[1].K[d], s.A[1].a, s.B[1].a, pr[1].p, pr[1].q, pr[1].Q[d], E2);
   hermite_e(I3, L3, pr[2].K[d], s.A[2].a, s.B[2].a, pr[2].p, pr[2].q, pr[2].Q[d], E3);
+  const int X1 = s.T[1][d] + 1, X2 = s.T[2][d] + 1;   // D's compact extents
   real acc = R_(0.0);
   for (int t1 = 0; t1 <= I1 + L1; t1++)
     for (int t2 = 0; t2 <= I2 + L2; t2++)
       for (int t3 = 0; t3 <= I3 + L3; t3++)
-        acc += E1[t1] * E2[t2] * E3[t3] * s.D[d][(t1 * TD + t2) * TD + t3];
+        acc += E1[t1] * E2[t2] * E3[t3] * s.D[d][(t1 * X1 + t2) * X2 + t3];
   return acc;
 }
 
@@ -608,6 +609,7 @@ NX_BIG void g3_wvec(const G3& s, int d, real bf, real bg, real bh,
               pr[i].p, pr[i].q, pr[i].Q[d], E[i]);
   }
   const int N = tl[0] + tl[1] + tl[2];
+  const int X1 = s.T[1][d] + 1, X2 = s.T[2][d] + 1;   // D's compact extents
   for (int n = 0; n <= N; n++) W[n] = R_(0.0);
   real pf[TD], pg[TD], ph[TD];
   pf[0] = pg[0] = ph[0] = R_(1.0);
@@ -625,7 +627,7 @@ NX_BIG void g3_wvec(const G3& s, int d, real bf, real bg, real bh,
             for (int x3 = 0; x3 <= t3; x3++) {
               real c = binom(t1, x1) * binom(t2, x2) * binom(t3, x3) *
                          pf[x1] * pg[x2] * ph[x3] *
-                         s.D[d][((t1 - x1) * TD + (t2 - x2)) * TD + (t3 - x3)];
+                         s.D[d][((t1 - x1) * X1 + (t2 - x2)) * X2 + (t3 - x3)];
               W[x1 + x2 + x3] += e * c;
             }
       }

@@ -5,7 +5,8 @@
 // a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi, ~2^-21 relative), and FP64 output.
 //
 // One CTA of 128 threads owns one 128-row tile of A and one 64-row tile of B
-// and loops over K in steps of 64:
+// and loops over K in steps of 64 (the FP32 accumulator in tensor memory
+// is folded into FP64 registers every kFoldTiles tiles):
 //   * every thread loads FP64 elements, splits them and stores the TF32
 //     halves in shared memory in the canonical no-swizzle K-major layout of
 //     the tensor-core descriptors (8-row x 16-byte core matrices, 128 B
@@ -18,7 +19,7 @@
 //   * every thread waits on the mbarrier (bounded: after kSpinLimit polls the
 //     kernel records an error flag instead of hanging);
 // and finally each warp reads its 32 accumulator lanes with tcgen05.ld and
-// writes (or adds) FP64 results.  Tensor memory (64 columns) is allocated
+// the CTA writes the FP64 tile through shared memory, coalesced.  Tensor memory (64 columns) is allocated
 // and freed by warp 0.  Operand rows past M or N and K past the end read as
 // zero.
 #pragma once
@@ -29,6 +30,8 @@ namespace neoxc {
 namespace tc {
 
 constexpr int kTileM = 128, kTileN = 64, kTileK = 64;
+// K tiles accumulated in tensor memory (FP32) between two FP64 folds
+constexpr int kFoldTiles = 4;
 constexpr int kThreads = 128;
 constexpr long long kSpinLimit = 1LL << 26;
 
@@ -36,6 +39,9 @@ constexpr long long kSpinLimit = 1LL << 26;
 constexpr int kABytes = kTileM * kTileK * 4;   // 32 KiB
 constexpr int kBBytes = kTileN * kTileK * 4;   // 16 KiB
 constexpr int kSmemBytes = 2 * kABytes + 2 * kBBytes + 64;
+// the epilogue's FP64 staging tile (kTileM rows of kTileN + 1) reuses the
+// operand buffers
+static_assert(kTileM * (kTileN + 1) * 8 <= 2 * kABytes + 2 * kBBytes, "epilogue tile");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -64,10 +70,35 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
   return r;
 }
 
+// FP64 -> FP32 by integer operations on the bit pattern, truncating the
+// significand to 23 bits (relative error < 2^-23): on this GPU an FP64
+// conversion instruction costs as much as an FP64 FMA, while these run on
+// the integer pipes.  Magnitudes below the FP32 normal range become signed
+// zero, above it infinity; NaN stays NaN.
+__device__ __forceinline__ float narrow_f64(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned top = (unsigned)(u >> 32);
+  const unsigned sign = top & 0x80000000u;
+  const int e = (int)((top >> 20) & 0x7ffu);
+  const int ef = e - 1023 + 127;
+  unsigned r;
+  if (e == 0x7ff)
+    r = sign | ((u & 0xfffffffffffffULL) ? 0x7fc00000u : 0x7f800000u);
+  else if (ef <= 0)
+    r = sign;
+  else if (ef >= 255)
+    r = sign | 0x7f800000u;
+  else
+    r = sign | ((unsigned)ef << 23) | (unsigned)((u >> 29) & 0x7fffffu);
+  return __uint_as_float(r);
+}
+
+// hi + lo carries the 22 leading bits of v, split in FP32 from narrow_f64
+// (f - hi is exact in FP32): no FP64-pipe instruction
 __device__ __forceinline__ void split_tf32(double v, uint32_t& hi, uint32_t& lo) {
-  const float f = (float)v;
+  const float f = narrow_f64(v);
   hi = to_tf32(f);
-  lo = to_tf32((float)(v - (double)__uint_as_float(hi)));
+  lo = to_tf32(f - __uint_as_float(hi));
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
