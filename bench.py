@@ -62,9 +62,10 @@ def parse():
     ap.add_argument("--npbf", type=int, default=NPBF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true",
-                    help="with --only gam3 / factored_tc: a small case (for ncu captures)")
+                    help="with --only gam2 / gam3 / gam3_batch / factored_tc: a small case "
+                         "(for ncu captures)")
     ap.add_argument("--only", choices=["open_shell", "xcuhf_scf", "rx_scf", "config1", "gam3",
-                                       "factored_tc", "gam3_batch"],
+                                       "factored_tc", "gam3_batch", "gam2"],
                     default=None,
                     help="run one side section and print its JSON (no headline line)")
     return ap.parse_args()
@@ -671,6 +672,37 @@ def gam3_section(neoxc, kw=None):
     return out
 
 
+def gam2_section(neoxc, small=False):
+    """The gam_2 build (GM2ICR / GM2sICR, k_md.cu) in FP64 and in the mixed
+    precision (FP32 tables, FP64 Boys function, seeds and sums, items above
+    the recompute threshold re-evaluated in FP64), timed as a one-iteration
+    XCHF SCF of a two-electron system (no gam_3: the gam_2 build dominates;
+    the one-body, GAM_1 and GAM_ee builds and one Fock build are included).
+    System: the first configuration's seeded basis with 2 electrons, or with
+    small=True the seeded nebf=8 (s/p, 3 primitives), npbf=4 (s/p/d) one."""
+    from neoxc import basis
+    if small:
+        kw = dict(seed=6, nat=3, nebf=8, nprim=3, npbf=4, ngtg=3, lmax_e=1, lmax_p=2, nelec=2)
+    else:
+        kw = dict(CONFIG1, nelec=2)
+    s = basis.synthetic(**kw)
+    out = {"workload": "one-iteration XCHF SCF, seeded nebf=%d (s/p), npbf=%d (s/p/d), NG=%d, "
+                       "nelec=2: ng2=%d" % (s.nebf, s.npbf, s.ngtg, s.nebf ** 4 * s.npbf ** 2),
+           "api": "neoxc_xchf_scf (maxit 1; host arrays)",
+           "gam2_recompute_threshold": neoxc.get_mixed_threshold()}
+    neoxc.xchf_scf(s, None, maxit=1, mixed="gam2")   # warm-up
+    E = {}
+    for name, mixed in (("mixed", "gam2"), ("fp64", False)):
+        t0 = time.perf_counter()
+        r = neoxc.xchf_scf(s, None, maxit=1, mixed=mixed)
+        dt = time.perf_counter() - t0
+        E[name] = r["initial"]["E_total"]
+        out[name] = {"seconds": dt, "E_init": E[name]}
+    out["mixed"]["E_err_vs_fp64_Eh"] = E["mixed"] - E["fp64"]
+    out["fp64_over_mixed_time"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    return out
+
+
 def gam3_batch_section(neoxc, nsys=48):
     """Many uneven systems' gam_3 in persistent launches
     (neoxc_gam3_ic1_batch): seeded molecules of 3-6 nuclei with the proton
@@ -814,6 +846,9 @@ def main():
     if args.only == "gam3":
         kw = dict(CONFIG1, nebf=6, npbf=4) if args.small else None
         print(json.dumps(gam3_section(neoxc, kw)))
+        return
+    if args.only == "gam2":
+        print(json.dumps(gam2_section(neoxc, args.small)))
         return
     if args.only == "gam3_batch":
         print(json.dumps(gam3_batch_section(neoxc, 8 if args.small else 48)))

@@ -333,15 +333,16 @@ __global__ void fockp_reduce_kernel(int np, int nchunk,
 // from HBM.  These narrow each element to FP32 on the integer pipes
 // (tc::narrow_f64) and multiply in FP32; partial sums are FP32 over at most
 // kMixChunk terms and FP64 beyond, so the result carries ~1e-7 relative
-// rounding (the GAM_2s values themselves are FP64 in memory).
+// rounding (the GAM_2s values themselves are FP64 in memory).  GAM_2s is
+// read once per pass with evict-first loads (__ldcs), which leaves L2 to
+// the re-read operands (DP, the narrowed W).
 constexpr int kMixChunk = 64;
 constexpr int kDpShared = 12288;   // np^2 up to this: DP staged in shared memory
 
 // G[r] = sum_p DP(p) GAM_2s[p][r]  (DP column-major, p = ip*np + jp as above);
 // two consecutive elements per thread (16-byte loads) when every row p * n4
 // stays 16-byte aligned, i.e. n4 even.
-__global__ void __launch_bounds__(256, 4)
-dp_contract_mixed_kernel(long long n4, int np, const double* __restrict__ g2s,
+__global__ void dp_contract_mixed_kernel(long long n4, int np, const double* __restrict__ g2s,
                          const double* __restrict__ DP, double* __restrict__ G) {
   extern __shared__ float sdp[];   // [np*np] in the loop order of g2s, if staged
   const int np2 = np * np;
@@ -363,13 +364,13 @@ dp_contract_mixed_kernel(long long n4, int np, const double* __restrict__ g2s,
 #pragma unroll 8
         for (int p = p0; p < p1; p++) {
           const float d = staged ? sdp[p] : tc::narrow_f64(DP[(p / np) + np * (p % np)]);
-          a0 = fmaf(d, tc::narrow_f64(__ldg(g2s + (long long)p * n4 + v)), a0);
+          a0 = fmaf(d, tc::narrow_f64(__ldcs(g2s + (long long)p * n4 + v)), a0);
         }
       } else {
 #pragma unroll 8
         for (int p = p0; p < p1; p++) {
           const float d = staged ? sdp[p] : tc::narrow_f64(DP[(p / np) + np * (p % np)]);
-          const double2 g = __ldg(reinterpret_cast<const double2*>(g2s + (long long)p * n4) + v);
+          const double2 g = __ldcs(reinterpret_cast<const double2*>(g2s + (long long)p * n4) + v);
           a0 = fmaf(d, tc::narrow_f64(g.x), a0);
           a1 = fmaf(d, tc::narrow_f64(g.y), a1);
         }
@@ -402,7 +403,7 @@ __global__ void narrow_kernel(long long n, const double* __restrict__ in,
 // that each Wf element it loads serves kDotP products.
 static_assert(kDotChunk / kDotTB == kMixChunk, "one FP32 partial sum per thread");
 constexpr int kDotP = 2;
-__global__ void __launch_bounds__(kDotTB, 4)
+__global__ void __launch_bounds__(kDotTB)
 fockp_dot_mixed_kernel(long long n4, int nchunk, int np2,
                        const double* __restrict__ g2s,
                        const float* __restrict__ Wf,
@@ -415,12 +416,11 @@ fockp_dot_mixed_kernel(long long n4, int nchunk, int np2,
   float a[kDotP];
 #pragma unroll
   for (int j = 0; j < kDotP; j++) a[j] = 0.0f;
-#pragma unroll 4
   for (long long r = base + threadIdx.x; r < end; r += blockDim.x) {
     const float w = __ldg(Wf + r);
 #pragma unroll
     for (int j = 0; j < kDotP; j++)
-      if (j < pn) a[j] = fmaf(tc::narrow_f64(__ldg(g2s + (long long)(p0 + j) * n4 + r)), w, a[j]);
+      if (j < pn) a[j] = fmaf(tc::narrow_f64(__ldcs(g2s + (long long)(p0 + j) * n4 + r)), w, a[j]);
   }
   // kDotP block sums in FP64: warp shuffles, then one warp over the warps
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
