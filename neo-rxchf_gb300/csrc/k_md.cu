@@ -329,11 +329,12 @@ __device__ __noinline__ void gam2_item64(const DevSystem& S, const Gam2Tuple& t,
 // `tau` in magnitude is discarded and re-evaluated in FP64 (dynamic
 // precision per primitive item, in the spirit of Luehr, Ufimtsev and
 // Martinez, J. Chem. Theory Comput. 7, 949 (2011), which selects the
-// precision per shell quartet from a Schwarz bound).  The contributions are
-// concentrated in few items (for the geminal Coulomb terms about 1% of the
-// items carry 95-99% of the sum), so the FP64 share of the work stays small
-// while the FP32 error left in the sum drops by one to two orders of
-// magnitude.  Each warp queues its large items in shared memory and
+// precision per shell quartet from a Schwarz bound).  The FP32 error left
+// in the sum is that of the small items only; how much FP64 work that takes
+// depends on the basis (at tau = 1e-5 about a quarter of the items of a
+// 12-function s/p basis with exponents up to 20, most items of a basis
+// with tight s primitives, where the mixed build costs more than the FP64
+// one).  Each warp queues its large items in shared memory and
 // re-evaluates them 32 at a time, so that the FP64 work runs on full warps.
 // The result is deterministic (fixed lane order, fixed queue order).
 template <int RX, bool F32>
