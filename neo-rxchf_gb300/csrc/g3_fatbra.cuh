@@ -255,7 +255,7 @@ G3_HD double fb_eval(const Bra<R, NW>& b, R pk, const R* Xk, const R (*Ek)[NK + 
   for (int i = 0; i <= nx; i++)
     for (int j = 0; j <= ny; j++) Bxy[i + j] += A[0][i] * A[1][j];
   // seeds (-alpha)^m F_m(T) and the final sum in FP64
-  const double s = boys_sum(L, (double)T, (double)alpha, [&](int m) {
+  const double s = boys_sum(L, T, (double)alpha, [&](int m) {
     R bm = R(0);
     const int lo = m - nz > 0 ? m - nz : 0, hi = m < nx + ny ? m : nx + ny;
     for (int i = lo; i <= hi; i++) bm += Bxy[i] * A[2][m - i];

@@ -54,58 +54,18 @@
 #ifndef NX_BOYS_RINV_DEFINED
 #define NX_BOYS_RINV_DEFINED
 namespace neoxc {
-// 1/(j + 1/2) for j = 0..191: the divisors of the Boys series (the largest
-// index the series reaches for T <= 20 and the supported orders is ~150).
-constexpr int kBoysRinv = 192;
+// 1/(2j + 1) for j = 0..31, the divisors of the Boys downward recursion
+// F_j = (2T F_(j+1) + exp(-T)) / (2j + 1) (orders up to 22 are used).
+constexpr int kBoysRinv = 32;
 #define NX_BOYS_RINV_VALUES \
-    2.0, 0.6666666666666666, 0.4, 0.2857142857142857, \
-    0.2222222222222222, 0.18181818181818182, 0.15384615384615385, 0.13333333333333333, \
-    0.11764705882352941, 0.10526315789473684, 0.09523809523809523, 0.08695652173913043, \
-    0.08, 0.07407407407407407, 0.06896551724137931, 0.06451612903225806, \
-    0.06060606060606061, 0.05714285714285714, 0.05405405405405406, 0.05128205128205128, \
-    0.04878048780487805, 0.046511627906976744, 0.044444444444444446, 0.0425531914893617, \
-    0.04081632653061224, 0.0392156862745098, 0.03773584905660377, 0.03636363636363636, \
-    0.03508771929824561, 0.03389830508474576, 0.03278688524590164, 0.031746031746031744, \
-    0.03076923076923077, 0.029850746268656716, 0.028985507246376812, 0.028169014084507043, \
-    0.0273972602739726, 0.02666666666666667, 0.025974025974025976, 0.02531645569620253, \
-    0.024691358024691357, 0.024096385542168676, 0.023529411764705882, 0.022988505747126436, \
-    0.02247191011235955, 0.02197802197802198, 0.021505376344086023, 0.021052631578947368, \
-    0.020618556701030927, 0.020202020202020204, 0.019801980198019802, 0.019417475728155338, \
-    0.01904761904761905, 0.018691588785046728, 0.01834862385321101, 0.018018018018018018, \
-    0.017699115044247787, 0.017391304347826087, 0.017094017094017096, 0.01680672268907563, \
-    0.01652892561983471, 0.016260162601626018, 0.016, 0.015748031496062992, \
-    0.015503875968992248, 0.015267175572519083, 0.015037593984962405, 0.014814814814814815, \
-    0.014598540145985401, 0.014388489208633094, 0.014184397163120567, 0.013986013986013986, \
-    0.013793103448275862, 0.013605442176870748, 0.013422818791946308, 0.013245033112582781, \
-    0.013071895424836602, 0.012903225806451613, 0.012738853503184714, 0.012578616352201259, \
-    0.012422360248447204, 0.012269938650306749, 0.012121212121212121, 0.011976047904191617, \
-    0.011834319526627219, 0.011695906432748537, 0.011560693641618497, 0.011428571428571429, \
-    0.011299435028248588, 0.0111731843575419, 0.011049723756906077, 0.01092896174863388, \
-    0.010810810810810811, 0.0106951871657754, 0.010582010582010581, 0.010471204188481676, \
-    0.010362694300518135, 0.010256410256410256, 0.01015228426395939, 0.010050251256281407, \
-    0.009950248756218905, 0.009852216748768473, 0.00975609756097561, 0.00966183574879227, \
-    0.009569377990430622, 0.009478672985781991, 0.009389671361502348, 0.009302325581395349, \
-    0.009216589861751152, 0.0091324200913242, 0.00904977375565611, 0.008968609865470852, \
-    0.008888888888888889, 0.00881057268722467, 0.008733624454148471, 0.008658008658008658, \
-    0.008583690987124463, 0.00851063829787234, 0.008438818565400843, 0.008368200836820083, \
-    0.008298755186721992, 0.00823045267489712, 0.00816326530612245, 0.008097165991902834, \
-    0.008032128514056224, 0.00796812749003984, 0.007905138339920948, 0.00784313725490196, \
-    0.007782101167315175, 0.007722007722007722, 0.007662835249042145, 0.0076045627376425855, \
-    0.007547169811320755, 0.00749063670411985, 0.007434944237918215, 0.007380073800738007, \
-    0.007326007326007326, 0.007272727272727273, 0.007220216606498195, 0.007168458781362007, \
-    0.0071174377224199285, 0.007067137809187279, 0.007017543859649123, 0.006968641114982578, \
-    0.006920415224913495, 0.006872852233676976, 0.006825938566552901, 0.006779661016949152, \
-    0.006734006734006734, 0.006688963210702341, 0.006644518272425249, 0.006600660066006601, \
-    0.006557377049180328, 0.006514657980456026, 0.006472491909385114, 0.006430868167202572, \
-    0.006389776357827476, 0.006349206349206349, 0.006309148264984227, 0.006269592476489028, \
-    0.006230529595015576, 0.006191950464396285, 0.006153846153846154, 0.0061162079510703364, \
-    0.0060790273556231, 0.006042296072507553, 0.006006006006006006, 0.005970149253731343, \
-    0.005934718100890208, 0.0058997050147492625, 0.005865102639296188, 0.0058309037900874635, \
-    0.005797101449275362, 0.005763688760806916, 0.0057306590257879654, 0.005698005698005698, \
-    0.0056657223796034, 0.005633802816901409, 0.0056022408963585435, 0.005571030640668524, \
-    0.00554016620498615, 0.005509641873278237, 0.005479452054794521, 0.005449591280653951, \
-    0.005420054200542005, 0.005390835579514825, 0.005361930294906166, 0.005333333333333333, \
-    0.005305039787798408, 0.005277044854881266, 0.005249343832020997, 0.005221932114882507
+    1.0, 0.3333333333333333, 0.2, 0.14285714285714285, \
+    0.1111111111111111, 0.09090909090909091, 0.07692307692307693, 0.06666666666666667, \
+    0.058823529411764705, 0.05263157894736842, 0.047619047619047616, 0.043478260869565216, \
+    0.04, 0.037037037037037035, 0.034482758620689655, 0.03225806451612903, \
+    0.030303030303030304, 0.02857142857142857, 0.02702702702702703, 0.02564102564102564, \
+    0.024390243902439025, 0.023255813953488372, 0.022222222222222223, 0.02127659574468085, \
+    0.02040816326530612, 0.0196078431372549, 0.018867924528301886, 0.01818181818181818, \
+    0.017543859649122806, 0.01694915254237288, 0.01639344262295082, 0.015873015873015872
 #if defined(__CUDACC__)
 static __device__ const double kBoysRinvDev[kBoysRinv] = {NX_BOYS_RINV_VALUES};
 #endif
@@ -227,7 +187,7 @@ NX_BIG void boys(int M, double T, double* F) {
       boys_tab(row + kBoysCols - 1) * (((((e[6] + e[5]) + e[4]) + e[3]) + e[2]) + e[1] + 1.0);
   const double t2 = 2.0 * T;
   for (int L = M - 1; L >= 0; L--) {
-    f = fma(f, t2, ex) * (0.5 * boys_rinv(L));   // (2T F_(L+1) + e^-T) / (2L + 1)
+    f = fma(f, t2, ex) * boys_rinv(L);   // (2T F_(L+1) + e^-T) / (2L + 1)
     F[L] = f;
   }
 }
@@ -238,9 +198,14 @@ NX_BIG void boys(int M, double T, double* F) {
 // (-alpha) (s <- s (-alpha) + F_m b(m)), F_L and exp(d) by Horner in d;
 // for T > 20 (and NaN) the asymptotic upward recursion runs alongside the
 // ascending sum.  b(m) is called once per m, from m = L down (T <= 20) or
-// from m = 0 up.  Equal to boys() followed by the sum to rounding.
-template <class BF>
-NX_HD double boys_sum(int L, double T, double alpha, BF&& b) {
+// from m = 0 up.  Equal to boys() followed by the sum to rounding.  For an
+// FP32 argument the grid index and the offset d = T_g - T are formed in
+// FP32: T_g and T then lie within 1/32 of each other, so the subtraction is
+// exact (Sterbenz) and gives the same d as in FP64 with fewer FP64
+// instructions.
+template <class TT, class BF>
+NX_HD double boys_sum(int L, TT Tin, double alpha, BF&& b) {
+  const double T = (double)Tin;
   const double ma = -alpha;
   if (!(T <= 20.0)) {
     const double rT = 1.0 / T;
@@ -253,9 +218,18 @@ NX_HD double boys_sum(int L, double T, double alpha, BF&& b) {
     }
     return s;
   }
-  int g = (int)(T * 16.0 + 0.5);
-  g = g < 0 ? 0 : (g > kBoysRows - 1 ? kBoysRows - 1 : g);
-  const double d = (double)g * 0.0625 - T;
+  int g;
+  double d;
+  if constexpr (sizeof(TT) == sizeof(float)) {
+    const float tf = (float)Tin;
+    g = (int)(tf * 16.0f + 0.5f);
+    g = g < 0 ? 0 : (g > kBoysRows - 1 ? kBoysRows - 1 : g);
+    d = (double)((float)g * 0.0625f - tf);
+  } else {
+    g = (int)(T * 16.0 + 0.5);
+    g = g < 0 ? 0 : (g > kBoysRows - 1 ? kBoysRows - 1 : g);
+    d = (double)g * 0.0625 - T;
+  }
   const int row = g * kBoysCols;
   const double d2 = d * 0.5, d3 = d * (1.0 / 3.0), d4 = d * 0.25, d5 = d * 0.2,
                d6 = d * (1.0 / 6.0);
@@ -278,7 +252,7 @@ NX_HD double boys_sum(int L, double T, double alpha, BF&& b) {
   const double ex = boys_tab(row + kBoysCols - 1) * ep;
   const double t2 = 2.0 * T;
   for (int m = L - 1; m >= 0; m--) {
-    f = fma(f, t2, ex) * (0.5 * boys_rinv(m));
+    f = fma(f, t2, ex) * boys_rinv(m);
     s = fma(s, ma, f * (double)b(m));
   }
   return s;
@@ -663,7 +637,7 @@ NX_BIG real contract_wr(const real* Wx, int nx, const real* Wy, int ny,
   for (int i = 0; i <= nx; i++)
     for (int j = 0; j <= ny; j++) Bxy[i + j] += A[0][i] * A[1][j];
   const int L = nx + ny + nz;
-  const double s = boys_sum(L, (double)T, (double)alpha, [&](int m) {
+  const double s = boys_sum(L, T, (double)alpha, [&](int m) {
     real bm = R_(0.0);
     const int lo = m - nz > 0 ? m - nz : 0, hi = m < nx + ny ? m : nx + ny;
     for (int i = lo; i <= hi; i++) bm += Bxy[i] * A[2][m - i];
@@ -688,7 +662,7 @@ NX_BIG real g3_coulomb(const G3& s, real C0, real C3, real bf, real bg, real bh,
       const real wd = ((s.pr[0].K[d] * s.pr[1].K[d]) * s.pr[2].K[d]) * s.D[d][0];
       w = d == 0 ? wd : w * wd;
     }
-    return C0 * C3 * (w * (real)boys_sum(0, (double)T, 0.0, [](int) { return 1.0; }));
+    return C0 * C3 * (w * (real)boys_sum(0, T, 0.0, [](int) { return 1.0; }));
   }
   real W[3][LTOT + 1];
   int n[3];
@@ -760,7 +734,7 @@ NX_BIG void g3_vxc_multi(const G3& s, int nat, const double* cat, real* out) {
     }
     const real T = alpha * R2;
     if (all_s) {
-      out[ia] = C0 * C3 * (w * (real)boys_sum(0, (double)T, 0.0, [](int) { return 1.0; }));
+      out[ia] = C0 * C3 * (w * (real)boys_sum(0, T, 0.0, [](int) { return 1.0; }));
     } else {
       out[ia] = C0 * C3 * contract_wr(W[0], n[0], W[1], n[1], W[2], n[2], T, alpha, Rv);
     }
@@ -854,7 +828,7 @@ NX_BIG real g4_coulomb(const G4& s, const GK4& gk, const real* cof,
       w *= s.pr[0].K[d] * s.pr[1].K[d] * s.pr[2].K[d] * s.pr[3].K[d];
     }
     w *= exp(expo);
-    return pref * (w * (real)boys_sum(0, (double)T, 0.0, [](int) { return 1.0; }));
+    return pref * (w * (real)boys_sum(0, T, 0.0, [](int) { return 1.0; }));
   }
   real W[3][LTOT + 1];
   int nmax[3];

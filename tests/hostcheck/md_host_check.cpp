@@ -63,6 +63,12 @@ double hc_gfvee(const HP* A1, const HP* A2, const HP* B1, const HP* B2) {
 double hc_gfke(const HP* A, const HP* B, double m) { return gfke(cv(*A), cv(*B), m); }
 double hc_gfvec(const HP* A, const HP* B, const double* C) { return gfvec(cv(*A), cv(*B), C); }
 double hc_boys(int m, double T) { double F[64]; neoxc::boys(m, T, F); return F[m]; }
+// sum_m (-alpha)^m F_m(T) b[m] by the fused recursion, with T passed as FP64
+// or (f32 = 1) as FP32
+double hc_boys_sum(int L, double T, double alpha, const double* b, int f32) {
+  auto bf = [&](int m) { return b[m]; };
+  return f32 ? neoxc::boys_sum(L, (float)T, alpha, bf) : neoxc::boys_sum(L, T, alpha, bf);
+}
 
 // the FP32 instance (mixed path): same integrals, FP32 tables, FP64 Boys
 static neoxc::md32::Prim cv32(const HP& h) {

@@ -211,6 +211,30 @@ def test_boys_function_matches_xgammaf(orc, hostcheck):
     assert worst < 5e-12, worst
 
 
+def test_fused_boys_seed_sum(orc, hostcheck):
+    """boys_sum (the Boys recursion fused with the Horner sum of the seeds
+    (-alpha)^m F_m(T) b_m) against XGAMMAF's restatement followed by the
+    plain sum; and for an FP32 argument (grid offset formed in FP32, exact)
+    bit-identical to the FP64 argument of the same value."""
+    L, H = orc.lib(), hostcheck
+    H.hc_boys_sum.restype = C.c_double
+    H.hc_boys_sum.argtypes = [C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int]
+    rng = np.random.default_rng(8)
+    F = np.zeros(17)
+    for trial in range(300):
+        Lm = int(rng.integers(0, 17))
+        T = float(np.float32(rng.choice([rng.uniform(0, 22), np.exp(rng.uniform(-12, 3))])))
+        alpha = float(np.exp(rng.uniform(-2, 3)))
+        b = rng.uniform(-1, 1, Lm + 1)
+        pb = b.ctypes.data_as(C.POINTER(C.c_double))
+        got = H.hc_boys_sum(Lm, T, alpha, pb, 0)
+        L.orc_xgammaf(orc.ptr(F), T, 16)
+        ref = sum((-alpha) ** m * F[m] * b[m] for m in range(Lm + 1))
+        scale = sum(abs((-alpha) ** m * F[m] * b[m]) for m in range(Lm + 1))
+        assert abs(got - ref) <= 1e-11 * scale, (Lm, T, alpha, got, ref)
+        assert H.hc_boys_sum(Lm, T, alpha, pb, 1) == got, (Lm, T)
+
+
 def test_composite_bra_form_matches_g4_integrals(orc, hostcheck):
     """The gam_3 builder evaluates G4_MD_xgVeeg / G4_MD_xgVepg as a Coulomb
     integral between a composite bra (three pair densities, both geminals
