@@ -54,6 +54,12 @@
 //   |G4Vep| <~ S1 S2 Q3 Qp,   |G4Vee| <~ S3 Sp Q1 Q2
 // (a bound for s functions, an estimate for p/d); a (bra, ket) whose
 // estimate times sum_kl |b_k b_l| falls below `screen` is skipped.
+//
+// Many systems (launch_gam3_batch_pairs): the blocks of one angular class
+// from every system and both passes form one work space that a persistent
+// grid drains through a device counter (gam3_fb_persistent); the per-block
+// arithmetic is that of gam3_fb_kernel, so each system's R4 is bit-identical
+// to its separate build.
 #include <type_traits>
 #include <vector>
 
