@@ -386,11 +386,14 @@ int neoxc_dev_gam4_fock_factored(void* stream, int64_t ne, int64_t np,
 /* Mixed-precision form of neoxc_dev_gam4_fock_factored (gam_4_OMP.f:712-1192
  * element, gam4_DSCF_OMP.f:266-307 contraction; the factorisation is new):
  * the one-index transforms and the focke contraction run on the tensor
- * cores (tcgen05.mma kind::tf32, each FP64 operand split into two TF32
- * halves, three products, FP32 accumulation, FP64 results: ~1e-6
- * relative); the two passes over GAM_2s, the traces, gradients and every
- * reduction are FP64.  Same accumulate/overwrite contract; returns after
- * the stream has drained (it checks the kernels' bounded-wait flag). */
+ * cores (tcgen05.mma kind::tf32, each FP64 operand narrowed to FP32 and
+ * split into two TF32 halves, three products, FP32 accumulation folded into
+ * FP64 every 256 K, FP64 results); the two passes over GAM_2s multiply
+ * FP32-narrowed elements with FP32 partial sums over 64 terms and FP64
+ * beyond; the traces, gradients and final reductions are FP64 (~3e-6
+ * relative in E_gam4 at nebf = 60, npbf = 24).  Same accumulate/overwrite
+ * contract; returns after the stream has drained (it checks the kernels'
+ * bounded-wait flag). */
 int neoxc_dev_gam4_fock_factored_tc(void* stream, int64_t ne, int64_t np,
                                     const double* d_GAM_ee,
                                     const double* d_GAM_2s, const double* d_DE,
