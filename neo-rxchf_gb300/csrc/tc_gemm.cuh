@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "narrow.cuh"
+
 namespace neoxc {
 namespace tc {
 
@@ -68,29 +70,6 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return r;
-}
-
-// FP64 -> FP32 by integer operations on the bit pattern, truncating the
-// significand to 23 bits (relative error < 2^-23): on this GPU an FP64
-// conversion instruction costs as much as an FP64 FMA, while these run on
-// the integer pipes.  Magnitudes below the FP32 normal range become signed
-// zero, above it infinity; NaN stays NaN.
-__device__ __forceinline__ float narrow_f64(double v) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-  const unsigned top = (unsigned)(u >> 32);
-  const unsigned sign = top & 0x80000000u;
-  const int e = (int)((top >> 20) & 0x7ffu);
-  const int ef = e - 1023 + 127;
-  unsigned r;
-  if (e == 0x7ff)
-    r = sign | ((u & 0xfffffffffffffULL) ? 0x7fc00000u : 0x7f800000u);
-  else if (ef <= 0)
-    r = sign;
-  else if (ef >= 255)
-    r = sign | 0x7f800000u;
-  else
-    r = sign | ((unsigned)ef << 23) | (unsigned)((u >> 29) & 0x7fffffu);
-  return __uint_as_float(r);
 }
 
 // hi + lo carries the 22 leading bits of v, split in FP32 from narrow_f64

@@ -25,7 +25,8 @@ UNITS = ["abi.cu", "abi_fortran.cu", "abi_io.cu", "k_gam4.cu", "k_gam4f.cu", "k_
          "k_md.cu", "k_gam3.cu", "k_scf.cu", "k_spin.cu", "k_rx.cu", "k_rxscf.cu", "k_probe.cu",
          "k_noalloc.cu"]
 HEADERS = ["neoxc_internal.h", "md_math.cuh", "md_math32.cuh", "md_math_body.cuh",
-           "boys_table.inc", "g3_fatbra.cuh", "tc_gemm.cuh"]
+           "boys_table.inc", "g3_fatbra.cuh", "tc_gemm.cuh",
+           "narrow.cuh"]
 
 
 def nvcc() -> str:

@@ -5,6 +5,7 @@
 #include "../../neo-rxchf_gb300/csrc/md_math.cuh"
 #include "../../neo-rxchf_gb300/csrc/md_math32.cuh"
 #include "../../neo-rxchf_gb300/csrc/g3_fatbra.cuh"
+#include "../../neo-rxchf_gb300/csrc/narrow.cuh"
 
 using namespace neoxc::md;
 
@@ -63,6 +64,8 @@ double hc_gfvee(const HP* A1, const HP* A2, const HP* B1, const HP* B2) {
 double hc_gfke(const HP* A, const HP* B, double m) { return gfke(cv(*A), cv(*B), m); }
 double hc_gfvec(const HP* A, const HP* B, const double* C) { return gfvec(cv(*A), cv(*B), C); }
 double hc_boys(int m, double T) { double F[64]; neoxc::boys(m, T, F); return F[m]; }
+// the tensor-core path's integer-pipe FP64 -> FP32 narrowing
+float hc_narrow(double v) { return neoxc::tc::narrow_f64(v); }
 // sum_m (-alpha)^m F_m(T) b[m] by the fused recursion, with T passed as FP64
 // or (f32 = 1) as FP32
 double hc_boys_sum(int L, double T, double alpha, const double* b, int f32) {

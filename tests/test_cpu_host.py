@@ -211,6 +211,33 @@ def test_boys_function_matches_xgammaf(orc, hostcheck):
     assert worst < 5e-12, worst
 
 
+def test_integer_narrowing_to_fp32(hostcheck):
+    """tc::narrow_f64 (the tensor-core path's FP64 -> FP32 conversion on the
+    integer pipes): significand truncated toward zero (|f| <= |v|, relative
+    error below 2^-23, the FP32 rounding of v within one unit in the last
+    place), signed zero below the FP32 normal range, infinity above it, NaN
+    kept."""
+    H = hostcheck
+    H.hc_narrow.restype = C.c_float
+    H.hc_narrow.argtypes = [C.c_double]
+    rng = np.random.default_rng(12)
+    vals = np.concatenate([rng.standard_normal(2000) * np.exp(rng.uniform(-80, 80, 2000)),
+                           [1.0, -1.0, 3.0, 1.0 / 3.0, 2.0 ** -126, -(2.0 ** -126) * 1.5,
+                            3.4e38, -3.4e38]])
+    for v in vals:
+        f = float(H.hc_narrow(float(v)))
+        assert abs(f) <= abs(v) and np.sign(f) == np.sign(v), v
+        assert abs(f - v) < 2.0 ** -23 * abs(v), v
+        assert abs(f - float(np.float32(v))) <= float(np.spacing(np.float32(abs(v)))), v
+    for v, want in ((0.0, 0.0), (1e-40, 0.0), (-1e-300, -0.0), (5e-324, 0.0)):
+        f = float(H.hc_narrow(v))
+        assert f == 0.0 and np.signbit(f) == np.signbit(want), v
+    assert float(H.hc_narrow(1e39)) == float("inf")
+    assert float(H.hc_narrow(-1e300)) == float("-inf")
+    assert float(H.hc_narrow(float("inf"))) == float("inf")
+    assert np.isnan(H.hc_narrow(float("nan")))
+
+
 def test_fused_boys_seed_sum(orc, hostcheck):
     """boys_sum (the Boys recursion fused with the Horner sum of the seeds
     (-alpha)^m F_m(T) b_m) against XGAMMAF's restatement followed by the
